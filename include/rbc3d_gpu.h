@@ -1,0 +1,214 @@
+/*
+ * rbc3d_gpu.h -- C ABI of the GB300 implementation of RBC3D's Ewald-split
+ * boundary-integral matvec (real-space Stokeslet/stresslet pair sums over cell
+ * lists, PME spread / k-space influence / gather, singular and near-singular
+ * polar-patch corrections, wall triangle quadrature, wall no-slip GMRES).
+ *
+ * Every entry point replaces one Fortran module procedure of RBC3D (cited per
+ * function, paths relative to the RBC3D source tree).  Conventions:
+ *
+ *  - Plain pointers and sizes only.  All arrays are caller-owned HOST buffers;
+ *    device buffers are owned by the context.  Calls are synchronous at the ABI
+ *    edge.  One context per host thread.
+ *  - Layouts follow the Fortran column-major arrays of the reference:
+ *      point arrays   x(N,3)   -> x[c*N + p], c = 0..2 (SoA)
+ *      cell point p  = icell*nlat*nlon + ilon*nlat + ilat   (ilat fastest),
+ *                      i.e. the order of SourceList_UpdateCoord / TargetList_Update
+ *      spline tables  per cell: u, u1, u2, u12 (in this order), each
+ *                      (m=2*nlat, n=nlon, nvar) column-major -> 4*m*n*nvar doubles
+ *                      per cell (t_spline of ModDataStruct), cells consecutive
+ *      wall e2v(nele,3) 1-based vertex ids (ModWall), column-major
+ *  - Velocity outputs ACCUMULATE into v (v += ...), like the reference L2
+ *    routines, except the L3 drivers that overwrite (documented per call).
+ *  - Every call returns an rbc3d_status; rbc3d_last_error() gives text.
+ */
+#ifndef RBC3D_GPU_H
+#define RBC3D_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RBC3D_ABI_VERSION 1
+#define RBC3D_MAX_CELLTYPES 8
+#define RBC3D_NBR_MAX 32 /* NMax of NbrRbcList_Create, ModRbcSingInt.F90:319 */
+
+typedef int rbc3d_status;
+enum {
+  RBC3D_OK = 0,
+  RBC3D_ERR_ARG = 1,      /* bad argument / size */
+  RBC3D_ERR_CUDA = 2,     /* CUDA runtime or cuFFT failure */
+  RBC3D_ERR_TIMEOUT = 3,  /* a bounded device wait ran out */
+  RBC3D_ERR_NOCONV = 4,   /* GMRES reached max_it without meeting rtol */
+  RBC3D_ERR_OVERFLOW = 5, /* neighbour-cell list above RBC3D_NBR_MAX, or a
+                             work list above its capacity */
+  RBC3D_ERR_STATE = 6,    /* call order (e.g. no cells set) */
+  RBC3D_ERR_NOMEM = 7
+};
+
+/* Arithmetic of one matvec. */
+enum {
+  RBC3D_FP64 = 0,  /* plain form: everything FP64 */
+  RBC3D_FP32C = 1  /* pair sums, spread, FFT, gather in FP32 with per-target
+                      compensated accumulation; self / near-singular
+                      corrections FP64 */
+};
+
+/* Target lists (t_TargetList instances of ModData.F90:19-20). */
+enum {
+  RBC3D_TLIST_RBC = 0,  /* tlist_rbc: all cell surface points */
+  RBC3D_TLIST_WALL = 1, /* tlist_wall: all wall vertices (Acoef = 2) */
+  RBC3D_TLIST_RAW = 2   /* TargetList_CreateFromRaw (Acoef = 2, indx = -1) */
+};
+
+/* Term selection for rbc3d_matvec. */
+enum {
+  RBC3D_TERM_REAL = 1u,   /* AddIntOnRbcs pair sums (incl. mask) */
+  RBC3D_TERM_CORR = 2u,   /* RBC_SingInt + RBC_NearSingInt */
+  RBC3D_TERM_LINEAR = 4u, /* AddLinearInt */
+  RBC3D_TERM_PME = 8u,    /* PME_Distrib_Source/Transform/Add_Interp_Vel */
+  RBC3D_TERM_WALLS = 16u, /* AddIntOnWalls */
+  RBC3D_TERM_ALL = 31u
+};
+
+typedef struct rbc3d_params {
+  double Lb[3];  /* periodic box (ModConf Lb) */
+  double alpha;  /* Ewald splitting parameter alpha_Ewd */
+  double rc;     /* real-space cut-off rc_Ewd */
+  double eps;    /* Ewald tolerance eps_Ewd (informational / default rtol) */
+  int Nb[3];     /* PME mesh Nb_Ewd */
+  int P;         /* B-spline points PBspln_Ewd */
+  int nlat, nlon;/* cell surface grid (Gauss x uniform), shared by all cells */
+  int ncelltypes;
+  double viscRat[RBC3D_MAX_CELLTYPES]; /* -> Acoef/Bcoef by initCOEFs */
+  double vBkg[3];                      /* background velocity */
+} rbc3d_params;
+
+typedef struct rbc3d_counts {
+  long long pairs_within_rc;  /* (target, source) pairs with r < rc, last real-space pass */
+  long long nbr_items;        /* (target, other cell) near-singular candidates */
+  long long nearsing_items;   /* candidates that passed the distance check */
+  long long self_items;       /* targets given RBC_SingInt */
+  long long wall_pairs;       /* (target, triangle) pairs within rc */
+  long long wall_duffy;       /* of which integrated with Duffy's rule */
+  int nbr_overflow;           /* targets whose neighbour list exceeded RBC3D_NBR_MAX */
+} rbc3d_counts;
+
+typedef struct rbc3d_solve_opts {
+  double rtol;   /* ||r|| <= rtol*||b|| (KSPSetTolerances rtol) */
+  int max_it;    /* KSPSetTolerances max_it */
+  int restart;   /* GMRES restart (PETSc default 30) */
+  int prec;      /* matvec arithmetic, RBC3D_FP64 or RBC3D_FP32C */
+  int guess;     /* 0: zero increment (reference); 1: caller-supplied guess */
+} rbc3d_solve_opts;
+
+typedef struct rbc3d_solve_stats {
+  int iterations;
+  int converged;       /* 1 if ||r||/||b|| <= rtol */
+  double rnorm0;       /* ||b - A x0|| */
+  double rnorm;        /* final residual norm (true residual, recomputed) */
+  double bnorm;
+  double ms;           /* wall time of the solve */
+  int matvecs;
+} rbc3d_solve_stats;
+
+typedef struct rbc3d_ctx rbc3d_ctx;
+
+/* ---- context --------------------------------------------------------- */
+/* Replaces PME_Init (ModPME.F90:252) + the Ewald tables of ModEwaldFunc.F90
+ * + initCOEFs (ModConf.F90:327) + RbcPolarPatch_Create (ModPolarPatch.F90:27). */
+rbc3d_status rbc3d_create(const rbc3d_params* prm, rbc3d_ctx** out);
+/* Replaces PME_Finalize (ModPME.F90:342). */
+rbc3d_status rbc3d_destroy(rbc3d_ctx* ctx);
+const char* rbc3d_last_error(const rbc3d_ctx* ctx);
+int rbc3d_abi_version(void);
+
+/* Derived Ewald parameters: SetEwaldPrms (ModConf.F90:348-408), single rank.
+ * Returns rc (capped at min(Lb)/3.001) and Nb for the given alpha/eps. */
+rbc3d_status rbc3d_ewald_prms(double alpha, double eps, const double Lb[3],
+                              int P, double* rc, int Nb[3]);
+
+/* ---- surfaces -------------------------------------------------------- */
+/* Cell grid: th(nlat) Gauss colatitudes, phi(nlon), w(nlat) = Gauss weight *
+ * 2*pi/nlon (RBC_Create, ModRbc.F90:92-94). */
+rbc3d_status rbc3d_set_cell_grid(rbc3d_ctx* ctx, const double* th,
+                                 const double* phi, const double* w);
+/* Cell geometry: SourceList_UpdateCoord + TargetList_Update for rbcs
+ * (ModSourceList.F90:92, ModTargetList.F90:95) plus the geometry consumed by
+ * the corrections (RBC_ComputeGeometry / Rbc_BuildSurfaceSource xFlag,
+ * ModRbc.F90:404,716): x, a3 (N x 3), detJ (N), area, meshSize (ncell),
+ * celltype (ncell, 0-based), spline tables of x (nvar 3), a3 (3), detJ (1). */
+rbc3d_status rbc3d_set_cells(rbc3d_ctx* ctx, int ncell, const int* celltype,
+                             const double* x, const double* a3,
+                             const double* detJ, const double* area,
+                             const double* meshSize, const double* spl_x,
+                             const double* spl_a3, const double* spl_detJ);
+/* Cell densities: SourceList_UpdateDensity (ModSourceList.F90:160) + the
+ * FdetJ / GdetJ splines (Rbc_BuildSurfaceSource fFlag/gFlag).  f, g are the
+ * raw surface densities (N x 3); either pair may be NULL (left unchanged). */
+rbc3d_status rbc3d_set_cell_density(rbc3d_ctx* ctx, const double* f,
+                                    const double* g, const double* spl_FdetJ,
+                                    const double* spl_GdetJ);
+/* Walls (one wall): Wall_ComputeGeometry + SourceList_UpdateCoord(walls) +
+ * TargetList_Update(walls) (ModWall.F90:118, ModTimeInt.F90:80-82).
+ * x (nvert x 3), e2v (nele x 3, 1-based), indxVertGlb (nvert, 1-based unique
+ * vertex id, GlobData_Init ModData.F90:47-58). */
+rbc3d_status rbc3d_set_walls(rbc3d_ctx* ctx, int nvert, int nele,
+                             const double* x, const int* e2v,
+                             const int* indxVertGlb);
+rbc3d_status rbc3d_set_wall_density(rbc3d_ctx* ctx, const double* f);
+rbc3d_status rbc3d_get_wall_density(rbc3d_ctx* ctx, double* f);
+/* TargetList_CreateFromRaw (ModTargetList.F90:137). */
+rbc3d_status rbc3d_set_raw_targets(rbc3d_ctx* ctx, int n, const double* x);
+int rbc3d_num_targets(const rbc3d_ctx* ctx, int tlist);
+
+/* ---- L2 operators (accumulate into v) -------------------------------- */
+/* AddIntOnRbcs(c1,c2,tlist,v), ModIntOnRbcs.F90:25: real-space pair sums with
+ * the same-cell mask, RBC_SingInt, RBC_NearSingInt per neighbour cell and
+ * AddLinearInt. */
+rbc3d_status rbc3d_add_int_on_rbcs(rbc3d_ctx* ctx, int tlist, double c1,
+                                   double c2, int prec, double* v);
+/* AddIntOnWalls(c1,tlist,v), ModIntOnWalls.F90:37 (self wall via the sparse
+ * operator of rbc3d_prepare_sing_int_on_wall for wall targets). */
+rbc3d_status rbc3d_add_int_on_walls(rbc3d_ctx* ctx, int tlist, double c1,
+                                    int prec, double* v);
+/* PrepareSingIntOnWall(wall), ModIntOnWalls.F90:181: assembles the self-wall
+ * 3nvert x 3nvert operator once (CSR, FP64). */
+rbc3d_status rbc3d_prepare_sing_int_on_wall(rbc3d_ctx* ctx);
+/* PME_Distrib_Source(c1,c2,cells,walls), ModPME.F90:58 */
+rbc3d_status rbc3d_pme_distrib_source(rbc3d_ctx* ctx, double c1, double c2,
+                                      int cells, int walls, int prec);
+/* PME_Transform, ModPME.F90:137 */
+rbc3d_status rbc3d_pme_transform(rbc3d_ctx* ctx);
+/* PME_Add_Interp_Vel(tlist,v), ModPME.F90:228 */
+rbc3d_status rbc3d_pme_add_interp_vel(rbc3d_ctx* ctx, int tlist, double* v);
+
+/* Composite matvec, all terms on the device with one download: the sum that
+ * Compute_Rhs / CalcVelocityField / Compute_Wall_Residual_Vel assemble from
+ * the L2 calls above (ModVelSolver.F90:476-490, ModPostProcess.F90:39-51,
+ * ModNoSlip.F90:175-184), without background velocity.  v += result. */
+rbc3d_status rbc3d_matvec(rbc3d_ctx* ctx, int tlist, double c1, double c2,
+                          unsigned terms, int prec, double* v);
+
+/* ---- L3 drivers ------------------------------------------------------- */
+/* Compute_Wall_Residual_Vel(v), ModNoSlip.F90:153.  Overwrites v (nvert x 3). */
+rbc3d_status rbc3d_compute_wall_residual_vel(rbc3d_ctx* ctx, int prec,
+                                             double* v);
+/* NoSlipWall, ModNoSlip.F90:45: GMRES on the wall-density increment (PCNONE),
+ * wall f <- f0 + finc.  guess: NULL or a dof-length (3*unique vertices,
+ * xyz-interleaved per unique vertex as AssembleArray) initial increment. */
+rbc3d_status rbc3d_no_slip_wall(rbc3d_ctx* ctx, const rbc3d_solve_opts* opt,
+                                const double* guess, rbc3d_solve_stats* st);
+/* MyMatMult of ModNoSlip.F90:255 on a dof-length vector: y = A u. */
+rbc3d_status rbc3d_wall_matmult(rbc3d_ctx* ctx, int prec, const double* u,
+                                double* y);
+/* CalcVelocityField(tlist,v), ModPostProcess.F90:29.  Overwrites v. */
+rbc3d_status rbc3d_calc_velocity_field(rbc3d_ctx* ctx, int tlist, int prec,
+                                       double* v);
+
+rbc3d_status rbc3d_get_counts(const rbc3d_ctx* ctx, rbc3d_counts* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RBC3D_GPU_H */

@@ -1,0 +1,601 @@
+// api.cu -- C ABI of the GB300 Ewald-split boundary-integral matvec
+// (include/rbc3d_gpu.h): context set-up, uploads and the entry points that
+// replace RBC3D's module procedures.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ctx.hpp"
+
+rbc3d_status ctx_fail(rbc3d_ctx* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return code;
+}
+rbc3d_status ctx_fail_cuda(rbc3d_ctx* ctx, cudaError_t e, const char* what) {
+  if (ctx) ctx->err = std::string(what) + ": " + cudaGetErrorString(e);
+  return RBC3D_ERR_CUDA;
+}
+
+// GauLeg (ModQuadRule.F90:135-214): Numerical Recipes Gauss-Legendre nodes by
+// simultaneous Newton iteration, EPS = 3e-14.
+void host_gauleg(double x1, double x2, int n, double* x, double* w) {
+  const double EPS = 3.e-14;
+  int m = (n + 1) / 2;
+  double xm = 0.5 * (x2 + x1), xl = 0.5 * (x2 - x1);
+  std::vector<double> p1(m), p2(m), p3(m), pp(m), z(m), z1(m);
+  std::vector<char> act(m, 1);
+  for (int j = 0; j < m; ++j) z[j] = std::cos(RBC3D_PI * ((j + 1) - 0.25) / (n + 0.5));
+  for (int its = 1; its <= 10; ++its) {
+    for (int k = 0; k < m; ++k)
+      if (act[k]) { p1[k] = 1.0; p2[k] = 0.0; }
+    for (int j = 1; j <= n; ++j)
+      for (int k = 0; k < m; ++k)
+        if (act[k]) { p3[k] = p2[k]; p2[k] = p1[k]; p1[k] = ((2.0 * j - 1.0) * z[k] * p2[k] - (j - 1.0) * p3[k]) / j; }
+    bool any = false;
+    for (int k = 0; k < m; ++k)
+      if (act[k]) {
+        pp[k] = n * (z[k] * p1[k] - p2[k]) / (z[k] * z[k] - 1.0);
+        z1[k] = z[k];
+        z[k] = z1[k] - p1[k] / pp[k];
+        act[k] = std::fabs(z[k] - z1[k]) > EPS;
+        any = any || act[k];
+      }
+    if (!any) break;
+  }
+  for (int k = 0; k < m; ++k) {
+    x[k] = xm - xl * z[k];
+    x[n - 1 - k] = xm + xl * z[k];
+    w[k] = 2.0 * xl / ((1.0 - z[k] * z[k]) * pp[k] * pp[k]);
+    w[n - 1 - k] = w[k];
+  }
+}
+
+namespace {
+
+inline int nblk(long long n, int b) { return (int)((n + b - 1) / b); }
+
+static double mask_exact(double x) {  // MaskFunc_Exact, ModBasicMath.F90:332-346
+  double t = std::fabs(x);
+  if (t < 0.01) return 1.;
+  if (t > 0.99) return 0.;
+  return std::exp(2 * (std::exp(-1. / t)) / (t - 1));
+}
+
+// Host copy of MaskFunc (table lerp) for the patch weights.
+static double mask_lerp(const std::vector<double>& tab, double x) {
+  double s = std::fabs(x) * MASK_NTAB;
+  int i = (int)std::floor(s);
+  if (i >= MASK_NTAB) return 0.;
+  return tab[i] * (i + 1 - s) + tab[i + 1] * (s - i);
+}
+
+// Spline table repack: ABI layout per cell [kind][var][j][i] (nvar vars) ->
+// device layout [cell][set][node=i+m*j][kind*3+var].
+__global__ void k_repack(int ncell, int m, int n, int nvar, int set, const double* __restrict__ src,
+                         double* __restrict__ dst) {
+  long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long per = (long long)m * n;
+  long long total = (long long)ncell * per;
+  if (idx >= total) return;
+  int cell = (int)(idx / per);
+  int node = (int)(idx - cell * per);
+  const double* s = src + (size_t)cell * 4 * per * nvar;
+  double* d = dst + (((size_t)cell * SPL_NSET + set) * per + node) * SPL_NODE;
+  for (int kind = 0; kind < 4; ++kind)
+    for (int v = 0; v < 3; ++v) d[kind * 3 + v] = (v < nvar) ? s[(size_t)kind * per * nvar + node + per * v] : 0.0;
+}
+
+__global__ void k_fill_meta(int n, int nv, int nlat, int4* meta) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  int cell = p / nv, r = p - cell * nv;
+  meta[p] = make_int4(cell + 1, r % nlat, r / nlat, 0);
+}
+__global__ void k_fill_acoef(int n, int nv, const int* celltype, const double* Ac, double* A) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  A[p] = Ac[celltype[p / nv]];
+}
+__global__ void k_fill_const(int n, int4 mv, double av, int4* meta, double* A) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  meta[p] = mv;
+  A[p] = av;
+}
+
+rbc3d_status upload_splines(rbc3d_ctx* ctx, const double* h, int nvar, int set) {
+  if (!h) return RBC3D_OK;
+  size_t per = (size_t)ctx->m * ctx->nlon;
+  size_t cnt = (size_t)ctx->ncell * 4 * per * nvar;
+  DBuf<double> tmp;
+  CUDA_TRY(tmp.upload(h, cnt, ctx->st));
+  long long total = (long long)ctx->ncell * per;
+  k_repack<<<nblk(total, 256), 256, 0, ctx->st>>>(ctx->ncell, ctx->m, ctx->nlon, nvar, set, tmp.p, ctx->spl.p);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  return RBC3D_OK;
+}
+
+TargetSet* tset(rbc3d_ctx* ctx, int which) {
+  if (which < 0 || which > 2) return nullptr;
+  return &ctx->tl[which];
+}
+
+rbc3d_status begin(rbc3d_ctx* ctx, TargetSet& t) {
+  CUDA_TRY(t.v.alloc(3 * (size_t)std::max(t.n, 1)));
+  CUDA_TRY(cudaMemsetAsync(t.v.p, 0, sizeof(double) * 3 * t.n, ctx->st));
+  return RBC3D_OK;
+}
+rbc3d_status finish_add(rbc3d_ctx* ctx, TargetSet& t, double* v) {
+  std::vector<double> tmp(3 * (size_t)t.n);
+  CUDA_TRY(cudaMemcpyAsync(tmp.data(), t.v.p, sizeof(double) * tmp.size(), cudaMemcpyDeviceToHost, ctx->st));
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  for (size_t i = 0; i < tmp.size(); ++i) v[i] += tmp[i];
+  return RBC3D_OK;
+}
+
+// Real space + corrections + linear term of AddIntOnRbcs on device (no download).
+rbc3d_status rbcs_dev(rbc3d_ctx* ctx, int which, double c1, double c2, int prec, unsigned terms) {
+  if (ctx->npt == 0) return RBC3D_OK;
+  // a density that was never set is zero (the reference's cells start with f = g = 0)
+  if (!ctx->has_f) c1 = 0.0;
+  if (!ctx->has_g) c2 = 0.0;
+  TargetSet& t = ctx->tl[which];
+  bool corr = (terms & RBC3D_TERM_CORR) != 0;
+  rbc3d_status s;
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    CUDA_TRY(cudaMemsetAsync(ctx->dcnt.p, 0, sizeof(unsigned long long) * 3, ctx->st));
+    if (terms & RBC3D_TERM_REAL || corr) {
+      if ((s = run_pair_sum(ctx, which, (terms & RBC3D_TERM_REAL) ? c1 : 0.0, (terms & RBC3D_TERM_REAL) ? c2 : 0.0,
+                            prec, corr)))
+        return s;
+    }
+    if (!corr) break;
+    unsigned long long h[3];
+    CUDA_TRY(cudaMemcpyAsync(h, ctx->dcnt.p, sizeof(h), cudaMemcpyDeviceToHost, ctx->st));
+    CUDA_TRY(cudaStreamSynchronize(ctx->st));
+    if (h[2]) return ctx_fail(ctx, RBC3D_ERR_OVERFLOW, "neighbour-cell list above NMax=32 for some target");
+    if (h[0] <= (unsigned long long)ctx->items_cap) break;
+    // grow the work list and redo the pass
+    ctx->items_cap = (int)std::min<unsigned long long>(h[0] + h[0] / 4 + 1024, 0x7fffffffull);
+    CUDA_TRY(ctx->items.alloc(ctx->items_cap));
+    CUDA_TRY(cudaMemsetAsync(t.v.p, 0, sizeof(double) * 3 * t.n, ctx->st));
+  }
+  if (corr) {
+    CUDA_TRY(cudaMemsetAsync(ctx->dcnt.p + 3, 0, sizeof(unsigned long long), ctx->st));
+    if ((s = run_self_corr(ctx, which, c1, c2))) return s;
+    if ((s = run_near_corr(ctx, which, c1, c2, prec))) return s;
+  }
+  if (terms & RBC3D_TERM_LINEAR)
+    if ((s = run_linear(ctx, which, c2))) return s;
+  unsigned long long h[4];
+  CUDA_TRY(cudaMemcpyAsync(h, ctx->dcnt.p, sizeof(h), cudaMemcpyDeviceToHost, ctx->st));
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  ctx->counts.pairs_within_rc = (long long)h[1];
+  if (corr) {
+    ctx->counts.nbr_items = (long long)h[0];
+    ctx->counts.nearsing_items = (long long)h[3];
+    ctx->counts.self_items = (which == RBC3D_TLIST_RBC) ? t.n : 0;
+  }
+  ctx->counts.nbr_overflow = (int)h[2];
+  return RBC3D_OK;
+}
+
+}  // namespace
+
+// Composite device-resident matvec used by the ABI calls (defined here so the
+// wall solver can call it too).
+rbc3d_status matvec_dev(rbc3d_ctx* ctx, int which, double c1, double c2, unsigned terms, int prec) {
+  TargetSet& t = ctx->tl[which];
+  rbc3d_status s;
+  if ((s = begin(ctx, t))) return s;
+  if (terms & (RBC3D_TERM_REAL | RBC3D_TERM_CORR | RBC3D_TERM_LINEAR))
+    if ((s = rbcs_dev(ctx, which, c1, c2, prec, terms))) return s;
+  if (terms & RBC3D_TERM_WALLS) {
+    if (which == RBC3D_TLIST_WALL) { if ((s = run_wall_self(ctx, c1))) return s; }
+    else if ((s = run_wall_quad(ctx, which, c1, prec))) return s;
+  }
+  if (terms & RBC3D_TERM_PME) {
+    if ((s = pme_spread(ctx, c1, c2, 1, (terms & RBC3D_TERM_WALLS) ? 1 : 0, prec))) return s;
+    if ((s = pme_transform(ctx))) return s;
+    if ((s = pme_gather(ctx, which))) return s;
+  }
+  return RBC3D_OK;
+}
+
+extern "C" {
+
+int rbc3d_abi_version(void) { return RBC3D_ABI_VERSION; }
+
+// SetEwaldPrms (ModConf.F90:348-408), single rank
+rbc3d_status rbc3d_ewald_prms(double alpha, double eps, const double Lb[3], int P, double* rc, int Nb[3]) {
+  if (!(alpha > 0) || !(eps > 0) || !Lb || !rc || !Nb) return RBC3D_ERR_ARG;
+  double s = 1.;
+  for (int it = 0; it < 10; ++it) {
+    s = 0.75 * std::sqrt(RBC3D_PI) * eps / (s * s * s + 1.5 * s + 0.75 / s);
+    s = std::sqrt(-std::log(s));
+  }
+  double r = std::sqrt(alpha / RBC3D_PI) * s;
+  r = std::min(std::min(Lb[0] / 3.001, Lb[1] / 3.001), std::min(Lb[2] / 3.001, r));
+  *rc = r;
+  for (int d = 0; d < 3; ++d) Nb[d] = 2 * (int)std::ceil(std::sqrt(-std::log(eps) / (RBC3D_PI * alpha)) * Lb[d]);
+  Nb[2] = std::max(Nb[2], P);
+  return RBC3D_OK;
+}
+
+rbc3d_status rbc3d_create(const rbc3d_params* prm, rbc3d_ctx** out) {
+  if (!prm || !out) return RBC3D_ERR_ARG;
+  *out = nullptr;
+  if (prm->ncelltypes < 1 || prm->ncelltypes > RBC3D_MAX_CELLTYPES || prm->P < 2 || prm->P > 8 || !(prm->rc > 0) ||
+      !(prm->alpha > 0) || prm->nlat < 2 || prm->nlon < 4 || prm->nlon % 2)
+    return RBC3D_ERR_ARG;
+  for (int d = 0; d < 3; ++d)
+    if (!(prm->Lb[d] > 0) || prm->Nb[d] < prm->P || prm->rc > prm->Lb[d] / 3.0) return RBC3D_ERR_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return RBC3D_ERR_CUDA;
+  rbc3d_ctx* ctx = new rbc3d_ctx();
+  ctx->prm = *prm;
+  cudaGetDevice(&ctx->device);
+  for (int d = 0; d < 3; ++d) ctx->iLb[d] = 1. / prm->Lb[d];
+  for (int l = 0; l < prm->ncelltypes; ++l) {  // initCOEFs, ModConf.F90:327-344
+    if (prm->viscRat[l] > 0) { ctx->Acoef[l] = 1. + prm->viscRat[l]; ctx->Bcoef[l] = 1. - prm->viscRat[l]; }
+    else { ctx->Acoef[l] = 1.; ctx->Bcoef[l] = -1.; }
+  }
+  rbc3d_status s = RBC3D_OK;
+  auto bail = [&](rbc3d_status code) { rbc3d_destroy(ctx); return code; };
+  if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) return bail(RBC3D_ERR_CUDA);
+  // Ewald tables, ModEwaldFunc.F90:96-104, 151-162
+  const int N = EWALD_NTAB;
+  const double alpha = prm->alpha, rc = prm->rc;
+  std::vector<double> c1(N + 1), c2(N + 1), dl(N + 1), mk(MASK_NTAB + 1);
+  for (int i = 0; i <= N; ++i) {
+    double r_t = std::sqrt(RBC3D_PI / alpha) * ((double)i * rc / N);
+    c1[i] = std::erfc(r_t);
+    c2[i] = 2 / std::sqrt(alpha) * std::exp(-(r_t * r_t));
+    dl[i] = -8 / std::sqrt(RBC3D_PI) * (std::exp(-(r_t * r_t)) * (1.5 * r_t + r_t * r_t * r_t) +
+                                        0.75 * std::sqrt(RBC3D_PI) * std::erfc(r_t));
+  }
+  for (int i = 0; i <= MASK_NTAB; ++i) mk[i] = mask_exact((double)i / MASK_NTAB);
+  std::vector<float4> sl32(N);
+  std::vector<float2> dl32(N), mk32(MASK_NTAB);
+  for (int i = 0; i < N; ++i) {
+    sl32[i] = make_float4((float)c1[i], (float)(c1[i + 1] - c1[i]), (float)c2[i], (float)(c2[i + 1] - c2[i]));
+    dl32[i] = make_float2((float)dl[i], (float)(dl[i + 1] - dl[i]));
+  }
+  for (int i = 0; i < MASK_NTAB; ++i) mk32[i] = make_float2((float)mk[i], (float)(mk[i + 1] - mk[i]));
+  if (ctx->t_sl1.upload(c1.data(), c1.size(), ctx->st) || ctx->t_sl2.upload(c2.data(), c2.size(), ctx->st) ||
+      ctx->t_dl.upload(dl.data(), dl.size(), ctx->st) || ctx->t_mask.upload(mk.data(), mk.size(), ctx->st) ||
+      ctx->t_sl32.upload(sl32.data(), sl32.size(), ctx->st) || ctx->t_dl32.upload(dl32.data(), dl32.size(), ctx->st) ||
+      ctx->t_mask32.upload(mk32.data(), mk32.size(), ctx->st) || ctx->dcnt.alloc(8) || ctx->xvint.alloc(3))
+    return bail(RBC3D_ERR_CUDA);
+  Tables& T = ctx->T;
+  T.sl_c1 = ctx->t_sl1.p; T.sl_c2 = ctx->t_sl2.p; T.dl_c1 = ctx->t_dl.p; T.mask = ctx->t_mask.p;
+  T.sl32 = ctx->t_sl32.p; T.dl32 = ctx->t_dl32.p; T.mask32 = ctx->t_mask32.p;
+  T.rc = rc; T.r_eps = 1.e-3 * std::sqrt(alpha / RBC3D_PI); T.ntab_over_rc = N / rc;
+  T.rc_f = (float)rc; T.r_eps_f = (float)T.r_eps; T.ntab_over_rc_f = (float)(N / rc);
+  // cell list
+  for (int d = 0; d < 3; ++d) {
+    ctx->hg.Nc[d] = std::max((int)std::floor(prm->Lb[d] / prm->rc), 3);
+    ctx->hg.L[d] = prm->Lb[d];
+    ctx->hg.h[d] = prm->Lb[d] / ctx->hg.Nc[d];
+  }
+  ctx->hg.ncells = ctx->hg.Nc[0] * ctx->hg.Nc[1] * ctx->hg.Nc[2];
+  ctx->nlat = prm->nlat; ctx->nlon = prm->nlon; ctx->m = 2 * prm->nlat;
+  if ((s = pme_setup(ctx))) return bail(s);
+  // ReAdd rules (ModRbcSingInt.F90:254-261): GauLeg(-1,1,16) for the sinh map
+  std::vector<double> gs(16), gw(16);
+  host_gauleg(-1., 1., 16, gs.data(), gw.data());
+  if (ctx->rd_s.upload(gs.data(), 16, ctx->st) || ctx->rd_w.upload(gw.data(), 16, ctx->st)) return bail(RBC3D_ERR_CUDA);
+  cudaStreamSynchronize(ctx->st);
+  *out = ctx;
+  return RBC3D_OK;
+}
+
+rbc3d_status rbc3d_destroy(rbc3d_ctx* ctx) {
+  if (!ctx) return RBC3D_OK;
+  pme_release(ctx);
+  if (ctx->st) cudaStreamSynchronize(ctx->st);
+  cudaStream_t st = ctx->st;
+  delete ctx;
+  if (st) cudaStreamDestroy(st);
+  return RBC3D_OK;
+}
+
+const char* rbc3d_last_error(const rbc3d_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+// RBC_Create grid (ModRbc.F90:92-94) + RbcPolarPatch_Create (ModPolarPatch.F90:27-75)
+rbc3d_status rbc3d_set_cell_grid(rbc3d_ctx* ctx, const double* th, const double* phi, const double* w) {
+  if (!ctx || !th || !phi || !w) return RBC3D_ERR_ARG;
+  const int nlat = ctx->nlat, nlon = ctx->nlon;
+  ctx->h_th.assign(th, th + nlat); ctx->h_phi.assign(phi, phi + nlon); ctx->h_w.assign(w, w + nlat);
+  CUDA_TRY(ctx->th.upload(th, nlat, ctx->st)); CUDA_TRY(ctx->phi.upload(phi, nlon, ctx->st));
+  CUDA_TRY(ctx->w.upload(w, nlat, ctx->st));
+  std::vector<float4> us(nlat * nlon);
+  for (int j = 0; j < nlon; ++j)
+    for (int i = 0; i < nlat; ++i)
+      us[i + nlat * j] = make_float4((float)(std::sin(th[i]) * std::cos(phi[j])), (float)(std::sin(th[i]) * std::sin(phi[j])),
+                                     (float)std::cos(th[i]), 0.f);
+  CUDA_TRY(ctx->usph.upload(us.data(), us.size(), ctx->st));
+  // polar patch
+  std::vector<double> mk(MASK_NTAB + 1);
+  for (int i = 0; i <= MASK_NTAB; ++i) mk[i] = mask_exact((double)i / MASK_NTAB);
+  ctx->radius = RBC3D_PI / std::sqrt((double)nlat);
+  double h = RBC3D_PI / nlat;
+  ctx->nrad = 2 * (int)std::round(ctx->radius / h);
+  ctx->nazm = 2 * ctx->nrad;
+  const int nrad = ctx->nrad, nazm = ctx->nazm, NQ = nrad * nazm;
+  std::vector<double> thL(nrad), pw(nrad), phiL(nazm);
+  host_gauleg(0., ctx->radius, nrad, thL.data(), pw.data());
+  for (int i = 0; i < nrad; ++i) {
+    pw[i] = pw[i] * std::sin(thL[i]) * (RBC3D_TWO_PI / nazm);
+    pw[i] = pw[i] * mask_lerp(mk, thL[i] / ctx->radius);
+  }
+  for (int j = 0; j < nazm; ++j) phiL[j] = j * RBC3D_TWO_PI / nazm;
+  // PolarPatch_Build: thG depends on th0 only; phiG = atan2(...) + phi0 with a
+  // wrap, so the atan2 part is stored and phi0 added in the kernel.
+  std::vector<double> thG((size_t)NQ * nlat), phiA((size_t)NQ * nlat);
+  for (int i0 = 0; i0 < nlat; ++i0) {
+    double st0 = std::sin(th[i0]), ct0 = std::cos(th[i0]);
+    for (int ir = 0; ir < nrad; ++ir) {
+      double sth = std::sin(thL[ir]), cth = std::cos(thL[ir]);
+      for (int ia = 0; ia < nazm; ++ia) {
+        double x0 = sth * std::cos(phiL[ia]), x1 = sth * std::sin(phiL[ia]), x2 = cth;
+        double y0 = ct0 * x0 + 0. * x1 + st0 * x2, y1 = 0. * x0 + 1. * x1 + 0. * x2, y2 = -st0 * x0 + 0. * x1 + ct0 * x2;
+        y2 = std::fmax(-1.0, std::fmin(1.0, y2));
+        size_t q = (size_t)i0 * NQ + ir + nrad * ia;
+        thG[q] = std::acos(y2);
+        phiA[q] = std::atan2(y1, y0);
+      }
+    }
+  }
+  CUDA_TRY(ctx->pw.upload(pw.data(), nrad, ctx->st));
+  CUDA_TRY(ctx->thG.upload(thG.data(), thG.size(), ctx->st));
+  CUDA_TRY(ctx->phiA.upload(phiA.data(), phiA.size(), ctx->st));
+  std::vector<double> x0(16), w0(16);
+  host_gauleg(0., ctx->radius, 16, x0.data(), w0.data());
+  CUDA_TRY(ctx->rd_x0.upload(x0.data(), 16, ctx->st));
+  CUDA_TRY(ctx->rd_w0.upload(w0.data(), 16, ctx->st));
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  return RBC3D_OK;
+}
+
+rbc3d_status rbc3d_set_cells(rbc3d_ctx* ctx, int ncell, const int* celltype, const double* x, const double* a3,
+                             const double* detJ, const double* area, const double* meshSize, const double* spl_x,
+                             const double* spl_a3, const double* spl_detJ) {
+  if (!ctx || ncell < 0 || (ncell > 0 && (!celltype || !x || !a3 || !detJ || !area || !meshSize || !spl_x ||
+                                         !spl_a3 || !spl_detJ)))
+    return ctx_fail(ctx, RBC3D_ERR_ARG, "set_cells: bad arguments");
+  if (ctx->h_th.empty()) return ctx_fail(ctx, RBC3D_ERR_STATE, "cell grid not set");
+  for (int c = 0; c < ncell; ++c)
+    if (celltype[c] < 0 || celltype[c] >= ctx->prm.ncelltypes) return ctx_fail(ctx, RBC3D_ERR_ARG, "bad celltype");
+  const int nv = ctx->nlat * ctx->nlon;
+  ctx->ncell = ncell;
+  ctx->npt = ncell * nv;
+  ctx->has_f = ctx->has_g = false;
+  ctx->src_density = false;
+  if (ncell == 0) return RBC3D_OK;
+  size_t N = ctx->npt;
+  ctx->h_celltype.assign(celltype, celltype + ncell);
+  CUDA_TRY(ctx->celltype.upload(celltype, ncell, ctx->st));
+  CUDA_TRY(ctx->x.upload(x, 3 * N, ctx->st)); CUDA_TRY(ctx->a3.upload(a3, 3 * N, ctx->st));
+  CUDA_TRY(ctx->detJ.upload(detJ, N, ctx->st));
+  CUDA_TRY(ctx->area.upload(area, ncell, ctx->st)); CUDA_TRY(ctx->meshSize.upload(meshSize, ncell, ctx->st));
+  CUDA_TRY(ctx->f.alloc(3 * N)); CUDA_TRY(ctx->g.alloc(3 * N)); CUDA_TRY(ctx->sf.alloc(3 * N)); CUDA_TRY(ctx->sg.alloc(3 * N));
+  CUDA_TRY(cudaMemsetAsync(ctx->sg.p, 0, sizeof(double) * 3 * N, ctx->st));
+  CUDA_TRY(cudaMemsetAsync(ctx->g.p, 0, sizeof(double) * 3 * N, ctx->st));
+  CUDA_TRY(ctx->spl.alloc((size_t)ncell * SPL_NSET * ctx->m * ctx->nlon * SPL_NODE));
+  rbc3d_status s;
+  if ((s = upload_splines(ctx, spl_x, 3, SPL_X))) return s;
+  if ((s = upload_splines(ctx, spl_a3, 3, SPL_A3))) return s;
+  if ((s = upload_splines(ctx, spl_detJ, 1, SPL_DJ))) return s;
+  if ((s = build_source_list(ctx))) return s;
+  // tlist_rbc (TargetList_Update, ModTargetList.F90:95-131)
+  TargetSet& t = ctx->tl[RBC3D_TLIST_RBC];
+  t.n = ctx->npt;
+  t.sorted = false;
+  DBuf<double> Ac;
+  CUDA_TRY(Ac.upload(ctx->Acoef, RBC3D_MAX_CELLTYPES, ctx->st));
+  CUDA_TRY(t.x.alloc(3 * N)); CUDA_TRY(t.Acoef.alloc(N)); CUDA_TRY(t.meta.alloc(N));
+  CUDA_TRY(cudaMemcpyAsync(t.x.p, ctx->x.p, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, ctx->st));
+  k_fill_acoef<<<nblk(N, 256), 256, 0, ctx->st>>>(t.n, nv, ctx->celltype.p, Ac.p, t.Acoef.p);
+  k_fill_meta<<<nblk(N, 256), 256, 0, ctx->st>>>(t.n, nv, ctx->nlat, t.meta.p);
+  CUDA_TRY(cudaGetLastError());
+  int want = 12 * std::max(ctx->npt, 1024);
+  if (ctx->items_cap < want) { ctx->items_cap = want; CUDA_TRY(ctx->items.alloc(want)); }
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  return RBC3D_OK;
+}
+
+rbc3d_status rbc3d_set_cell_density(rbc3d_ctx* ctx, const double* f, const double* g, const double* spl_F,
+                                    const double* spl_G) {
+  if (!ctx) return RBC3D_ERR_ARG;
+  if (ctx->npt == 0) return RBC3D_OK;
+  if ((f && !spl_F) || (g && !spl_G)) return ctx_fail(ctx, RBC3D_ERR_ARG, "density without spline table");
+  size_t N = ctx->npt;
+  rbc3d_status s;
+  if (f) {
+    CUDA_TRY(ctx->f.upload(f, 3 * N, ctx->st));
+    if ((s = upload_splines(ctx, spl_F, 3, SPL_F))) return s;
+    ctx->has_f = true;
+  }
+  if (g) {
+    CUDA_TRY(ctx->g.upload(g, 3 * N, ctx->st));
+    if ((s = upload_splines(ctx, spl_G, 3, SPL_G))) return s;
+    ctx->has_g = true;
+  }
+  return build_source_density(ctx);
+}
+
+rbc3d_status rbc3d_set_walls(rbc3d_ctx* ctx, int nvert, int nele, const double* x, const int* e2v, const int* glb) {
+  if (!ctx || nvert < 0 || nele < 0 || (nvert > 0 && (!x || !e2v || !glb)))
+    return ctx_fail(ctx, RBC3D_ERR_ARG, "set_walls: bad arguments");
+  WallState& W = ctx->wall;
+  W.nvert = nvert; W.nele = nele;
+  W.hx.assign(x, x + 3 * (size_t)nvert);
+  W.he2v.resize(3 * (size_t)nele);
+  for (size_t i = 0; i < W.he2v.size(); ++i) {
+    W.he2v[i] = e2v[i] - 1;
+    if (W.he2v[i] < 0 || W.he2v[i] >= nvert) return ctx_fail(ctx, RBC3D_ERR_ARG, "e2v out of range");
+  }
+  W.hglb.resize(nvert);
+  W.ndof = 0;
+  for (int i = 0; i < nvert; ++i) {
+    W.hglb[i] = glb[i] - 1;
+    if (W.hglb[i] < 0) return ctx_fail(ctx, RBC3D_ERR_ARG, "indxVertGlb out of range");
+    W.ndof = std::max(W.ndof, 3 * glb[i]);
+  }
+  W.hf.assign(3 * (size_t)nvert, 0.);
+  W.prepared = false;
+  rbc3d_status s = wall_setup(ctx);
+  if (s) return s;
+  // tlist_wall (TargetList_Update walls: Acoef = 2, ModTargetList.F90:119-127)
+  TargetSet& t = ctx->tl[RBC3D_TLIST_WALL];
+  t.n = nvert;
+  t.sorted = false;
+  CUDA_TRY(t.x.upload(x, 3 * (size_t)nvert, ctx->st));
+  CUDA_TRY(t.Acoef.alloc(nvert)); CUDA_TRY(t.meta.alloc(nvert));
+  if (nvert) k_fill_const<<<nblk(nvert, 256), 256, 0, ctx->st>>>(nvert, make_int4(-1000, -1, -1, 0), 2.0, t.meta.p, t.Acoef.p);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  return RBC3D_OK;
+}
+
+rbc3d_status rbc3d_set_wall_density(rbc3d_ctx* ctx, const double* f) {
+  if (!ctx || (!f && ctx->wall.nvert)) return RBC3D_ERR_ARG;
+  WallState& W = ctx->wall;
+  W.hf.assign(f, f + 3 * (size_t)W.nvert);
+  CUDA_TRY(W.f.upload(f, 3 * (size_t)W.nvert, ctx->st));
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  return RBC3D_OK;
+}
+rbc3d_status rbc3d_get_wall_density(rbc3d_ctx* ctx, double* f) {
+  if (!ctx || (!f && ctx->wall.nvert)) return RBC3D_ERR_ARG;
+  WallState& W = ctx->wall;
+  if (W.nvert) {
+    CUDA_TRY(cudaMemcpyAsync(f, W.f.p, sizeof(double) * 3 * W.nvert, cudaMemcpyDeviceToHost, ctx->st));
+    CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  }
+  return RBC3D_OK;
+}
+
+rbc3d_status rbc3d_set_raw_targets(rbc3d_ctx* ctx, int n, const double* x) {
+  if (!ctx || n < 0 || (n > 0 && !x)) return RBC3D_ERR_ARG;
+  TargetSet& t = ctx->tl[RBC3D_TLIST_RAW];
+  t.n = n;
+  t.sorted = false;
+  if (n == 0) return RBC3D_OK;
+  CUDA_TRY(t.x.upload(x, 3 * (size_t)n, ctx->st));
+  CUDA_TRY(t.Acoef.alloc(n)); CUDA_TRY(t.meta.alloc(n));
+  k_fill_const<<<nblk(n, 256), 256, 0, ctx->st>>>(n, make_int4(-1, -1, -1, 0), 2.0, t.meta.p, t.Acoef.p);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  return RBC3D_OK;
+}
+
+int rbc3d_num_targets(const rbc3d_ctx* ctx, int which) {
+  if (!ctx || which < 0 || which > 2) return -1;
+  return ctx->tl[which].n;
+}
+
+rbc3d_status rbc3d_add_int_on_rbcs(rbc3d_ctx* ctx, int which, double c1, double c2, int prec, double* v) {
+  TargetSet* t = ctx ? tset(ctx, which) : nullptr;
+  if (!t || !v || (prec != RBC3D_FP64 && prec != RBC3D_FP32C)) return ctx_fail(ctx, RBC3D_ERR_ARG, "add_int_on_rbcs");
+  rbc3d_status s;
+  if ((s = begin(ctx, *t))) return s;
+  if ((s = rbcs_dev(ctx, which, c1, c2, prec, RBC3D_TERM_REAL | RBC3D_TERM_CORR | RBC3D_TERM_LINEAR))) return s;
+  return finish_add(ctx, *t, v);
+}
+
+rbc3d_status rbc3d_add_int_on_walls(rbc3d_ctx* ctx, int which, double c1, int prec, double* v) {
+  TargetSet* t = ctx ? tset(ctx, which) : nullptr;
+  if (!t || !v) return ctx_fail(ctx, RBC3D_ERR_ARG, "add_int_on_walls");
+  rbc3d_status s;
+  if ((s = begin(ctx, *t))) return s;
+  if (which == RBC3D_TLIST_WALL) s = run_wall_self(ctx, c1);
+  else s = run_wall_quad(ctx, which, c1, prec);
+  if (s) return s;
+  return finish_add(ctx, *t, v);
+}
+
+rbc3d_status rbc3d_prepare_sing_int_on_wall(rbc3d_ctx* ctx) {
+  if (!ctx) return RBC3D_ERR_ARG;
+  return wall_prepare_self(ctx);
+}
+
+rbc3d_status rbc3d_pme_distrib_source(rbc3d_ctx* ctx, double c1, double c2, int cells, int walls, int prec) {
+  if (!ctx || (prec != RBC3D_FP64 && prec != RBC3D_FP32C)) return RBC3D_ERR_ARG;
+  return pme_spread(ctx, c1, c2, cells, walls, prec);
+}
+rbc3d_status rbc3d_pme_transform(rbc3d_ctx* ctx) {
+  if (!ctx) return RBC3D_ERR_ARG;
+  return pme_transform(ctx);
+}
+rbc3d_status rbc3d_pme_add_interp_vel(rbc3d_ctx* ctx, int which, double* v) {
+  TargetSet* t = ctx ? tset(ctx, which) : nullptr;
+  if (!t || !v) return ctx_fail(ctx, RBC3D_ERR_ARG, "pme_add_interp_vel");
+  rbc3d_status s;
+  if ((s = begin(ctx, *t))) return s;
+  if ((s = pme_gather(ctx, which))) return s;
+  return finish_add(ctx, *t, v);
+}
+
+rbc3d_status rbc3d_matvec(rbc3d_ctx* ctx, int which, double c1, double c2, unsigned terms, int prec, double* v) {
+  TargetSet* t = ctx ? tset(ctx, which) : nullptr;
+  if (!t || !v || (prec != RBC3D_FP64 && prec != RBC3D_FP32C)) return ctx_fail(ctx, RBC3D_ERR_ARG, "matvec");
+  rbc3d_status s = matvec_dev(ctx, which, c1, c2, terms, prec);
+  if (s) return s;
+  return finish_add(ctx, *t, v);
+}
+
+// CalcVelocityField, ModPostProcess.F90:29-63 (overwrites v)
+rbc3d_status rbc3d_calc_velocity_field(rbc3d_ctx* ctx, int which, int prec, double* v) {
+  TargetSet* t = ctx ? tset(ctx, which) : nullptr;
+  if (!t || !v) return ctx_fail(ctx, RBC3D_ERR_ARG, "calc_velocity_field");
+  double c = 1.0 / (4. * RBC3D_PI);
+  rbc3d_status s = matvec_dev(ctx, which, c, c, RBC3D_TERM_ALL, prec);
+  if (s) return s;
+  std::fill(v, v + 3 * (size_t)t->n, 0.);
+  if ((s = finish_add(ctx, *t, v))) return s;
+  for (int k = 0; k < 3; ++k)
+    for (int i = 0; i < t->n; ++i) v[i + (size_t)k * t->n] += ctx->prm.vBkg[k];
+  return RBC3D_OK;
+}
+
+rbc3d_status rbc3d_compute_wall_residual_vel(rbc3d_ctx* ctx, int prec, double* v) {
+  if (!ctx || !v) return RBC3D_ERR_ARG;
+  rbc3d_status s = wall_residual_dev(ctx, prec);
+  if (s) return s;
+  TargetSet& t = ctx->tl[RBC3D_TLIST_WALL];
+  std::fill(v, v + 3 * (size_t)t.n, 0.);
+  return finish_add(ctx, t, v);
+}
+
+rbc3d_status rbc3d_wall_matmult(rbc3d_ctx* ctx, int prec, const double* u, double* y) {
+  if (!ctx || !u || !y) return RBC3D_ERR_ARG;
+  int n = ctx->wall.ndof;
+  DBuf<double> du, dy;
+  CUDA_TRY(du.upload(u, n, ctx->st));
+  CUDA_TRY(dy.alloc(n));
+  rbc3d_status s = wall_matmult_dev(ctx, prec, du.p, dy.p);
+  if (s) return s;
+  CUDA_TRY(cudaMemcpyAsync(y, dy.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->st));
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  return RBC3D_OK;
+}
+
+rbc3d_status rbc3d_no_slip_wall(rbc3d_ctx* ctx, const rbc3d_solve_opts* opt, const double* guess,
+                                rbc3d_solve_stats* st) {
+  if (!ctx || !opt) return RBC3D_ERR_ARG;
+  return wall_solve(ctx, opt, guess, st);
+}
+
+rbc3d_status rbc3d_get_counts(const rbc3d_ctx* ctx, rbc3d_counts* out) {
+  if (!ctx || !out) return RBC3D_ERR_ARG;
+  *out = ctx->counts;
+  return RBC3D_OK;
+}
+
+}  // extern "C"

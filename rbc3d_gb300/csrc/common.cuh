@@ -1,0 +1,158 @@
+// common.cuh -- device helpers shared by the kernels of the GB300 Ewald matvec.
+#pragma once
+#include <cuda_runtime.h>
+#include <math_constants.h>
+#include <stdint.h>
+
+#define RBC3D_PI 3.14159265358979323846
+#define RBC3D_TWO_PI (2.0 * RBC3D_PI)
+#define RBC3D_I_2PI (1.0 / RBC3D_TWO_PI)
+#define EWALD_NTAB 8192  // Ntable, ModEwaldFunc.F90:9
+#define MASK_NTAB 8192   // MaskFunc table size, ModBasicMath.F90:356
+
+// Number of doubles per spline node per variable set: 4 kinds (u, u1, u2,
+// u12) x 3 variables.  Sets: x, a3, FdetJ, GdetJ, detJ (detJ uses var 0).
+#define SPL_NODE 12
+enum { SPL_X = 0, SPL_A3 = 1, SPL_F = 2, SPL_G = 3, SPL_DJ = 4, SPL_NSET = 5 };
+
+// Device view of the Ewald / mask tables.
+struct Tables {
+  // FP64 tables exactly as ModEwaldFunc / ModBasicMath build them (N+1 entries)
+  const double* sl_c1;
+  const double* sl_c2;
+  const double* dl_c1;
+  const double* mask;
+  // FP32 lerp tables: {v_i, v_{i+1}-v_i} pairs
+  const float4* sl32;  // {c1, dc1, c2, dc2}
+  const float2* dl32;  // {dl, ddl}
+  const float2* mask32;
+  double rc, r_eps, ntab_over_rc;
+  float rc_f, r_eps_f, ntab_over_rc_f;
+};
+
+// ---------------------------------------------------------------------------
+// EwaldCoeff_SL / EwaldCoeff_DL (ModEwaldFunc.F90:86-180), FP64.
+__device__ __forceinline__ void ewald_sl64(const Tables& T, double r, double& A, double& B) {
+  if (r < T.r_eps) { A = 0.; B = 0.; return; }
+  double s = EWALD_NTAB * r / T.rc;
+  int i = (int)floor(s);
+  if (i >= EWALD_NTAB) { A = 0.; B = 0.; return; }
+  double c1 = __ldg(T.sl_c1 + i) * (i + 1 - s) + __ldg(T.sl_c1 + i + 1) * (s - i);
+  double c2 = __ldg(T.sl_c2 + i) * (i + 1 - s) + __ldg(T.sl_c2 + i + 1) * (s - i);
+  double ir = 1. / r, ir2 = ir * ir;
+  A = c1 * ir * ir2 + c2 * ir2;
+  B = c1 * ir - c2;
+}
+__device__ __forceinline__ double ewald_dl64(const Tables& T, double r) {
+  if (r < T.r_eps) return 0.;
+  double s = EWALD_NTAB * r / T.rc;
+  int i = (int)floor(s);
+  if (i >= EWALD_NTAB) return 0.;
+  double c1 = __ldg(T.dl_c1 + i) * (i + 1 - s) + __ldg(T.dl_c1 + i + 1) * (s - i);
+  double r2 = r * r;
+  return c1 / (r2 * r2 * r);
+}
+// MaskFunc (ModBasicMath.F90:351-379), FP64
+__device__ __forceinline__ double mask64(const Tables& T, double x) {
+  double s = fabs(x) * MASK_NTAB;
+  int i = (int)floor(s);
+  if (i >= MASK_NTAB) return 0.;
+  return __ldg(T.mask + i) * (i + 1 - s) + __ldg(T.mask + i + 1) * (s - i);
+}
+// DistOnSphere (ModPolarPatch.F90:249-257)
+__device__ __forceinline__ double dist_on_sphere(double th0, double phi0, double th1, double phi1) {
+  double d = cos(th0 - th1) - sin(th0) * sin(th1) * (1. - cos(phi0 - phi1));
+  d = fmin(1., fmax(-1., d));
+  return acos(d);
+}
+
+// ---------------------------------------------------------------------------
+// Bicubic Hermite interpolation on the doubled-sphere grid (Spline_Interp,
+// ModSpline.F90:150-191).  Node layout: spl[node*SPL_NODE + kind*3 + var].
+struct SplW {
+  int n11, n12, n21, n22;  // node ids (i1,j1) (i1,j2) (i2,j1) (i2,j2)
+  double cx[4], cy[4];
+};
+__device__ __forceinline__ int imod(int a, int b) { int r = a % b; return r < 0 ? r + b : r; }
+
+__device__ __forceinline__ void spline_weights(double x, double y, int m, int n, SplW& W) {
+  const double hx = RBC3D_TWO_PI / m, hy = RBC3D_TWO_PI / n;
+  const double ihx = 1. / hx, ihy = 1. / hy;
+  int i1 = (int)floor(x * ihx), j1 = (int)floor(y * ihy);
+  double s = x * ihx - i1, t = y * ihy - j1;
+  i1 = imod(i1, m); j1 = imod(j1, n);
+  int i2 = imod(i1 + 1, m), j2 = imod(j1 + 1, n);
+  W.cx[0] = 1 + s * s * (-3. + 2. * s); W.cx[1] = s * s * (3. - 2. * s);
+  W.cx[2] = hx * s * (1. + s * (-2. + s)); W.cx[3] = hx * s * s * (-1. + s);
+  W.cy[0] = 1 + t * t * (-3. + 2. * t); W.cy[1] = t * t * (3. - 2. * t);
+  W.cy[2] = hy * t * (1. + t * (-2. + t)); W.cy[3] = hy * t * t * (-1. + t);
+  W.n11 = i1 + m * j1; W.n12 = i1 + m * j2; W.n21 = i2 + m * j1; W.n22 = i2 + m * j2;
+}
+// Interpolate nvar (<=3) variables of one spline set (pointer to node 0).
+__device__ __forceinline__ void spline_eval(const double* __restrict__ spl, const SplW& W, int nvar, double* f) {
+  const double* a = spl + (size_t)W.n11 * SPL_NODE;
+  const double* b = spl + (size_t)W.n12 * SPL_NODE;
+  const double* c = spl + (size_t)W.n21 * SPL_NODE;
+  const double* d = spl + (size_t)W.n22 * SPL_NODE;
+#pragma unroll
+  for (int l = 0; l < 3; ++l) {
+    if (l >= nvar) break;
+    // rows of u(4,4) in Spline_Interp: (u, u2 @ i1), (u, u2 @ i2), (u1, u12 @ i1), (u1, u12 @ i2)
+    double r0 = __ldg(a + l) * W.cy[0] + __ldg(b + l) * W.cy[1] + __ldg(a + 6 + l) * W.cy[2] + __ldg(b + 6 + l) * W.cy[3];
+    double r1 = __ldg(c + l) * W.cy[0] + __ldg(d + l) * W.cy[1] + __ldg(c + 6 + l) * W.cy[2] + __ldg(d + 6 + l) * W.cy[3];
+    double r2 = __ldg(a + 3 + l) * W.cy[0] + __ldg(b + 3 + l) * W.cy[1] + __ldg(a + 9 + l) * W.cy[2] + __ldg(b + 9 + l) * W.cy[3];
+    double r3 = __ldg(c + 3 + l) * W.cy[0] + __ldg(d + 3 + l) * W.cy[1] + __ldg(c + 9 + l) * W.cy[2] + __ldg(d + 9 + l) * W.cy[3];
+    f[l] = W.cx[0] * r0 + W.cx[1] * r1 + W.cx[2] * r2 + W.cx[3] * r3;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Warp reductions
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_sumf(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Compensated (Kahan) accumulation in FP32.  Uses round-to-nearest intrinsics
+// so the compiler can neither contract nor reassociate the error terms.
+struct Kahan3 {
+  float s[3], c[3];
+  __device__ __forceinline__ void zero() { for (int k = 0; k < 3; ++k) { s[k] = 0.f; c[k] = 0.f; } }
+  __device__ __forceinline__ void add(int k, float x) {
+    float y = __fsub_rn(x, c[k]);
+    float t = __fadd_rn(s[k], y);
+    c[k] = __fsub_rn(__fsub_rn(t, s[k]), y);
+    s[k] = t;
+  }
+};
+
+// B-spline weights (BsplineFunc, ModBasicMath.F90:392-417).  w[0..P-1] maps
+// to mesh indices imin..imin+P-1.
+template <typename R>
+__device__ __forceinline__ void bspline_w(R xc, int P, int& imin, R* w) {
+  R u[8];
+  imin = (int)floor(xc) - (P - 1);
+  u[0] = (R)imin - (xc - (R)P);
+#pragma unroll
+  for (int j = 1; j < 8; ++j) u[j] = u[j - 1] + (R)1;
+  w[0] = (R)1;
+#pragma unroll
+  for (int j = 1; j < 8; ++j) w[j] = (R)0;
+  for (int pp = 2; pp <= P; ++pp) {
+    R inv = (R)1 / (R)(pp - 1);
+    for (int j = pp; j >= 2; --j) w[j - 1] = u[j - 1] * inv * w[j - 1] + ((R)pp - u[j - 1]) * inv * w[j - 2];
+    w[0] = u[0] * inv * w[0];
+  }
+}
+
+#define CUDA_TRY(x)                                                   \
+  do {                                                                \
+    cudaError_t e__ = (x);                                            \
+    if (e__ != cudaSuccess) return ctx_fail_cuda(ctx, e__, #x);        \
+  } while (0)

@@ -1,0 +1,478 @@
+// corr.cu -- FP64 singular and near-singular polar-patch corrections on the
+// GPU: RBC_SingInt (ModRbcSingInt.F90:29-90) and RBC_NearSingInt with its
+// Subtract / ReAdd halves (ModRbcSingInt.F90:103-310), including
+// Spline_FindProjection (ModSpline.F90:203-269) and QuadFit_2D (normal
+// equations + Cholesky, ModBasicMath.F90:234-284).
+//
+// Mapping: one warp per target for the self patch (nrad*nazm quadrature points
+// spread over the lanes), one warp per (target, neighbour cell) work item for
+// the near-singular correction.  In the projection the 17 fit points sit on
+// lanes 0..16 and the 27 normal-equation sums are butterfly warp reductions,
+// which leave bit-identical values on every lane so the subsequent 6x6 solve
+// and every branch stay warp-uniform.  In ReAdd lane = azimuth (nazm = 32).
+#include "ctx.hpp"
+
+namespace {
+
+struct CorrArgs {
+  int nt;
+  const double* tx;
+  const double* tA;
+  const int4* tmeta;
+  double* v;
+  int ncell, nlat, nlon, m;
+  const double* th;
+  const double* phi;
+  const double* w;
+  const double* x;
+  const double* a3;
+  const double* detJ;
+  const double* f;
+  const double* g;
+  const double* area;
+  const double* meshSize;
+  const int* celltype;
+  const double* Bc;
+  const double* spl;  // ncell * SPL_NSET * m*nlon * SPL_NODE
+  int npt;
+  // patch
+  int nrad, nazm;
+  double radius;
+  const double* pw;
+  const double* thG;
+  const double* phiA;
+  const double* rd_s;
+  const double* rd_w;
+  const double* rd_x0;
+  const double* rd_w0;
+  double c1, c2;
+  double L[3], iL[3];
+  Tables T;
+  const int4* items;
+  const unsigned long long* nitems;
+  int cap;
+  unsigned long long* cnt;
+};
+
+__device__ __forceinline__ const double* set_ptr(const CorrArgs& a, int cell, int set) {
+  return a.spl + ((size_t)cell * SPL_NSET + set) * (size_t)a.m * a.nlon * SPL_NODE;
+}
+
+// RBC_SingInt: one warp per cell target
+__global__ void __launch_bounds__(256) k_self(CorrArgs a) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (warp >= a.nt) return;
+  int4 mt = a.tmeta[warp];
+  int cell = mt.x - 1;
+  if (cell < 0 || cell >= a.ncell || mt.y < 0) return;
+  const int ilat0 = mt.y, ilon0 = mt.z;
+  const double c1 = a.c1, c2m = a.c2 * a.Bc[a.celltype[cell]];
+  const double* sx = set_ptr(a, cell, SPL_X);
+  const double* sF = set_ptr(a, cell, SPL_F);
+  const double* sG = set_ptr(a, cell, SPL_G);
+  const double* sA = set_ptr(a, cell, SPL_A3);
+  SplW W;
+  double xi[3];
+  spline_weights(a.th[ilat0], a.phi[ilon0], a.m, a.nlon, W);
+  spline_eval(sx, W, 3, xi);
+  const int NQ = a.nrad * a.nazm;
+  const double phi0 = a.phi[ilon0];
+  double dv[3] = {0, 0, 0};
+  for (int q = lane; q < NQ; q += 32) {
+    int irad = q % a.nrad;
+    double th_j = a.thG[(size_t)ilat0 * NQ + q];
+    double p = a.phiA[(size_t)ilat0 * NQ + q] + phi0;  // PolarPatch_Build: atan2(...) + phi0
+    double phi_j = p - floor(p * RBC3D_I_2PI) * RBC3D_TWO_PI;
+    spline_weights(th_j, phi_j, a.m, a.nlon, W);
+    double xj[3], xx[3];
+    spline_eval(sx, W, 3, xj);
+    for (int k = 0; k < 3; ++k) xx[k] = xj[k] - xi[k];
+    double rr = sqrt(xx[0] * xx[0] + xx[1] * xx[1] + xx[2] * xx[2]);
+    if (rr >= a.T.rc) continue;
+    double wq = a.pw[irad];
+    if (c1 != 0.) {
+      double fj[3], EA, EB;
+      spline_eval(sF, W, 3, fj);
+      for (int k = 0; k < 3; ++k) fj[k] = wq * fj[k];
+      ewald_sl64(a.T, rr, EA, EB);
+      double d = xx[0] * fj[0] + xx[1] * fj[1] + xx[2] * fj[2];
+      for (int k = 0; k < 3; ++k) dv[k] += c1 * (EA * xx[k] * d + EB * fj[k]);
+    }
+    if (c2m != 0.) {
+      double gj[3], aj[3];
+      spline_eval(sG, W, 3, gj);
+      for (int k = 0; k < 3; ++k) gj[k] = wq * gj[k];
+      spline_eval(sA, W, 3, aj);
+      double EA = ewald_dl64(a.T, rr);
+      double dg = xx[0] * gj[0] + xx[1] * gj[1] + xx[2] * gj[2];
+      double da = xx[0] * aj[0] + xx[1] * aj[1] + xx[2] * aj[2];
+      for (int k = 0; k < 3; ++k) dv[k] += c2m * (EA * xx[k] * dg * da);
+    }
+  }
+  for (int k = 0; k < 3; ++k) dv[k] = warp_sum(dv[k]);
+  if (lane == 0) {
+    double iA = 1.0 / a.tA[warp];
+    for (int k = 0; k < 3; ++k) a.v[warp + (size_t)k * a.nt] += dv[k] * iA;
+  }
+}
+
+// One point of PolarPatch_Build (ModPolarPatch.F90:99-148)
+__device__ __forceinline__ void patch_point(double st0, double ct0, double phi0, double sth, double cth, double cph,
+                                            double sph, double& thG, double& phiG) {
+  double x0 = sth * cph, x1 = sth * sph, x2 = cth;
+  double y0 = ct0 * x0 + st0 * x2;
+  double y1 = x1;
+  double y2 = -st0 * x0 + ct0 * x2;
+  y2 = fmax(-1.0, fmin(1.0, y2));
+  thG = acos(y2);
+  double p = atan2(y1, y0) + phi0;
+  phiG = p - floor(p * RBC3D_I_2PI) * RBC3D_TWO_PI;
+}
+
+// PolarPatch_Map (ModPolarPatch.F90:218-244)
+__device__ __forceinline__ void patch_map(double th0, double phi0, double dth, double dphi, double& th, double& phi) {
+  double st0 = sin(th0), ct0 = cos(th0), sp0 = sin(phi0), cp0 = cos(phi0);
+  double s1[3] = {ct0 * cp0, ct0 * sp0, -st0};
+  double s2[3] = {-sp0, cp0, 0.};
+  double x0[3] = {st0 * cp0, st0 * sp0, ct0};
+  double x[3] = {sin(dth) * cos(dphi), sin(dth) * sin(dphi), cos(dth)};
+  double y[3];
+  for (int c = 0; c < 3; ++c) y[c] = x[0] * s1[c] + x[1] * s2[c] + x[2] * x0[c];
+  double nrm = sqrt(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]);
+  for (int c = 0; c < 3; ++c) y[c] /= nrm;
+  y[2] = fmax(-1., fmin(1., y[2]));
+  th = acos(y[2]);
+  phi = atan2(y[1], y[0]);
+  if (phi < 0) phi += RBC3D_TWO_PI;
+}
+
+// dposv on the 6x6 normal equations (upper Cholesky); leaves b unchanged when
+// the matrix is not positive definite, as LAPACK does for info > 0.
+__device__ void chol6(const double* A /*21 packed upper, row-major a<=b*/, double* b) {
+  double U[6][6];
+  double M[6][6];
+  int p = 0;
+  for (int i = 0; i < 6; ++i)
+    for (int j = i; j < 6; ++j) { M[i][j] = A[p]; M[j][i] = A[p]; ++p; }
+  for (int j = 0; j < 6; ++j) {
+    double s = M[j][j];
+    for (int k = 0; k < j; ++k) s -= U[k][j] * U[k][j];
+    if (!(s > 0)) return;
+    U[j][j] = sqrt(s);
+    for (int i = j + 1; i < 6; ++i) {
+      double t = M[j][i];
+      for (int k = 0; k < j; ++k) t -= U[k][j] * U[k][i];
+      U[j][i] = t / U[j][j];
+    }
+  }
+  double y[6];
+  for (int i = 0; i < 6; ++i) {
+    double t = b[i];
+    for (int k = 0; k < i; ++k) t -= U[k][i] * y[k];
+    y[i] = t / U[i][i];
+  }
+  for (int i = 5; i >= 0; --i) {
+    double t = y[i];
+    for (int k = i + 1; k < 6; ++k) t -= U[i][k] * b[k];
+    b[i] = t / U[i][i];
+  }
+}
+
+// Spline_FindProjection, warp-cooperative.  All lanes return the same result.
+__device__ void find_projection(const double* sx, int m, int n, const double* xt, double& th0, double& phi0,
+                                double* x0) {
+  const int lane = threadIdx.x & 31;
+  SplW W;
+  spline_weights(th0, phi0, m, n, W);
+  spline_eval(sx, W, 3, x0);
+  double h = fmax(RBC3D_TWO_PI / m, RBC3D_TWO_PI / n);
+  for (int iter = 0; iter < 3; ++iter) {
+    double px = 0, py = 0, d2 = 0;
+    bool on = lane <= 16;
+    if (lane < 16) {
+      int ith = lane % 2, iphi = lane / 2;
+      double thL = (ith + 1) * h / 2;
+      double phL = iphi * RBC3D_TWO_PI / 8;
+      double thP, phP;
+      patch_point(sin(th0), cos(th0), phi0, sin(thL), cos(thL), cos(phL), sin(phL), thP, phP);
+      px = thL * cos(phL);
+      py = thL * sin(phL);
+      double xx[3];
+      spline_weights(thP, phP, m, n, W);
+      spline_eval(sx, W, 3, xx);
+      for (int k = 0; k < 3; ++k) xx[k] -= xt[k];
+      d2 = xx[0] * xx[0] + xx[1] * xx[1] + xx[2] * xx[2];
+    } else if (lane == 16) {
+      double xx[3];
+      spline_weights(th0, phi0, m, n, W);
+      spline_eval(sx, W, 3, xx);
+      for (int k = 0; k < 3; ++k) xx[k] -= xt[k];
+      d2 = xx[0] * xx[0] + xx[1] * xx[1] + xx[2] * xx[2];
+    }
+    double d2c = __shfl_sync(0xffffffffu, d2, 16);
+    double u[6] = {on ? 1. : 0., px, py, px * px, px * py, py * py};
+    double A[21], b[6];
+    int p = 0;
+    for (int i = 0; i < 6; ++i)
+      for (int j = i; j < 6; ++j) A[p++] = warp_sum(u[i] * u[j]);
+    for (int i = 0; i < 6; ++i) b[i] = warp_sum(u[i] * d2);
+    chol6(A, b);
+    // Min_Quad_2D
+    double l11 = 2. * b[3], l12 = b[4], l22 = 2. * b[5];
+    double det = l11 * l22 - l12 * l12;
+    double xm0 = 0., xm1 = 0.;
+    if (det > 0) {
+      double idet = 1. / det;
+      xm0 = idet * (l22 * (-b[1]) - l12 * (-b[2]));
+      xm1 = idet * (-l12 * (-b[1]) + l11 * (-b[2]));
+    }
+    double thMinL = sqrt(xm0 * xm0 + xm1 * xm1), phiMinL = atan2(xm1, xm0);
+    double thMin, phiMin, xMin[3];
+    patch_map(th0, phi0, thMinL, phiMinL, thMin, phiMin);
+    spline_weights(thMin, phiMin, m, n, W);
+    spline_eval(sx, W, 3, xMin);
+    double e0 = xMin[0] - xt[0], e1 = xMin[1] - xt[1], e2 = xMin[2] - xt[2];
+    double d2Min = e0 * e0 + e1 * e1 + e2 * e2;
+    if (d2Min > d2c) break;
+    th0 = thMin; phi0 = phiMin;
+    for (int k = 0; k < 3; ++k) x0[k] = xMin[k];
+    h = 0.5 * h;
+  }
+}
+
+// RBC_NearSingInt_Subtract: lane = latitude row of PolarPatch_FindPoints
+__device__ void near_subtract(const CorrArgs& a, int cell, double c1, double c2, const double* xi, double th0,
+                              double phi0, double radPat, double* dv) {
+  const int lane = threadIdx.x & 31;
+  dv[0] = dv[1] = dv[2] = 0.;
+  const double eps = 1.e-10;
+  const double h_phi = RBC3D_TWO_PI / a.nlon, ih_phi = 1.0 / h_phi;
+  const double cosr0 = cos(radPat);
+  const size_t cb = (size_t)cell * a.nlat * a.nlon;
+  for (int i = lane; i < a.nlat; i += 32) {
+    double thi = a.th[i];
+    if (thi <= th0 - radPat || thi >= th0 + radPat) continue;
+    double dth = thi - th0;
+    double dphi = 1. - (cos(dth) - cosr0) / ((sin(thi) + eps) * (sin(th0) + eps));
+    dphi = fmax(-1., fmin(1., dphi));
+    dphi = acos(dphi);
+    int jmin, jmax;
+    if (dphi > RBC3D_PI - eps) { jmin = 1; jmax = a.nlon; }
+    else {
+      jmin = (int)ceil((phi0 - dphi - a.phi[0]) * ih_phi) + 1;
+      jmax = (int)floor((phi0 + dphi - a.phi[0]) * ih_phi) + 1;
+    }
+    for (int j = jmin; j <= jmax; ++j) {
+      int ilon = imod(j - 1, a.nlon);
+      size_t q = cb + (size_t)ilon * a.nlat + i;
+      double xx[3];
+      for (int k = 0; k < 3; ++k) xx[k] = a.x[q + (size_t)k * a.npt] - xi[k];
+      double rr = sqrt(xx[0] * xx[0] + xx[1] * xx[1] + xx[2] * xx[2]);
+      if (rr > a.T.rc) continue;
+      double dd = dist_on_sphere(th0, phi0, thi, a.phi[ilon]);
+      double mask = mask64(a.T, dd / radPat);
+      double ds1 = a.detJ[q], ds2 = a.w[i];
+      if (c1 != 0.) {
+        double fj[3], EA, EB;
+        for (int k = 0; k < 3; ++k) fj[k] = a.f[q + (size_t)k * a.npt] * ds1 * ds2;
+        ewald_sl64(a.T, rr, EA, EB);
+        double d = xx[0] * fj[0] + xx[1] * fj[1] + xx[2] * fj[2];
+        for (int k = 0; k < 3; ++k) dv[k] -= c1 * mask * (EA * xx[k] * d + EB * fj[k]);
+      }
+      if (c2 != 0.) {
+        double gj[3], aj[3];
+        for (int k = 0; k < 3; ++k) {
+          gj[k] = a.g[q + (size_t)k * a.npt] * ds1 * ds2;
+          aj[k] = a.a3[q + (size_t)k * a.npt];
+        }
+        double EA = ewald_dl64(a.T, rr);
+        double dg = xx[0] * gj[0] + xx[1] * gj[1] + xx[2] * gj[2];
+        double da = xx[0] * aj[0] + xx[1] * aj[1] + xx[2] * aj[2];
+        for (int k = 0; k < 3; ++k) dv[k] -= c2 * mask * (EA * xx[k] * dg * da);
+      }
+    }
+  }
+  for (int k = 0; k < 3; ++k) dv[k] = warp_sum(dv[k]);
+}
+
+// RBC_NearSingInt_ReAdd: nrad = 16, nazm = 32, lane = azimuth
+__device__ void near_readd(const CorrArgs& a, int cell, double c1, double c2, const double* xi, const double* x0,
+                           double th0, double phi0, double radPat, double* dv) {
+  const int lane = threadIdx.x & 31;
+  const int nrad = 16, nazm = 32;
+  double d = sqrt((xi[0] - x0[0]) * (xi[0] - x0[0]) + (xi[1] - x0[1]) * (xi[1] - x0[1]) +
+                  (xi[2] - x0[2]) * (xi[2] - x0[2]));
+  double sizePat = radPat * sqrt(a.area[cell] / (4 * RBC3D_PI));
+  // GauLeg_Sinh(0, radPat, 0, d*(radPat/sizePat), 16) (ModQuadRule.F90:223-263)
+  bool sinh_rule = d > 2.2250738585072014e-308;
+  double xm = 0.5 * radPat, xl = 0.5 * radPat, a0 = 0, b0 = 0, mu = 0, eta = 0;
+  if (sinh_rule) {
+    d = d * (radPat / sizePat);
+    a0 = (0. - xm) / xl;
+    b0 = d * xl;
+    double f1 = (1 + a0) / b0, f2 = (1 - a0) / b0;
+    double u1 = log(f1 + sqrt(1 + f1 * f1)), u2 = log(f2 + sqrt(1 + f2 * f2));
+    mu = 0.5 * (u1 + u2);
+    eta = 0.5 * (u1 - u2);
+  }
+  const double* sx = set_ptr(a, cell, SPL_X);
+  const double* sF = set_ptr(a, cell, SPL_F);
+  const double* sG = set_ptr(a, cell, SPL_G);
+  const double* sA = set_ptr(a, cell, SPL_A3);
+  const double st0 = sin(th0), ct0 = cos(th0);
+  const double phL = lane * RBC3D_TWO_PI / nazm;
+  const double cph = cos(phL), sph = sin(phL);
+  double acc[3] = {0, 0, 0};
+  for (int irad = 0; irad < nrad; ++irad) {
+    double thP, wt;
+    if (sinh_rule) {
+      double s = a.rd_s[irad];
+      thP = a0 + b0 * sinh(mu * s - eta);
+      wt = a.rd_w[irad] * b0 * mu * cosh(mu * s - eta);
+      wt = xl * wt;
+      thP = xm + xl * thP;
+    } else {
+      thP = a.rd_x0[irad];
+      wt = a.rd_w0[irad];
+    }
+    wt = wt * sin(thP) * (RBC3D_TWO_PI / nazm);
+    wt = wt * mask64(a.T, thP / radPat);
+    double thG, phG;
+    patch_point(st0, ct0, phi0, sin(thP), cos(thP), cph, sph, thG, phG);
+    SplW W;
+    spline_weights(thG, phG, a.m, a.nlon, W);
+    double xj[3], xx[3];
+    spline_eval(sx, W, 3, xj);
+    for (int k = 0; k < 3; ++k) xx[k] = xj[k] - xi[k];
+    double rr = sqrt(xx[0] * xx[0] + xx[1] * xx[1] + xx[2] * xx[2]);
+    if (rr > a.T.rc) continue;
+    if (c1 != 0.) {
+      double fj[3], EA, EB;
+      spline_eval(sF, W, 3, fj);
+      for (int k = 0; k < 3; ++k) fj[k] = wt * fj[k];
+      ewald_sl64(a.T, rr, EA, EB);
+      double dd = xx[0] * fj[0] + xx[1] * fj[1] + xx[2] * fj[2];
+      for (int k = 0; k < 3; ++k) acc[k] += c1 * (EA * xx[k] * dd + EB * fj[k]);
+    }
+    if (c2 != 0.) {
+      double aj[3], gj[3];
+      spline_eval(sA, W, 3, aj);
+      spline_eval(sG, W, 3, gj);
+      for (int k = 0; k < 3; ++k) gj[k] = wt * gj[k];
+      double EA = ewald_dl64(a.T, rr);
+      double dg = xx[0] * gj[0] + xx[1] * gj[1] + xx[2] * gj[2];
+      double da = xx[0] * aj[0] + xx[1] * aj[1] + xx[2] * aj[2];
+      for (int k = 0; k < 3; ++k) acc[k] += c2 * (EA * xx[k] * dg * da);
+    }
+  }
+  for (int k = 0; k < 3; ++k) dv[k] = warp_sum(acc[k]);
+}
+
+// RBC_NearSingInt over the work list (persistent warps)
+__global__ void __launch_bounds__(128) k_near(CorrArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int wpb = blockDim.x >> 5;
+  unsigned long long nitem = *a.nitems;
+  if (nitem > (unsigned long long)a.cap) nitem = a.cap;
+  for (long long it = (long long)blockIdx.x * wpb + (threadIdx.x >> 5); it < (long long)nitem;
+       it += (long long)gridDim.x * wpb) {
+    int4 item = a.items[it];
+    int t = item.x, cell = item.y - 1, ilat0 = item.z, ilon0 = item.w;
+    if (cell < 0 || cell >= a.ncell) continue;
+    double th0 = a.th[ilat0], phi0 = a.phi[ilon0];
+    size_t q0 = (size_t)cell * a.nlat * a.nlon + (size_t)ilon0 * a.nlat + ilat0;
+    double x0[3], xt[3];
+    for (int k = 0; k < 3; ++k) {
+      x0[k] = a.x[q0 + (size_t)k * a.npt];
+      double xx = a.tx[t + (size_t)k * a.nt] - x0[k];
+      xx = xx - round(xx * a.iL[k]) * a.L[k];
+      xt[k] = x0[k] + xx;
+    }
+    const double* sx = set_ptr(a, cell, SPL_X);
+    find_projection(sx, a.m, a.nlon, xt, th0, phi0, x0);
+    const double c1 = a.c1, c2 = a.c2 * a.Bc[a.celltype[cell]];
+    SplW W;
+    double a30[3];
+    spline_weights(th0, phi0, a.m, a.nlon, W);
+    spline_eval(set_ptr(a, cell, SPL_A3), W, 3, a30);
+    double dist = a30[0] * (xt[0] - x0[0]) + a30[1] * (xt[1] - x0[1]) + a30[2] * (xt[2] - x0[2]);
+    if (dist > 2 * a.meshSize[cell]) continue;
+    if (lane == 0) atomicAdd(a.cnt + 3, 1ull);
+    double sizePat = a.radius * sqrt(a.area[cell] / (4 * RBC3D_PI));
+    double dist1 = copysign(fabs(0.01 * sizePat), dist);
+    double dv[3], tmp[3];
+    near_subtract(a, cell, c1, c2, xt, th0, phi0, a.radius, dv);
+    if (fabs(dist) >= fabs(dist1)) {
+      near_readd(a, cell, c1, c2, xt, x0, th0, phi0, a.radius, tmp);
+      for (int k = 0; k < 3; ++k) dv[k] += tmp[k];
+    } else {
+      double xi1[3], dv1[3], dv0[3];
+      for (int k = 0; k < 3; ++k) xi1[k] = x0[k] + dist1 * a30[k];
+      near_readd(a, cell, c1, c2, xi1, x0, th0, phi0, a.radius, dv1);
+      near_readd(a, cell, c1, c2, x0, x0, th0, phi0, a.radius, dv0);
+      if (c2 != 0.) {
+        double dJ0[3], g0[3];
+        spline_eval(set_ptr(a, cell, SPL_DJ), W, 1, dJ0);
+        spline_eval(set_ptr(a, cell, SPL_G), W, 3, g0);
+        for (int k = 0; k < 3; ++k) g0[k] = g0[k] / dJ0[0];
+        for (int k = 0; k < 3; ++k) dv0[k] = (dist > 0) ? dv0[k] + c2 * 4 * RBC3D_PI * g0[k] : dv0[k] - c2 * 4 * RBC3D_PI * g0[k];
+      }
+      for (int k = 0; k < 3; ++k) dv[k] += dv0[k] + dist / dist1 * (dv1[k] - dv0[k]);
+    }
+    if (lane == 0) {
+      double iA = 1.0 / a.tA[t];
+      for (int k = 0; k < 3; ++k) atomicAdd(a.v + t + (size_t)k * a.nt, dv[k] * iA);
+    }
+  }
+}
+
+void fill_args(rbc3d_ctx* ctx, int tlist, double c1, double c2, CorrArgs& a, const double* Bc) {
+  TargetSet& t = ctx->tl[tlist];
+  a.nt = t.n; a.tx = t.x.p; a.tA = t.Acoef.p; a.tmeta = t.meta.p; a.v = t.v.p;
+  a.ncell = ctx->ncell; a.nlat = ctx->nlat; a.nlon = ctx->nlon; a.m = ctx->m;
+  a.th = ctx->th.p; a.phi = ctx->phi.p; a.w = ctx->w.p;
+  a.x = ctx->x.p; a.a3 = ctx->a3.p; a.detJ = ctx->detJ.p; a.f = ctx->f.p; a.g = ctx->g.p;
+  a.area = ctx->area.p; a.meshSize = ctx->meshSize.p; a.celltype = ctx->celltype.p; a.Bc = Bc;
+  a.spl = ctx->spl.p; a.npt = ctx->npt;
+  a.nrad = ctx->nrad; a.nazm = ctx->nazm; a.radius = ctx->radius; a.pw = ctx->pw.p; a.thG = ctx->thG.p; a.phiA = ctx->phiA.p;
+  a.rd_s = ctx->rd_s.p; a.rd_w = ctx->rd_w.p; a.rd_x0 = ctx->rd_x0.p; a.rd_w0 = ctx->rd_w0.p;
+  a.c1 = c1; a.c2 = c2;
+  for (int d = 0; d < 3; ++d) { a.L[d] = ctx->prm.Lb[d]; a.iL[d] = ctx->iLb[d]; }
+  a.T = ctx->T;
+  a.items = ctx->items.p; a.nitems = ctx->dcnt.p; a.cap = ctx->items_cap; a.cnt = ctx->dcnt.p;
+}
+
+}  // namespace
+
+rbc3d_status run_self_corr(rbc3d_ctx* ctx, int tlist, double c1, double c2) {
+  TargetSet& t = ctx->tl[tlist];
+  if (tlist != RBC3D_TLIST_RBC || t.n == 0 || ctx->ncell == 0) return RBC3D_OK;
+  DBuf<double> Bc;
+  CUDA_TRY(Bc.upload(ctx->Bcoef, RBC3D_MAX_CELLTYPES, ctx->st));
+  CorrArgs a;
+  fill_args(ctx, tlist, c1, (c2 != 0 && ctx->has_g) ? c2 : 0.0, a, Bc.p);
+  if (c1 != 0 && !ctx->has_f) a.c1 = 0;
+  long long threads = (long long)t.n * 32;
+  k_self<<<(int)((threads + 255) / 256), 256, 0, ctx->st>>>(a);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  return RBC3D_OK;
+}
+
+rbc3d_status run_near_corr(rbc3d_ctx* ctx, int tlist, double c1, double c2, int prec) {
+  (void)prec;
+  TargetSet& t = ctx->tl[tlist];
+  if (t.n == 0 || ctx->ncell == 0) return RBC3D_OK;
+  DBuf<double> Bc;
+  CUDA_TRY(Bc.upload(ctx->Bcoef, RBC3D_MAX_CELLTYPES, ctx->st));
+  CorrArgs a;
+  fill_args(ctx, tlist, c1, (c2 != 0 && ctx->has_g) ? c2 : 0.0, a, Bc.p);
+  if (c1 != 0 && !ctx->has_f) a.c1 = 0;
+  int nsm = 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);
+  k_near<<<nsm * 8, 128, 0, ctx->st>>>(a);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  return RBC3D_OK;
+}

@@ -1,0 +1,181 @@
+// ctx.hpp -- device-resident state of one rbc3d context (one CUDA stream).
+#pragma once
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/rbc3d_gpu.h"
+#include "common.cuh"
+
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaError_t alloc(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    release();
+    n = count;
+    if (count == 0) return cudaSuccess;
+    return cudaMalloc((void**)&p, count * sizeof(T));
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t upload(const T* h, size_t count, cudaStream_t s) {
+    cudaError_t e = alloc(count);
+    if (e) return e;
+    return cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s);
+  }
+  ~DBuf() { release(); }
+};
+
+// Uniform cell list over the periodic box (HashTable_ComputeNumBlocks,
+// ModHashTable.F90:99-126, single rank): Nc = max(floor(L/rc), 3) per axis.
+struct HashGrid {
+  int Nc[3] = {0, 0, 0};
+  double h[3] = {0, 0, 0};
+  double L[3] = {0, 0, 0};
+  int ncells = 0;
+};
+
+// One target list (t_TargetList) on the device, sorted by cell-list cell.
+struct TargetSet {
+  int n = 0;
+  DBuf<double> x;       // 3n, FP64 SoA
+  DBuf<double> Acoef;   // n
+  DBuf<int4> meta;      // (surf, ilat, ilon, 0); surf 1-based, -1 for raw
+  DBuf<int> order;      // sorted position -> target index
+  DBuf<int> cstart, cend;
+  DBuf<int4> units;     // (hash cell, first sorted position, count, 0)
+  int nunits = 0;
+  bool sorted = false;
+  DBuf<double> v;       // 3n accumulator of the current matvec
+};
+
+struct PmeState {
+  int N1 = 0, N2 = 0, N3 = 0, NH = 0;
+  size_t G = 0, GC = 0;
+  DBuf<float> grid32;      // 12*G real grids
+  DBuf<double> grid64;
+  DBuf<float2> spec32;     // 12*GC spectra
+  DBuf<double2> spec64;
+  DBuf<float2> vspec32;    // 3*GC
+  DBuf<double2> vspec64;
+  DBuf<float> vel32;       // 3*G velocity grid
+  DBuf<double> vel64;
+  DBuf<double> bbx, bby, bbz;
+  cufftHandle r2c32_3 = 0, r2c32_12 = 0, c2r32_3 = 0;
+  cufftHandle r2c64_3 = 0, r2c64_12 = 0, c2r64_3 = 0;
+  bool planned32 = false, planned64 = false;
+  bool sl = false, dl = false;
+  int prec = RBC3D_FP64;
+  bool ready = false;  // velocity grid valid
+};
+
+struct WallState {
+  int nvert = 0, nele = 0, ndof = 0;
+  std::vector<double> hx, hf;       // host copies (x, density)
+  std::vector<int> he2v, hglb;
+  DBuf<double> x, f, area, eps, cen;  // vertices 3*nvert, density 3*nvert, per element
+  DBuf<int> e2v;                      // 3*nele (0-based)
+  DBuf<int> glb;                      // nvert (0-based unique id)
+  DBuf<int> writer;                   // 1 for the last vertex of each unique id (AssembleArray order)
+  DBuf<int> order, cstart, cend;      // centroid cell list
+  bool prepared = false;
+  DBuf<int> rowptr, col;              // self-wall CSR (3nvert x 3nvert)
+  DBuf<double> val;
+  long long nnz = 0;
+};
+
+struct rbc3d_ctx {
+  rbc3d_params prm{};
+  double iLb[3]{};
+  double Acoef[RBC3D_MAX_CELLTYPES]{}, Bcoef[RBC3D_MAX_CELLTYPES]{};
+  std::string err;
+  cudaStream_t st = nullptr;
+  int device = 0;
+
+  // Ewald / mask tables
+  Tables T{};
+  DBuf<double> t_sl1, t_sl2, t_dl, t_mask;
+  DBuf<float4> t_sl32;
+  DBuf<float2> t_dl32, t_mask32;
+
+  HashGrid hg;
+
+  // cell surface grid and polar patch
+  int nlat = 0, nlon = 0, m = 0;  // m = 2*nlat spline rows
+  std::vector<double> h_th, h_phi, h_w;
+  DBuf<double> th, phi, w;
+  DBuf<float4> usph;              // unit-sphere coordinates per grid point (FP32)
+  int nrad = 0, nazm = 0;
+  double radius = 0;
+  DBuf<double> pw, thG, phiA;     // patch weights (nrad); thG/phiA [ilat0][q]
+  DBuf<double> rd_s, rd_w;        // GauLeg(-1,1,16) for RBC_NearSingInt_ReAdd
+  DBuf<double> rd_x0, rd_w0;      // GauLeg(0,radius,16)
+
+  // cells
+  int ncell = 0, npt = 0;
+  std::vector<int> h_celltype;
+  DBuf<int> celltype;
+  DBuf<double> x, a3, detJ, f, g, sf, sg, area, meshSize;
+  DBuf<double> spl;               // ncell * SPL_NSET * m*nlon * SPL_NODE
+  bool has_f = false, has_g = false;
+
+  // sorted sources (cell surface points)
+  DBuf<int> s_order, s_cstart, s_cend;
+  DBuf<double> s_x, s_f, s_g, s_a3;  // sorted, SoA 3*npt; s_g carries Bcoef
+  DBuf<int4> s_meta;                 // (surf, ilat, ilon, original index)
+  bool src_sorted = false, src_density = false;
+
+  TargetSet tl[3];
+
+  // near-singular work list
+  DBuf<int4> items;               // (target, surf, ilat, ilon)
+  int items_cap = 0;
+  DBuf<unsigned long long> dcnt;  // device counters: [0] items, [1] pairs, [2] overflow targets, [3] nearsing, [4] wall pairs, [5] duffy
+  DBuf<double> xvint;             // linear-term reduction (3)
+
+  PmeState pme;
+  WallState wall;
+
+  DBuf<double> scratch;           // GMRES basis / temporaries
+  rbc3d_counts counts{};
+};
+
+rbc3d_status ctx_fail(rbc3d_ctx* ctx, int code, const std::string& msg);
+rbc3d_status ctx_fail_cuda(rbc3d_ctx* ctx, cudaError_t e, const char* what);
+
+// pair.cu
+rbc3d_status build_source_list(rbc3d_ctx* ctx);
+rbc3d_status sort_points_by_cell(rbc3d_ctx* ctx, int n, const double* x_dev, DBuf<int>& order, DBuf<int>& cs,
+                                DBuf<int>& ce);
+rbc3d_status matvec_dev(rbc3d_ctx* ctx, int which, double c1, double c2, unsigned terms, int prec);
+rbc3d_status build_source_density(rbc3d_ctx* ctx);
+rbc3d_status sort_targets(rbc3d_ctx* ctx, int tlist);
+rbc3d_status run_pair_sum(rbc3d_ctx* ctx, int tlist, double c1, double c2, int prec, bool collect_nbr);
+rbc3d_status run_linear(rbc3d_ctx* ctx, int tlist, double c2);
+// corr.cu
+rbc3d_status run_self_corr(rbc3d_ctx* ctx, int tlist, double c1, double c2);
+rbc3d_status run_near_corr(rbc3d_ctx* ctx, int tlist, double c1, double c2, int prec);
+// pme.cu
+rbc3d_status pme_setup(rbc3d_ctx* ctx);
+rbc3d_status pme_release(rbc3d_ctx* ctx);
+rbc3d_status pme_spread(rbc3d_ctx* ctx, double c1, double c2, int cells, int walls, int prec);
+rbc3d_status pme_transform(rbc3d_ctx* ctx);
+rbc3d_status pme_gather(rbc3d_ctx* ctx, int tlist);
+// walls.cu
+rbc3d_status wall_setup(rbc3d_ctx* ctx);
+rbc3d_status wall_prepare_self(rbc3d_ctx* ctx);
+rbc3d_status run_wall_quad(rbc3d_ctx* ctx, int tlist, double c1, int prec);
+rbc3d_status run_wall_self(rbc3d_ctx* ctx, double c1);
+rbc3d_status wall_solve(rbc3d_ctx* ctx, const rbc3d_solve_opts* opt, const double* guess, rbc3d_solve_stats* st);
+rbc3d_status wall_matmult_dev(rbc3d_ctx* ctx, int prec, const double* u_dev, double* y_dev);
+rbc3d_status wall_residual_dev(rbc3d_ctx* ctx, int prec);
+
+// shared host helper: GauLeg of ModQuadRule.F90:135-214
+void host_gauleg(double x1, double x2, int n, double* x, double* w);

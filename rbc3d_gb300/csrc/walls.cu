@@ -1,0 +1,686 @@
+// walls.cu -- wall quadrature, the self-wall operator and the NoSlipWall GMRES.
+//
+//   AddIntOnWalls (ModIntOnWalls.F90:37-128): cell / raw targets against every
+//     wall triangle whose centroid lies in the 27 neighbour cells, translated
+//     to the nearest image, MinDistToTri (Eberly) <= rc, 7-point gqTri7 rule
+//     or Duffy's 3 x 4 x 4 rule when closer than sqrt(area).
+//   PrepareSingIntOnWall (ModIntOnWalls.F90:181-308): assembled once on the
+//     GPU: (vertex, triangle) pair list -> per-pair 3x3x3 influence blocks ->
+//     radix sort by (row vertex, column vertex) -> segmented sums -> block-CSR
+//     with 3x3 blocks (rows and columns component-major as the PETSc matrix).
+//   NoSlipWall (ModNoSlip.F90:45-150): restarted GMRES on the wall-density
+//     increment, FP64 Arnoldi (classical Gram-Schmidt as PETSc's default) and
+//     FP64 Givens / Hessenberg least squares, all on the device.
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <vector>
+
+#include "ctx.hpp"
+
+namespace {
+
+inline int nblk(long long n, int b) { return (int)((n + b - 1) / b); }
+
+struct TriRules {
+  double r7[7], s7[7], w7[7];  // gqTri7, ModQuadRule.F90:69-94
+  double rg[4], wg[4];         // GauLeg(0,1,4) for Duffy, ModIntOnWalls.F90:400
+};
+__constant__ TriRules c_rules;
+
+__device__ __forceinline__ double dot3(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+// MinDistToTri, ModIntOnWalls.F90:480-577.  xv[l][c]: vertex l component c.
+__device__ double min_dist_to_tri(const double* xt, const double xv[3][3], double& s0, double& t0) {
+  double x12[3], x13[3], x1T[3];
+  for (int c = 0; c < 3; ++c) { x12[c] = xv[1][c] - xv[0][c]; x13[c] = xv[2][c] - xv[0][c]; x1T[c] = xv[0][c] - xt[c]; }
+  double a = dot3(x12, x12), b = dot3(x12, x13), c = dot3(x13, x13);
+  double det = a * c - b * b, invDet = 1. / det;
+  double d = dot3(x12, x1T), e = dot3(x13, x1T), f = dot3(x1T, x1T);
+  double s = b * e - c * d, t = b * d - a * e;
+  int region;
+  if (s + t <= det) {
+    if (s < 0) region = (t < 0) ? 4 : 3;
+    else if (t < 0) region = 5;
+    else region = 0;
+  } else {
+    if (s < 0) region = 2;
+    else if (t < 0) region = 6;
+    else region = 1;
+  }
+  if (region == 2) region = (-(c + e) < 0) ? 3 : 1;
+  else if (region == 4) region = (d < 0) ? 5 : 3;
+  else if (region == 6) region = (b + e - a - d < 0) ? 1 : 5;
+  switch (region) {
+    case 0: s = invDet * s; t = invDet * t; break;
+    case 1: s = (c + e - b - d) / (a - 2 * b + c); s = fmin(1., fmax(0., s)); t = 1. - s; break;
+    case 3: s = 0.; t = -e / c; t = fmin(1., fmax(0., t)); break;
+    case 5: t = 0.; s = -d / a; s = fmin(1., fmax(0., s)); break;
+  }
+  s0 = s; t0 = t;
+  return sqrt(a * s * s + 2 * b * s * t + c * t * t + 2 * d * s + 2 * e * t + f);
+}
+
+// One quadrature point: rhs += K(xt - xg) (ds*fg); lhs[l] += wv[l] * ds * K
+template <bool LHS>
+__device__ __forceinline__ void quad_point(const Tables& T, const double* xt, const double* xg, const double* fg, double ds,
+                                           const double* wv, double* rhs, double (*lhs)[9]) {
+  double xx[3] = {xt[0] - xg[0], xt[1] - xg[1], xt[2] - xg[2]};
+  double rr = sqrt(dot3(xx, xx)), EA, EB;
+  ewald_sl64(T, rr, EA, EB);
+  double f3[3] = {ds * fg[0], ds * fg[1], ds * fg[2]};
+  double xf = dot3(xx, f3);
+  for (int c = 0; c < 3; ++c) rhs[c] += EA * xx[c] * xf + EB * f3[c];
+  if (LHS) {
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) {
+        double Lrc = ds * (EA * xx[r] * xx[c] + (r == c ? EB : 0.));
+        for (int l = 0; l < 3; ++l) lhs[l][r * 3 + c] += wv[l] * Lrc;
+      }
+  }
+}
+
+// Tri_Int_Regular, ModIntOnWalls.F90:319-363
+template <bool LHS>
+__device__ void tri_int_regular(const Tables& T, const double xv[3][3], const double fv[3][3], const double* xt,
+                                double* rhs, double (*lhs)[9]) {
+  double a[3], b[3];
+  for (int c = 0; c < 3; ++c) { a[c] = xv[1][c] - xv[0][c]; b[c] = xv[2][c] - xv[0][c]; }
+  double cr[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+  double detJ = 2 * (0.5 * sqrt(dot3(cr, cr)));
+  for (int q = 0; q < 7; ++q) {
+    double s = c_rules.r7[q], t = c_rules.s7[q];
+    double xg[3], fg[3];
+    for (int c = 0; c < 3; ++c) {
+      xg[c] = (1. - s - t) * xv[0][c] + s * xv[1][c] + t * xv[2][c];
+      fg[c] = (1. - s - t) * fv[0][c] + s * fv[1][c] + t * fv[2][c];
+    }
+    double wv[3] = {1 - s - t, s, t};
+    quad_point<LHS>(T, xt, xg, fg, c_rules.w7[q] * detJ, wv, rhs, lhs);
+  }
+}
+
+// Tri_Int_Duffy, ModIntOnWalls.F90:373-465
+template <bool LHS>
+__device__ void tri_int_duffy(const Tables& T, const double xv[3][3], const double fv[3][3], const double* xt,
+                              double s0, double t0, double* rhs, double (*lhs)[9]) {
+  double x0[3], f0[3];
+  for (int c = 0; c < 3; ++c) {
+    x0[c] = (1 - s0 - t0) * xv[0][c] + s0 * xv[1][c] + t0 * xv[2][c];
+    f0[c] = (1 - s0 - t0) * fv[0][c] + s0 * fv[1][c] + t0 * fv[2][c];
+  }
+  const double S1[3] = {0., 1., 0.}, T1[3] = {0., 0., 1.}, S2[3] = {1., 0., 0.}, T2[3] = {0., 1., 0.};
+  for (int n = 0; n < 3; ++n) {
+    const double* x1 = xv[n];
+    const double* x2 = xv[(n + 1) % 3];
+    const double* f1 = fv[n];
+    const double* f2 = fv[(n + 1) % 3];
+    double a[3], b[3];
+    for (int c = 0; c < 3; ++c) { a[c] = x1[c] - x0[c]; b[c] = x2[c] - x0[c]; }
+    double nr[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+    double detJ = sqrt(dot3(nr, nr));
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j) {
+        double s = c_rules.rg[i], t = s * c_rules.rg[j];
+        double xg[3], fg[3];
+        for (int c = 0; c < 3; ++c) {
+          xg[c] = (1. - s) * x0[c] + (s - t) * x1[c] + t * x2[c];
+          fg[c] = (1. - s) * f0[c] + (s - t) * f1[c] + t * f2[c];
+        }
+        double ds = c_rules.wg[i] * c_rules.wg[j] * detJ * s;
+        double wv[3] = {0, 0, 0};
+        if (LHS) {
+          double sG = (1. - s) * s0 + (s - t) * S1[n] + t * S2[n];
+          double tG = (1. - s) * t0 + (s - t) * T1[n] + t * T2[n];
+          wv[0] = 1. - sG - tG; wv[1] = sG; wv[2] = tG;
+        }
+        quad_point<LHS>(T, xt, xg, fg, ds, wv, rhs, lhs);
+      }
+  }
+}
+
+struct WallArgs {
+  int nvert, nele;
+  const double* x;
+  const double* f;
+  const int* e2v;
+  const double* eps;
+  const int* cs;
+  const int* ce;
+  const int* order;
+  int Nc[3];
+  double h[3], L[3], iL[3];
+  double rc;
+  Tables T;
+};
+
+__device__ __forceinline__ void load_tri(const WallArgs& a, int e, double xv[3][3], double fv[3][3], bool wf) {
+  for (int l = 0; l < 3; ++l) {
+    int iv = a.e2v[e + (size_t)l * a.nele];
+    for (int c = 0; c < 3; ++c) {
+      xv[l][c] = a.x[iv + (size_t)c * a.nvert];
+      fv[l][c] = wf ? a.f[iv + (size_t)c * a.nvert] : 0.;
+    }
+  }
+}
+__device__ __forceinline__ void translate_tri(const WallArgs& a, const double* xi, double xv[3][3]) {
+  for (int c = 0; c < 3; ++c) {
+    double sh = round((xi[c] - xv[0][c]) * a.iL[c]) * a.L[c];
+    for (int l = 0; l < 3; ++l) xv[l][c] += sh;
+  }
+}
+__device__ __forceinline__ int home_cell(const WallArgs& a, const double* xi, int& ci, int& cj, int& ck) {
+  ci = imod((int)floor(xi[0] * a.Nc[0] * a.iL[0]), a.Nc[0]);
+  cj = imod((int)floor(xi[1] * a.Nc[1] * a.iL[1]), a.Nc[1]);
+  ck = imod((int)floor(xi[2] * a.Nc[2] * a.iL[2]), a.Nc[2]);
+  return 0;
+}
+
+// AddIntOnWalls for cell / raw targets (one thread per target, cell-list order)
+__global__ void k_wall_quad(WallArgs a, int nt, const double* __restrict__ tx, const double* __restrict__ tA,
+                            const int* __restrict__ torder, double c1, double* __restrict__ v,
+                            unsigned long long* cnt) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nt) return;
+  int i = torder[q];
+  double xi[3] = {tx[i], tx[i + nt], tx[i + 2 * (size_t)nt]};
+  int ci, cj, ck;
+  home_cell(a, xi, ci, cj, ck);
+  double acc[3] = {0, 0, 0};
+  unsigned long long np = 0, nd = 0;
+  for (int nb = 0; nb < 27; ++nb) {
+    int nc = imod(ci + nb % 3 - 1, a.Nc[0]) + a.Nc[0] * (imod(cj + (nb / 3) % 3 - 1, a.Nc[1]) + a.Nc[1] * imod(ck + nb / 9 - 1, a.Nc[2]));
+    for (int p = a.cs[nc]; p < a.ce[nc]; ++p) {
+      int e = a.order[p];
+      double xv[3][3], fv[3][3];
+      load_tri(a, e, xv, fv, true);
+      translate_tri(a, xi, xv);
+      double s0, t0;
+      double rr = min_dist_to_tri(xi, xv, s0, t0);
+      if (rr > a.rc) continue;
+      ++np;
+      double dv[3] = {0, 0, 0};
+      if (rr < a.eps[e]) { tri_int_duffy<false>(a.T, xv, fv, xi, s0, t0, dv, nullptr); ++nd; }
+      else tri_int_regular<false>(a.T, xv, fv, xi, dv, nullptr);
+      for (int c = 0; c < 3; ++c) acc[c] += c1 * dv[c] / tA[i];
+    }
+  }
+  for (int c = 0; c < 3; ++c) v[i + (size_t)c * nt] += acc[c];
+  if (np) { atomicAdd(cnt + 4, np); if (nd) atomicAdd(cnt + 5, nd); }
+}
+
+// Self-wall assembly, pass 1/2: count (mode 0) or list (mode 1) the
+// (vertex, triangle) pairs within rc.
+__global__ void k_self_pairs(WallArgs a, int mode, int* __restrict__ count, const int* __restrict__ off,
+                             int2* __restrict__ pairs) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.nvert) return;
+  double xi[3] = {a.x[i], a.x[i + a.nvert], a.x[i + 2 * (size_t)a.nvert]};
+  int ci, cj, ck;
+  home_cell(a, xi, ci, cj, ck);
+  int n = 0, base = mode ? off[i] : 0;
+  for (int nb = 0; nb < 27; ++nb) {
+    int nc = imod(ci + nb % 3 - 1, a.Nc[0]) + a.Nc[0] * (imod(cj + (nb / 3) % 3 - 1, a.Nc[1]) + a.Nc[1] * imod(ck + nb / 9 - 1, a.Nc[2]));
+    for (int p = a.cs[nc]; p < a.ce[nc]; ++p) {
+      int e = a.order[p];
+      double xv[3][3], fv[3][3];
+      load_tri(a, e, xv, fv, false);
+      translate_tri(a, xi, xv);
+      double s0, t0;
+      if (min_dist_to_tri(xi, xv, s0, t0) > a.rc) continue;
+      if (mode) pairs[base + n] = make_int2(i, e);
+      ++n;
+    }
+  }
+  if (!mode) count[i] = n;
+}
+
+// pass 3: one 3x3x3 influence block per pair -> three keyed 3x3 blocks
+__global__ void k_self_blocks(WallArgs a, long long npair, const int2* __restrict__ pairs,
+                              unsigned long long* __restrict__ keys, int* __restrict__ idx, double* __restrict__ blk) {
+  long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npair) return;
+  int i = pairs[p].x, e = pairs[p].y;
+  double xi[3] = {a.x[i], a.x[i + a.nvert], a.x[i + 2 * (size_t)a.nvert]};
+  double xv[3][3], fv[3][3];
+  load_tri(a, e, xv, fv, false);
+  translate_tri(a, xi, xv);
+  double s0, t0;
+  double rr = min_dist_to_tri(xi, xv, s0, t0);
+  double rhs[3] = {0, 0, 0}, lhs[3][9];
+  for (int l = 0; l < 3; ++l)
+    for (int k = 0; k < 9; ++k) lhs[l][k] = 0.;
+  if (rr > a.eps[e]) tri_int_regular<true>(a.T, xv, fv, xi, rhs, lhs);
+  else tri_int_duffy<true>(a.T, xv, fv, xi, s0, t0, rhs, lhs);
+  for (int l = 0; l < 3; ++l) {
+    int iv = a.e2v[e + (size_t)l * a.nele];
+    long long slot = 3 * p + l;
+    keys[slot] = (unsigned long long)i * (unsigned long long)a.nvert + (unsigned long long)iv;
+    idx[slot] = (int)slot;
+    for (int k = 0; k < 9; ++k) blk[slot * 9 + k] = lhs[l][k];
+  }
+}
+
+__global__ void k_uniq_flags(long long n, const unsigned long long* __restrict__ k, int* __restrict__ flag) {
+  long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  flag[p] = (p == 0 || k[p] != k[p - 1]) ? 1 : 0;
+}
+// pass 4: segmented sums into block-CSR entries
+__global__ void k_self_reduce(long long n, int nvert, const unsigned long long* __restrict__ k, const int* __restrict__ perm,
+                              const int* __restrict__ seg, const double* __restrict__ blk, int* __restrict__ bcol,
+                              int* __restrict__ brow, double* __restrict__ bval) {
+  long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  if (p > 0 && k[p] == k[p - 1]) return;  // only segment heads
+  int u = seg[p] - 1;  // inclusive scan of head flags: 1-based segment ids
+  double s[9];
+  for (int c = 0; c < 9; ++c) s[c] = 0.;
+  for (long long q = p; q < n && k[q] == k[p]; ++q)
+    for (int c = 0; c < 9; ++c) s[c] += blk[(size_t)perm[q] * 9 + c];
+  for (int c = 0; c < 9; ++c) bval[(size_t)u * 9 + c] = s[c];
+  bcol[u] = (int)(k[p] % (unsigned long long)nvert);
+  brow[u] = (int)(k[p] / (unsigned long long)nvert);
+}
+__global__ void k_row_ptr(int nb, int nvert, const int* __restrict__ brow, int* __restrict__ rowptr) {
+  int u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= nb) return;
+  int r = brow[u];
+  if (u == 0) for (int q = 0; q <= r; ++q) rowptr[q] = 0;
+  if (u == nb - 1) for (int q = r + 1; q <= nvert; ++q) rowptr[q] = nb;
+  if (u > 0 && brow[u - 1] != r)
+    for (int q = brow[u - 1] + 1; q <= r; ++q) rowptr[q] = u;
+}
+
+// SingIntOnWall (ModIntOnWalls.F90:136-172): v += c1 * (M f) / Acoef, block-CSR
+__global__ void k_self_spmv(int nvert, const int* __restrict__ rowptr, const int* __restrict__ bcol,
+                            const double* __restrict__ bval, const double* __restrict__ f, const double* __restrict__ tA,
+                            double c1, double* __restrict__ v) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nvert) return;
+  double y[3] = {0, 0, 0};
+  for (int b = rowptr[i]; b < rowptr[i + 1]; ++b) {
+    int j = bcol[b];
+    const double* B = bval + (size_t)b * 9;
+    double fj[3] = {f[j], f[j + nvert], f[j + 2 * (size_t)nvert]};
+    for (int r = 0; r < 3; ++r) y[r] += B[r * 3 + 0] * fj[0] + B[r * 3 + 1] * fj[1] + B[r * 3 + 2] * fj[2];
+  }
+  for (int r = 0; r < 3; ++r) v[i + (size_t)r * nvert] += c1 * y[r] / tA[i];
+}
+
+__global__ void k_wall_geom(int nele, int nvert, const int* __restrict__ e2v, const double* __restrict__ x,
+                            double* __restrict__ area, double* __restrict__ eps, double* __restrict__ cen) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nele) return;
+  double xv[3][3];
+  for (int l = 0; l < 3; ++l) {
+    int iv = e2v[e + (size_t)l * nele];
+    for (int c = 0; c < 3; ++c) xv[l][c] = x[iv + (size_t)c * nvert];
+  }
+  double a[3], b[3];
+  for (int c = 0; c < 3; ++c) { a[c] = xv[1][c] - xv[0][c]; b[c] = xv[2][c] - xv[0][c]; }
+  double nr[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+  double an = sqrt(dot3(nr, nr));
+  area[e] = 0.5 * an;             // Wall_ComputeGeometry, ModWall.F90:118-145
+  eps[e] = sqrt(area[e]);
+  for (int c = 0; c < 3; ++c) cen[e + (size_t)c * nele] = (1.0 / 3) * (xv[0][c] + xv[1][c] + xv[2][c]);
+}
+
+// AssembleArray (ModNoSlip.F90:361-384)
+__global__ void k_expand(int nvert, const int* __restrict__ glb, const double* __restrict__ u, double* __restrict__ f) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nvert) return;
+  int g = glb[i];
+  for (int c = 0; c < 3; ++c) f[i + (size_t)c * nvert] = u[3 * (size_t)g + c];
+}
+__global__ void k_assemble(int nvert, const int* __restrict__ glb, const int* __restrict__ writer,
+                           const double* __restrict__ v, double scale, double* __restrict__ u) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nvert || !writer[i]) return;  // the last duplicate wins, as the sequential loop
+  int g = glb[i];
+  for (int c = 0; c < 3; ++c) u[3 * (size_t)g + c] = scale * v[i + (size_t)c * nvert];
+}
+__global__ void k_add_const(int n, double a0, double a1, double a2, double* v) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  v[i] += a0; v[i + n] += a1; v[i + 2 * (size_t)n] += a2;
+}
+
+// ---- GMRES kernels (FP64)
+__global__ void k_dots(int n, int nv, const double* __restrict__ V, size_t ld, const double* __restrict__ w,
+                       double* __restrict__ out) {
+  // block j computes V_j . w
+  int j = blockIdx.x;
+  if (j >= nv) return;
+  const double* vj = V + (size_t)j * ld;
+  double s = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += vj[i] * w[i];
+  __shared__ double red[32];
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double t = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.;
+    t = warp_sum(t);
+    if (threadIdx.x == 0) out[j] = t;
+  }
+}
+__global__ void k_orth(int n, int nv, const double* __restrict__ V, size_t ld, const double* __restrict__ h,
+                       double* __restrict__ w) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = w[i];
+  for (int j = 0; j < nv; ++j) s -= h[j] * V[(size_t)j * ld + i];
+  w[i] = s;
+}
+__global__ void k_axpby(int n, double a, const double* __restrict__ x, double b, double* __restrict__ y) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = a * x[i] + b * y[i];
+}
+// Givens / Hessenberg step for column k (single thread).  H column-major with
+// leading dimension ldh = restart+1.  Writes |g_{k+1}| to res.
+__global__ void k_givens(int k, int ldh, double* H, const double* hcol, double hn, double* cs, double* sn,
+                         double* g, double* res) {
+  if (threadIdx.x || blockIdx.x) return;
+  double* c = H + (size_t)ldh * k;
+  for (int j = 0; j <= k; ++j) c[j] = hcol[j];
+  c[k + 1] = hn;
+  for (int j = 0; j < k; ++j) {
+    double a = c[j], b = c[j + 1];
+    c[j] = cs[j] * a + sn[j] * b;
+    c[j + 1] = -sn[j] * a + cs[j] * b;
+  }
+  double a = c[k], b = c[k + 1];
+  double den = sqrt(a * a + b * b);
+  cs[k] = den > 0 ? a / den : 1.;
+  sn[k] = den > 0 ? b / den : 0.;
+  c[k] = den;
+  c[k + 1] = 0.;
+  g[k + 1] = -sn[k] * g[k];
+  g[k] = cs[k] * g[k];
+  *res = fabs(g[k + 1]);
+}
+__global__ void k_backsolve(int k, int ldh, const double* H, const double* g, double* y) {
+  if (threadIdx.x || blockIdx.x) return;
+  for (int i = k - 1; i >= 0; --i) {
+    double s = g[i];
+    for (int j = i + 1; j < k; ++j) s -= H[i + (size_t)ldh * j] * y[j];
+    y[i] = s / H[i + (size_t)ldh * i];
+  }
+}
+__global__ void k_xupdate(int n, int k, const double* __restrict__ V, size_t ld, const double* __restrict__ y,
+                          double* __restrict__ x) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = x[i];
+  for (int j = 0; j < k; ++j) s += y[j] * V[(size_t)j * ld + i];
+  x[i] = s;
+}
+
+WallArgs wall_args(rbc3d_ctx* ctx) {
+  WallState& W = ctx->wall;
+  WallArgs a;
+  a.nvert = W.nvert; a.nele = W.nele; a.x = W.x.p; a.f = W.f.p; a.e2v = W.e2v.p; a.eps = W.eps.p;
+  a.cs = W.cstart.p; a.ce = W.cend.p; a.order = W.order.p;
+  for (int d = 0; d < 3; ++d) { a.Nc[d] = ctx->hg.Nc[d]; a.h[d] = ctx->hg.h[d]; a.L[d] = ctx->hg.L[d]; a.iL[d] = ctx->iLb[d]; }
+  a.rc = ctx->prm.rc;
+  a.T = ctx->T;
+  return a;
+}
+
+double dev_norm(rbc3d_ctx* ctx, int n, const double* v, double* tmp) {
+  k_dots<<<1, 512, 0, ctx->st>>>(n, 1, v, 0, v, tmp);
+  double h = 0;
+  cudaMemcpyAsync(&h, tmp, sizeof(double), cudaMemcpyDeviceToHost, ctx->st);
+  cudaStreamSynchronize(ctx->st);
+  return std::sqrt(h);
+}
+
+}  // namespace
+
+static rbc3d_status writer_flags(rbc3d_ctx* ctx, DBuf<int>& wr) {
+  WallState& W = ctx->wall;
+  std::vector<int> last(W.ndof / 3, -1), flag(W.nvert, 0);
+  for (int i = 0; i < W.nvert; ++i) last[W.hglb[i]] = i;
+  for (int i = 0; i < W.nvert; ++i) flag[i] = last[W.hglb[i]] == i;
+  CUDA_TRY(wr.upload(flag.data(), flag.size(), ctx->st));
+  return RBC3D_OK;
+}
+
+rbc3d_status wall_setup(rbc3d_ctx* ctx) {
+  WallState& W = ctx->wall;
+  if (W.nvert == 0) return RBC3D_OK;
+  static bool rules_set = false;
+  if (!rules_set) {
+    TriRules R;
+    double r = (6. - std::sqrt(15.)) / 21., s = r, t = 1 - r - s;
+    double rr[7] = {r, s, t, 0, 0, 0, 1. / 3.}, ss[7] = {s, t, r, 0, 0, 0, 1. / 3.};
+    double w1 = (155. - std::sqrt(15.)) / 2400.;
+    r = (6. + std::sqrt(15.)) / 21.; s = r; t = 1 - r - s;
+    rr[3] = r; rr[4] = s; rr[5] = t; ss[3] = s; ss[4] = t; ss[5] = r;
+    double w2 = (155. + std::sqrt(15.)) / 2400.;
+    for (int i = 0; i < 7; ++i) { R.r7[i] = rr[i]; R.s7[i] = ss[i]; }
+    for (int i = 0; i < 3; ++i) { R.w7[i] = w1; R.w7[i + 3] = w2; }
+    R.w7[6] = 9. / 80.;
+    host_gauleg(0., 1., 4, R.rg, R.wg);
+    CUDA_TRY(cudaMemcpyToSymbol(c_rules, &R, sizeof(R)));
+    rules_set = true;
+  }
+  CUDA_TRY(W.x.upload(W.hx.data(), W.hx.size(), ctx->st));
+  CUDA_TRY(W.f.upload(W.hf.data(), W.hf.size(), ctx->st));
+  CUDA_TRY(W.e2v.upload(W.he2v.data(), W.he2v.size(), ctx->st));
+  CUDA_TRY(W.glb.upload(W.hglb.data(), W.hglb.size(), ctx->st));
+  CUDA_TRY(W.area.alloc(W.nele)); CUDA_TRY(W.eps.alloc(W.nele)); CUDA_TRY(W.cen.alloc(3 * (size_t)W.nele));
+  k_wall_geom<<<nblk(W.nele, 256), 256, 0, ctx->st>>>(W.nele, W.nvert, W.e2v.p, W.x.p, W.area.p, W.eps.p, W.cen.p);
+  CUDA_TRY(cudaGetLastError());
+  rbc3d_status s = writer_flags(ctx, W.writer);
+  if (s) return s;
+  return sort_points_by_cell(ctx, W.nele, W.cen.p, W.order, W.cstart, W.cend);
+}
+
+rbc3d_status wall_prepare_self(rbc3d_ctx* ctx) {
+  WallState& W = ctx->wall;
+  if (W.nvert == 0) return RBC3D_OK;
+  WallArgs a = wall_args(ctx);
+  DBuf<int> count, off;
+  CUDA_TRY(count.alloc(W.nvert + 1)); CUDA_TRY(off.alloc(W.nvert + 1));
+  CUDA_TRY(cudaMemsetAsync(count.p, 0, sizeof(int) * (W.nvert + 1), ctx->st));
+  k_self_pairs<<<nblk(W.nvert, 128), 128, 0, ctx->st>>>(a, 0, count.p, nullptr, nullptr);
+  size_t tmp = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, tmp, count.p, off.p, W.nvert + 1, ctx->st);
+  DBuf<char> tb;
+  CUDA_TRY(tb.alloc(tmp + 1));
+  CUDA_TRY(cub::DeviceScan::ExclusiveSum(tb.p, tmp, count.p, off.p, W.nvert + 1, ctx->st));
+  int npair = 0;
+  CUDA_TRY(cudaMemcpyAsync(&npair, off.p + W.nvert, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  if (npair == 0) {
+    CUDA_TRY(W.rowptr.alloc(W.nvert + 1));
+    CUDA_TRY(cudaMemsetAsync(W.rowptr.p, 0, sizeof(int) * (W.nvert + 1), ctx->st));
+    CUDA_TRY(cudaStreamSynchronize(ctx->st));
+    W.nnz = 0;
+    W.prepared = true;
+    return RBC3D_OK;
+  }
+  DBuf<int2> pairs;
+  CUDA_TRY(pairs.alloc(npair));
+  k_self_pairs<<<nblk(W.nvert, 128), 128, 0, ctx->st>>>(a, 1, nullptr, off.p, pairs.p);
+  long long ne = 3LL * npair;
+  DBuf<unsigned long long> k1, k2;
+  DBuf<int> i1, i2, flag, seg;
+  DBuf<double> blk;
+  CUDA_TRY(k1.alloc(ne)); CUDA_TRY(k2.alloc(ne)); CUDA_TRY(i1.alloc(ne)); CUDA_TRY(i2.alloc(ne));
+  CUDA_TRY(flag.alloc(ne)); CUDA_TRY(seg.alloc(ne)); CUDA_TRY(blk.alloc(9 * ne));
+  k_self_blocks<<<nblk(npair, 128), 128, 0, ctx->st>>>(a, npair, pairs.p, k1.p, i1.p, blk.p);
+  CUDA_TRY(cudaGetLastError());
+  tmp = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, tmp, k1.p, k2.p, i1.p, i2.p, (int)ne, 0, 64, ctx->st);
+  DBuf<char> tb2;
+  CUDA_TRY(tb2.alloc(tmp + 1));
+  CUDA_TRY(cub::DeviceRadixSort::SortPairs(tb2.p, tmp, k1.p, k2.p, i1.p, i2.p, (int)ne, 0, 64, ctx->st));
+  k_uniq_flags<<<nblk(ne, 256), 256, 0, ctx->st>>>(ne, k2.p, flag.p);
+  tmp = 0;
+  cub::DeviceScan::InclusiveSum(nullptr, tmp, flag.p, seg.p, (int)ne, ctx->st);
+  DBuf<char> tb3;
+  CUDA_TRY(tb3.alloc(tmp + 1));
+  CUDA_TRY(cub::DeviceScan::InclusiveSum(tb3.p, tmp, flag.p, seg.p, (int)ne, ctx->st));
+  int nb = 0;
+  CUDA_TRY(cudaMemcpyAsync(&nb, seg.p + ne - 1, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  DBuf<int> brow;
+  CUDA_TRY(W.col.alloc(nb)); CUDA_TRY(brow.alloc(nb)); CUDA_TRY(W.val.alloc(9 * (size_t)nb));
+  CUDA_TRY(W.rowptr.alloc(W.nvert + 1));
+  k_self_reduce<<<nblk(ne, 256), 256, 0, ctx->st>>>(ne, W.nvert, k2.p, i2.p, seg.p, blk.p, W.col.p, brow.p, W.val.p);
+  CUDA_TRY(cudaGetLastError());
+  if (nb > 0) k_row_ptr<<<nblk(nb, 256), 256, 0, ctx->st>>>(nb, W.nvert, brow.p, W.rowptr.p);
+  else CUDA_TRY(cudaMemsetAsync(W.rowptr.p, 0, sizeof(int) * (W.nvert + 1), ctx->st));
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  W.nnz = 9LL * nb;
+  W.prepared = true;
+  return RBC3D_OK;
+}
+
+rbc3d_status run_wall_quad(rbc3d_ctx* ctx, int tlist, double c1, int prec) {
+  (void)prec;
+  WallState& W = ctx->wall;
+  TargetSet& t = ctx->tl[tlist];
+  if (W.nele == 0 || t.n == 0 || tlist == RBC3D_TLIST_WALL) return RBC3D_OK;
+  rbc3d_status s = sort_targets(ctx, tlist);
+  if (s) return s;
+  WallArgs a = wall_args(ctx);
+  CUDA_TRY(cudaMemsetAsync(ctx->dcnt.p + 4, 0, 2 * sizeof(unsigned long long), ctx->st));
+  k_wall_quad<<<nblk(t.n, 128), 128, 0, ctx->st>>>(a, t.n, t.x.p, t.Acoef.p, t.order.p, c1, t.v.p, ctx->dcnt.p);
+  CUDA_TRY(cudaGetLastError());
+  unsigned long long h[2];
+  CUDA_TRY(cudaMemcpyAsync(h, ctx->dcnt.p + 4, sizeof(h), cudaMemcpyDeviceToHost, ctx->st));
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  ctx->counts.wall_pairs = (long long)h[0];
+  ctx->counts.wall_duffy = (long long)h[1];
+  return RBC3D_OK;
+}
+
+rbc3d_status run_wall_self(rbc3d_ctx* ctx, double c1) {
+  WallState& W = ctx->wall;
+  if (W.nvert == 0) return RBC3D_OK;
+  if (!W.prepared) return ctx_fail(ctx, RBC3D_ERR_STATE, "PrepareSingIntOnWall not called");
+  TargetSet& t = ctx->tl[RBC3D_TLIST_WALL];
+  k_self_spmv<<<nblk(W.nvert, 128), 128, 0, ctx->st>>>(W.nvert, W.rowptr.p, W.col.p, W.val.p, W.f.p, t.Acoef.p, c1,
+                                                        t.v.p);
+  CUDA_TRY(cudaGetLastError());
+  return RBC3D_OK;
+}
+
+// Compute_Wall_Residual_Vel (ModNoSlip.F90:153-193) into tl[WALL].v
+rbc3d_status wall_residual_dev(rbc3d_ctx* ctx, int prec) {
+  double c = 1. / (4. * RBC3D_PI);
+  rbc3d_status s = matvec_dev(ctx, RBC3D_TLIST_WALL, c, c, RBC3D_TERM_ALL, prec);
+  if (s) return s;
+  TargetSet& t = ctx->tl[RBC3D_TLIST_WALL];
+  k_add_const<<<nblk(t.n, 256), 256, 0, ctx->st>>>(t.n, ctx->prm.vBkg[0], ctx->prm.vBkg[1], ctx->prm.vBkg[2], t.v.p);
+  CUDA_TRY(cudaGetLastError());
+  return RBC3D_OK;
+}
+
+
+// MyMatMult (ModNoSlip.F90:255-308): y = assemble(SingIntOnWall + PME(walls)) of expand(u)
+rbc3d_status wall_matmult_dev(rbc3d_ctx* ctx, int prec, const double* u_dev, double* y_dev) {
+  WallState& W = ctx->wall;
+  TargetSet& t = ctx->tl[RBC3D_TLIST_WALL];
+  if (!W.prepared) return ctx_fail(ctx, RBC3D_ERR_STATE, "PrepareSingIntOnWall not called");
+  k_expand<<<nblk(W.nvert, 256), 256, 0, ctx->st>>>(W.nvert, W.glb.p, u_dev, W.f.p);
+  CUDA_TRY(t.v.alloc(3 * (size_t)t.n));
+  CUDA_TRY(cudaMemsetAsync(t.v.p, 0, sizeof(double) * 3 * t.n, ctx->st));
+  double c1 = 1. / (4. * RBC3D_PI);
+  rbc3d_status s;
+  if ((s = run_wall_self(ctx, c1))) return s;
+  if ((s = pme_spread(ctx, c1, 0., 0, 1, prec))) return s;
+  if ((s = pme_transform(ctx))) return s;
+  if ((s = pme_gather(ctx, RBC3D_TLIST_WALL))) return s;
+  k_assemble<<<nblk(W.nvert, 256), 256, 0, ctx->st>>>(W.nvert, W.glb.p, W.writer.p, t.v.p, 1.0, y_dev);
+  CUDA_TRY(cudaGetLastError());
+  return RBC3D_OK;
+}
+
+// NoSlipWall (ModNoSlip.F90:45-150)
+rbc3d_status wall_solve(rbc3d_ctx* ctx, const rbc3d_solve_opts* o, const double* guess, rbc3d_solve_stats* st) {
+  WallState& W = ctx->wall;
+  if (W.nvert == 0) return RBC3D_OK;
+  if (!W.prepared) return ctx_fail(ctx, RBC3D_ERR_STATE, "PrepareSingIntOnWall not called");
+  auto t0 = std::chrono::steady_clock::now();
+  rbc3d_solve_stats S{};
+  const int n = W.ndof, R = o->restart > 0 ? o->restart : 30;
+  const int prec = o->prec;
+  const size_t ld = (size_t)n;
+  // device storage: V (R+1 vectors), b, x, r, w, f0, small arrays
+  DBuf<double> V, b, x, r, w, f0, H, cs, sn, g, hcol, yv, tmp;
+  CUDA_TRY(V.alloc((size_t)(R + 1) * ld)); CUDA_TRY(b.alloc(n)); CUDA_TRY(x.alloc(n)); CUDA_TRY(r.alloc(n));
+  CUDA_TRY(w.alloc(n)); CUDA_TRY(f0.alloc(3 * (size_t)W.nvert));
+  CUDA_TRY(H.alloc((size_t)(R + 1) * R)); CUDA_TRY(cs.alloc(R)); CUDA_TRY(sn.alloc(R)); CUDA_TRY(g.alloc(R + 1));
+  CUDA_TRY(hcol.alloc(R + 1)); CUDA_TRY(yv.alloc(R)); CUDA_TRY(tmp.alloc(R + 2));
+  CUDA_TRY(cudaMemcpyAsync(f0.p, W.f.p, sizeof(double) * 3 * W.nvert, cudaMemcpyDeviceToDevice, ctx->st));
+  rbc3d_status s;
+  // rhs = -assemble(residual velocity)
+  if ((s = wall_residual_dev(ctx, prec))) return s;
+  k_assemble<<<nblk(W.nvert, 256), 256, 0, ctx->st>>>(W.nvert, W.glb.p, W.writer.p, ctx->tl[RBC3D_TLIST_WALL].v.p, -1.0,
+                                                       b.p);
+  CUDA_TRY(cudaGetLastError());
+  if (o->guess && guess) CUDA_TRY(cudaMemcpyAsync(x.p, guess, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->st));
+  else CUDA_TRY(cudaMemsetAsync(x.p, 0, sizeof(double) * n, ctx->st));
+  auto matvec = [&](const double* in, double* out) -> rbc3d_status {
+    S.matvecs++;
+    return wall_matmult_dev(ctx, prec, in, out);
+  };
+  auto residual = [&]() -> rbc3d_status {  // r = b - A x
+    rbc3d_status e = matvec(x.p, w.p);
+    if (e) return e;
+    CUDA_TRY(cudaMemcpyAsync(r.p, b.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->st));
+    k_axpby<<<nblk(n, 256), 256, 0, ctx->st>>>(n, -1.0, w.p, 1.0, r.p);
+    return RBC3D_OK;
+  };
+  if ((s = residual())) return s;
+  double beta = dev_norm(ctx, n, r.p, tmp.p);
+  S.rnorm0 = beta;
+  S.bnorm = dev_norm(ctx, n, b.p, tmp.p);
+  double ttol = std::max(o->rtol * beta, 1e-50);
+  int its = 0;
+  bool conv = beta <= ttol;
+  while (!conv && its < o->max_it) {
+    k_axpby<<<nblk(n, 256), 256, 0, ctx->st>>>(n, 1.0 / beta, r.p, 0.0, V.p);
+    std::vector<double> gh(R + 1, 0.);
+    gh[0] = beta;
+    CUDA_TRY(cudaMemcpyAsync(g.p, gh.data(), sizeof(double) * (R + 1), cudaMemcpyHostToDevice, ctx->st));
+    int k;
+    for (k = 0; k < R && its < o->max_it; ++k) {
+      if ((s = matvec(V.p + k * ld, w.p))) return s;
+      k_dots<<<k + 1, 512, 0, ctx->st>>>(n, k + 1, V.p, ld, w.p, hcol.p);
+      k_orth<<<nblk(n, 256), 256, 0, ctx->st>>>(n, k + 1, V.p, ld, hcol.p, w.p);
+      double hn = dev_norm(ctx, n, w.p, tmp.p);
+      if (hn > 0) k_axpby<<<nblk(n, 256), 256, 0, ctx->st>>>(n, 1.0 / hn, w.p, 0.0, V.p + (k + 1) * ld);
+      k_givens<<<1, 1, 0, ctx->st>>>(k, R + 1, H.p, hcol.p, hn, cs.p, sn.p, g.p, tmp.p + R + 1);
+      double res = 0;
+      CUDA_TRY(cudaMemcpyAsync(&res, tmp.p + R + 1, sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+      CUDA_TRY(cudaStreamSynchronize(ctx->st));
+      ++its;
+      if (res <= ttol || hn == 0) { ++k; conv = true; break; }
+    }
+    k_backsolve<<<1, 1, 0, ctx->st>>>(k, R + 1, H.p, g.p, yv.p);
+    k_xupdate<<<nblk(n, 256), 256, 0, ctx->st>>>(n, k, V.p, ld, yv.p, x.p);
+    if ((s = residual())) return s;
+    beta = dev_norm(ctx, n, r.p, tmp.p);
+    if (beta <= ttol) conv = true;
+  }
+  S.iterations = its;
+  S.converged = conv ? 1 : 0;
+  S.rnorm = beta;
+  // wall f = f0 + expand(x)
+  k_expand<<<nblk(W.nvert, 256), 256, 0, ctx->st>>>(W.nvert, W.glb.p, x.p, W.f.p);
+  k_axpby<<<nblk(3 * W.nvert, 256), 256, 0, ctx->st>>>(3 * W.nvert, 1.0, f0.p, 1.0, W.f.p);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  S.ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  if (st) *st = S;
+  return conv ? RBC3D_OK : ctx_fail(ctx, RBC3D_ERR_NOCONV, "GMRES reached max_it");
+}

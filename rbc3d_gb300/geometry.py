@@ -1,0 +1,365 @@
+"""Host-side FP64 producers of the matvec inputs.
+
+These replace, for analytically described cells, the geometry and spline
+builders of RBC3D that run before every matvec:
+
+* ``RBC_Create`` grid (Gauss colatitudes x uniform longitudes, weights with the
+  2*pi/nlon factor), ModRbc.F90:44-104;
+* ``RBC_MakeBiConcave`` (Evans-Fung / Pozrikidis shape), ModRbc.F90:368-398;
+* ``RBC_ComputeGeometry`` outputs used by the matvec: unit normal a3,
+  detJ = |x_theta x x_phi| / sin(theta), area, meshSize, ModRbc.F90:404-509
+  (here from the analytic surface derivatives instead of an SH gradient);
+* ``Spline_Build_on_Sphere`` (doubled-sphere bicubic Hermite tables with FFT
+  derivatives, Nyquist mode zeroed), ModSpline.F90:121-143 and
+  ModFFT.F90:25-93, fed from samples on the equiangular grid of
+  ``ShSynthEqu`` (nlat+1 colatitudes including both poles), ModRbc.F90:716-807;
+* ``Wall_ComputeGeometry``-ready Tri3 tube meshes with the periodic duplicate
+  vertex map of ``Wall_Build_V2V`` / ``GlobData_Init``, ModWall.F90:66-113,
+  ModData.F90:47-58.
+
+Everything is seeded (``numpy.random.default_rng``) so the oracle and the GPU
+consume bit-identical inputs.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+ALPH_BICONCAVE = 1.3858189  # ModRbc.F90:375
+
+
+# ---------------------------------------------------------------------------
+# Ewald parameters
+def ewald_s(eps: float) -> float:
+    """Fixed-point iteration of SetEwaldPrms (ModConf.F90:364-369)."""
+    s = 1.0
+    for _ in range(10):
+        s = 0.75 * math.sqrt(math.pi) * eps / (s ** 3 + 1.5 * s + 0.75 / s)
+        s = math.sqrt(-math.log(s))
+    return s
+
+
+def alpha_for_cutoff(rc: float, eps: float) -> float:
+    """alpha such that SetEwaldPrms derives the cut-off rc from eps."""
+    s = ewald_s(eps)
+    return math.pi * (rc / s) ** 2
+
+
+# ---------------------------------------------------------------------------
+# Cell grid
+def gauss_grid(nlat: int, nlon: int):
+    """Gauss-Legendre colatitudes (increasing), longitudes and weights
+    w = gauss_weight * 2*pi/nlon (RBC_Create, ModRbc.F90:92-94)."""
+    x, wg = np.polynomial.legendre.leggauss(nlat)
+    th = np.arccos(x)[::-1].copy()
+    wg = wg[::-1].copy()
+    phi = np.arange(nlon) * (2 * np.pi / nlon)
+    w = (2 * np.pi / nlon) * wg
+    return th, phi, w
+
+
+def _biconcave_profile(th, rc=1.0):
+    """r(th), z(th) and derivatives of RBC_MakeBiConcave (ModRbc.F90:368-398)."""
+    a = ALPH_BICONCAVE
+    s, c = np.sin(th), np.cos(th)
+    P = 0.207 + 2.003 * s ** 2 - 1.123 * s ** 4
+    dP = 4.006 * s - 4.492 * s ** 3
+    r = rc * a * s
+    z = rc * 0.5 * a * P * c
+    dr = rc * a * c
+    dz = rc * 0.5 * a * (dP * c * c - P * s)
+    return r, z, dr, dz
+
+
+def biconcave_surface(th, phi, R, xc, rc=1.0):
+    """Position, unit normal and detJ of a rotated, translated biconcave cell
+    at colatitudes th (any grid) and longitudes phi.  Arrays (nth, nphi, 3)."""
+    r, z, dr, dz = _biconcave_profile(th, rc)
+    cp, sp = np.cos(phi), np.sin(phi)
+    X = np.stack([r[:, None] * cp[None, :], r[:, None] * sp[None, :],
+                  np.broadcast_to(z[:, None], (th.size, phi.size))], axis=-1)
+    nrm = np.sqrt(dr ** 2 + dz ** 2)
+    N = np.stack([-dz[:, None] * cp[None, :] / nrm[:, None],
+                  -dz[:, None] * sp[None, :] / nrm[:, None],
+                  np.broadcast_to((dr / nrm)[:, None], (th.size, phi.size))], axis=-1)
+    detJ = np.broadcast_to((rc * ALPH_BICONCAVE * nrm)[:, None], (th.size, phi.size)).copy()
+    X = X @ R.T + xc
+    N = N @ R.T
+    return X, N, detJ
+
+
+def random_rotation(rng):
+    q = rng.normal(size=4)
+    q /= np.linalg.norm(q)
+    w, x, y, z = q
+    return np.array([
+        [1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+        [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+        [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
+# ---------------------------------------------------------------------------
+# Real spherical-harmonic fields
+def _assoc_legendre(lmax, x):
+    """Orthonormalised associated Legendre functions Nbar_lm(x) for m<=l<=lmax,
+    such that Y_lm = Nbar_lm(cos th) * {1, sqrt2 cos(m phi), sqrt2 sin(m phi)} is
+    orthonormal on the unit sphere.  Own recursion (stable for small lmax)."""
+    x = np.asarray(x, dtype=np.float64)
+    s = np.sqrt(np.maximum(0.0, 1 - x * x))
+    P = {}
+    P[(0, 0)] = np.full_like(x, math.sqrt(1 / (4 * math.pi)))
+    for m in range(1, lmax + 1):
+        P[(m, m)] = -math.sqrt((2 * m + 1) / (2 * m)) * s * P[(m - 1, m - 1)]
+    for m in range(0, lmax):
+        P[(m + 1, m)] = math.sqrt(2 * m + 3) * x * P[(m, m)]
+    for m in range(0, lmax + 1):
+        for l in range(m + 2, lmax + 1):
+            a = math.sqrt((4 * l * l - 1) / (l * l - m * m))
+            b = math.sqrt(((l - 1) ** 2 - m * m) / (4 * (l - 1) ** 2 - 1))
+            P[(l, m)] = a * (x * P[(l - 1, m)] - b * P[(l - 2, m)])
+    return P
+
+
+def random_sh_coeffs(rng, lmax=6, lmin=1):
+    """Coefficients a_lm ~ N(0, l^-2) of a real SH field, l in [lmin, lmax]."""
+    out = {}
+    for l in range(lmin, lmax + 1):
+        sd = 1.0 / l
+        for m in range(-l, l + 1):
+            out[(l, m)] = rng.normal(0.0, sd)
+    return out
+
+
+def sh_eval(coeffs, th, phi):
+    lmax = max(l for l, _ in coeffs)
+    P = _assoc_legendre(lmax, np.cos(th))
+    out = np.zeros((th.size, phi.size))
+    for (l, m), a in coeffs.items():
+        am = abs(m)
+        if m == 0:
+            ang = np.ones_like(phi)
+        elif m > 0:
+            ang = math.sqrt(2) * np.cos(m * phi)
+        else:
+            ang = math.sqrt(2) * np.sin(am * phi)
+        out += a * P[(l, am)][:, None] * ang[None, :]
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Splines
+def fft_diff(u, axis):
+    """FFT_Diff of ModFFT.F90:25-93 along one axis (domain mapped to 2*pi,
+    Nyquist mode zeroed)."""
+    n = u.shape[axis]
+    U = np.fft.rfft(u, axis=axis)
+    k = np.arange(n // 2 + 1, dtype=np.float64)
+    k[-1] = 0.0 if n % 2 == 0 else k[-1]
+    shape = [1] * u.ndim
+    shape[axis] = k.size
+    U = U * (1j * k).reshape(shape)
+    return np.fft.irfft(U, n=n, axis=axis)
+
+
+def spline_on_sphere(v):
+    """Spline_Build_on_Sphere (ModSpline.F90:121-143).
+
+    v: values on the equiangular grid, shape (nlat+1, nlon, nvar), rows at
+    th_i = i*pi/nlat (both poles included).  Returns the table
+    (4, nvar, nlon, 2*nlat) = u, u1, u2, u12 each Fortran-ordered (m, n, nvar).
+    """
+    nlat = v.shape[0] - 1
+    nlon = v.shape[1]
+    m = 2 * nlat
+    u = np.empty((m, nlon, v.shape[2]))
+    u[:nlat] = v[:nlat]
+    for i in range(nlat):
+        u[nlat + i] = np.roll(v[nlat - i], -(nlon // 2), axis=0)
+    u1 = fft_diff(u, 0)
+    u2 = fft_diff(u, 1)
+    u12 = fft_diff(u1, 1)
+    tab = np.stack([u, u1, u2, u12])          # (4, m, n, nvar)
+    return np.ascontiguousarray(tab.transpose(0, 3, 2, 1))  # (4, nvar, n, m)
+
+
+def equi_theta(nlat):
+    return np.arange(nlat + 1) * (np.pi / nlat)
+
+
+# ---------------------------------------------------------------------------
+@dataclass
+class Cells:
+    """Cell surfaces in the C-ABI layout (see include/rbc3d_gpu.h)."""
+    nlat: int
+    nlon: int
+    th: np.ndarray
+    phi: np.ndarray
+    w: np.ndarray
+    ncell: int
+    celltype: np.ndarray      # (ncell,) int32
+    x: np.ndarray             # (3, N)
+    a3: np.ndarray            # (3, N)
+    detJ: np.ndarray          # (N,)
+    area: np.ndarray          # (ncell,)
+    meshSize: np.ndarray      # (ncell,)
+    spl_x: np.ndarray         # (ncell, 4, 3, nlon, 2nlat)
+    spl_a3: np.ndarray
+    spl_detJ: np.ndarray      # (ncell, 4, 1, nlon, 2nlat)
+    f: np.ndarray = None      # (3, N)
+    g: np.ndarray = None
+    spl_F: np.ndarray = None
+    spl_G: np.ndarray = None
+    centres: np.ndarray = None
+    rotations: list = field(default_factory=list)
+
+
+def _to_points(a):
+    """(ncell, nlat, nlon, k) -> (k, N) with p = cell*nv + ilon*nlat + ilat."""
+    nc, nlat, nlon, k = a.shape
+    return np.ascontiguousarray(a.transpose(3, 0, 2, 1).reshape(k, nc * nlat * nlon))
+
+
+def place_cells(rng, ncell, L, min_dist, inside=None, max_tries=2_000_000):
+    """Uniform centres in the box with rejection at a minimum periodic centre
+    distance; ``inside(c)`` optionally restricts the region (tube)."""
+    L = np.asarray(L, dtype=np.float64)
+    C = []
+    tries = 0
+    while len(C) < ncell:
+        tries += 1
+        if tries > max_tries:
+            raise RuntimeError("cell placement did not converge")
+        c = rng.uniform(0, 1, 3) * L
+        if inside is not None and not inside(c):
+            continue
+        ok = True
+        for d in C:
+            dd = c - d
+            dd -= np.round(dd / L) * L
+            if np.dot(dd, dd) < min_dist ** 2:
+                ok = False
+                break
+        if ok:
+            C.append(c)
+    return np.array(C)
+
+
+def make_cells(rng, ncell, L, min_dist, nlat=25, nlon=50, celltype=0, rc=1.0,
+               inside=None, with_g=False, centres=None):
+    th, phi, w = gauss_grid(nlat, nlon)
+    the = equi_theta(nlat)
+    if centres is None:
+        centres = place_cells(rng, ncell, L, min_dist, inside)
+    X, A3, DJ, SX, SA, SD, F, G, SF, SG = [], [], [], [], [], [], [], [], [], []
+    rots = []
+    areas, msz = [], []
+    for ic in range(ncell):
+        R = random_rotation(rng)
+        rots.append(R)
+        x, n, dj = biconcave_surface(th, phi, R, centres[ic], rc)
+        xe, ne, dje = biconcave_surface(the, phi, R, centres[ic], rc)
+        X.append(x); A3.append(n); DJ.append(dj[..., None])
+        SX.append(spline_on_sphere(xe)); SA.append(spline_on_sphere(ne))
+        SD.append(spline_on_sphere(dje[..., None]))
+        area = float(np.sum(dj * w[:, None]))
+        areas.append(area)
+        msz.append(math.sqrt(area / nlat ** 2))
+        coeff = [random_sh_coeffs(rng) for _ in range(3)]
+        f = np.stack([sh_eval(cf, th, phi) for cf in coeff], axis=-1)
+        fe = np.stack([sh_eval(cf, the, phi) for cf in coeff], axis=-1)
+        F.append(f); SF.append(spline_on_sphere(fe * dje[..., None]))
+        if with_g:
+            coeffg = [random_sh_coeffs(rng) for _ in range(3)]
+            g = np.stack([sh_eval(cf, th, phi) for cf in coeffg], axis=-1)
+            ge = np.stack([sh_eval(cf, the, phi) for cf in coeffg], axis=-1)
+            G.append(g); SG.append(spline_on_sphere(ge * dje[..., None]))
+    cells = Cells(
+        nlat=nlat, nlon=nlon, th=th, phi=phi, w=w, ncell=ncell,
+        celltype=np.full(ncell, celltype, dtype=np.int32),
+        x=_to_points(np.array(X)), a3=_to_points(np.array(A3)),
+        detJ=_to_points(np.array(DJ))[0].copy(),
+        area=np.array(areas), meshSize=np.array(msz),
+        spl_x=np.ascontiguousarray(np.array(SX)), spl_a3=np.ascontiguousarray(np.array(SA)),
+        spl_detJ=np.ascontiguousarray(np.array(SD)),
+        f=_to_points(np.array(F)), spl_F=np.ascontiguousarray(np.array(SF)),
+        centres=centres, rotations=rots)
+    if with_g:
+        cells.g = _to_points(np.array(G))
+        cells.spl_G = np.ascontiguousarray(np.array(SG))
+    else:
+        cells.g = np.zeros_like(cells.f)
+        cells.spl_G = np.zeros_like(cells.spl_F)
+    return cells
+
+
+# ---------------------------------------------------------------------------
+@dataclass
+class Wall:
+    nvert: int
+    nele: int
+    x: np.ndarray          # (3, nvert)
+    e2v: np.ndarray        # (3, nele) int32, 1-based
+    glb: np.ndarray        # (nvert,) int32, 1-based unique vertex id
+    ndof: int
+
+
+def make_tube(radius, Lz, ntheta, nz, centre_xy):
+    """Straight periodic tube along z meshed with ntheta x nz quads split into
+    two Tri3 each.  The ring at z = Lz duplicates the ring at z = 0
+    (indxVertGlb points back to it, as Wall_Build_V2V / GlobData_Init)."""
+    th = np.arange(ntheta) * (2 * np.pi / ntheta)
+    zs = np.arange(nz + 1) * (Lz / nz)
+    nvert = ntheta * (nz + 1)
+    x = np.empty((3, nvert))
+    glb = np.empty(nvert, dtype=np.int32)
+    for k in range(nz + 1):
+        for i in range(ntheta):
+            v = k * ntheta + i
+            x[0, v] = centre_xy[0] + radius * np.cos(th[i])
+            x[1, v] = centre_xy[1] + radius * np.sin(th[i])
+            x[2, v] = zs[k]
+            kk = 0 if k == nz else k
+            glb[v] = kk * ntheta + i + 1
+    tris = []
+    for k in range(nz):
+        for i in range(ntheta):
+            a = k * ntheta + i
+            b = k * ntheta + (i + 1) % ntheta
+            c = (k + 1) * ntheta + i
+            d = (k + 1) * ntheta + (i + 1) % ntheta
+            tris.append((a, b, d))
+            tris.append((a, d, c))
+    e2v = np.ascontiguousarray(np.array(tris, dtype=np.int32).T + 1)
+    return Wall(nvert=nvert, nele=e2v.shape[1], x=x, e2v=e2v, glb=glb, ndof=3 * ntheta * nz)
+
+
+# ---------------------------------------------------------------------------
+# Named workloads (sizes of the benchmark configurations)
+def config(name: str, seed: int = 20261203, ncell: int | None = None):
+    """Build a named workload.  Returns (params dict, Cells, Wall|None)."""
+    rng = np.random.default_rng(seed)
+    eps = 1e-6
+    rc = 3.0
+    alpha = alpha_for_cutoff(rc, eps)
+    if name == "C1":        # 8 cells, L=12, SL only, 64^3
+        L = [12.0] * 3; n = ncell or 8; Nb = [64] * 3; md = 3.0; vr = 1.0; g = False
+    elif name == "C2":      # 256 cells, L=40, SL+DL, 128^3, viscRat 5
+        L = [40.0] * 3; n = ncell or 256; Nb = [128] * 3; md = 2.6; vr = 5.0; g = True
+    elif name == "C5":      # 2048 cells, L=80, SL+DL, 256^3
+        L = [80.0] * 3; n = ncell or 2048; Nb = [256] * 3; md = 2.6; vr = 5.0; g = True
+    elif name == "C3":      # 64 cells in a tube of radius 8, length 48
+        L = [16.5, 16.5, 48.0]; n = ncell or 64; Nb = [96, 96, 256]; md = 3.0; vr = 1.0; g = False
+    else:
+        raise ValueError(name)
+    prm = dict(Lb=L, alpha=alpha, rc=rc, eps=eps, Nb=Nb, P=6, nlat=25, nlon=50,
+               ncelltypes=1, viscRat=[vr], vBkg=[0.0, 0.0, 8.0] if name == "C3" else [0.0, 0.0, 0.0])
+    wall = None
+    inside = None
+    if name == "C3":
+        cxy = (L[0] / 2, L[1] / 2)
+        inside = lambda c: (c[0] - cxy[0]) ** 2 + (c[1] - cxy[1]) ** 2 < 6.5 ** 2
+        wall = make_tube(8.0, L[2], 48, 192, cxy)
+    cells = make_cells(rng, n, L, md, inside=inside, with_g=g)
+    return prm, cells, wall
