@@ -1,0 +1,359 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 Ewald-split boundary-integral matvec.
+
+Metric: Ewald matvec targets/s.  One step = one full matvec of AddIntOnRbcs
+(real-space Stokeslet + stresslet pair sums with the same-cell mask, FP64
+self and near-singular polar-patch corrections, linear term) plus
+PME_Distrib_Source / PME_Transform / PME_Add_Interp_Vel, evaluated at every
+cell surface point (c1 = c2 = 1/(4 pi), as CalcVelocityField), on the
+256-cell periodic workload: L = 40, 25x50 surface grid per cell (320,000
+targets), alpha = 1.5757 (rc = 3), PME mesh 128^3, B-spline order 6,
+viscosity ratio 5.  Inputs are seeded synthetic cells (biconcave shape,
+random placement and rotation, SH densities), generated identically for the
+GPU and the CPU oracle.
+
+  value  -- FP32-compensated matvec with every input resident in HBM.
+  e2e    -- the same matvec through the C ABI with host buffers: upload of
+            geometry, densities and spline tables from pinned memory, and the
+            download of the velocities, inside the timed region.
+
+`python bench.py --impl reference` times the CPU oracle (FP64 restatement
+of the reference path, all host threads) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+if int(os.environ.get("WORLD_SIZE", "1")) > 1 and "LOCAL_RANK" in os.environ:
+    # one process per GPU: each rank sees only its own device
+    os.environ["CUDA_VISIBLE_DEVICES"] = os.environ["LOCAL_RANK"]
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+# Algorithmic flops per unit of work (plain arithmetic of the reference
+# formulas; add/sub/mul/div/sqrt = 1 flop, FMA = 2 flops):
+FLOP_PAIR_SL = 39   # EwaldCoeff_SL lerp + Stokeslet term, ModIntOnRbcs.F90:91-97
+FLOP_PAIR_DL = 27   # EwaldCoeff_DL lerp + stresslet term, ModIntOnRbcs.F90:99-106
+FLOP_SELFQ_SL = 294  # one RBC_SingInt patch point, SL: 2 bicubic 3-var interps + kernel
+FLOP_SELFQ_SLDL = 550  # one patch point, SL+DL: 4 bicubic 3-var interps + both kernels
+
+WORKLOAD = {
+    "workload": "Ewald-split SL+DL matvec, 256 biconcave cells, 25x50 grid (320000 targets), "
+                "periodic L=40, rc=3 (alpha=1.5757), PME 128^3 P=6, viscRat=5",
+    "config": "C2",
+}
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self):
+        self.p = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if not self.p:
+            return None
+        time.sleep(0.25)
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = max(mx, float(r[2]))
+                for i, n in enumerate(names):
+                    if r[5 + i].strip().lower() == "active":
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                pass
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return None
+    import torch.distributed as dist
+    dist.init_process_group("gloo")
+    return dist
+
+
+def dist_max(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def make_inputs(seed):
+    from rbc3d_gb300 import geometry as G
+    prm, cells, _ = G.config("C2", seed=seed)
+    return prm, cells
+
+
+def oracle_lib():
+    from rbc3d_gb300.abi import Library
+    path = os.path.join(HERE, "oracle", "liboracle_rbc3d.so")
+    if not os.path.exists(path):
+        subprocess.run(["make", "-C", os.path.join(HERE, "oracle"), "-s"], check=True)
+    return Library(path, "rbc3d_oracle_")
+
+
+def time_oracle(prm, cells, steps, threads=None):
+    """Full FP64 CPU matvec (oracle) on the host cores; returns (s per step, cores)."""
+    import ctypes
+    from rbc3d_gb300.abi import Context, TLIST_RBC, TERM_ALL
+    L = oracle_lib()
+    cores = os.cpu_count() or 1
+    setn = getattr(L.lib, "rbc3d_oracle_set_threads")
+    setn.restype = ctypes.c_int
+    setn.argtypes = [ctypes.c_int]
+    used = setn(threads or cores)
+    ctx = Context(L, prm)
+    ctx.set_cells(cells)
+    ctx.set_cell_density(f=cells.f, g=cells.g, spl_F=cells.spl_F, spl_G=cells.spl_G)
+    c = 1.0 / (4 * math.pi)
+    ts = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        ctx.matvec(TLIST_RBC, c, c, TERM_ALL)
+        ts.append(time.perf_counter() - t0)
+    ctx.close()
+    return ts, used
+
+
+def run_reference(args, dist):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    prm, cells = make_inputs(args.seed)
+    N = cells.x.shape[1]
+    ts, cores = time_oracle(prm, cells, args.warmup + args.steps)
+    t = sum(ts[args.warmup:]) / max(args.steps, 1)
+    val = N / t
+    line = {"impl": "reference", "metric": "Ewald matvec targets/s", "value": val, "unit": "targets/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)", "config": WORKLOAD,
+            "cpu_baseline": {"value": val, "unit": "targets/s", "cores": cores, "kind": "port",
+                             "sample": f"full matvec, {N} targets, {args.steps} timed steps"},
+            "e2e": {"value": val, "unit": "targets/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--seed", type=int, default=20261203)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    dist = dist_init()
+    if args.impl == "reference":
+        return run_reference(args, dist)
+
+    rank = int(os.environ.get("RANK", "0"))
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    from rbc3d_gb300 import build as B
+    B.build()
+    from rbc3d_gb300 import library
+    from rbc3d_gb300.abi import FP32C, FP64, TERM_ALL, TLIST_RBC, Context, STAGES
+
+    t0 = time.perf_counter()
+    prm, cells = make_inputs(args.seed + rank)
+    log(f"inputs generated in {time.perf_counter() - t0:.1f}s")
+    N = cells.x.shape[1]
+    lib = library()
+    ctx = Context(lib, prm)
+    ctx.set_cells(cells)
+    ctx.set_cell_density(f=cells.f, g=cells.g, spl_F=cells.spl_F, spl_G=cells.spl_G)
+    c = 1.0 / (4 * math.pi)
+
+    def step(prec):
+        ctx.matvec(TLIST_RBC, c, c, TERM_ALL, prec, device_only=True)
+
+    # ---- FP32-compensated matvec, inputs resident in HBM
+    for _ in range(args.warmup):
+        step(FP32C)
+    counts = ctx.counts()
+    l0 = counts["kernel_launches"]
+    clk = Clocks()
+    barrier(dist)
+    clk.start()
+    ctx.set_profiling(1)
+    ctx.timer_start()
+    for _ in range(args.steps):
+        step(FP32C)
+    ms = ctx.timer_stop()
+    clocks = clk.stop()
+    stages = ctx.stage_times()
+    ctx.set_profiling(0)
+    counts = ctx.counts()
+    launches = counts["kernel_launches"] - l0
+    ms = dist_max(dist, ms)
+    ms_step = ms / args.steps
+    value = ws * N / (ms_step * 1e-3)
+
+    # ---- FP64 plain form (same algorithm, everything FP64)
+    for _ in range(2):
+        step(FP64)
+    k64 = max(2, args.steps // 3)
+    ctx.timer_start()
+    for _ in range(k64):
+        step(FP64)
+    ms64 = dist_max(dist, ctx.timer_stop()) / k64
+    fp64_value = ws * N / (ms64 * 1e-3)
+
+    # ---- end to end through the C ABI with pinned host buffers
+    pin = {}
+    for k in ("x", "a3", "detJ", "area", "meshSize", "spl_x", "spl_a3", "spl_detJ", "f", "g", "spl_F", "spl_G"):
+        a = np.ascontiguousarray(getattr(cells, k), dtype=np.float64)
+        p = lib.pinned(a.shape)
+        p[...] = a
+        pin[k] = p
+    vout = lib.pinned((3, N))
+
+    class PinnedCells:
+        pass
+
+    pc = PinnedCells()
+    for k in ("nlat", "nlon", "th", "phi", "w", "ncell", "celltype"):
+        setattr(pc, k, getattr(cells, k))
+    for k, p in pin.items():
+        setattr(pc, k, p)
+    h2d = sum(p.nbytes for p in pin.values())
+    d2h = vout.nbytes
+
+    def e2e_step():
+        ctx.set_cells(pc)
+        ctx.set_cell_density(f=pc.f, g=pc.g, spl_F=pc.spl_F, spl_G=pc.spl_G)
+        vout[...] = 0.0
+        ctx.matvec(TLIST_RBC, c, c, TERM_ALL, FP32C, v=vout)
+
+    for _ in range(2):
+        e2e_step()
+    barrier(dist)
+    te = time.perf_counter()
+    ke = max(3, args.steps // 2)
+    for _ in range(ke):
+        e2e_step()
+    te = dist_max(dist, (time.perf_counter() - te) / ke)
+    e2e_value = ws * N / te
+
+    # ---- roofline of the dominant stage (device time measured above)
+    nq = 200  # RBC_SingInt points per target on the 25x50 grid (nrad 10 x nazm 20)
+    peak32 = lib.fma_peak(FP32C)
+    peak64 = lib.fma_peak(FP64)
+    st_ms = {k: v[0] / args.steps for k, v in stages.items()}
+    dom = max(st_ms, key=lambda k: st_ms[k])
+    pairs = counts["pairs_within_rc"]
+    roof = None
+    if dom == "self":
+        flops = counts["self_items"] * nq * FLOP_SELFQ_SLDL
+        ach = flops / (st_ms["self"] * 1e-3) / 1e12
+        roof = {"kernel": "k_self (RBC_SingInt, FP64)", "bound": "fp64", "achieved": ach, "peak": peak64,
+                "unit": "TFLOP/s", "frac": ach / peak64, "traffic": None,
+                "peak_source": "measured FP64 FMA chain (rbc3d_fma_peak), same GPU, same run"}
+    elif dom == "pair":
+        flops = pairs * (FLOP_PAIR_SL + FLOP_PAIR_DL)
+        ach = flops / (st_ms["pair"] * 1e-3) / 1e12
+        roof = {"kernel": "k_pair32 (AddIntOnRbcs pair sums, FP32)", "bound": "fp32", "achieved": ach,
+                "peak": peak32, "unit": "TFLOP/s", "frac": ach / peak32, "traffic": None,
+                "peak_source": "measured FP32 FMA chain (rbc3d_fma_peak), same GPU, same run"}
+    else:
+        roof = {"kernel": dom, "bound": "fp64", "achieved": None, "peak": peak64, "unit": "TFLOP/s",
+                "frac": None, "traffic": None}
+    tpath = os.path.join(HERE, "profiles", "traffic.json")
+    if os.path.exists(tpath) and roof is not None:
+        try:
+            tr = json.load(open(tpath))
+            roof["traffic"] = tr.get(roof["kernel"].split()[0])
+        except Exception:
+            pass
+
+    # ---- CPU baseline (rank 0, N = 1 only): oracle, all host threads
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        try:
+            ts, cores = time_oracle(prm, cells, 1)
+            cpu = {"value": N / ts[0], "unit": "targets/s", "cores": cores, "kind": "port",
+                   "sample": f"one full FP64 matvec of the same workload ({N} targets), {ts[0]:.1f}s"}
+        except Exception as e:  # the baseline is reported, not required
+            cpu = {"value": None, "unit": "targets/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"unavailable: {e}"}
+
+    if rank == 0:
+        line = {
+            "metric": "Ewald matvec targets/s", "value": value, "unit": "targets/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32c+f64corr",
+            "data": "synthetic (seeded biconcave cells, SH densities)",
+            "config": dict(WORKLOAD, targets=N, l2="working set (spline tables 307 MB, PME grids) > 129 MB L2"),
+            "fp64_plain": {"value": fp64_value, "unit": "targets/s", "ms_per_step": ms64,
+                           "fp32c_over_fp64": value / fp64_value},
+            "e2e": {"value": e2e_value, "unit": "targets/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": te * 1e3},
+            "stages_ms_per_step": st_ms,
+            "counts": {k: counts[k] for k in ("pairs_within_rc", "nbr_items", "nearsing_items", "self_items")},
+            "roofline": roof,
+            "fma_peaks_tflops": {"fp32": peak32, "fp64": peak64},
+            "cpu_baseline": cpu,
+            "gpu_launches": launches,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -92,6 +92,9 @@ typedef struct rbc3d_counts {
   long long wall_pairs;       /* (target, triangle) pairs within rc */
   long long wall_duffy;       /* of which integrated with Duffy's rule */
   int nbr_overflow;           /* targets whose neighbour list exceeded RBC3D_NBR_MAX */
+  long long kernel_launches;  /* kernels of this library launched so far on the context */
+  long long screen_misses;    /* FP32C near-singular screen: screened items the FP64
+                                 test would correct (counted with RBC3D_VERIFY_SCREEN=1) */
 } rbc3d_counts;
 
 typedef struct rbc3d_solve_opts {
@@ -186,7 +189,8 @@ rbc3d_status rbc3d_pme_add_interp_vel(rbc3d_ctx* ctx, int tlist, double* v);
 /* Composite matvec, all terms on the device with one download: the sum that
  * Compute_Rhs / CalcVelocityField / Compute_Wall_Residual_Vel assemble from
  * the L2 calls above (ModVelSolver.F90:476-490, ModPostProcess.F90:39-51,
- * ModNoSlip.F90:175-184), without background velocity.  v += result. */
+ * ModNoSlip.F90:175-184), without background velocity.  v += result; with
+ * v == NULL the result stays in device memory (no transfer). */
 rbc3d_status rbc3d_matvec(rbc3d_ctx* ctx, int tlist, double c1, double c2,
                           unsigned terms, int prec, double* v);
 
@@ -207,6 +211,28 @@ rbc3d_status rbc3d_calc_velocity_field(rbc3d_ctx* ctx, int tlist, int prec,
                                        double* v);
 
 rbc3d_status rbc3d_get_counts(const rbc3d_ctx* ctx, rbc3d_counts* out);
+
+/* ---- device timing (replaces the per-step MPI_WTime print of TimeInt_*,
+ * ModTimeInt.F90:119,166-174, with CUDA events on the context stream) ---- */
+#define RBC3D_NSTAGE 8
+/* Stages: 0 pair sums, 1 self patch, 2 near-singular, 3 linear term,
+ * 4 wall quadrature / self-wall SpMV, 5 PME spread, 6 PME FFT + influence,
+ * 7 PME gather. */
+rbc3d_status rbc3d_set_profiling(rbc3d_ctx* ctx, int on);
+/* Sum of the device time per stage (ms) since the last call, and the number of
+ * recorded executions per stage; resets the record. */
+rbc3d_status rbc3d_stage_times(rbc3d_ctx* ctx, double ms[RBC3D_NSTAGE], int count[RBC3D_NSTAGE]);
+/* Event pair on the context stream around any sequence of calls. */
+rbc3d_status rbc3d_timer_start(rbc3d_ctx* ctx);
+rbc3d_status rbc3d_timer_stop(rbc3d_ctx* ctx, double* ms);
+
+/* Page-locked host buffers for the caller's staging arrays (faster uploads). */
+rbc3d_status rbc3d_host_alloc(unsigned long long bytes, void** out);
+rbc3d_status rbc3d_host_free(void* p);
+/* Measured FMA throughput of this GPU (TFLOP/s, 2 flops per FMA) for FP32
+ * (prec = RBC3D_FP32C) or FP64 (RBC3D_FP64): a register-resident FMA chain
+ * over all SMs, used as the roofline of the CUDA-core-bound kernels. */
+rbc3d_status rbc3d_fma_peak(int prec, double* tflops);
 
 #ifdef __cplusplus
 }

@@ -31,7 +31,8 @@ class Counts(C.Structure):
     _fields_ = [("pairs_within_rc", C.c_longlong), ("nbr_items", C.c_longlong),
                 ("nearsing_items", C.c_longlong), ("self_items", C.c_longlong),
                 ("wall_pairs", C.c_longlong), ("wall_duffy", C.c_longlong),
-                ("nbr_overflow", C.c_int)]
+                ("nbr_overflow", C.c_int), ("kernel_launches", C.c_longlong),
+                ("screen_misses", C.c_longlong)]
 
 
 class SolveOpts(C.Structure):
@@ -96,6 +97,17 @@ SIGNATURES = [
     ("calc_velocity_field", C.c_int, [_vp, C.c_int, C.c_int, _dp]),
     ("get_counts", C.c_int, [_vp, C.POINTER(Counts)]),
 ]
+# Device-timing entry points of the GPU library only.
+GPU_SIGNATURES = [
+    ("set_profiling", C.c_int, [_vp, C.c_int]),
+    ("stage_times", C.c_int, [_vp, _dp, _ip]),
+    ("timer_start", C.c_int, [_vp]),
+    ("timer_stop", C.c_int, [_vp, _dp]),
+    ("host_alloc", C.c_int, [C.c_ulonglong, C.POINTER(C.c_void_p)]),
+    ("host_free", C.c_int, [_vp]),
+    ("fma_peak", C.c_int, [C.c_int, _dp]),
+]
+STAGES = ["pair", "self", "near", "linear", "walls", "pme_spread", "pme_fft_infl", "pme_gather"]
 
 
 def _ptr(a, dtype=np.float64):
@@ -125,6 +137,31 @@ class Library:
             f.restype = res
             f.argtypes = args
             self.fn[name] = f
+        for name, res, args in GPU_SIGNATURES:
+            f = getattr(self.lib, prefix + name, None)
+            if f is not None:
+                f.restype = res
+                f.argtypes = args
+                self.fn[name] = f
+
+    def fma_peak(self, prec):
+        t = C.c_double()
+        st = self.fn["fma_peak"](prec, C.byref(t))
+        if st:
+            raise RBC3DError(st, "fma_peak")
+        return t.value
+
+    def pinned(self, shape, dtype=np.float64):
+        """numpy array in page-locked host memory (freed with the library)."""
+        n = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        p = C.c_void_p()
+        st = self.fn["host_alloc"](n, C.byref(p))
+        if st:
+            raise RBC3DError(st, "host_alloc")
+        self._pinned = getattr(self, "_pinned", [])
+        self._pinned.append(p)
+        buf = (C.c_char * n).from_address(p.value)
+        return np.frombuffer(buf, dtype=dtype).reshape(shape)
 
     def ewald_prms(self, alpha, eps, Lb, P):
         rc = C.c_double()
@@ -196,8 +233,11 @@ class Context:
         return self.L.fn["num_targets"](self.h, tlist)
 
     def _vout(self, tlist, v):
+        n = self.num_targets(tlist)
+        if n < 0:
+            raise RBC3DError(1, f"bad target list {tlist}")
         if v is None:
-            v = np.zeros((3, self.num_targets(tlist)))
+            v = np.zeros((3, n))
         assert v.dtype == np.float64 and v.flags.c_contiguous
         return v
 
@@ -222,10 +262,31 @@ class Context:
         self._check(self.L.fn["pme_add_interp_vel"](self.h, tlist, _ptr(v)))
         return v
 
-    def matvec(self, tlist, c1, c2, terms=TERM_ALL, prec=FP64, v=None):
+    def matvec(self, tlist, c1, c2, terms=TERM_ALL, prec=FP64, v=None, device_only=False):
+        if device_only:
+            self._check(self.L.fn["matvec"](self.h, tlist, c1, c2, terms, prec, None))
+            return None
         v = self._vout(tlist, v)
         self._check(self.L.fn["matvec"](self.h, tlist, c1, c2, terms, prec, _ptr(v)))
         return v
+
+    # ---- device timing (GPU library)
+    def set_profiling(self, on):
+        self._check(self.L.fn["set_profiling"](self.h, int(on)))
+
+    def stage_times(self):
+        ms = (C.c_double * 8)()
+        cnt = (C.c_int * 8)()
+        self._check(self.L.fn["stage_times"](self.h, ms, cnt))
+        return {s: (ms[i], cnt[i]) for i, s in enumerate(STAGES)}
+
+    def timer_start(self):
+        self._check(self.L.fn["timer_start"](self.h))
+
+    def timer_stop(self):
+        ms = C.c_double()
+        self._check(self.L.fn["timer_stop"](self.h, C.byref(ms)))
+        return ms.value
 
     # ---- L3
     def calc_velocity_field(self, tlist, prec=FP64):

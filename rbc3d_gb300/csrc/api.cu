@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -51,6 +52,22 @@ void host_gauleg(double x1, double x2, int n, double* x, double* w) {
     w[k] = 2.0 * xl / ((1.0 - z[k] * z[k]) * pp[k] * pp[k]);
     w[n - 1 - k] = w[k];
   }
+}
+
+StageScope::StageScope(rbc3d_ctx* ctx, int stage) : c(ctx), slot(-1) {
+  if (!c->prof) return;
+  if (2 * (c->nrec + 1) > c->evpool.size()) {
+    size_t old = c->evpool.size();
+    c->evpool.resize(old + 512);
+    for (size_t i = old; i < c->evpool.size(); ++i) cudaEventCreate(&c->evpool[i]);
+    c->rec_stage.resize(c->evpool.size() / 2);
+  }
+  slot = (int)c->nrec++;
+  c->rec_stage[slot] = stage;
+  cudaEventRecord(c->evpool[2 * slot], c->st);
+}
+StageScope::~StageScope() {
+  if (slot >= 0) cudaEventRecord(c->evpool[2 * slot + 1], c->st);
 }
 
 namespace {
@@ -113,7 +130,7 @@ rbc3d_status upload_splines(rbc3d_ctx* ctx, const double* h, int nvar, int set) 
   DBuf<double> tmp;
   CUDA_TRY(tmp.upload(h, cnt, ctx->st));
   long long total = (long long)ctx->ncell * per;
-  k_repack<<<nblk(total, 256), 256, 0, ctx->st>>>(ctx->ncell, ctx->m, ctx->nlon, nvar, set, tmp.p, ctx->spl.p);
+  { k_repack<<<nblk(total, 256), 256, 0, ctx->st>>>(ctx->ncell, ctx->m, ctx->nlon, nvar, set, tmp.p, ctx->spl.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaStreamSynchronize(ctx->st));
   return RBC3D_OK;
@@ -149,6 +166,7 @@ rbc3d_status rbcs_dev(rbc3d_ctx* ctx, int which, double c1, double c2, int prec,
   for (int attempt = 0; attempt < 2; ++attempt) {
     CUDA_TRY(cudaMemsetAsync(ctx->dcnt.p, 0, sizeof(unsigned long long) * 3, ctx->st));
     if (terms & RBC3D_TERM_REAL || corr) {
+      StageScope sc(ctx, 0);
       if ((s = run_pair_sum(ctx, which, (terms & RBC3D_TERM_REAL) ? c1 : 0.0, (terms & RBC3D_TERM_REAL) ? c2 : 0.0,
                             prec, corr)))
         return s;
@@ -166,18 +184,28 @@ rbc3d_status rbcs_dev(rbc3d_ctx* ctx, int which, double c1, double c2, int prec,
   }
   if (corr) {
     CUDA_TRY(cudaMemsetAsync(ctx->dcnt.p + 3, 0, sizeof(unsigned long long), ctx->st));
-    if ((s = run_self_corr(ctx, which, c1, c2))) return s;
-    if ((s = run_near_corr(ctx, which, c1, c2, prec))) return s;
+    CUDA_TRY(cudaMemsetAsync(ctx->dcnt.p + 6, 0, sizeof(unsigned long long), ctx->st));
+    {
+      StageScope sc(ctx, 1);
+      if ((s = run_self_corr(ctx, which, c1, c2))) return s;
+    }
+    {
+      StageScope sc(ctx, 2);
+      if ((s = run_near_corr(ctx, which, c1, c2, prec))) return s;
+    }
   }
-  if (terms & RBC3D_TERM_LINEAR)
+  if (terms & RBC3D_TERM_LINEAR) {
+    StageScope sc(ctx, 3);
     if ((s = run_linear(ctx, which, c2))) return s;
-  unsigned long long h[4];
+  }
+  unsigned long long h[7];
   CUDA_TRY(cudaMemcpyAsync(h, ctx->dcnt.p, sizeof(h), cudaMemcpyDeviceToHost, ctx->st));
   CUDA_TRY(cudaStreamSynchronize(ctx->st));
   ctx->counts.pairs_within_rc = (long long)h[1];
   if (corr) {
     ctx->counts.nbr_items = (long long)h[0];
     ctx->counts.nearsing_items = (long long)h[3];
+    ctx->counts.screen_misses = (long long)h[6];
     ctx->counts.self_items = (which == RBC3D_TLIST_RBC) ? t.n : 0;
   }
   ctx->counts.nbr_overflow = (int)h[2];
@@ -195,13 +223,23 @@ rbc3d_status matvec_dev(rbc3d_ctx* ctx, int which, double c1, double c2, unsigne
   if (terms & (RBC3D_TERM_REAL | RBC3D_TERM_CORR | RBC3D_TERM_LINEAR))
     if ((s = rbcs_dev(ctx, which, c1, c2, prec, terms))) return s;
   if (terms & RBC3D_TERM_WALLS) {
+    StageScope sc(ctx, 4);
     if (which == RBC3D_TLIST_WALL) { if ((s = run_wall_self(ctx, c1))) return s; }
     else if ((s = run_wall_quad(ctx, which, c1, prec))) return s;
   }
   if (terms & RBC3D_TERM_PME) {
-    if ((s = pme_spread(ctx, c1, c2, 1, (terms & RBC3D_TERM_WALLS) ? 1 : 0, prec))) return s;
-    if ((s = pme_transform(ctx))) return s;
-    if ((s = pme_gather(ctx, which))) return s;
+    {
+      StageScope sc(ctx, 5);
+      if ((s = pme_spread(ctx, c1, c2, 1, (terms & RBC3D_TERM_WALLS) ? 1 : 0, prec))) return s;
+    }
+    {
+      StageScope sc(ctx, 6);
+      if ((s = pme_transform(ctx))) return s;
+    }
+    {
+      StageScope sc(ctx, 7);
+      if ((s = pme_gather(ctx, which))) return s;
+    }
   }
   return RBC3D_OK;
 }
@@ -239,6 +277,10 @@ rbc3d_status rbc3d_create(const rbc3d_params* prm, rbc3d_ctx** out) {
   rbc3d_ctx* ctx = new rbc3d_ctx();
   ctx->prm = *prm;
   cudaGetDevice(&ctx->device);
+  {
+    const char* e = getenv("RBC3D_VERIFY_SCREEN");
+    ctx->verify_screen = e && e[0] == '1';
+  }
   for (int d = 0; d < 3; ++d) ctx->iLb[d] = 1. / prm->Lb[d];
   for (int l = 0; l < prm->ncelltypes; ++l) {  // initCOEFs, ModConf.F90:327-344
     if (prm->viscRat[l] > 0) { ctx->Acoef[l] = 1. + prm->viscRat[l]; ctx->Bcoef[l] = 1. - prm->viscRat[l]; }
@@ -298,6 +340,8 @@ rbc3d_status rbc3d_destroy(rbc3d_ctx* ctx) {
   if (!ctx) return RBC3D_OK;
   pme_release(ctx);
   if (ctx->st) cudaStreamSynchronize(ctx->st);
+  for (cudaEvent_t e : ctx->evpool) cudaEventDestroy(e);
+  if (ctx->t0) { cudaEventDestroy(ctx->t0); cudaEventDestroy(ctx->t1); }
   cudaStream_t st = ctx->st;
   delete ctx;
   if (st) cudaStreamDestroy(st);
@@ -379,6 +423,11 @@ rbc3d_status rbc3d_set_cells(rbc3d_ctx* ctx, int ncell, const int* celltype, con
   if (ncell == 0) return RBC3D_OK;
   size_t N = ctx->npt;
   ctx->h_celltype.assign(celltype, celltype + ncell);
+  {
+    double mn = meshSize[0];
+    for (int c = 1; c < ncell; ++c) mn = std::min(mn, meshSize[c]);
+    ctx->near_rthr = 0.5 * mn;
+  }
   CUDA_TRY(ctx->celltype.upload(celltype, ncell, ctx->st));
   CUDA_TRY(ctx->x.upload(x, 3 * N, ctx->st)); CUDA_TRY(ctx->a3.upload(a3, 3 * N, ctx->st));
   CUDA_TRY(ctx->detJ.upload(detJ, N, ctx->st));
@@ -400,8 +449,8 @@ rbc3d_status rbc3d_set_cells(rbc3d_ctx* ctx, int ncell, const int* celltype, con
   CUDA_TRY(Ac.upload(ctx->Acoef, RBC3D_MAX_CELLTYPES, ctx->st));
   CUDA_TRY(t.x.alloc(3 * N)); CUDA_TRY(t.Acoef.alloc(N)); CUDA_TRY(t.meta.alloc(N));
   CUDA_TRY(cudaMemcpyAsync(t.x.p, ctx->x.p, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, ctx->st));
-  k_fill_acoef<<<nblk(N, 256), 256, 0, ctx->st>>>(t.n, nv, ctx->celltype.p, Ac.p, t.Acoef.p);
-  k_fill_meta<<<nblk(N, 256), 256, 0, ctx->st>>>(t.n, nv, ctx->nlat, t.meta.p);
+  { k_fill_acoef<<<nblk(N, 256), 256, 0, ctx->st>>>(t.n, nv, ctx->celltype.p, Ac.p, t.Acoef.p); ++ctx->launches; }
+  { k_fill_meta<<<nblk(N, 256), 256, 0, ctx->st>>>(t.n, nv, ctx->nlat, t.meta.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   int want = 12 * std::max(ctx->npt, 1024);
   if (ctx->items_cap < want) { ctx->items_cap = want; CUDA_TRY(ctx->items.alloc(want)); }
@@ -457,7 +506,7 @@ rbc3d_status rbc3d_set_walls(rbc3d_ctx* ctx, int nvert, int nele, const double* 
   t.sorted = false;
   CUDA_TRY(t.x.upload(x, 3 * (size_t)nvert, ctx->st));
   CUDA_TRY(t.Acoef.alloc(nvert)); CUDA_TRY(t.meta.alloc(nvert));
-  if (nvert) k_fill_const<<<nblk(nvert, 256), 256, 0, ctx->st>>>(nvert, make_int4(-1000, -1, -1, 0), 2.0, t.meta.p, t.Acoef.p);
+  if (nvert) { k_fill_const<<<nblk(nvert, 256), 256, 0, ctx->st>>>(nvert, make_int4(-1000, -1, -1, 0), 2.0, t.meta.p, t.Acoef.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaStreamSynchronize(ctx->st));
   return RBC3D_OK;
@@ -489,7 +538,7 @@ rbc3d_status rbc3d_set_raw_targets(rbc3d_ctx* ctx, int n, const double* x) {
   if (n == 0) return RBC3D_OK;
   CUDA_TRY(t.x.upload(x, 3 * (size_t)n, ctx->st));
   CUDA_TRY(t.Acoef.alloc(n)); CUDA_TRY(t.meta.alloc(n));
-  k_fill_const<<<nblk(n, 256), 256, 0, ctx->st>>>(n, make_int4(-1, -1, -1, 0), 2.0, t.meta.p, t.Acoef.p);
+  { k_fill_const<<<nblk(n, 256), 256, 0, ctx->st>>>(n, make_int4(-1, -1, -1, 0), 2.0, t.meta.p, t.Acoef.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaStreamSynchronize(ctx->st));
   return RBC3D_OK;
@@ -544,10 +593,48 @@ rbc3d_status rbc3d_pme_add_interp_vel(rbc3d_ctx* ctx, int which, double* v) {
 
 rbc3d_status rbc3d_matvec(rbc3d_ctx* ctx, int which, double c1, double c2, unsigned terms, int prec, double* v) {
   TargetSet* t = ctx ? tset(ctx, which) : nullptr;
-  if (!t || !v || (prec != RBC3D_FP64 && prec != RBC3D_FP32C)) return ctx_fail(ctx, RBC3D_ERR_ARG, "matvec");
+  if (!t || (prec != RBC3D_FP64 && prec != RBC3D_FP32C)) return ctx_fail(ctx, RBC3D_ERR_ARG, "matvec");
   rbc3d_status s = matvec_dev(ctx, which, c1, c2, terms, prec);
   if (s) return s;
+  if (!v) return RBC3D_OK;  // result stays on the device
   return finish_add(ctx, *t, v);
+}
+
+rbc3d_status rbc3d_set_profiling(rbc3d_ctx* ctx, int on) {
+  if (!ctx) return RBC3D_ERR_ARG;
+  ctx->prof = on != 0;
+  ctx->nrec = 0;
+  return RBC3D_OK;
+}
+
+rbc3d_status rbc3d_stage_times(rbc3d_ctx* ctx, double ms[RBC3D_NSTAGE], int count[RBC3D_NSTAGE]) {
+  if (!ctx || !ms) return RBC3D_ERR_ARG;
+  for (int i = 0; i < RBC3D_NSTAGE; ++i) { ms[i] = 0.; if (count) count[i] = 0; }
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  for (size_t r = 0; r < ctx->nrec; ++r) {
+    float e = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&e, ctx->evpool[2 * r], ctx->evpool[2 * r + 1]));
+    ms[ctx->rec_stage[r]] += e;
+    if (count) count[ctx->rec_stage[r]]++;
+  }
+  ctx->nrec = 0;
+  return RBC3D_OK;
+}
+
+rbc3d_status rbc3d_timer_start(rbc3d_ctx* ctx) {
+  if (!ctx) return RBC3D_ERR_ARG;
+  if (!ctx->t0) { CUDA_TRY(cudaEventCreate(&ctx->t0)); CUDA_TRY(cudaEventCreate(&ctx->t1)); }
+  CUDA_TRY(cudaEventRecord(ctx->t0, ctx->st));
+  return RBC3D_OK;
+}
+rbc3d_status rbc3d_timer_stop(rbc3d_ctx* ctx, double* ms) {
+  if (!ctx || !ms || !ctx->t0) return RBC3D_ERR_ARG;
+  CUDA_TRY(cudaEventRecord(ctx->t1, ctx->st));
+  CUDA_TRY(cudaEventSynchronize(ctx->t1));
+  float e = 0.f;
+  CUDA_TRY(cudaEventElapsedTime(&e, ctx->t0, ctx->t1));
+  *ms = e;
+  return RBC3D_OK;
 }
 
 // CalcVelocityField, ModPostProcess.F90:29-63 (overwrites v)
@@ -576,10 +663,15 @@ rbc3d_status rbc3d_compute_wall_residual_vel(rbc3d_ctx* ctx, int prec, double* v
 rbc3d_status rbc3d_wall_matmult(rbc3d_ctx* ctx, int prec, const double* u, double* y) {
   if (!ctx || !u || !y) return RBC3D_ERR_ARG;
   int n = ctx->wall.ndof;
-  DBuf<double> du, dy;
+  DBuf<double> du, dy, fsave;
   CUDA_TRY(du.upload(u, n, ctx->st));
   CUDA_TRY(dy.alloc(n));
+  // MyMatMult overwrites the wall density; keep the caller's density intact
+  size_t nf = 3 * (size_t)ctx->wall.nvert;
+  CUDA_TRY(fsave.alloc(nf));
+  CUDA_TRY(cudaMemcpyAsync(fsave.p, ctx->wall.f.p, sizeof(double) * nf, cudaMemcpyDeviceToDevice, ctx->st));
   rbc3d_status s = wall_matmult_dev(ctx, prec, du.p, dy.p);
+  CUDA_TRY(cudaMemcpyAsync(ctx->wall.f.p, fsave.p, sizeof(double) * nf, cudaMemcpyDeviceToDevice, ctx->st));
   if (s) return s;
   CUDA_TRY(cudaMemcpyAsync(y, dy.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->st));
   CUDA_TRY(cudaStreamSynchronize(ctx->st));
@@ -595,7 +687,19 @@ rbc3d_status rbc3d_no_slip_wall(rbc3d_ctx* ctx, const rbc3d_solve_opts* opt, con
 rbc3d_status rbc3d_get_counts(const rbc3d_ctx* ctx, rbc3d_counts* out) {
   if (!ctx || !out) return RBC3D_ERR_ARG;
   *out = ctx->counts;
+  out->kernel_launches = ctx->launches;
   return RBC3D_OK;
+}
+
+rbc3d_status rbc3d_host_alloc(unsigned long long bytes, void** out) {
+  if (!out) return RBC3D_ERR_ARG;
+  return cudaMallocHost(out, bytes) == cudaSuccess ? RBC3D_OK : RBC3D_ERR_NOMEM;
+}
+rbc3d_status rbc3d_host_free(void* p) { return cudaFreeHost(p) == cudaSuccess ? RBC3D_OK : RBC3D_ERR_CUDA; }
+
+rbc3d_status rbc3d_fma_peak(int prec, double* tflops) {
+  if (!tflops) return RBC3D_ERR_ARG;
+  return fma_peak(prec, tflops);
 }
 
 }  // extern "C"

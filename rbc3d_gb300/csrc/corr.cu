@@ -52,6 +52,9 @@ struct CorrArgs {
   const unsigned long long* nitems;
   int cap;
   unsigned long long* cnt;
+  int screen;  // screen items before the FP64 projection (FP32C path)
+  double rthr;  // FP32C path: cross-surface pairs closer than rthr are added here in FP64
+  int verify;  // evaluate screened items in FP64 anyway and count disagreements
 };
 
 __device__ __forceinline__ const double* set_ptr(const CorrArgs& a, int cell, int set) {
@@ -243,7 +246,7 @@ __device__ void find_projection(const double* sx, int m, int n, const double* xt
 
 // RBC_NearSingInt_Subtract: lane = latitude row of PolarPatch_FindPoints
 __device__ void near_subtract(const CorrArgs& a, int cell, double c1, double c2, const double* xi, double th0,
-                              double phi0, double radPat, double* dv) {
+                              double phi0, double radPat, double rthr, double* dv) {
   const int lane = threadIdx.x & 31;
   dv[0] = dv[1] = dv[2] = 0.;
   const double eps = 1.e-10;
@@ -272,6 +275,9 @@ __device__ void near_subtract(const CorrArgs& a, int cell, double c1, double c2,
       if (rr > a.T.rc) continue;
       double dd = dist_on_sphere(th0, phi0, thi, a.phi[ilon]);
       double mask = mask64(a.T, dd / radPat);
+      // FP32C: the pair sum skipped this point (rr < rthr); weight 1 - mask here
+      // (each mesh point once: the index range of a row may wrap past nlon)
+      if (rr < rthr && j - jmin < a.nlon) mask -= 1.0;
       double ds1 = a.detJ[q], ds2 = a.w[i];
       if (c1 != 0.) {
         double fj[3], EA, EB;
@@ -369,6 +375,140 @@ __device__ void near_readd(const CorrArgs& a, int cell, double c1, double c2, co
   for (int k = 0; k < 3; ++k) dv[k] = warp_sum(acc[k]);
 }
 
+// ---- FP32 replay of Spline_FindProjection, used only to screen items whose
+// projection distance is clearly above 2*meshSize (no correction) -----------
+__device__ __forceinline__ void spline_weights32(float x, float y, int m, int n, int& n11, int& n12, int& n21,
+                                                 int& n22, float* cx, float* cy) {
+  const float hx = (float)(RBC3D_TWO_PI / m), hy = (float)(RBC3D_TWO_PI / n);
+  const float ihx = 1.f / hx, ihy = 1.f / hy;
+  int i1 = (int)floorf(x * ihx), j1 = (int)floorf(y * ihy);
+  float s = x * ihx - i1, t = y * ihy - j1;
+  i1 = imod(i1, m); j1 = imod(j1, n);
+  int i2 = imod(i1 + 1, m), j2 = imod(j1 + 1, n);
+  cx[0] = 1 + s * s * (-3.f + 2.f * s); cx[1] = s * s * (3.f - 2.f * s);
+  cx[2] = hx * s * (1.f + s * (-2.f + s)); cx[3] = hx * s * s * (-1.f + s);
+  cy[0] = 1 + t * t * (-3.f + 2.f * t); cy[1] = t * t * (3.f - 2.f * t);
+  cy[2] = hy * t * (1.f + t * (-2.f + t)); cy[3] = hy * t * t * (-1.f + t);
+  n11 = i1 + m * j1; n12 = i1 + m * j2; n21 = i2 + m * j1; n22 = i2 + m * j2;
+}
+__device__ __forceinline__ void spline_eval32(const double* __restrict__ spl, float th, float ph, int m, int n,
+                                              float* f) {
+  int n11, n12, n21, n22;
+  float cx[4], cy[4];
+  spline_weights32(th, ph, m, n, n11, n12, n21, n22, cx, cy);
+  const double* a = spl + (size_t)n11 * SPL_NODE;
+  const double* b = spl + (size_t)n12 * SPL_NODE;
+  const double* c = spl + (size_t)n21 * SPL_NODE;
+  const double* d = spl + (size_t)n22 * SPL_NODE;
+  for (int l = 0; l < 3; ++l) {
+    float r0 = (float)a[l] * cy[0] + (float)b[l] * cy[1] + (float)a[6 + l] * cy[2] + (float)b[6 + l] * cy[3];
+    float r1 = (float)c[l] * cy[0] + (float)d[l] * cy[1] + (float)c[6 + l] * cy[2] + (float)d[6 + l] * cy[3];
+    float r2 = (float)a[3 + l] * cy[0] + (float)b[3 + l] * cy[1] + (float)a[9 + l] * cy[2] + (float)b[9 + l] * cy[3];
+    float r3 = (float)c[3 + l] * cy[0] + (float)d[3 + l] * cy[1] + (float)c[9 + l] * cy[2] + (float)d[9 + l] * cy[3];
+    f[l] = cx[0] * r0 + cx[1] * r1 + cx[2] * r2 + cx[3] * r3;
+  }
+}
+__device__ __forceinline__ float warp_sumf_(float v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+// Returns the projection's signed distance a3(x0).(xt - x0) in FP32.
+__device__ float projection_dist32(const double* sx, const double* sa, int m, int n, const double* xtd, double th0d,
+                                   double phi0d) {
+  const int lane = threadIdx.x & 31;
+  const float TWO_PI_F = (float)RBC3D_TWO_PI;
+  float xt[3] = {(float)xtd[0], (float)xtd[1], (float)xtd[2]};
+  float th0 = (float)th0d, phi0 = (float)phi0d;
+  float x0[3];
+  spline_eval32(sx, th0, phi0, m, n, x0);
+  float h = fmaxf(TWO_PI_F / m, TWO_PI_F / n);
+  for (int iter = 0; iter < 3; ++iter) {
+    float px = 0, py = 0, d2 = 0;
+    float st0 = sinf(th0), ct0 = cosf(th0);
+    if (lane < 16) {
+      int ith = lane % 2, iphi = lane / 2;
+      float thL = (ith + 1) * h / 2;
+      float phL = iphi * TWO_PI_F / 8;
+      float sth = sinf(thL), cth = cosf(thL), cph = cosf(phL), sph = sinf(phL);
+      float q0 = sth * cph, q1 = sth * sph, q2 = cth;
+      float y0 = ct0 * q0 + st0 * q2, y1 = q1, y2 = fmaxf(-1.f, fminf(1.f, -st0 * q0 + ct0 * q2));
+      float thP = acosf(y2), pp = atan2f(y1, y0) + phi0;
+      float phP = pp - floorf(pp / TWO_PI_F) * TWO_PI_F;
+      px = thL * cph;
+      py = thL * sph;
+      float xx[3];
+      spline_eval32(sx, thP, phP, m, n, xx);
+      d2 = (xx[0] - xt[0]) * (xx[0] - xt[0]) + (xx[1] - xt[1]) * (xx[1] - xt[1]) + (xx[2] - xt[2]) * (xx[2] - xt[2]);
+    } else if (lane == 16) {
+      float xx[3];
+      spline_eval32(sx, th0, phi0, m, n, xx);
+      d2 = (xx[0] - xt[0]) * (xx[0] - xt[0]) + (xx[1] - xt[1]) * (xx[1] - xt[1]) + (xx[2] - xt[2]) * (xx[2] - xt[2]);
+    }
+    float d2c = __shfl_sync(0xffffffffu, d2, 16);
+    float u[6] = {lane <= 16 ? 1.f : 0.f, px, py, px * px, px * py, py * py};
+    float M[6][6], b[6];
+    for (int i = 0; i < 6; ++i)
+      for (int j = i; j < 6; ++j) { M[i][j] = warp_sumf_(u[i] * u[j]); M[j][i] = M[i][j]; }
+    for (int i = 0; i < 6; ++i) b[i] = warp_sumf_(u[i] * d2);
+    // Cholesky
+    float U[6][6];
+    bool ok = true;
+    for (int j = 0; j < 6 && ok; ++j) {
+      float s = M[j][j];
+      for (int k = 0; k < j; ++k) s -= U[k][j] * U[k][j];
+      if (!(s > 0)) { ok = false; break; }
+      U[j][j] = sqrtf(s);
+      for (int i = j + 1; i < 6; ++i) {
+        float t = M[j][i];
+        for (int k = 0; k < j; ++k) t -= U[k][j] * U[k][i];
+        U[j][i] = t / U[j][j];
+      }
+    }
+    if (ok) {
+      float y[6];
+      for (int i = 0; i < 6; ++i) {
+        float t = b[i];
+        for (int k = 0; k < i; ++k) t -= U[k][i] * y[k];
+        y[i] = t / U[i][i];
+      }
+      for (int i = 5; i >= 0; --i) {
+        float t = y[i];
+        for (int k = i + 1; k < 6; ++k) t -= U[i][k] * b[k];
+        b[i] = t / U[i][i];
+      }
+    }
+    float l11 = 2.f * b[3], l12 = b[4], l22 = 2.f * b[5];
+    float det = l11 * l22 - l12 * l12;
+    float xm0 = 0.f, xm1 = 0.f;
+    if (det > 0) {
+      float idet = 1.f / det;
+      xm0 = idet * (l22 * (-b[1]) - l12 * (-b[2]));
+      xm1 = idet * (-l12 * (-b[1]) + l11 * (-b[2]));
+    }
+    float dth = sqrtf(xm0 * xm0 + xm1 * xm1), dph = atan2f(xm1, xm0);
+    float sp0 = sinf(phi0), cp0 = cosf(phi0);
+    float s1[3] = {ct0 * cp0, ct0 * sp0, -st0}, s2[3] = {-sp0, cp0, 0.f}, e0[3] = {st0 * cp0, st0 * sp0, ct0};
+    float qx[3] = {sinf(dth) * cosf(dph), sinf(dth) * sinf(dph), cosf(dth)};
+    float yv[3];
+    for (int c = 0; c < 3; ++c) yv[c] = qx[0] * s1[c] + qx[1] * s2[c] + qx[2] * e0[c];
+    float nr = sqrtf(yv[0] * yv[0] + yv[1] * yv[1] + yv[2] * yv[2]);
+    yv[2] = fmaxf(-1.f, fminf(1.f, yv[2] / nr));
+    float thMin = acosf(yv[2]), phiMin = atan2f(yv[1] / nr, yv[0] / nr);
+    if (phiMin < 0) phiMin += TWO_PI_F;
+    float xMin[3];
+    spline_eval32(sx, thMin, phiMin, m, n, xMin);
+    float d2Min = (xMin[0] - xt[0]) * (xMin[0] - xt[0]) + (xMin[1] - xt[1]) * (xMin[1] - xt[1]) +
+                  (xMin[2] - xt[2]) * (xMin[2] - xt[2]);
+    if (d2Min > d2c) break;
+    th0 = thMin; phi0 = phiMin;
+    for (int k = 0; k < 3; ++k) x0[k] = xMin[k];
+    h = 0.5f * h;
+  }
+  float a30[3];
+  spline_eval32(sa, th0, phi0, m, n, a30);
+  return a30[0] * (xt[0] - x0[0]) + a30[1] * (xt[1] - x0[1]) + a30[2] * (xt[2] - x0[2]);
+}
+
 // RBC_NearSingInt over the work list (persistent warps)
 __global__ void __launch_bounds__(128) k_near(CorrArgs a) {
   const int lane = threadIdx.x & 31;
@@ -390,6 +530,20 @@ __global__ void __launch_bounds__(128) k_near(CorrArgs a) {
       xt[k] = x0[k] + xx;
     }
     const double* sx = set_ptr(a, cell, SPL_X);
+    const double msz = a.meshSize[cell];
+    bool skip = false;
+    if (a.screen) {
+      // (1) far target on the outer side of its closest mesh point: the
+      //     projection distance is ~|xt - x0| >= 6*meshSize > 2*meshSize
+      double dx0 = xt[0] - x0[0], dx1 = xt[1] - x0[1], dx2 = xt[2] - x0[2];
+      double d = sqrt(dx0 * dx0 + dx1 * dx1 + dx2 * dx2);
+      double nd = a.a3[q0] * dx0 + a.a3[q0 + a.npt] * dx1 + a.a3[q0 + 2 * (size_t)a.npt] * dx2;
+      if (d > 6.0 * msz && nd > 0.9 * d) skip = true;
+      // (2) FP32 replay of the projection, margin 0.3*meshSize
+      else if ((double)projection_dist32(sx, set_ptr(a, cell, SPL_A3), a.m, a.nlon, xt, th0, phi0) > 2.3 * msz)
+        skip = true;
+      if (skip && !a.verify) continue;
+    }
     find_projection(sx, a.m, a.nlon, xt, th0, phi0, x0);
     const double c1 = a.c1, c2 = a.c2 * a.Bc[a.celltype[cell]];
     SplW W;
@@ -397,12 +551,15 @@ __global__ void __launch_bounds__(128) k_near(CorrArgs a) {
     spline_weights(th0, phi0, a.m, a.nlon, W);
     spline_eval(set_ptr(a, cell, SPL_A3), W, 3, a30);
     double dist = a30[0] * (xt[0] - x0[0]) + a30[1] * (xt[1] - x0[1]) + a30[2] * (xt[2] - x0[2]);
-    if (dist > 2 * a.meshSize[cell]) continue;
-    if (lane == 0) atomicAdd(a.cnt + 3, 1ull);
+    if (dist > 2 * msz) continue;
+    if (lane == 0) {
+      atomicAdd(a.cnt + 3, 1ull);
+      if (skip) atomicAdd(a.cnt + 6, 1ull);  // a screened item that needs a correction
+    }
     double sizePat = a.radius * sqrt(a.area[cell] / (4 * RBC3D_PI));
     double dist1 = copysign(fabs(0.01 * sizePat), dist);
     double dv[3], tmp[3];
-    near_subtract(a, cell, c1, c2, xt, th0, phi0, a.radius, dv);
+    near_subtract(a, cell, c1, c2, xt, th0, phi0, a.radius, a.screen ? a.rthr : -1.0, dv);
     if (fabs(dist) >= fabs(dist1)) {
       near_readd(a, cell, c1, c2, xt, x0, th0, phi0, a.radius, tmp);
       for (int k = 0; k < 3; ++k) dv[k] += tmp[k];
@@ -454,14 +611,13 @@ rbc3d_status run_self_corr(rbc3d_ctx* ctx, int tlist, double c1, double c2) {
   fill_args(ctx, tlist, c1, (c2 != 0 && ctx->has_g) ? c2 : 0.0, a, Bc.p);
   if (c1 != 0 && !ctx->has_f) a.c1 = 0;
   long long threads = (long long)t.n * 32;
-  k_self<<<(int)((threads + 255) / 256), 256, 0, ctx->st>>>(a);
+  { k_self<<<(int)((threads + 255) / 256), 256, 0, ctx->st>>>(a); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaStreamSynchronize(ctx->st));
   return RBC3D_OK;
 }
 
 rbc3d_status run_near_corr(rbc3d_ctx* ctx, int tlist, double c1, double c2, int prec) {
-  (void)prec;
   TargetSet& t = ctx->tl[tlist];
   if (t.n == 0 || ctx->ncell == 0) return RBC3D_OK;
   DBuf<double> Bc;
@@ -469,9 +625,12 @@ rbc3d_status run_near_corr(rbc3d_ctx* ctx, int tlist, double c1, double c2, int 
   CorrArgs a;
   fill_args(ctx, tlist, c1, (c2 != 0 && ctx->has_g) ? c2 : 0.0, a, Bc.p);
   if (c1 != 0 && !ctx->has_f) a.c1 = 0;
+  a.screen = (prec != RBC3D_FP64) ? 1 : 0;
+  a.rthr = ctx->near_rthr;
+  a.verify = ctx->verify_screen ? 1 : 0;
   int nsm = 0;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);
-  k_near<<<nsm * 8, 128, 0, ctx->st>>>(a);
+  { k_near<<<nsm * 8, 128, 0, ctx->st>>>(a); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaStreamSynchronize(ctx->st));
   return RBC3D_OK;

@@ -125,6 +125,7 @@ struct rbc3d_ctx {
   DBuf<double> x, a3, detJ, f, g, sf, sg, area, meshSize;
   DBuf<double> spl;               // ncell * SPL_NSET * m*nlon * SPL_NODE
   bool has_f = false, has_g = false;
+  double near_rthr = 0;            // 0.5 * min(meshSize): FP32C cross-surface pairs below it go to FP64
 
   // sorted sources (cell surface points)
   DBuf<int> s_order, s_cstart, s_cend;
@@ -137,7 +138,7 @@ struct rbc3d_ctx {
   // near-singular work list
   DBuf<int4> items;               // (target, surf, ilat, ilon)
   int items_cap = 0;
-  DBuf<unsigned long long> dcnt;  // device counters: [0] items, [1] pairs, [2] overflow targets, [3] nearsing, [4] wall pairs, [5] duffy
+  DBuf<unsigned long long> dcnt;  // device counters: [0] items, [1] pairs, [2] overflow targets, [3] nearsing, [4] wall pairs, [5] duffy, [6] screen misses
   DBuf<double> xvint;             // linear-term reduction (3)
 
   PmeState pme;
@@ -145,6 +146,23 @@ struct rbc3d_ctx {
 
   DBuf<double> scratch;           // GMRES basis / temporaries
   rbc3d_counts counts{};
+
+  // stage timers: event pairs recorded around each stage, read on demand
+  bool prof = false;
+  bool verify_screen = false;  // RBC3D_VERIFY_SCREEN=1: check near-singular screens in FP64
+  long long launches = 0;  // kernels of this library launched on the context
+  std::vector<cudaEvent_t> evpool;
+  std::vector<int> rec_stage;
+  size_t nrec = 0;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+};
+
+// RAII stage timer (records nothing when profiling is off)
+struct StageScope {
+  rbc3d_ctx* c;
+  int slot;
+  StageScope(rbc3d_ctx* ctx, int stage);
+  ~StageScope();
 };
 
 rbc3d_status ctx_fail(rbc3d_ctx* ctx, int code, const std::string& msg);
@@ -176,6 +194,9 @@ rbc3d_status run_wall_self(rbc3d_ctx* ctx, double c1);
 rbc3d_status wall_solve(rbc3d_ctx* ctx, const rbc3d_solve_opts* opt, const double* guess, rbc3d_solve_stats* st);
 rbc3d_status wall_matmult_dev(rbc3d_ctx* ctx, int prec, const double* u_dev, double* y_dev);
 rbc3d_status wall_residual_dev(rbc3d_ctx* ctx, int prec);
+
+// peak.cu
+rbc3d_status fma_peak(int prec, double* tflops);
 
 // shared host helper: GauLeg of ModQuadRule.F90:135-214
 void host_gauleg(double x1, double x2, int n, double* x, double* w);

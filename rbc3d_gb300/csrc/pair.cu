@@ -113,6 +113,7 @@ struct PairArgs {
   float c1f, c2f;
   double rc2;
   float rc2_f, reps2_f;
+  float rthr2_f;  // FP32 path: cross-surface pairs closer than this are left to the FP64 near-singular pass
   Tables T;
   // near-singular work list
   int collect;
@@ -240,8 +241,12 @@ __global__ void __launch_bounds__(TILE) k_pair32(PairArgs a) {
                 wgt = 1.f - (e.x + (s - (float)i) * e.y);
               } else wgt = 1.f;
             }
-          } else if (a.collect) {
-            if (r2 < run_d2) { run_d2 = r2; run_id = sm.id[j]; }
+          } else {
+            if (a.collect && r2 < run_d2) { run_d2 = r2; run_id = sm.id[j]; }
+            // A pair this close to another surface is re-evaluated in FP64 by
+            // the near-singular pass (its FP32 rounding would survive the
+            // cancellation with the FP64 subtraction).
+            if (a.collect && r2 < a.rthr2_f) continue;
           }
           if (r2 < a.reps2_f) continue;
           float rinv = rsqrtf(r2);
@@ -429,8 +434,8 @@ rbc3d_status sort_points(rbc3d_ctx* ctx, int n, const double* x_dev, DBuf<int>& 
   DBuf<int> key, key2, idx;
   CUDA_TRY(key.alloc(n)); CUDA_TRY(key2.alloc(n)); CUDA_TRY(idx.alloc(n)); CUDA_TRY(order.alloc(n));
   CUDA_TRY(cs.alloc(hg.ncells)); CUDA_TRY(ce.alloc(hg.ncells));
-  k_hash_keys<<<nblk(n, 256), 256, 0, ctx->st>>>(n, x_dev, hg.Nc[0], hg.Nc[1], hg.Nc[2], hg.Nc[0] / hg.L[0],
-                                                  hg.Nc[1] / hg.L[1], hg.Nc[2] / hg.L[2], key.p, idx.p);
+  { k_hash_keys<<<nblk(n, 256), 256, 0, ctx->st>>>(n, x_dev, hg.Nc[0], hg.Nc[1], hg.Nc[2], hg.Nc[0] / hg.L[0],
+                                                  hg.Nc[1] / hg.L[1], hg.Nc[2] / hg.L[2], key.p, idx.p); ++ctx->launches; }
   size_t tmp = 0;
   cub::DeviceRadixSort::SortPairs(nullptr, tmp, key.p, key2.p, idx.p, order.p, n, 0, 32, ctx->st);
   DBuf<char> tbuf;
@@ -438,7 +443,7 @@ rbc3d_status sort_points(rbc3d_ctx* ctx, int n, const double* x_dev, DBuf<int>& 
   CUDA_TRY(cub::DeviceRadixSort::SortPairs(tbuf.p, tmp, key.p, key2.p, idx.p, order.p, n, 0, 32, ctx->st));
   CUDA_TRY(cudaMemsetAsync(cs.p, 0, sizeof(int) * hg.ncells, ctx->st));
   CUDA_TRY(cudaMemsetAsync(ce.p, 0, sizeof(int) * hg.ncells, ctx->st));
-  k_cell_ranges<<<nblk(n, 256), 256, 0, ctx->st>>>(n, key2.p, cs.p, ce.p);
+  { k_cell_ranges<<<nblk(n, 256), 256, 0, ctx->st>>>(n, key2.p, cs.p, ce.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaStreamSynchronize(ctx->st));
   return RBC3D_OK;
@@ -472,8 +477,8 @@ rbc3d_status build_source_list(rbc3d_ctx* ctx) {
   if (s) return s;
   CUDA_TRY(ctx->s_x.alloc(3 * (size_t)n)); CUDA_TRY(ctx->s_a3.alloc(3 * (size_t)n)); CUDA_TRY(ctx->s_meta.alloc(n));
   CUDA_TRY(ctx->s_f.alloc(3 * (size_t)n)); CUDA_TRY(ctx->s_g.alloc(3 * (size_t)n));
-  k_gather_src<<<nblk(n, 256), 256, 0, ctx->st>>>(n, ctx->nlat, ctx->nlat * ctx->nlon, ctx->s_order.p, ctx->x.p,
-                                                   ctx->a3.p, ctx->s_x.p, ctx->s_a3.p, ctx->s_meta.p);
+  { k_gather_src<<<nblk(n, 256), 256, 0, ctx->st>>>(n, ctx->nlat, ctx->nlat * ctx->nlon, ctx->s_order.p, ctx->x.p,
+                                                   ctx->a3.p, ctx->s_x.p, ctx->s_a3.p, ctx->s_meta.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   ctx->src_sorted = true;
   // tlist_rbc shares the source order
@@ -487,10 +492,10 @@ rbc3d_status build_source_density(rbc3d_ctx* ctx) {
   if (n == 0) return RBC3D_OK;
   DBuf<double> Bc;
   CUDA_TRY(Bc.upload(ctx->Bcoef, RBC3D_MAX_CELLTYPES, ctx->st));
-  if (ctx->has_f) k_density<<<nblk(n, 256), 256, 0, ctx->st>>>(n, ctx->nlat, nv, ctx->f.p, ctx->detJ.p, ctx->w.p, ctx->sf.p);
-  if (ctx->has_g) k_density<<<nblk(n, 256), 256, 0, ctx->st>>>(n, ctx->nlat, nv, ctx->g.p, ctx->detJ.p, ctx->w.p, ctx->sg.p);
-  k_gather_density<<<nblk(n, 256), 256, 0, ctx->st>>>(n, nv, ctx->s_order.p, ctx->sf.p, ctx->sg.p, ctx->celltype.p,
-                                                       Bc.p, ctx->s_f.p, ctx->s_g.p, ctx->has_f, ctx->has_g);
+  if (ctx->has_f) { k_density<<<nblk(n, 256), 256, 0, ctx->st>>>(n, ctx->nlat, nv, ctx->f.p, ctx->detJ.p, ctx->w.p, ctx->sf.p); ++ctx->launches; }
+  if (ctx->has_g) { k_density<<<nblk(n, 256), 256, 0, ctx->st>>>(n, ctx->nlat, nv, ctx->g.p, ctx->detJ.p, ctx->w.p, ctx->sg.p); ++ctx->launches; }
+  { k_gather_density<<<nblk(n, 256), 256, 0, ctx->st>>>(n, nv, ctx->s_order.p, ctx->sf.p, ctx->sg.p, ctx->celltype.p,
+                                                       Bc.p, ctx->s_f.p, ctx->s_g.p, ctx->has_f, ctx->has_g); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaStreamSynchronize(ctx->st));
   ctx->src_density = true;
@@ -532,16 +537,17 @@ rbc3d_status run_pair_sum(rbc3d_ctx* ctx, int tlist, double c1, double c2, int p
   a.chord2_max = (float)(cm * cm);
   a.c1 = c1; a.c2 = c2; a.c1f = (float)c1; a.c2f = (float)c2;
   a.rc2 = ctx->prm.rc * ctx->prm.rc; a.rc2_f = (float)a.rc2; a.reps2_f = (float)(ctx->T.r_eps * ctx->T.r_eps);
+  a.rthr2_f = (float)(ctx->near_rthr * ctx->near_rthr);
   a.T = ctx->T;
   a.collect = collect_nbr ? 1 : 0;
   a.items = ctx->items.p; a.cap = ctx->items_cap; a.cnt = ctx->dcnt.p;
   bool dl = (c2 != 0.0) && ctx->has_g;
   if (prec == RBC3D_FP32C) {
-    if (dl) k_pair32<true><<<t.nunits, TILE, 0, ctx->st>>>(a);
-    else k_pair32<false><<<t.nunits, TILE, 0, ctx->st>>>(a);
+    if (dl) { k_pair32<true><<<t.nunits, TILE, 0, ctx->st>>>(a); ++ctx->launches; }
+    else { k_pair32<false><<<t.nunits, TILE, 0, ctx->st>>>(a); ++ctx->launches; }
   } else {
-    if (dl) k_pair64<true><<<t.nunits, TILE, 0, ctx->st>>>(a);
-    else k_pair64<false><<<t.nunits, TILE, 0, ctx->st>>>(a);
+    if (dl) { k_pair64<true><<<t.nunits, TILE, 0, ctx->st>>>(a); ++ctx->launches; }
+    else { k_pair64<false><<<t.nunits, TILE, 0, ctx->st>>>(a); ++ctx->launches; }
   }
   CUDA_TRY(cudaGetLastError());
   return RBC3D_OK;
@@ -554,10 +560,10 @@ rbc3d_status run_linear(rbc3d_ctx* ctx, int tlist, double c2) {
   CUDA_TRY(Bc.upload(ctx->Bcoef, RBC3D_MAX_CELLTYPES, ctx->st));
   CUDA_TRY(ctx->xvint.alloc(3));
   CUDA_TRY(cudaMemsetAsync(ctx->xvint.p, 0, 3 * sizeof(double), ctx->st));
-  k_linear_reduce<<<304, 256, 0, ctx->st>>>(ctx->npt, ctx->nlat * ctx->nlon, ctx->x.p, ctx->sg.p, ctx->a3.p,
-                                            ctx->celltype.p, Bc.p, ctx->xvint.p);
+  { k_linear_reduce<<<304, 256, 0, ctx->st>>>(ctx->npt, ctx->nlat * ctx->nlon, ctx->x.p, ctx->sg.p, ctx->a3.p,
+                                            ctx->celltype.p, Bc.p, ctx->xvint.p); ++ctx->launches; }
   double pil = ctx->iLb[0] * ctx->iLb[1] * ctx->iLb[2];
-  if (t.n) k_linear_add<<<nblk(t.n, 256), 256, 0, ctx->st>>>(t.n, t.Acoef.p, ctx->xvint.p, c2 * (-8 * RBC3D_PI * pil), t.v.p);
+  if (t.n) { k_linear_add<<<nblk(t.n, 256), 256, 0, ctx->st>>>(t.n, t.Acoef.p, ctx->xvint.p, c2 * (-8 * RBC3D_PI * pil), t.v.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaStreamSynchronize(ctx->st));
   return RBC3D_OK;

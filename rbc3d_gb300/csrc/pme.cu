@@ -350,8 +350,8 @@ rbc3d_status pme_spread(rbc3d_ctx* ctx, double c1, double c2, int cells, int wal
     a.n = ctx->npt; a.x = ctx->s_x.p; a.f = ctx->s_f.p; a.g = ctx->s_g.p; a.a3 = ctx->s_a3.p;
     a.sl = P.sl && ctx->has_f; a.dl = P.dl && ctx->has_g;
     if (a.sl || a.dl) {
-      if (prec == RBC3D_FP32C) k_spread<float><<<nblk(a.n, 128), 128, 0, ctx->st>>>(a, P.grid32.p);
-      else k_spread<double><<<nblk(a.n, 128), 128, 0, ctx->st>>>(a, P.grid64.p);
+      if (prec == RBC3D_FP32C) { k_spread<float><<<nblk(a.n, 128), 128, 0, ctx->st>>>(a, P.grid32.p); ++ctx->launches; }
+      else { k_spread<double><<<nblk(a.n, 128), 128, 0, ctx->st>>>(a, P.grid64.p); ++ctx->launches; }
       CUDA_TRY(cudaGetLastError());
     }
   }
@@ -359,10 +359,10 @@ rbc3d_status pme_spread(rbc3d_ctx* ctx, double c1, double c2, int cells, int wal
     WallState& W = ctx->wall;
     DBuf<double> xs, fs;
     CUDA_TRY(xs.alloc(3 * (size_t)W.nele)); CUDA_TRY(fs.alloc(3 * (size_t)W.nele));
-    k_wall_sources<<<nblk(W.nele, 256), 256, 0, ctx->st>>>(W.nele, W.nvert, W.e2v.p, W.x.p, W.f.p, W.area.p, xs.p, fs.p);
+    { k_wall_sources<<<nblk(W.nele, 256), 256, 0, ctx->st>>>(W.nele, W.nvert, W.e2v.p, W.x.p, W.f.p, W.area.p, xs.p, fs.p); ++ctx->launches; }
     a.n = W.nele; a.x = xs.p; a.f = fs.p; a.g = nullptr; a.a3 = nullptr; a.sl = 1; a.dl = 0;
-    if (prec == RBC3D_FP32C) k_spread<float><<<nblk(a.n, 128), 128, 0, ctx->st>>>(a, P.grid32.p);
-    else k_spread<double><<<nblk(a.n, 128), 128, 0, ctx->st>>>(a, P.grid64.p);
+    if (prec == RBC3D_FP32C) { k_spread<float><<<nblk(a.n, 128), 128, 0, ctx->st>>>(a, P.grid32.p); ++ctx->launches; }
+    else { k_spread<double><<<nblk(a.n, 128), 128, 0, ctx->st>>>(a, P.grid64.p); ++ctx->launches; }
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaStreamSynchronize(ctx->st));
   }
@@ -383,14 +383,14 @@ rbc3d_status pme_transform(rbc3d_ctx* ctx) {
     CUDA_TRY(P.spec32.alloc(12 * P.GC)); CUDA_TRY(P.vspec32.alloc(3 * P.GC)); CUDA_TRY(P.vel32.alloc(3 * P.G));
     if (P.dl) { if (cufftExecR2C(P.r2c32_12, P.grid32.p, (cufftComplex*)P.spec32.p)) return ctx_fail(ctx, RBC3D_ERR_CUDA, "cufftExecR2C"); }
     else if (cufftExecR2C(P.r2c32_3, P.grid32.p, (cufftComplex*)P.spec32.p)) return ctx_fail(ctx, RBC3D_ERR_CUDA, "cufftExecR2C");
-    k_influence<float, float2><<<nblk(P.GC, 256), 256, 0, ctx->st>>>(a, P.spec32.p, P.vspec32.p);
+    { k_influence<float, float2><<<nblk(P.GC, 256), 256, 0, ctx->st>>>(a, P.spec32.p, P.vspec32.p); ++ctx->launches; }
     CUDA_TRY(cudaGetLastError());
     if (cufftExecC2R(P.c2r32_3, (cufftComplex*)P.vspec32.p, P.vel32.p)) return ctx_fail(ctx, RBC3D_ERR_CUDA, "cufftExecC2R");
   } else {
     CUDA_TRY(P.spec64.alloc(12 * P.GC)); CUDA_TRY(P.vspec64.alloc(3 * P.GC)); CUDA_TRY(P.vel64.alloc(3 * P.G));
     if (P.dl) { if (cufftExecD2Z(P.r2c64_12, P.grid64.p, (cufftDoubleComplex*)P.spec64.p)) return ctx_fail(ctx, RBC3D_ERR_CUDA, "cufftExecD2Z"); }
     else if (cufftExecD2Z(P.r2c64_3, P.grid64.p, (cufftDoubleComplex*)P.spec64.p)) return ctx_fail(ctx, RBC3D_ERR_CUDA, "cufftExecD2Z");
-    k_influence<double, double2><<<nblk(P.GC, 256), 256, 0, ctx->st>>>(a, P.spec64.p, P.vspec64.p);
+    { k_influence<double, double2><<<nblk(P.GC, 256), 256, 0, ctx->st>>>(a, P.spec64.p, P.vspec64.p); ++ctx->launches; }
     CUDA_TRY(cudaGetLastError());
     if (cufftExecZ2D(P.c2r64_3, (cufftDoubleComplex*)P.vspec64.p, P.vel64.p)) return ctx_fail(ctx, RBC3D_ERR_CUDA, "cufftExecZ2D");
   }
@@ -407,8 +407,8 @@ rbc3d_status pme_gather(rbc3d_ctx* ctx, int tlist) {
   a.n = t.n; a.x = t.x.p; a.A = t.Acoef.p; a.v = t.v.p;
   for (int d = 0; d < 3; ++d) { a.N[d] = ctx->prm.Nb[d]; a.ih[d] = ctx->prm.Nb[d] / ctx->prm.Lb[d]; }
   a.P = ctx->prm.P; a.G = P.G;
-  if (P.prec == RBC3D_FP32C) k_gather<float><<<nblk(a.n, 128), 128, 0, ctx->st>>>(a, P.vel32.p);
-  else k_gather<double><<<nblk(a.n, 128), 128, 0, ctx->st>>>(a, P.vel64.p);
+  if (P.prec == RBC3D_FP32C) { k_gather<float><<<nblk(a.n, 128), 128, 0, ctx->st>>>(a, P.vel32.p); ++ctx->launches; }
+  else { k_gather<double><<<nblk(a.n, 128), 128, 0, ctx->st>>>(a, P.vel64.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   return RBC3D_OK;
 }

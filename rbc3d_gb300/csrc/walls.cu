@@ -431,7 +431,7 @@ WallArgs wall_args(rbc3d_ctx* ctx) {
 }
 
 double dev_norm(rbc3d_ctx* ctx, int n, const double* v, double* tmp) {
-  k_dots<<<1, 512, 0, ctx->st>>>(n, 1, v, 0, v, tmp);
+  { k_dots<<<1, 512, 0, ctx->st>>>(n, 1, v, 0, v, tmp); ++ctx->launches; }
   double h = 0;
   cudaMemcpyAsync(&h, tmp, sizeof(double), cudaMemcpyDeviceToHost, ctx->st);
   cudaStreamSynchronize(ctx->st);
@@ -473,7 +473,7 @@ rbc3d_status wall_setup(rbc3d_ctx* ctx) {
   CUDA_TRY(W.e2v.upload(W.he2v.data(), W.he2v.size(), ctx->st));
   CUDA_TRY(W.glb.upload(W.hglb.data(), W.hglb.size(), ctx->st));
   CUDA_TRY(W.area.alloc(W.nele)); CUDA_TRY(W.eps.alloc(W.nele)); CUDA_TRY(W.cen.alloc(3 * (size_t)W.nele));
-  k_wall_geom<<<nblk(W.nele, 256), 256, 0, ctx->st>>>(W.nele, W.nvert, W.e2v.p, W.x.p, W.area.p, W.eps.p, W.cen.p);
+  { k_wall_geom<<<nblk(W.nele, 256), 256, 0, ctx->st>>>(W.nele, W.nvert, W.e2v.p, W.x.p, W.area.p, W.eps.p, W.cen.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   rbc3d_status s = writer_flags(ctx, W.writer);
   if (s) return s;
@@ -487,7 +487,7 @@ rbc3d_status wall_prepare_self(rbc3d_ctx* ctx) {
   DBuf<int> count, off;
   CUDA_TRY(count.alloc(W.nvert + 1)); CUDA_TRY(off.alloc(W.nvert + 1));
   CUDA_TRY(cudaMemsetAsync(count.p, 0, sizeof(int) * (W.nvert + 1), ctx->st));
-  k_self_pairs<<<nblk(W.nvert, 128), 128, 0, ctx->st>>>(a, 0, count.p, nullptr, nullptr);
+  { k_self_pairs<<<nblk(W.nvert, 128), 128, 0, ctx->st>>>(a, 0, count.p, nullptr, nullptr); ++ctx->launches; }
   size_t tmp = 0;
   cub::DeviceScan::ExclusiveSum(nullptr, tmp, count.p, off.p, W.nvert + 1, ctx->st);
   DBuf<char> tb;
@@ -506,21 +506,21 @@ rbc3d_status wall_prepare_self(rbc3d_ctx* ctx) {
   }
   DBuf<int2> pairs;
   CUDA_TRY(pairs.alloc(npair));
-  k_self_pairs<<<nblk(W.nvert, 128), 128, 0, ctx->st>>>(a, 1, nullptr, off.p, pairs.p);
+  { k_self_pairs<<<nblk(W.nvert, 128), 128, 0, ctx->st>>>(a, 1, nullptr, off.p, pairs.p); ++ctx->launches; }
   long long ne = 3LL * npair;
   DBuf<unsigned long long> k1, k2;
   DBuf<int> i1, i2, flag, seg;
   DBuf<double> blk;
   CUDA_TRY(k1.alloc(ne)); CUDA_TRY(k2.alloc(ne)); CUDA_TRY(i1.alloc(ne)); CUDA_TRY(i2.alloc(ne));
   CUDA_TRY(flag.alloc(ne)); CUDA_TRY(seg.alloc(ne)); CUDA_TRY(blk.alloc(9 * ne));
-  k_self_blocks<<<nblk(npair, 128), 128, 0, ctx->st>>>(a, npair, pairs.p, k1.p, i1.p, blk.p);
+  { k_self_blocks<<<nblk(npair, 128), 128, 0, ctx->st>>>(a, npair, pairs.p, k1.p, i1.p, blk.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   tmp = 0;
   cub::DeviceRadixSort::SortPairs(nullptr, tmp, k1.p, k2.p, i1.p, i2.p, (int)ne, 0, 64, ctx->st);
   DBuf<char> tb2;
   CUDA_TRY(tb2.alloc(tmp + 1));
   CUDA_TRY(cub::DeviceRadixSort::SortPairs(tb2.p, tmp, k1.p, k2.p, i1.p, i2.p, (int)ne, 0, 64, ctx->st));
-  k_uniq_flags<<<nblk(ne, 256), 256, 0, ctx->st>>>(ne, k2.p, flag.p);
+  { k_uniq_flags<<<nblk(ne, 256), 256, 0, ctx->st>>>(ne, k2.p, flag.p); ++ctx->launches; }
   tmp = 0;
   cub::DeviceScan::InclusiveSum(nullptr, tmp, flag.p, seg.p, (int)ne, ctx->st);
   DBuf<char> tb3;
@@ -532,9 +532,9 @@ rbc3d_status wall_prepare_self(rbc3d_ctx* ctx) {
   DBuf<int> brow;
   CUDA_TRY(W.col.alloc(nb)); CUDA_TRY(brow.alloc(nb)); CUDA_TRY(W.val.alloc(9 * (size_t)nb));
   CUDA_TRY(W.rowptr.alloc(W.nvert + 1));
-  k_self_reduce<<<nblk(ne, 256), 256, 0, ctx->st>>>(ne, W.nvert, k2.p, i2.p, seg.p, blk.p, W.col.p, brow.p, W.val.p);
+  { k_self_reduce<<<nblk(ne, 256), 256, 0, ctx->st>>>(ne, W.nvert, k2.p, i2.p, seg.p, blk.p, W.col.p, brow.p, W.val.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
-  if (nb > 0) k_row_ptr<<<nblk(nb, 256), 256, 0, ctx->st>>>(nb, W.nvert, brow.p, W.rowptr.p);
+  if (nb > 0) { k_row_ptr<<<nblk(nb, 256), 256, 0, ctx->st>>>(nb, W.nvert, brow.p, W.rowptr.p); ++ctx->launches; }
   else CUDA_TRY(cudaMemsetAsync(W.rowptr.p, 0, sizeof(int) * (W.nvert + 1), ctx->st));
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaStreamSynchronize(ctx->st));
@@ -552,7 +552,7 @@ rbc3d_status run_wall_quad(rbc3d_ctx* ctx, int tlist, double c1, int prec) {
   if (s) return s;
   WallArgs a = wall_args(ctx);
   CUDA_TRY(cudaMemsetAsync(ctx->dcnt.p + 4, 0, 2 * sizeof(unsigned long long), ctx->st));
-  k_wall_quad<<<nblk(t.n, 128), 128, 0, ctx->st>>>(a, t.n, t.x.p, t.Acoef.p, t.order.p, c1, t.v.p, ctx->dcnt.p);
+  { k_wall_quad<<<nblk(t.n, 128), 128, 0, ctx->st>>>(a, t.n, t.x.p, t.Acoef.p, t.order.p, c1, t.v.p, ctx->dcnt.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   unsigned long long h[2];
   CUDA_TRY(cudaMemcpyAsync(h, ctx->dcnt.p + 4, sizeof(h), cudaMemcpyDeviceToHost, ctx->st));
@@ -567,8 +567,8 @@ rbc3d_status run_wall_self(rbc3d_ctx* ctx, double c1) {
   if (W.nvert == 0) return RBC3D_OK;
   if (!W.prepared) return ctx_fail(ctx, RBC3D_ERR_STATE, "PrepareSingIntOnWall not called");
   TargetSet& t = ctx->tl[RBC3D_TLIST_WALL];
-  k_self_spmv<<<nblk(W.nvert, 128), 128, 0, ctx->st>>>(W.nvert, W.rowptr.p, W.col.p, W.val.p, W.f.p, t.Acoef.p, c1,
-                                                        t.v.p);
+  { k_self_spmv<<<nblk(W.nvert, 128), 128, 0, ctx->st>>>(W.nvert, W.rowptr.p, W.col.p, W.val.p, W.f.p, t.Acoef.p, c1,
+                                                        t.v.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   return RBC3D_OK;
 }
@@ -579,7 +579,7 @@ rbc3d_status wall_residual_dev(rbc3d_ctx* ctx, int prec) {
   rbc3d_status s = matvec_dev(ctx, RBC3D_TLIST_WALL, c, c, RBC3D_TERM_ALL, prec);
   if (s) return s;
   TargetSet& t = ctx->tl[RBC3D_TLIST_WALL];
-  k_add_const<<<nblk(t.n, 256), 256, 0, ctx->st>>>(t.n, ctx->prm.vBkg[0], ctx->prm.vBkg[1], ctx->prm.vBkg[2], t.v.p);
+  { k_add_const<<<nblk(t.n, 256), 256, 0, ctx->st>>>(t.n, ctx->prm.vBkg[0], ctx->prm.vBkg[1], ctx->prm.vBkg[2], t.v.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   return RBC3D_OK;
 }
@@ -590,7 +590,7 @@ rbc3d_status wall_matmult_dev(rbc3d_ctx* ctx, int prec, const double* u_dev, dou
   WallState& W = ctx->wall;
   TargetSet& t = ctx->tl[RBC3D_TLIST_WALL];
   if (!W.prepared) return ctx_fail(ctx, RBC3D_ERR_STATE, "PrepareSingIntOnWall not called");
-  k_expand<<<nblk(W.nvert, 256), 256, 0, ctx->st>>>(W.nvert, W.glb.p, u_dev, W.f.p);
+  { k_expand<<<nblk(W.nvert, 256), 256, 0, ctx->st>>>(W.nvert, W.glb.p, u_dev, W.f.p); ++ctx->launches; }
   CUDA_TRY(t.v.alloc(3 * (size_t)t.n));
   CUDA_TRY(cudaMemsetAsync(t.v.p, 0, sizeof(double) * 3 * t.n, ctx->st));
   double c1 = 1. / (4. * RBC3D_PI);
@@ -599,7 +599,7 @@ rbc3d_status wall_matmult_dev(rbc3d_ctx* ctx, int prec, const double* u_dev, dou
   if ((s = pme_spread(ctx, c1, 0., 0, 1, prec))) return s;
   if ((s = pme_transform(ctx))) return s;
   if ((s = pme_gather(ctx, RBC3D_TLIST_WALL))) return s;
-  k_assemble<<<nblk(W.nvert, 256), 256, 0, ctx->st>>>(W.nvert, W.glb.p, W.writer.p, t.v.p, 1.0, y_dev);
+  { k_assemble<<<nblk(W.nvert, 256), 256, 0, ctx->st>>>(W.nvert, W.glb.p, W.writer.p, t.v.p, 1.0, y_dev); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   return RBC3D_OK;
 }
@@ -624,8 +624,8 @@ rbc3d_status wall_solve(rbc3d_ctx* ctx, const rbc3d_solve_opts* o, const double*
   rbc3d_status s;
   // rhs = -assemble(residual velocity)
   if ((s = wall_residual_dev(ctx, prec))) return s;
-  k_assemble<<<nblk(W.nvert, 256), 256, 0, ctx->st>>>(W.nvert, W.glb.p, W.writer.p, ctx->tl[RBC3D_TLIST_WALL].v.p, -1.0,
-                                                       b.p);
+  { k_assemble<<<nblk(W.nvert, 256), 256, 0, ctx->st>>>(W.nvert, W.glb.p, W.writer.p, ctx->tl[RBC3D_TLIST_WALL].v.p, -1.0,
+                                                       b.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   if (o->guess && guess) CUDA_TRY(cudaMemcpyAsync(x.p, guess, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->st));
   else CUDA_TRY(cudaMemsetAsync(x.p, 0, sizeof(double) * n, ctx->st));
@@ -637,7 +637,7 @@ rbc3d_status wall_solve(rbc3d_ctx* ctx, const rbc3d_solve_opts* o, const double*
     rbc3d_status e = matvec(x.p, w.p);
     if (e) return e;
     CUDA_TRY(cudaMemcpyAsync(r.p, b.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->st));
-    k_axpby<<<nblk(n, 256), 256, 0, ctx->st>>>(n, -1.0, w.p, 1.0, r.p);
+    { k_axpby<<<nblk(n, 256), 256, 0, ctx->st>>>(n, -1.0, w.p, 1.0, r.p); ++ctx->launches; }
     return RBC3D_OK;
   };
   if ((s = residual())) return s;
@@ -648,26 +648,26 @@ rbc3d_status wall_solve(rbc3d_ctx* ctx, const rbc3d_solve_opts* o, const double*
   int its = 0;
   bool conv = beta <= ttol;
   while (!conv && its < o->max_it) {
-    k_axpby<<<nblk(n, 256), 256, 0, ctx->st>>>(n, 1.0 / beta, r.p, 0.0, V.p);
+    { k_axpby<<<nblk(n, 256), 256, 0, ctx->st>>>(n, 1.0 / beta, r.p, 0.0, V.p); ++ctx->launches; }
     std::vector<double> gh(R + 1, 0.);
     gh[0] = beta;
     CUDA_TRY(cudaMemcpyAsync(g.p, gh.data(), sizeof(double) * (R + 1), cudaMemcpyHostToDevice, ctx->st));
     int k;
     for (k = 0; k < R && its < o->max_it; ++k) {
       if ((s = matvec(V.p + k * ld, w.p))) return s;
-      k_dots<<<k + 1, 512, 0, ctx->st>>>(n, k + 1, V.p, ld, w.p, hcol.p);
-      k_orth<<<nblk(n, 256), 256, 0, ctx->st>>>(n, k + 1, V.p, ld, hcol.p, w.p);
+      { k_dots<<<k + 1, 512, 0, ctx->st>>>(n, k + 1, V.p, ld, w.p, hcol.p); ++ctx->launches; }
+      { k_orth<<<nblk(n, 256), 256, 0, ctx->st>>>(n, k + 1, V.p, ld, hcol.p, w.p); ++ctx->launches; }
       double hn = dev_norm(ctx, n, w.p, tmp.p);
-      if (hn > 0) k_axpby<<<nblk(n, 256), 256, 0, ctx->st>>>(n, 1.0 / hn, w.p, 0.0, V.p + (k + 1) * ld);
-      k_givens<<<1, 1, 0, ctx->st>>>(k, R + 1, H.p, hcol.p, hn, cs.p, sn.p, g.p, tmp.p + R + 1);
+      if (hn > 0) { k_axpby<<<nblk(n, 256), 256, 0, ctx->st>>>(n, 1.0 / hn, w.p, 0.0, V.p + (k + 1) * ld); ++ctx->launches; }
+      { k_givens<<<1, 1, 0, ctx->st>>>(k, R + 1, H.p, hcol.p, hn, cs.p, sn.p, g.p, tmp.p + R + 1); ++ctx->launches; }
       double res = 0;
       CUDA_TRY(cudaMemcpyAsync(&res, tmp.p + R + 1, sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
       CUDA_TRY(cudaStreamSynchronize(ctx->st));
       ++its;
       if (res <= ttol || hn == 0) { ++k; conv = true; break; }
     }
-    k_backsolve<<<1, 1, 0, ctx->st>>>(k, R + 1, H.p, g.p, yv.p);
-    k_xupdate<<<nblk(n, 256), 256, 0, ctx->st>>>(n, k, V.p, ld, yv.p, x.p);
+    { k_backsolve<<<1, 1, 0, ctx->st>>>(k, R + 1, H.p, g.p, yv.p); ++ctx->launches; }
+    { k_xupdate<<<nblk(n, 256), 256, 0, ctx->st>>>(n, k, V.p, ld, yv.p, x.p); ++ctx->launches; }
     if ((s = residual())) return s;
     beta = dev_norm(ctx, n, r.p, tmp.p);
     if (beta <= ttol) conv = true;
@@ -676,8 +676,8 @@ rbc3d_status wall_solve(rbc3d_ctx* ctx, const rbc3d_solve_opts* o, const double*
   S.converged = conv ? 1 : 0;
   S.rnorm = beta;
   // wall f = f0 + expand(x)
-  k_expand<<<nblk(W.nvert, 256), 256, 0, ctx->st>>>(W.nvert, W.glb.p, x.p, W.f.p);
-  k_axpby<<<nblk(3 * W.nvert, 256), 256, 0, ctx->st>>>(3 * W.nvert, 1.0, f0.p, 1.0, W.f.p);
+  { k_expand<<<nblk(W.nvert, 256), 256, 0, ctx->st>>>(W.nvert, W.glb.p, x.p, W.f.p); ++ctx->launches; }
+  { k_axpby<<<nblk(3 * W.nvert, 256), 256, 0, ctx->st>>>(3 * W.nvert, 1.0, f0.p, 1.0, W.f.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaStreamSynchronize(ctx->st));
   S.ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();

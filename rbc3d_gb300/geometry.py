@@ -90,6 +90,52 @@ def biconcave_surface(th, phi, R, xc, rc=1.0):
     return X, N, detJ
 
 
+def sphere_surface(th, phi, radius, xc):
+    """Sphere of given radius (RBC_MakeSphere, ModRbc.F90:147-171): position,
+    unit normal and detJ = |x_th x x_phi| / sin(th) = radius^2."""
+    st, ct = np.sin(th), np.cos(th)
+    cp, sp = np.cos(phi), np.sin(phi)
+    N = np.stack([st[:, None] * cp[None, :], st[:, None] * sp[None, :],
+                  np.broadcast_to(ct[:, None], (th.size, phi.size))], axis=-1)
+    X = radius * N + xc
+    detJ = np.full((th.size, phi.size), radius * radius)
+    return X, N.copy(), detJ
+
+
+def make_sphere_cells(centres, radius=1.0, nlat=25, nlon=50):
+    """Spherical cells (zero densities) in the C-ABI layout."""
+    th, phi, w = gauss_grid(nlat, nlon)
+    the = equi_theta(nlat)
+    X, A3, DJ, SX, SA, SD, areas, msz = [], [], [], [], [], [], [], []
+    for c in centres:
+        x, n, dj = sphere_surface(th, phi, radius, c)
+        xe, ne, dje = sphere_surface(the, phi, radius, c)
+        X.append(x); A3.append(n); DJ.append(dj[..., None])
+        SX.append(spline_on_sphere(xe)); SA.append(spline_on_sphere(ne)); SD.append(spline_on_sphere(dje[..., None]))
+        area = float(np.sum(dj * w[:, None]))
+        areas.append(area)
+        msz.append(math.sqrt(area / nlat ** 2))
+    nc = len(centres)
+    cells = Cells(nlat=nlat, nlon=nlon, th=th, phi=phi, w=w, ncell=nc, celltype=np.zeros(nc, dtype=np.int32),
+                  x=_to_points(np.array(X)), a3=_to_points(np.array(A3)), detJ=_to_points(np.array(DJ))[0].copy(),
+                  area=np.array(areas), meshSize=np.array(msz), spl_x=np.ascontiguousarray(np.array(SX)),
+                  spl_a3=np.ascontiguousarray(np.array(SA)), spl_detJ=np.ascontiguousarray(np.array(SD)),
+                  centres=np.asarray(centres))
+    cells.f = np.zeros_like(cells.x)
+    cells.g = np.zeros_like(cells.x)
+    cells.spl_F = np.zeros((nc, 4, 3, nlon, 2 * nlat))
+    cells.spl_G = np.zeros_like(cells.spl_F)
+    return cells
+
+
+def sphere_uniform_spline(cells, fvec, radius=1.0):
+    """FdetJ spline of a constant density fvec on spherical cells."""
+    the = equi_theta(cells.nlat)
+    v = np.broadcast_to(np.asarray(fvec) * radius * radius, (the.size, cells.nlon, 3)).copy()
+    tab = spline_on_sphere(v)
+    return np.ascontiguousarray(np.broadcast_to(tab, (cells.ncell,) + tab.shape).copy())
+
+
 def random_rotation(rng):
     q = rng.normal(size=4)
     q /= np.linalg.norm(q)
@@ -247,7 +293,7 @@ def place_cells(rng, ncell, L, min_dist, inside=None, max_tries=2_000_000):
 
 
 def make_cells(rng, ncell, L, min_dist, nlat=25, nlon=50, celltype=0, rc=1.0,
-               inside=None, with_g=False, centres=None):
+               inside=None, with_g=False, centres=None, rotations=None):
     th, phi, w = gauss_grid(nlat, nlon)
     the = equi_theta(nlat)
     if centres is None:
@@ -256,7 +302,7 @@ def make_cells(rng, ncell, L, min_dist, nlat=25, nlon=50, celltype=0, rc=1.0,
     rots = []
     areas, msz = [], []
     for ic in range(ncell):
-        R = random_rotation(rng)
+        R = random_rotation(rng) if rotations is None else np.asarray(rotations[ic])
         rots.append(R)
         x, n, dj = biconcave_surface(th, phi, R, centres[ic], rc)
         xe, ne, dje = biconcave_surface(the, phi, R, centres[ic], rc)

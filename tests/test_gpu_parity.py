@@ -1,0 +1,196 @@
+"""Parity of the CUDA path (through the C ABI) with the FP64 oracle.
+
+Bar (the benchmark spec): relative L2 velocity error <= 1e-6 for the FP32C matvec;
+the FP64 plain form agrees with the oracle to rounding (1e-10).  Counts of
+pairs within rc, neighbour-cell items and near-singular corrections must be
+identical."""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from rbc3d_gb300 import RBC3DError
+from rbc3d_gb300 import geometry as G
+from rbc3d_gb300.abi import (Context, FP32C, FP64, TERM_ALL, TERM_CORR, TERM_LINEAR, TERM_PME, TERM_REAL,
+                             TLIST_RAW, TLIST_RBC, TLIST_WALL)
+
+pytestmark = pytest.mark.gpu
+C = 1 / (4 * math.pi)
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def setup(lib, prm, cells, dl):
+    ctx = Context(lib, prm)
+    ctx.set_cells(cells)
+    ctx.set_cell_density(f=cells.f, g=cells.g if dl else None, spl_F=cells.spl_F, spl_G=cells.spl_G if dl else None)
+    return ctx
+
+
+@pytest.fixture(scope="module")
+def c1_case():
+    prm, cells, _ = G.config("C1")
+    return prm, cells
+
+
+@pytest.fixture(scope="module")
+def sldl_case():
+    prm, cells, _ = G.config("C2", ncell=24)
+    prm["Lb"] = [20.0] * 3
+    return prm, cells
+
+
+@pytest.mark.parametrize("prec,tol", [(FP64, 1e-12), (FP32C, 1e-6)])
+def test_c1_single_layer(gpu, oracle, c1_case, prec, tol):
+    prm, cells = c1_case
+    o = setup(oracle, prm, cells, False)
+    g = setup(gpu, prm, cells, False)
+    vo = o.add_int_on_rbcs(TLIST_RBC, C, 0.0)
+    vg = g.add_int_on_rbcs(TLIST_RBC, C, 0.0, prec=prec)
+    assert rel(vg, vo) < tol
+    co, cg = o.counts(), g.counts()
+    assert cg["pairs_within_rc"] == co["pairs_within_rc"]
+    assert cg["nbr_items"] == co["nbr_items"] and cg["self_items"] == co["self_items"]
+    po = o.pme(TLIST_RBC, C, 0.0)
+    pg = g.pme(TLIST_RBC, C, 0.0, prec=prec)
+    assert rel(pg, po) < max(tol, 1e-6 if prec == FP32C else 1e-12)
+    assert rel(vg + pg, vo + po) < tol
+
+
+@pytest.mark.parametrize("prec,tol", [(FP64, 1e-10), (FP32C, 1e-6)])
+def test_sldl_with_near_singular(gpu, oracle, sldl_case, prec, tol):
+    prm, cells = sldl_case
+    o = setup(oracle, prm, cells, True)
+    g = setup(gpu, prm, cells, True)
+    vo = o.matvec(TLIST_RBC, C, C, TERM_ALL)
+    vg = g.matvec(TLIST_RBC, C, C, TERM_ALL, prec)
+    assert rel(vg, vo) < tol
+    co, cg = o.counts(), g.counts()
+    assert cg["nearsing_items"] == co["nearsing_items"] > 0
+    assert cg["nbr_items"] == co["nbr_items"]
+
+
+def test_near_screen_agrees_with_fp64(gpu, sldl_case, monkeypatch):
+    """FP32C screens the projections; with RBC3D_VERIFY_SCREEN=1 every
+    screened item is also decided in FP64: no disagreement allowed."""
+    monkeypatch.setenv("RBC3D_VERIFY_SCREEN", "1")
+    prm, cells = sldl_case
+    g = setup(gpu, prm, cells, True)
+    g.matvec(TLIST_RBC, C, C, TERM_ALL, FP32C)
+    cnt = g.counts()
+    assert cnt["screen_misses"] == 0 and cnt["nearsing_items"] > 0
+
+
+def test_l2_entry_points_compose(gpu, sldl_case):
+    """AddIntOnRbcs + PME_* called separately equal the composite matvec."""
+    prm, cells = sldl_case
+    g = setup(gpu, prm, cells, True)
+    v1 = g.add_int_on_rbcs(TLIST_RBC, C, C, prec=FP64)
+    v1 = g.pme(TLIST_RBC, C, C, prec=FP64, v=v1)
+    v2 = g.matvec(TLIST_RBC, C, C, TERM_REAL | TERM_CORR | TERM_LINEAR | TERM_PME, FP64)
+    assert rel(v1, v2) < 1e-13
+
+
+def test_raw_targets_near_surfaces(gpu, oracle, sldl_case):
+    prm, cells = sldl_case
+    rng = np.random.default_rng(9)
+    pick = rng.choice(cells.x.shape[1], 64, replace=False)
+    raw = np.concatenate([cells.x[:, pick] + d * cells.a3[:, pick] for d in (0.002, -0.002, 0.1, -0.3)], axis=1)
+    raw = np.ascontiguousarray(np.concatenate([raw, rng.uniform(0, 20, (3, 64))], axis=1))
+    out = {}
+    for lab, lib in (("o", oracle), ("g", gpu)):
+        ctx = setup(lib, prm, cells, True)
+        ctx.set_raw_targets(raw)
+        out[lab] = (ctx.calc_velocity_field(TLIST_RAW, FP64), ctx.counts())
+    assert rel(out["g"][0], out["o"][0]) < 1e-10
+    assert out["g"][1]["nearsing_items"] == out["o"][1]["nearsing_items"] > 0
+
+
+def test_fp32c_vs_fp64_full_size_c2(gpu):
+    """Full 256-cell SL+DL workload: FP32C within 1e-6 of the FP64 plain form
+    (which matches the oracle at the sizes above)."""
+    prm, cells, _ = G.config("C2")
+    g = setup(gpu, prm, cells, True)
+    v64 = g.matvec(TLIST_RBC, C, C, TERM_ALL, FP64)
+    v32 = g.matvec(TLIST_RBC, C, C, TERM_ALL, FP32C)
+    assert rel(v32, v64) < 1e-6
+
+
+def test_linearity_in_density(gpu, sldl_case):
+    prm, cells = sldl_case
+    g = setup(gpu, prm, cells, True)
+    a = g.matvec(TLIST_RBC, C, C, TERM_ALL, FP64)
+    g.set_cell_density(f=2 * cells.f, g=-cells.g, spl_F=2 * cells.spl_F, spl_G=-cells.spl_G)
+    b = g.matvec(TLIST_RBC, C, 0.0, TERM_ALL, FP64)
+    c = g.matvec(TLIST_RBC, 0.0, C, TERM_ALL, FP64)
+    g.set_cell_density(f=cells.f, g=cells.g, spl_F=cells.spl_F, spl_G=cells.spl_G)
+    s = g.matvec(TLIST_RBC, C, 0.0, TERM_ALL, FP64)
+    d = g.matvec(TLIST_RBC, 0.0, C, TERM_ALL, FP64)
+    assert rel(b, 2 * s) < 1e-12 and rel(c, -d) < 1e-12 and rel(s + d, a) < 1e-12
+
+
+def _tube_case():
+    rng = np.random.default_rng(5)
+    L = [9.0, 9.0, 12.0]
+    prm = dict(Lb=L, alpha=G.alpha_for_cutoff(2.9, 1e-6), rc=2.9, eps=1e-6, Nb=[48, 48, 64], P=6, nlat=25,
+               nlon=50, ncelltypes=1, viscRat=[1.0], vBkg=[0, 0, 8.0])
+    wall = G.make_tube(4.0, 12.0, 24, 48, (4.5, 4.5))
+    cells = G.make_cells(rng, 4, L, 3.0, inside=lambda c: (c[0] - 4.5) ** 2 + (c[1] - 4.5) ** 2 < 1.5 ** 2)
+    return prm, cells, wall
+
+
+def test_walls_and_no_slip_solve(gpu, oracle):
+    prm, cells, wall = _tube_case()
+    res = {}
+    fw = np.ascontiguousarray(np.sin(wall.x))
+    u = np.ascontiguousarray(np.cos(np.arange(wall.ndof) * 0.37))
+    for lab, lib in (("o", oracle), ("g", gpu)):
+        ctx = setup(lib, prm, cells, False)
+        ctx.set_walls(wall)
+        ctx.set_wall_density(fw)
+        ctx.prepare_sing_int_on_wall()
+        vq = ctx.add_int_on_walls(TLIST_RBC, C)
+        vs = ctx.add_int_on_walls(TLIST_WALL, C)
+        y = ctx.wall_matmult(u)
+        r = ctx.compute_wall_residual_vel()
+        ctx.set_wall_density(np.zeros((3, wall.nvert)))
+        st, code = ctx.no_slip_wall(1e-8, 200)
+        res[lab] = (vq, vs, y, r, ctx.get_wall_density(wall.nvert), st, code, ctx.counts())
+    o, g = res["o"], res["g"]
+    for i in range(4):
+        assert rel(g[i], o[i]) < 1e-12, i
+    assert g[6] == 0 and o[6] == 0 and g[5].converged == 1
+    assert abs(g[5].iterations - o[5].iterations) <= 1
+    assert g[5].rnorm / g[5].bnorm <= 1.01e-8
+    assert rel(g[4], o[4]) < 1e-8
+    assert g[7]["wall_pairs"] == o[7]["wall_pairs"]
+
+
+def test_error_paths(gpu, c1_case):
+    prm, cells = c1_case
+    g = setup(gpu, prm, cells, False)
+    with pytest.raises(RBC3DError) as e:
+        g.matvec(7, C, 0.0)
+    assert e.value.code == 1
+    import ctypes
+    g2 = Context(gpu, prm)
+    dummy = np.zeros(3)
+    code = g2.L.fn["pme_add_interp_vel"](g2.h, TLIST_RBC, dummy.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    assert code == 6  # PME_Transform not called yet
+    # empty raw target list is a no-op
+    g.set_raw_targets(np.zeros((3, 0)))
+    assert g.matvec(TLIST_RAW, C, 0.0).shape == (3, 0)
+
+
+def test_wall_solve_error_codes(gpu):
+    prm, cells, wall = _tube_case()
+    ctx = setup(gpu, prm, cells, False)
+    ctx.set_walls(wall)
+    st, code = ctx.no_slip_wall(1e-8, 10, check=False)
+    assert code == 6  # PrepareSingIntOnWall not called
+    ctx.prepare_sing_int_on_wall()
+    st, code = ctx.no_slip_wall(1e-12, 2, check=False)
+    assert code == 4 and st.iterations == 2 and st.converged == 0  # NOCONV, bounded
