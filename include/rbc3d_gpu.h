@@ -212,6 +212,26 @@ rbc3d_status rbc3d_calc_velocity_field(rbc3d_ctx* ctx, int tlist, int prec,
 
 rbc3d_status rbc3d_get_counts(const rbc3d_ctx* ctx, rbc3d_counts* out);
 
+/* Allocation-free linear double-layer term.  No counterpart in the reference:
+ * it serves callers that cannot allocate device memory -- programs whose
+ * device arrays belong to another owner (OpenACC / CUDA Fortran data regions,
+ * an application memory pool) or loops in which a cudaMalloc would
+ * synchronise the device.  It computes the AddLinearInt term
+ * (v += c2 * xvint / Acoef for nt targets) from caller-owned DEVICE arrays
+ * laid out as the rest of this ABI (x, g, a3: 3N; detJ: N; w: nlat;
+ * celltype: ncell; Acoef: nt; v: 3 nt), enqueued on `stream` (a
+ * cudaStream_t, NULL for the default stream).  It allocates nothing: its
+ * per-cell scratch is a fixed array inside the library, so ncell is limited
+ * to 8192 (larger values return RBC3D_ERR_ARG).  The first call on a device
+ * looks up that array's device address; make this first call before any
+ * stream capture.  The array is shared by every call: calls that overlap on
+ * the GPU race. */
+rbc3d_status rbc3d_add_linear_int_noalloc(int ncell, int nlat, int nlon, const double* x, const double* g,
+                                          const double* a3, const double* detJ, const double* w,
+                                          const int* celltype, int ncelltypes, const double* viscRat,
+                                          const double Lb[3], double c2, int nt, const double* Acoef, double* v,
+                                          void* stream);
+
 /* ---- device timing (replaces the per-step MPI_WTime print of TimeInt_*,
  * ModTimeInt.F90:119,166-174, with CUDA events on the context stream) ---- */
 #define RBC3D_NSTAGE 8
