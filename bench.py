@@ -130,9 +130,12 @@ def barrier(dist):
         dist.barrier()
 
 
-def make_inputs(seed):
+def make_inputs(seed, ncell=None):
     from rbc3d_gb300 import geometry as G
-    prm, cells, _ = G.config("C2", seed=seed)
+    prm, cells, _ = G.config("C2", seed=seed, ncell=ncell)
+    if ncell:  # same cell density as the 256-cell box (profiling runs)
+        prm["Lb"] = [40.0 * (ncell / 256.0) ** (1 / 3)] * 3
+        prm, cells, _ = G.config("C2", seed=seed, ncell=ncell, L=prm["Lb"][0])
     return prm, cells
 
 
@@ -195,6 +198,8 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline")
+    ap.add_argument("--cells", type=int, default=None, help="smaller workload (profiling)")
+    ap.add_argument("--quick", action="store_true", help="FP32C timing only (profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     dist = dist_init()
@@ -209,7 +214,7 @@ def main():
     from rbc3d_gb300.abi import FP32C, FP64, TERM_ALL, TLIST_RBC, Context, STAGES
 
     t0 = time.perf_counter()
-    prm, cells = make_inputs(args.seed + rank)
+    prm, cells = make_inputs(args.seed + rank, args.cells)
     log(f"inputs generated in {time.perf_counter() - t0:.1f}s")
     N = cells.x.shape[1]
     lib = library()
@@ -243,14 +248,25 @@ def main():
     ms_step = ms / args.steps
     value = ws * N / (ms_step * 1e-3)
 
+    if args.quick:
+        if rank == 0:
+            print(json.dumps({"quick": True, "ms_per_step": ms_step, "targets": N, "value": value,
+                              "stages_ms_per_step": {k: v[0] / args.steps for k, v in stages.items()},
+                              "gpu_launches": launches}), flush=True)
+        ctx.close()
+        return 0
+
     # ---- FP64 plain form (same algorithm, everything FP64)
     for _ in range(2):
         step(FP64)
     k64 = max(2, args.steps // 3)
+    ctx.set_profiling(1)
     ctx.timer_start()
     for _ in range(k64):
         step(FP64)
     ms64 = dist_max(dist, ctx.timer_stop()) / k64
+    st64 = {k: v[0] / k64 for k, v in ctx.stage_times().items()}
+    ctx.set_profiling(0)
     fp64_value = ws * N / (ms64 * 1e-3)
 
     # ---- end to end through the C ABI with pinned host buffers
@@ -339,11 +355,12 @@ def main():
             "data": "synthetic (seeded biconcave cells, SH densities)",
             "config": dict(WORKLOAD, targets=N, l2="working set (spline tables 307 MB, PME grids) > 129 MB L2"),
             "fp64_plain": {"value": fp64_value, "unit": "targets/s", "ms_per_step": ms64,
-                           "fp32c_over_fp64": value / fp64_value},
+                           "fp32c_over_fp64": value / fp64_value, "stages_ms_per_step": st64},
             "e2e": {"value": e2e_value, "unit": "targets/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": te * 1e3},
             "stages_ms_per_step": st_ms,
-            "counts": {k: counts[k] for k in ("pairs_within_rc", "nbr_items", "nearsing_items", "self_items")},
+            "counts": {k: counts[k] for k in ("pairs_within_rc", "nbr_items", "nearsing_items", "self_items",
+                                              "screen_misses")},
             "roofline": roof,
             "fma_peaks_tflops": {"fp32": peak32, "fp64": peak64},
             "cpu_baseline": cpu,

@@ -15,6 +15,7 @@
 #include <cub/cub.cuh>
 
 #include <algorithm>
+#include <cmath>
 #include <vector>
 
 #include "ctx.hpp"
@@ -114,6 +115,7 @@ struct PairArgs {
   double rc2;
   float rc2_f, reps2_f;
   float rthr2_f;  // FP32 path: cross-surface pairs closer than this are left to the FP64 near-singular pass
+  float sqpa_f, two_isqa_f, m8_ispi_f, q75_spi_f;  // sqrt(pi/alpha), 2/sqrt(alpha), -8/sqrt(pi), 0.75 sqrt(pi)
   Tables T;
   // near-singular work list
   int collect;
@@ -251,12 +253,13 @@ __global__ void __launch_bounds__(TILE) k_pair32(PairArgs a) {
           if (r2 < a.reps2_f) continue;
           float rinv = rsqrtf(r2);
           float r = r2 * rinv;
-          float s = r * a.T.ntab_over_rc_f;
-          int i = (int)s;
-          if (i >= EWALD_NTAB) continue;
-          float fr = s - (float)i;
-          float4 e = __ldg(a.T.sl32 + i);
-          float c1 = fmaf(fr, e.y, e.x), c2 = fmaf(fr, e.w, e.z);
+          // Ewald coefficients evaluated directly (erfc / exp in FP32) rather
+          // than by per-lane gathers into the 8193-entry tables: the tables'
+          // lerp differs from the exact functions by ~2e-8 relative, below
+          // FP32 resolution (the FP64 plain form keeps the tables).
+          float st = r * a.sqpa_f;  // r*sqrt(pi/alpha)
+          float ex = expf(-st * st);
+          float c1 = erfcf(st), c2 = a.two_isqa_f * ex;
           float ir2 = rinv * rinv;
           float A = (c1 * rinv + c2) * ir2;
           float B = c1 * rinv - c2;
@@ -266,8 +269,8 @@ __global__ void __launch_bounds__(TILE) k_pair32(PairArgs a) {
           float vy = Ad * yy + B * sm.fy[j];
           float vz = Ad * zz + B * sm.fz[j];
           if (DL) {
-            float2 d = __ldg(a.T.dl32 + i);
-            float cdl = fmaf(fr, d.y, d.x);
+            // -8/sqrt(pi) [exp(-t^2)(1.5 t + t^3) + 0.75 sqrt(pi) erfc(t)] / r^5
+            float cdl = a.m8_ispi_f * (ex * (st * (1.5f + st * st)) + a.q75_spi_f * c1);
             float Adl = cdl * ir2 * ir2 * rinv;
             float dg = xx * sm.gx[j] + yy * sm.gy[j] + zz * sm.gz[j];
             float da = xx * sm.ax[j] + yy * sm.ay[j] + zz * sm.az[j];
@@ -538,6 +541,10 @@ rbc3d_status run_pair_sum(rbc3d_ctx* ctx, int tlist, double c1, double c2, int p
   a.c1 = c1; a.c2 = c2; a.c1f = (float)c1; a.c2f = (float)c2;
   a.rc2 = ctx->prm.rc * ctx->prm.rc; a.rc2_f = (float)a.rc2; a.reps2_f = (float)(ctx->T.r_eps * ctx->T.r_eps);
   a.rthr2_f = (float)(ctx->near_rthr * ctx->near_rthr);
+  a.sqpa_f = (float)sqrt(RBC3D_PI / ctx->prm.alpha);
+  a.two_isqa_f = (float)(2.0 / sqrt(ctx->prm.alpha));
+  a.m8_ispi_f = (float)(-8.0 / sqrt(RBC3D_PI));
+  a.q75_spi_f = (float)(0.75 * sqrt(RBC3D_PI));
   a.T = ctx->T;
   a.collect = collect_nbr ? 1 : 0;
   a.items = ctx->items.p; a.cap = ctx->items_cap; a.cnt = ctx->dcnt.p;

@@ -383,8 +383,10 @@ def make_tube(radius, Lz, ntheta, nz, centre_xy):
 
 # ---------------------------------------------------------------------------
 # Named workloads (sizes of the benchmark configurations)
-def config(name: str, seed: int = 20261203, ncell: int | None = None):
-    """Build a named workload.  Returns (params dict, Cells, Wall|None)."""
+def config(name: str, seed: int = 20261203, ncell: int | None = None, L: float | None = None):
+    """Build a named workload.  Returns (params dict, Cells, Wall|None).
+    ``ncell`` / ``L`` override the cell count and the periodic box side."""
+    L_override = L
     rng = np.random.default_rng(seed)
     eps = 1e-6
     rc = 3.0
@@ -399,6 +401,8 @@ def config(name: str, seed: int = 20261203, ncell: int | None = None):
         L = [16.5, 16.5, 48.0]; n = ncell or 64; Nb = [96, 96, 256]; md = 3.0; vr = 1.0; g = False
     else:
         raise ValueError(name)
+    if L_override is not None:
+        L = [float(L_override)] * 3
     prm = dict(Lb=L, alpha=alpha, rc=rc, eps=eps, Nb=Nb, P=6, nlat=25, nlon=50,
                ncelltypes=1, viscRat=[vr], vBkg=[0.0, 0.0, 8.0] if name == "C3" else [0.0, 0.0, 0.0])
     wall = None
