@@ -211,7 +211,7 @@ def main():
     from rbc3d_gb300 import build as B
     B.build()
     from rbc3d_gb300 import library
-    from rbc3d_gb300.abi import FP32C, FP64, TERM_ALL, TLIST_RBC, Context, STAGES
+    from rbc3d_gb300.abi import FP32C, FP32M, FP64, TERM_ALL, TLIST_RBC, Context, STAGES
 
     t0 = time.perf_counter()
     prm, cells = make_inputs(args.seed + rank, args.cells)
@@ -267,6 +267,23 @@ def main():
     ms64 = dist_max(dist, ctx.timer_stop()) / k64
     st64 = {k: v[0] / k64 for k, v in ctx.stage_times().items()}
     ctx.set_profiling(0)
+
+    # ---- FP32M: FP32C with the own-cell polar patch in FP32 + hi/lo geometry
+    for _ in range(2):
+        step(FP32M)
+    ctx.set_profiling(1)
+    ctx.timer_start()
+    for _ in range(args.steps):
+        step(FP32M)
+    msm = dist_max(dist, ctx.timer_stop()) / args.steps
+    stm = {k: v[0] / args.steps for k, v in ctx.stage_times().items()}
+    ctx.set_profiling(0)
+    fp32m_value = ws * N / (msm * 1e-3)
+
+    # ---- relative L2 error of the FP32 modes against the FP64 plain form
+    v64 = ctx.matvec(TLIST_RBC, c, c, TERM_ALL, FP64)
+    err32c = float(np.linalg.norm(ctx.matvec(TLIST_RBC, c, c, TERM_ALL, FP32C) - v64) / np.linalg.norm(v64))
+    err32m = float(np.linalg.norm(ctx.matvec(TLIST_RBC, c, c, TERM_ALL, FP32M) - v64) / np.linalg.norm(v64))
     fp64_value = ws * N / (ms64 * 1e-3)
 
     # ---- end to end through the C ABI with pinned host buffers
@@ -354,8 +371,13 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32c+f64corr",
             "data": "synthetic (seeded biconcave cells, SH densities)",
             "config": dict(WORKLOAD, targets=N, l2="working set (spline tables 307 MB, PME grids) > 129 MB L2"),
+            "rel_l2_vs_fp64_plain": err32c,
             "fp64_plain": {"value": fp64_value, "unit": "targets/s", "ms_per_step": ms64,
                            "fp32c_over_fp64": value / fp64_value, "stages_ms_per_step": st64},
+            "fp32m": {"value": fp32m_value, "unit": "targets/s", "ms_per_step": msm,
+                      "over_fp64": fp32m_value / fp64_value, "rel_l2_vs_fp64_plain": err32m,
+                      "stages_ms_per_step": stm,
+                      "note": "own-cell polar patch in FP32 with FP64-accurate (hi/lo) geometry"},
             "e2e": {"value": e2e_value, "unit": "targets/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": te * 1e3},
             "stages_ms_per_step": st_ms,

@@ -49,9 +49,12 @@ enum {
 /* Arithmetic of one matvec. */
 enum {
   RBC3D_FP64 = 0,  /* plain form: everything FP64 */
-  RBC3D_FP32C = 1  /* pair sums, spread, FFT, gather in FP32 with per-target
+  RBC3D_FP32C = 1, /* pair sums, spread, FFT, gather in FP32 with per-target
                       compensated accumulation; self / near-singular
                       corrections FP64 */
+  RBC3D_FP32M = 2  /* as FP32C, but the own-cell polar patch (RBC_SingInt) in
+                      FP32 with FP64-accurate (hi/lo) positions; needs the
+                      uniform longitude grid phi(j) = j*2*pi/nlon */
 };
 
 /* Target lists (t_TargetList instances of ModData.F90:19-20). */

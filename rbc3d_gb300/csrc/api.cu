@@ -187,7 +187,10 @@ rbc3d_status rbcs_dev(rbc3d_ctx* ctx, int which, double c1, double c2, int prec,
     CUDA_TRY(cudaMemsetAsync(ctx->dcnt.p + 6, 0, sizeof(unsigned long long), ctx->st));
     {
       StageScope sc(ctx, 1);
-      if ((s = run_self_corr(ctx, which, c1, c2))) return s;
+      if (prec == RBC3D_FP32M) {
+        if (!ctx->phi_uniform) return ctx_fail(ctx, RBC3D_ERR_ARG, "FP32M needs phi(j) = j*2*pi/nlon");
+        if ((s = run_self_mixed(ctx, which, c1, c2))) return s;
+      } else if ((s = run_self_corr(ctx, which, c1, c2))) return s;
     }
     {
       StageScope sc(ctx, 2);
@@ -396,6 +399,13 @@ rbc3d_status rbc3d_set_cell_grid(rbc3d_ctx* ctx, const double* th, const double*
     }
   }
   CUDA_TRY(ctx->pw.upload(pw.data(), nrad, ctx->st));
+  ctx->phi_uniform = true;
+  for (int j = 0; j < nlon; ++j)
+    if (std::fabs(phi[j] - j * RBC3D_TWO_PI / nlon) > 1e-12) ctx->phi_uniform = false;
+  {
+    rbc3d_status s = self_mixed_grid(ctx, thG, phiA, pw);
+    if (s) return s;
+  }
   CUDA_TRY(ctx->thG.upload(thG.data(), thG.size(), ctx->st));
   CUDA_TRY(ctx->phiA.upload(phiA.data(), phiA.size(), ctx->st));
   std::vector<double> x0(16), w0(16);
@@ -441,6 +451,7 @@ rbc3d_status rbc3d_set_cells(rbc3d_ctx* ctx, int ncell, const int* celltype, con
   if ((s = upload_splines(ctx, spl_a3, 3, SPL_A3))) return s;
   if ((s = upload_splines(ctx, spl_detJ, 1, SPL_DJ))) return s;
   if ((s = build_source_list(ctx))) return s;
+  if ((s = self_mixed_geom(ctx, x))) return s;
   // tlist_rbc (TargetList_Update, ModTargetList.F90:95-131)
   TargetSet& t = ctx->tl[RBC3D_TLIST_RBC];
   t.n = ctx->npt;
@@ -475,6 +486,7 @@ rbc3d_status rbc3d_set_cell_density(rbc3d_ctx* ctx, const double* f, const doubl
     if ((s = upload_splines(ctx, spl_G, 3, SPL_G))) return s;
     ctx->has_g = true;
   }
+  if ((s = self_mixed_density(ctx, f != nullptr, g != nullptr))) return s;
   return build_source_density(ctx);
 }
 
@@ -551,7 +563,7 @@ int rbc3d_num_targets(const rbc3d_ctx* ctx, int which) {
 
 rbc3d_status rbc3d_add_int_on_rbcs(rbc3d_ctx* ctx, int which, double c1, double c2, int prec, double* v) {
   TargetSet* t = ctx ? tset(ctx, which) : nullptr;
-  if (!t || !v || (prec != RBC3D_FP64 && prec != RBC3D_FP32C)) return ctx_fail(ctx, RBC3D_ERR_ARG, "add_int_on_rbcs");
+  if (!t || !v || !valid_prec(prec)) return ctx_fail(ctx, RBC3D_ERR_ARG, "add_int_on_rbcs");
   rbc3d_status s;
   if ((s = begin(ctx, *t))) return s;
   if ((s = rbcs_dev(ctx, which, c1, c2, prec, RBC3D_TERM_REAL | RBC3D_TERM_CORR | RBC3D_TERM_LINEAR))) return s;
@@ -575,7 +587,7 @@ rbc3d_status rbc3d_prepare_sing_int_on_wall(rbc3d_ctx* ctx) {
 }
 
 rbc3d_status rbc3d_pme_distrib_source(rbc3d_ctx* ctx, double c1, double c2, int cells, int walls, int prec) {
-  if (!ctx || (prec != RBC3D_FP64 && prec != RBC3D_FP32C)) return RBC3D_ERR_ARG;
+  if (!ctx || !valid_prec(prec)) return RBC3D_ERR_ARG;
   return pme_spread(ctx, c1, c2, cells, walls, prec);
 }
 rbc3d_status rbc3d_pme_transform(rbc3d_ctx* ctx) {
@@ -593,7 +605,7 @@ rbc3d_status rbc3d_pme_add_interp_vel(rbc3d_ctx* ctx, int which, double* v) {
 
 rbc3d_status rbc3d_matvec(rbc3d_ctx* ctx, int which, double c1, double c2, unsigned terms, int prec, double* v) {
   TargetSet* t = ctx ? tset(ctx, which) : nullptr;
-  if (!t || (prec != RBC3D_FP64 && prec != RBC3D_FP32C)) return ctx_fail(ctx, RBC3D_ERR_ARG, "matvec");
+  if (!t || !valid_prec(prec)) return ctx_fail(ctx, RBC3D_ERR_ARG, "matvec");
   rbc3d_status s = matvec_dev(ctx, which, c1, c2, terms, prec);
   if (s) return s;
   if (!v) return RBC3D_OK;  // result stays on the device

@@ -144,6 +144,13 @@ struct rbc3d_ctx {
   PmeState pme;
   WallState wall;
 
+  // FP32M self patch: FP32 node records, per-(latitude, patch point) weights,
+  // target positions relative to the cell centre (hi/lo)
+  DBuf<float> mix_rec, mix_pw;
+  DBuf<char> mix_w;
+  DBuf<float4> mix_thi, mix_tlo;
+  bool phi_uniform = false;
+
   DBuf<double> scratch;           // GMRES basis / temporaries
   rbc3d_counts counts{};
 
@@ -194,6 +201,14 @@ rbc3d_status run_wall_self(rbc3d_ctx* ctx, double c1);
 rbc3d_status wall_solve(rbc3d_ctx* ctx, const rbc3d_solve_opts* opt, const double* guess, rbc3d_solve_stats* st);
 rbc3d_status wall_matmult_dev(rbc3d_ctx* ctx, int prec, const double* u_dev, double* y_dev);
 rbc3d_status wall_residual_dev(rbc3d_ctx* ctx, int prec);
+
+// selfmix.cu
+rbc3d_status self_mixed_grid(rbc3d_ctx* ctx, const std::vector<double>& thG, const std::vector<double>& phiA,
+                             const std::vector<double>& pw);
+rbc3d_status self_mixed_geom(rbc3d_ctx* ctx, const double* x_host);
+rbc3d_status self_mixed_density(rbc3d_ctx* ctx, bool f, bool g);
+rbc3d_status run_self_mixed(rbc3d_ctx* ctx, int tlist, double c1, double c2);
+inline bool valid_prec(int p) { return p == RBC3D_FP64 || p == RBC3D_FP32C || p == RBC3D_FP32M; }
 
 // peak.cu
 rbc3d_status fma_peak(int prec, double* tflops);

@@ -549,7 +549,7 @@ rbc3d_status run_pair_sum(rbc3d_ctx* ctx, int tlist, double c1, double c2, int p
   a.collect = collect_nbr ? 1 : 0;
   a.items = ctx->items.p; a.cap = ctx->items_cap; a.cnt = ctx->dcnt.p;
   bool dl = (c2 != 0.0) && ctx->has_g;
-  if (prec == RBC3D_FP32C) {
+  if (prec != RBC3D_FP64) {
     if (dl) { k_pair32<true><<<t.nunits, TILE, 0, ctx->st>>>(a); ++ctx->launches; }
     else { k_pair32<false><<<t.nunits, TILE, 0, ctx->st>>>(a); ++ctx->launches; }
   } else {

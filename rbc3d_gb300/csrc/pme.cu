@@ -330,6 +330,7 @@ rbc3d_status pme_release(rbc3d_ctx* ctx) {
 
 rbc3d_status pme_spread(rbc3d_ctx* ctx, double c1, double c2, int cells, int walls, int prec) {
   PmeState& P = ctx->pme;
+  if (prec != RBC3D_FP64) prec = RBC3D_FP32C;  // FP32C and FP32M share the FP32 PME
   P.sl = std::fabs(c1) > 1.e-10;  // flag_sing_lay, ModPME.F90:74
   P.dl = std::fabs(c2) > 1.e-10;  // flag_doub_lay
   P.prec = prec;

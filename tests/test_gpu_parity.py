@@ -12,7 +12,7 @@ import pytest
 
 from rbc3d_gb300 import RBC3DError
 from rbc3d_gb300 import geometry as G
-from rbc3d_gb300.abi import (Context, FP32C, FP64, TERM_ALL, TERM_CORR, TERM_LINEAR, TERM_PME, TERM_REAL,
+from rbc3d_gb300.abi import (Context, FP32C, FP32M, FP64, TERM_ALL, TERM_CORR, TERM_LINEAR, TERM_PME, TERM_REAL,
                              TLIST_RAW, TLIST_RBC, TLIST_WALL)
 
 pytestmark = pytest.mark.gpu
@@ -43,7 +43,7 @@ def sldl_case():
     return prm, cells
 
 
-@pytest.mark.parametrize("prec,tol", [(FP64, 1e-12), (FP32C, 1e-6)])
+@pytest.mark.parametrize("prec,tol", [(FP64, 1e-12), (FP32C, 1e-6), (FP32M, 1e-6)])
 def test_c1_single_layer(gpu, oracle, c1_case, prec, tol):
     prm, cells = c1_case
     o = setup(oracle, prm, cells, False)
@@ -56,11 +56,11 @@ def test_c1_single_layer(gpu, oracle, c1_case, prec, tol):
     assert cg["nbr_items"] == co["nbr_items"] and cg["self_items"] == co["self_items"]
     po = o.pme(TLIST_RBC, C, 0.0)
     pg = g.pme(TLIST_RBC, C, 0.0, prec=prec)
-    assert rel(pg, po) < max(tol, 1e-6 if prec == FP32C else 1e-12)
+    assert rel(pg, po) < max(tol, 1e-6 if prec != FP64 else 1e-12)
     assert rel(vg + pg, vo + po) < tol
 
 
-@pytest.mark.parametrize("prec,tol", [(FP64, 1e-10), (FP32C, 1e-6)])
+@pytest.mark.parametrize("prec,tol", [(FP64, 1e-10), (FP32C, 1e-6), (FP32M, 1e-6)])
 def test_sldl_with_near_singular(gpu, oracle, sldl_case, prec, tol):
     prm, cells = sldl_case
     o = setup(oracle, prm, cells, True)
@@ -117,6 +117,8 @@ def test_fp32c_vs_fp64_full_size_c2(gpu):
     v64 = g.matvec(TLIST_RBC, C, C, TERM_ALL, FP64)
     v32 = g.matvec(TLIST_RBC, C, C, TERM_ALL, FP32C)
     assert rel(v32, v64) < 1e-6
+    v32m = g.matvec(TLIST_RBC, C, C, TERM_ALL, FP32M)
+    assert rel(v32m, v64) < 1e-6
 
 
 def test_linearity_in_density(gpu, sldl_case):
