@@ -200,6 +200,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline")
     ap.add_argument("--cells", type=int, default=None, help="smaller workload (profiling)")
     ap.add_argument("--quick", action="store_true", help="FP32C timing only (profiling)")
+    ap.add_argument("--no-wall", action="store_true", help="skip the learned-guess wall GMRES comparison")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     dist = dist_init()
@@ -353,6 +354,20 @@ def main():
         except Exception:
             pass
 
+    # ---- wall no-slip GMRES on the tube workload: plain vs history vs learned guess
+    wall = None
+    if not args.quick and not args.no_wall:
+        from rbc3d_gb300.learned_run import run as wall_run
+        t1 = time.perf_counter()
+        w = wall_run(ncell=64, warm_steps=12, test_steps=4, rtol=1e-8, restart=300, max_it=900, train_iters=30,
+                     seed=args.seed + rank)
+        log(f"wall GMRES comparison in {time.perf_counter() - t1:.1f}s")
+        wall = {"workload": "C3 tube (R=8, L=48, 64 cells), FP64 matvec + FP64 Arnoldi, ||r|| < 1e-8 ||b||",
+                **{k: w[k] for k in ("wall_dof", "restart", "history", "plain", "history_only", "learned",
+                                     "speedup_learned", "speedup_history_only", "train_ms_per_step",
+                                     "speedup_learned_incl_training", "mlp")},
+                "steps": "12 warm-up steps (plain solves, history + online training), 4 compared steps"}
+
     # ---- CPU baseline (rank 0, N = 1 only): oracle, all host threads
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
@@ -384,6 +399,7 @@ def main():
             "counts": {k: counts[k] for k in ("pairs_within_rc", "nbr_items", "nearsing_items", "self_items",
                                               "screen_misses")},
             "roofline": roof,
+            "wall_gmres": wall,
             "fma_peaks_tflops": {"fp32": peak32, "fp64": peak64},
             "cpu_baseline": cpu,
             "gpu_launches": launches,

@@ -101,11 +101,17 @@ typedef struct rbc3d_counts {
 } rbc3d_counts;
 
 typedef struct rbc3d_solve_opts {
-  double rtol;   /* ||r|| <= rtol*||b|| (KSPSetTolerances rtol) */
+  double rtol;   /* converged when ||r|| < rtol*||b||, b the right-hand side
+                    (KSPSetTolerances rtol, KSPConvergedDefault) */
   int max_it;    /* KSPSetTolerances max_it */
   int restart;   /* GMRES restart (PETSc default 30) */
   int prec;      /* matvec arithmetic, RBC3D_FP64 or RBC3D_FP32C */
-  int guess;     /* 0: zero increment (reference); 1: caller-supplied guess */
+  int guess;     /* 0: zero increment (reference); 1: caller-supplied guess;
+                    2: caller-supplied guess scaled by a = <b,Ax0>/||Ax0||^2
+                    (never a larger initial residual than 0);
+                    3: two guess vectors x1, x2 (2 x dof doubles), combined
+                    as p x1 + q x2 with the least-squares p, q (one extra
+                    matvec) */
 } rbc3d_solve_opts;
 
 typedef struct rbc3d_solve_stats {
@@ -203,7 +209,8 @@ rbc3d_status rbc3d_compute_wall_residual_vel(rbc3d_ctx* ctx, int prec,
                                              double* v);
 /* NoSlipWall, ModNoSlip.F90:45: GMRES on the wall-density increment (PCNONE),
  * wall f <- f0 + finc.  guess: NULL or a dof-length (3*unique vertices,
- * xyz-interleaved per unique vertex as AssembleArray) initial increment. */
+ * xyz-interleaved per unique vertex as AssembleArray) initial increment
+ * (two of them back to back for guess mode 3). */
 rbc3d_status rbc3d_no_slip_wall(rbc3d_ctx* ctx, const rbc3d_solve_opts* opt,
                                 const double* guess, rbc3d_solve_stats* st);
 /* MyMatMult of ModNoSlip.F90:255 on a dof-length vector: y = A u. */
@@ -214,6 +221,25 @@ rbc3d_status rbc3d_calc_velocity_field(rbc3d_ctx* ctx, int tlist, int prec,
                                        double* v);
 
 rbc3d_status rbc3d_get_counts(const rbc3d_ctx* ctx, rbc3d_counts* out);
+
+/* ---- learned wall-density initial guess (no counterpart in the reference) --
+ * A per-vertex MLP: nin -> width (SiLU) x depth -> nout.  GEMMs run on the
+ * tensor cores with BF16 operands and FP32 accumulation (mma.sync m16n8k16);
+ * master weights, Adam moments and the loss are FP32.  Row-major FP32 host
+ * arrays.  Parameters are packed [W_0 (dout x din), b_0, W_1, b_1, ...]. */
+typedef struct rbc3d_mlp rbc3d_mlp;
+rbc3d_status rbc3d_mlp_create(int nin, int width, int depth, int nout, unsigned long long seed, rbc3d_mlp** out);
+rbc3d_status rbc3d_mlp_destroy(rbc3d_mlp* m);
+long long rbc3d_mlp_num_params(const rbc3d_mlp* m);
+rbc3d_status rbc3d_mlp_params(rbc3d_mlp* m, float* host, int get);
+rbc3d_status rbc3d_mlp_forward(rbc3d_mlp* m, int n, const float* x, float* y);
+/* Mean-squared-error loss and packed FP32 gradients of the batch (x, t). */
+rbc3d_status rbc3d_mlp_gradients(rbc3d_mlp* m, int n, const float* x, const float* t, float* grads, float* loss);
+/* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) on the batch; loss before the step. */
+rbc3d_status rbc3d_mlp_train_step(rbc3d_mlp* m, int n, const float* x, const float* t, float lr, float* loss);
+/* Right-hand side of the wall solve, b = -AssembleArray(Compute_Wall_Residual_Vel)
+ * (ModNoSlip.F90:110-113) for the current wall density: ndof values. */
+rbc3d_status rbc3d_wall_rhs(rbc3d_ctx* ctx, int prec, double* b);
 
 /* Allocation-free linear double-layer term.  No counterpart in the reference:
  * it serves callers that cannot allocate device memory -- programs whose

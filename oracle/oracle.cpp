@@ -890,7 +890,8 @@ static rbc3d_status wall_residual(Ctx* c, double* v) {
 static double nrm2(const std::vector<double>& a) { double s = 0; for (double x : a) s += x * x; return std::sqrt(s); }
 
 // Restarted GMRES with PETSc KSPGMRES defaults (classical Gram-Schmidt without
-// refinement, PCNONE, convergence ||r_k|| <= max(rtol*||r_0||, abstol)).
+// refinement, PCNONE, convergence ||r_k|| < max(rtol*||b||, abstol)); a cycle
+// ends on the Givens estimate and the true residual after it decides.
 template <class MV>
 static int gmres(int n, MV&& A, const std::vector<double>& b, std::vector<double>& x, double rtol, int max_it,
                  int restart, rbc3d_solve_stats* st, rbc3d_status* err) {
@@ -902,7 +903,8 @@ static int gmres(int n, MV&& A, const std::vector<double>& b, std::vector<double
     return true;
   };
   if (!resid()) return -1;
-  double rnorm0 = nrm2(r), ttol = std::max(rtol * rnorm0, 1.e-50);
+  // KSPConvergedDefault: ||r|| < max(rtol * ||b||, abstol) with ||b|| of the right-hand side
+  double rnorm0 = nrm2(r), ttol = std::max(rtol * nrm2(b), 1.e-50);
   st->rnorm0 = rnorm0;
   int its = 0;
   double beta = rnorm0;
@@ -957,7 +959,7 @@ static int gmres(int n, MV&& A, const std::vector<double>& b, std::vector<double
       for (int i = 0; i < n; ++i) x[i] += yv[j] * V[j][i];
     if (!resid()) return -1;
     beta = nrm2(r);
-    if (beta <= ttol) conv = true;
+    conv = beta <= ttol;  // the true residual decides, not the Givens estimate
   }
   st->iterations = its;
   st->converged = conv ? 1 : 0;

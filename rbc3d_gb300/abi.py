@@ -305,9 +305,9 @@ class Context:
         self._check(self.L.fn["wall_matmult"](self.h, prec, _ptr(u), _ptr(y)))
         return y
 
-    def no_slip_wall(self, rtol, max_it, restart=30, prec=FP64, guess=None, check=True):
+    def no_slip_wall(self, rtol, max_it, restart=30, prec=FP64, guess=None, check=True, guess_mode=1):
         o = SolveOpts(rtol=rtol, max_it=max_it, restart=restart, prec=prec,
-                      guess=0 if guess is None else 1)
+                      guess=0 if guess is None else guess_mode)
         st = SolveStats()
         g = f64(guess)
         code = self.L.fn["no_slip_wall"](self.h, C.byref(o), _ptr(g), C.byref(st))

@@ -692,7 +692,9 @@ rbc3d_status rbc3d_wall_matmult(rbc3d_ctx* ctx, int prec, const double* u, doubl
 
 rbc3d_status rbc3d_no_slip_wall(rbc3d_ctx* ctx, const rbc3d_solve_opts* opt, const double* guess,
                                 rbc3d_solve_stats* st) {
-  if (!ctx || !opt) return RBC3D_ERR_ARG;
+  if (!ctx || !opt || opt->guess < 0 || opt->guess > 3 || (opt->guess > 0 && !guess) || opt->rtol < 0 ||
+      opt->max_it < 0 || !valid_prec(opt->prec))
+    return RBC3D_ERR_ARG;
   return wall_solve(ctx, opt, guess, st);
 }
 

@@ -81,6 +81,7 @@ struct WallState {
   std::vector<double> hx, hf;       // host copies (x, density)
   std::vector<int> he2v, hglb;
   DBuf<double> x, f, area, eps, cen;  // vertices 3*nvert, density 3*nvert, per element
+  DBuf<double> src_x, src_f;          // PME centroid sources (3*nele)
   DBuf<int> e2v;                      // 3*nele (0-based)
   DBuf<int> glb;                      // nvert (0-based unique id)
   DBuf<int> writer;                   // 1 for the last vertex of each unique id (AssembleArray order)

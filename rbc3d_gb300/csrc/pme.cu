@@ -358,14 +358,13 @@ rbc3d_status pme_spread(rbc3d_ctx* ctx, double c1, double c2, int cells, int wal
   }
   if (walls && ctx->wall.nele > 0 && P.sl) {
     WallState& W = ctx->wall;
-    DBuf<double> xs, fs;
-    CUDA_TRY(xs.alloc(3 * (size_t)W.nele)); CUDA_TRY(fs.alloc(3 * (size_t)W.nele));
-    { k_wall_sources<<<nblk(W.nele, 256), 256, 0, ctx->st>>>(W.nele, W.nvert, W.e2v.p, W.x.p, W.f.p, W.area.p, xs.p, fs.p); ++ctx->launches; }
-    a.n = W.nele; a.x = xs.p; a.f = fs.p; a.g = nullptr; a.a3 = nullptr; a.sl = 1; a.dl = 0;
+    CUDA_TRY(W.src_x.alloc(3 * (size_t)W.nele));
+    CUDA_TRY(W.src_f.alloc(3 * (size_t)W.nele));
+    { k_wall_sources<<<nblk(W.nele, 256), 256, 0, ctx->st>>>(W.nele, W.nvert, W.e2v.p, W.x.p, W.f.p, W.area.p, W.src_x.p, W.src_f.p); ++ctx->launches; }
+    a.n = W.nele; a.x = W.src_x.p; a.f = W.src_f.p; a.g = nullptr; a.a3 = nullptr; a.sl = 1; a.dl = 0;
     if (prec == RBC3D_FP32C) { k_spread<float><<<nblk(a.n, 128), 128, 0, ctx->st>>>(a, P.grid32.p); ++ctx->launches; }
     else { k_spread<double><<<nblk(a.n, 128), 128, 0, ctx->st>>>(a, P.grid64.p); ++ctx->launches; }
     CUDA_TRY(cudaGetLastError());
-    CUDA_TRY(cudaStreamSynchronize(ctx->st));
   }
   return RBC3D_OK;
 }

@@ -629,6 +629,11 @@ rbc3d_status wall_solve(rbc3d_ctx* ctx, const rbc3d_solve_opts* o, const double*
   CUDA_TRY(cudaGetLastError());
   if (o->guess && guess) CUDA_TRY(cudaMemcpyAsync(x.p, guess, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->st));
   else CUDA_TRY(cudaMemsetAsync(x.p, 0, sizeof(double) * n, ctx->st));
+  DBuf<double> x2, w2;  // guess mode 3: second guess vector and its image
+  if (o->guess == 3 && guess) {
+    CUDA_TRY(x2.alloc(n)); CUDA_TRY(w2.alloc(n));
+    CUDA_TRY(cudaMemcpyAsync(x2.p, guess + n, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->st));
+  }
   auto matvec = [&](const double* in, double* out) -> rbc3d_status {
     S.matvecs++;
     return wall_matmult_dev(ctx, prec, in, out);
@@ -641,10 +646,49 @@ rbc3d_status wall_solve(rbc3d_ctx* ctx, const rbc3d_solve_opts* o, const double*
     return RBC3D_OK;
   };
   if ((s = residual())) return s;
+  if (o->guess == 2 && guess) {
+    // minimum-residual scaling of the guess: x0 <- a x0, a = <b, A x0> / ||A x0||^2,
+    // so that ||b - A x0|| <= ||b|| whatever the guess (w holds A x0)
+    { k_dots<<<1, 512, 0, ctx->st>>>(n, 1, w.p, 0, b.p, tmp.p); ++ctx->launches; }
+    { k_dots<<<1, 512, 0, ctx->st>>>(n, 1, w.p, 0, w.p, tmp.p + 1); ++ctx->launches; }
+    double bw[2] = {0, 0};
+    CUDA_TRY(cudaMemcpyAsync(bw, tmp.p, sizeof(double) * 2, cudaMemcpyDeviceToHost, ctx->st));
+    CUDA_TRY(cudaStreamSynchronize(ctx->st));
+    const double a = bw[1] > 0 ? bw[0] / bw[1] : 0.0;
+    { k_axpby<<<nblk(n, 256), 256, 0, ctx->st>>>(n, 0.0, w.p, a, x.p); ++ctx->launches; }
+    CUDA_TRY(cudaMemcpyAsync(r.p, b.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->st));
+    { k_axpby<<<nblk(n, 256), 256, 0, ctx->st>>>(n, -a, w.p, 1.0, r.p); ++ctx->launches; }
+  }
+  if (o->guess == 3 && guess) {
+    // x0 = p x1 + q x2 minimising ||b - p A x1 - q A x2|| (2x2 normal equations;
+    // w holds A x1), so the initial residual is no larger than either vector's
+    if ((s = matvec(x2.p, w2.p))) return s;
+    const double* pa[5] = {w.p, w.p, w2.p, w.p, w2.p};
+    const double* pb[5] = {w.p, w2.p, w2.p, b.p, b.p};
+    for (int i = 0; i < 5; ++i) { k_dots<<<1, 512, 0, ctx->st>>>(n, 1, pa[i], 0, pb[i], tmp.p + i); ++ctx->launches; }
+    double m[5] = {0, 0, 0, 0, 0};
+    CUDA_TRY(cudaMemcpyAsync(m, tmp.p, sizeof(double) * 5, cudaMemcpyDeviceToHost, ctx->st));
+    CUDA_TRY(cudaStreamSynchronize(ctx->st));
+    double p = 0, q = 0;
+    const double det = m[0] * m[2] - m[1] * m[1];
+    if (det > 1e-14 * m[0] * m[2] && det > 0) {
+      p = (m[3] * m[2] - m[4] * m[1]) / det;
+      q = (m[4] * m[0] - m[3] * m[1]) / det;
+    } else if (m[0] >= m[2] && m[0] > 0) {
+      p = m[3] / m[0];
+    } else if (m[2] > 0) {
+      q = m[4] / m[2];
+    }
+    { k_axpby<<<nblk(n, 256), 256, 0, ctx->st>>>(n, q, x2.p, p, x.p); ++ctx->launches; }
+    CUDA_TRY(cudaMemcpyAsync(r.p, b.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->st));
+    { k_axpby<<<nblk(n, 256), 256, 0, ctx->st>>>(n, -p, w.p, 1.0, r.p); ++ctx->launches; }
+    { k_axpby<<<nblk(n, 256), 256, 0, ctx->st>>>(n, -q, w2.p, 1.0, r.p); ++ctx->launches; }
+  }
   double beta = dev_norm(ctx, n, r.p, tmp.p);
   S.rnorm0 = beta;
   S.bnorm = dev_norm(ctx, n, b.p, tmp.p);
-  double ttol = std::max(o->rtol * beta, 1e-50);
+  // KSPConvergedDefault: ||r|| < max(rtol * ||b||, abstol), ||b|| of the right-hand side
+  double ttol = std::max(o->rtol * S.bnorm, 1e-50);
   int its = 0;
   bool conv = beta <= ttol;
   while (!conv && its < o->max_it) {
@@ -670,7 +714,7 @@ rbc3d_status wall_solve(rbc3d_ctx* ctx, const rbc3d_solve_opts* o, const double*
     { k_xupdate<<<nblk(n, 256), 256, 0, ctx->st>>>(n, k, V.p, ld, yv.p, x.p); ++ctx->launches; }
     if ((s = residual())) return s;
     beta = dev_norm(ctx, n, r.p, tmp.p);
-    if (beta <= ttol) conv = true;
+    conv = beta <= ttol;  // the true residual decides, not the Givens estimate
   }
   S.iterations = its;
   S.converged = conv ? 1 : 0;
@@ -683,4 +727,20 @@ rbc3d_status wall_solve(rbc3d_ctx* ctx, const rbc3d_solve_opts* o, const double*
   S.ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   if (st) *st = S;
   return conv ? RBC3D_OK : ctx_fail(ctx, RBC3D_ERR_NOCONV, "GMRES reached max_it");
+}
+
+// b = -AssembleArray(Compute_Wall_Residual_Vel) (ModNoSlip.F90:110-113), host copy
+extern "C" rbc3d_status rbc3d_wall_rhs(rbc3d_ctx* ctx, int prec, double* b) {
+  if (!ctx || !b || !valid_prec(prec)) return RBC3D_ERR_ARG;
+  WallState& W = ctx->wall;
+  if (W.nvert == 0) return RBC3D_OK;
+  if (!W.prepared) return ctx_fail(ctx, RBC3D_ERR_STATE, "PrepareSingIntOnWall not called");
+  rbc3d_status s = wall_residual_dev(ctx, prec);
+  if (s) return s;
+  DBuf<double> db;
+  CUDA_TRY(db.alloc(W.ndof));
+  { k_assemble<<<nblk(W.nvert, 256), 256, 0, ctx->st>>>(W.nvert, W.glb.p, W.writer.p, ctx->tl[RBC3D_TLIST_WALL].v.p, -1.0, db.p); ++ctx->launches; }
+  CUDA_TRY(cudaMemcpyAsync(b, db.p, sizeof(double) * W.ndof, cudaMemcpyDeviceToHost, ctx->st));
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  return RBC3D_OK;
 }

@@ -413,3 +413,58 @@ def config(name: str, seed: int = 20261203, ncell: int | None = None, L: float |
         wall = make_tube(8.0, L[2], 48, 192, cxy)
     cells = make_cells(rng, n, L, md, inside=inside, with_g=g)
     return prm, cells, wall
+
+
+# ---------------------------------------------------------------------------
+# Rigid motion of cells (a kinematic stand-in for the membrane dynamics of
+# TimeInt_RK2, used to produce sequences of correlated wall solves)
+def _rot(axis, angle):
+    axis = np.asarray(axis, dtype=np.float64)
+    n = np.linalg.norm(axis)
+    if n < 1e-300 or angle == 0.0:
+        return np.eye(3)
+    k = axis / n
+    K = np.array([[0, -k[2], k[1]], [k[2], 0, -k[0]], [-k[1], k[0], 0]])
+    return np.eye(3) + math.sin(angle) * K + (1 - math.cos(angle)) * (K @ K)
+
+
+def move_cells(cells, dx, dR):
+    """New Cells with cell c rotated by dR[c] about its centre and shifted by
+    dx[c]: positions, normals and tractions transform exactly, and so do
+    their spline tables (the bicubic tables are linear in the values)."""
+    nv = cells.nlat * cells.nlon
+    out = Cells(**{k: getattr(cells, k) for k in cells.__dataclass_fields__})
+    x = cells.x.copy(); a3 = cells.a3.copy(); f = cells.f.copy(); g = cells.g.copy()
+    sx = cells.spl_x.copy(); sa = cells.spl_a3.copy(); sF = cells.spl_F.copy(); sG = cells.spl_G.copy()
+    cen = np.asarray(cells.centres, dtype=np.float64).copy()
+    for c in range(cells.ncell):
+        R, d, c0 = dR[c], dx[c], cen[c]
+        sl = slice(c * nv, (c + 1) * nv)
+        x[:, sl] = R @ (cells.x[:, sl] - c0[:, None]) + (c0 + d)[:, None]
+        a3[:, sl] = R @ cells.a3[:, sl]
+        f[:, sl] = R @ cells.f[:, sl]
+        g[:, sl] = R @ cells.g[:, sl]
+        # tables (4 kinds, 3 vars, n, m): rotate the var axis; translate the u kind of x
+        for tab, src in ((sx, cells.spl_x), (sa, cells.spl_a3), (sF, cells.spl_F), (sG, cells.spl_G)):
+            tab[c] = np.einsum("ij,kjnm->kinm", R, src[c])
+        sx[c, 0] = np.einsum("ij,jnm->inm", R, cells.spl_x[c, 0] - c0[:, None, None]) + (c0 + d)[:, None, None]
+        cen[c] = c0 + d
+    out.x, out.a3, out.f, out.g = x, a3, f, g
+    out.spl_x, out.spl_a3, out.spl_F, out.spl_G = sx, sa, sF, sG
+    out.centres = cen
+    return out
+
+
+def poiseuille_step(cells, axis_xy, radius, umax, dt):
+    """Advect cell centres along z with u = umax (1 - r^2/R^2) and rotate them
+    with the local shear rate (about e_z x e_r)."""
+    cen = np.asarray(cells.centres)
+    dx, dR = [], []
+    for c in cen:
+        rx, ry = c[0] - axis_xy[0], c[1] - axis_xy[1]
+        r2 = rx * rx + ry * ry
+        u = umax * max(0.0, 1 - r2 / radius ** 2)
+        shear = 2 * umax * math.sqrt(r2) / radius ** 2
+        dx.append(np.array([0.0, 0.0, u * dt]))
+        dR.append(_rot([-ry, rx, 0.0], -0.5 * shear * dt))
+    return move_cells(cells, dx, dR)

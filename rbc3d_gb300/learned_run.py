@@ -1,0 +1,114 @@
+"""Learned vs plain wall GMRES along a run of the tube workload.
+
+Cells (biconcave, SH tractions) are advected through the straight periodic
+tube by a Poiseuille profile and rotated by its shear (a kinematic stand-in
+for the membrane dynamics); at every step the wall no-slip density is solved
+to ||r|| < rtol ||b|| with GMRES (FP64 matvec and Arnoldi).  The first
+`warm_steps` steps are plain solves (zero increment, i.e. warm start from the
+previous density as NoSlipWall) that fill the history and train the network
+online; afterwards every step is solved three times from the same state --
+plain, history guess only, history + network guess -- and iterations, times
+and final residuals are compared.  The plain solution continues the run and
+is recorded for the guess, so all arms see the same states.
+
+    python -m rbc3d_gb300.learned_run --cells 64 --warm 30 --test 10
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import numpy as np
+
+from . import geometry as G
+from . import library
+from .abi import FP64, Context
+from .learned import WallGuess
+
+
+def _unique_increment(wall, f1, f0):
+    un = np.zeros((wall.ndof // 3, 3))
+    un[wall.glb - 1] = (f1 - f0).T
+    return un.reshape(-1)
+
+
+def run(ncell=64, warm_steps=30, test_steps=10, rtol=1e-8, restart=100, max_it=800, dt=5e-3, umax=8.0,
+        train_iters=10, width=512, depth=4, history=6, seed=20261203, prec=FP64, log=None):
+    prm, cells, wall = G.config("C3", seed=seed, ncell=ncell)
+    lib = library()
+    ctx = Context(lib, prm)
+    ctx.set_cells(cells)
+    ctx.set_cell_density(f=cells.f, spl_F=cells.spl_F)
+    ctx.set_walls(wall)
+    ctx.prepare_sing_int_on_wall()
+    guess = WallGuess(lib, wall, width=width, depth=depth, seed=seed, history=history)
+    axis = (prm["Lb"][0] / 2, prm["Lb"][1] / 2)
+    rng = np.random.default_rng(seed)
+    ctx.no_slip_wall(rtol, max_it, restart, prec, check=False)  # initial density
+    arms = {"plain": [], "history": [], "learned": []}
+    losses, train_ms = [], []
+    for step in range(warm_steps + test_steps):
+        cells = G.poiseuille_step(cells, axis, 8.0, umax, dt)
+        ctx.set_cells(cells)
+        ctx.set_cell_density(f=cells.f, spl_F=cells.spl_F)
+        f0 = ctx.get_wall_density(wall.nvert)
+        testing = step >= warm_steps
+        if testing:
+            for mode in ("history", "learned"):
+                st, ok, ms, _ = guess.solve(ctx, wall, rtol, max_it, restart, prec, mode=mode)
+                arms[mode].append(dict(its=st.iterations, ms=ms, rel=st.rnorm / st.bnorm, accepted=ok,
+                                       r0=st.rnorm0 / st.bnorm))
+                ctx.set_wall_density(f0)
+        b = guess.rhs(ctx, prec)
+        t0 = time.perf_counter()
+        st, code = ctx.no_slip_wall(rtol, max_it, restart, prec, check=False)
+        ms = (time.perf_counter() - t0) * 1e3
+        arms["plain"].append(dict(its=st.iterations, ms=ms, rel=st.rnorm / st.bnorm, accepted=True, r0=1.0))
+        guess.record(b, _unique_increment(wall, ctx.get_wall_density(wall.nvert), f0))
+        t1 = time.perf_counter()
+        loss = guess.train(iters=train_iters, rng=rng)
+        train_ms.append((time.perf_counter() - t1) * 1e3)
+        if loss is not None:
+            losses.append(loss)
+        if log:
+            msg = f"step {step} plain its {st.iterations} ms {ms:.0f}"
+            if testing:
+                for mode in ("history", "learned"):
+                    a = arms[mode][-1]
+                    msg += f" | {mode} its {a['its']} ms {a['ms']:.0f} r0 {a['r0']:.2e}"
+            elif loss is not None:
+                msg += f" loss {loss:.3e}"
+            log(msg)
+
+    def summary(mode):
+        a = arms[mode][-test_steps:]
+        return {"its": float(np.mean([x["its"] for x in a])), "ms": float(np.mean([x["ms"] for x in a])),
+                "initial_rel_residual": float(np.mean([x["r0"] for x in a])),
+                "accepted": int(sum(x["accepted"] for x in a)),
+                "max_final_rel_residual": float(max(x["rel"] for x in a))}
+
+    res = {"cells": ncell, "wall_dof": int(wall.ndof), "warm_steps": warm_steps, "test_steps": test_steps,
+           "rtol": rtol, "restart": restart, "history": history,
+           "plain": summary("plain"), "history_only": summary("history"), "learned": summary("learned")}
+    res["speedup_learned"] = res["plain"]["ms"] / res["learned"]["ms"]
+    res["speedup_history_only"] = res["plain"]["ms"] / res["history_only"]["ms"]
+    res["train_ms_per_step"] = float(np.mean(train_ms))
+    res["speedup_learned_incl_training"] = res["plain"]["ms"] / (res["learned"]["ms"] + res["train_ms_per_step"])
+    res["final_loss"] = float(losses[-1]) if losses else None
+    res["mlp"] = {"layers": f"{guess.mlp.dims[0]} -> {width} x {depth} (SiLU) -> 3", "weights": "bf16",
+                  "accumulation": "fp32", "params": int(guess.mlp.nparam)}
+    guess.mlp.close()
+    ctx.close()
+    return res
+
+
+if __name__ == "__main__":
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--cells", type=int, default=64)
+    ap.add_argument("--warm", type=int, default=30)
+    ap.add_argument("--test", type=int, default=10)
+    ap.add_argument("--restart", type=int, default=100)
+    ap.add_argument("--train-iters", type=int, default=10)
+    a = ap.parse_args()
+    print(json.dumps(run(a.cells, a.warm, a.test, restart=a.restart, train_iters=a.train_iters, log=print)))

@@ -1,0 +1,98 @@
+"""Learned initial guess for the wall GMRES: the BF16 MLP against its FP64
+numpy restatement, online training, and the guarded solve (every accepted
+solve reaches the same rtol * ||b|| as the plain one)."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import mlp_ref
+from rbc3d_gb300 import geometry as G
+
+
+def test_bf16_rounding_matches_torch():
+    torch = pytest.importorskip("torch")
+    x = np.random.default_rng(1).standard_normal(10000).astype(np.float32) * 10.0 ** np.random.default_rng(2).integers(-8, 8, 10000)
+    ref = torch.from_numpy(x).to(torch.bfloat16).to(torch.float32).numpy()
+    assert np.array_equal(mlp_ref.bf16(x), ref)
+
+
+def test_rigid_motion_keeps_geometry():
+    prm, cells, wall = G.config("C3", ncell=4)
+    c2 = G.poiseuille_step(cells, (prm["Lb"][0] / 2, prm["Lb"][1] / 2), 8.0, 8.0, 5e-3)
+    nv = cells.nlat * cells.nlon
+    for c in range(cells.ncell):
+        sl = slice(c * nv, (c + 1) * nv)
+        d0 = cells.x[:, sl] - np.asarray(cells.centres[c])[:, None]
+        d1 = c2.x[:, sl] - np.asarray(c2.centres[c])[:, None]
+        # rigid: pairwise distances to the centre and unit normals preserved
+        assert np.allclose(np.linalg.norm(d0, axis=0), np.linalg.norm(d1, axis=0), atol=1e-12)
+        assert np.allclose(np.linalg.norm(c2.a3[:, sl], axis=0), 1.0, atol=1e-12)
+        assert np.allclose(np.linalg.norm(c2.f[:, sl], axis=0), np.linalg.norm(cells.f[:, sl], axis=0), atol=1e-12)
+
+
+def test_vertex_frames_orthonormal():
+    from rbc3d_gb300.learned import vertex_frames
+    prm, cells, wall = G.config("C3", ncell=1)
+    F = vertex_frames(wall)
+    I = np.einsum("vac,vbc->vab", F, F)
+    assert np.allclose(I, np.eye(3)[None], atol=1e-12)
+    # the normal of a straight tube is radial
+    x = np.zeros((wall.ndof // 3, 3)); x[wall.glb - 1] = wall.x.T
+    r = x[:, :2] - np.array(prm["Lb"][:2]) / 2
+    r /= np.linalg.norm(r, axis=1, keepdims=True)
+    assert np.abs(np.abs(np.einsum("vc,vc->v", F[:, 0, :2], r)) - 1).max() < 1e-2
+
+
+@pytest.mark.gpu
+def test_mlp_gradients_match_restatement(gpu):
+    from rbc3d_gb300.learned import MLP
+    nin, width, depth, nout, n = 6, 96, 3, 3, 700  # ragged vs the 64-wide tiles
+    m = MLP(gpu, nin, width, depth, nout, seed=7)
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal((n, nin)).astype(np.float32)
+    t = rng.standard_normal((n, nout)).astype(np.float32)
+    p = m.params()
+    assert p.size == m.nparam == sum(a * b + b for a, b in zip([nin] + [width] * depth, [width] * depth + [nout]))
+    loss, g = m.gradients(x, t)
+    lref, gref = mlp_ref.loss_and_grads(p, x, t, nin, width, depth, nout)
+    # BF16 operands rounded at the same points; FP32 vs FP64 accumulation order
+    assert abs(loss - lref) <= 1e-4 * lref
+    assert np.linalg.norm(g - gref) <= 1e-2 * np.linalg.norm(gref)
+    y = m.forward(x)
+    layers = mlp_ref.unpack(p, nin, width, depth, nout)
+    a = mlp_ref.bf16(x).astype(np.float64)
+    for l, (W, b) in enumerate(layers):
+        z = a @ mlp_ref.bf16(W).astype(np.float64).T + b
+        a = mlp_ref.bf16(mlp_ref.silu(z).astype(np.float32)).astype(np.float64) if l < depth else z
+    assert np.linalg.norm(y - a) <= 1e-3 * np.linalg.norm(a)
+    m.close()
+
+
+@pytest.mark.gpu
+def test_mlp_training_fits_smooth_map(gpu):
+    from rbc3d_gb300.learned import MLP
+    m = MLP(gpu, 6, 128, 3, 3, seed=11)
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal((4096, 6)).astype(np.float32)
+    A = rng.standard_normal((6, 3)) / math.sqrt(6)
+    t = (np.tanh(x @ A) + 0.1 * x[:, :3]).astype(np.float32)
+    first = m.train_step(x, t, 2e-3)
+    for _ in range(300):
+        last = m.train_step(x, t, 2e-3)
+    assert last < 0.05 * first
+    m.close()
+
+
+@pytest.mark.gpu
+def test_learned_guess_reaches_plain_tolerance(gpu):
+    from rbc3d_gb300.learned_run import run
+    res = run(ncell=8, warm_steps=8, test_steps=2, rtol=1e-8, restart=100, max_it=600, width=128, depth=2,
+              train_iters=20)
+    for arm in ("plain", "history_only", "learned"):
+        # every accepted solve meets the plain solve's ||r|| < rtol ||b||
+        assert res[arm]["max_final_rel_residual"] <= 1e-8
+    # the least-squares combination (guess mode 3) starts no higher than the history guess
+    assert res["learned"]["initial_rel_residual"] <= res["history_only"]["initial_rel_residual"] * (1 + 1e-9)
+    # what the guess gains over the plain solve (iterations from the same states)
+    assert res["learned"]["its"] < res["plain"]["its"]
