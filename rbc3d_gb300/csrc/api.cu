@@ -510,6 +510,7 @@ rbc3d_status rbc3d_set_walls(rbc3d_ctx* ctx, int nvert, int nele, const double* 
   }
   W.hf.assign(3 * (size_t)nvert, 0.);
   W.prepared = false;
+  ctx->pme.wplan.valid = false;
   rbc3d_status s = wall_setup(ctx);
   if (s) return s;
   // tlist_wall (TargetList_Update walls: Acoef = 2, ModTargetList.F90:119-127)

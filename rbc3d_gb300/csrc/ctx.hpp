@@ -56,7 +56,20 @@ struct TargetSet {
   DBuf<double> v;       // 3n accumulator of the current matvec
 };
 
+// Sources binned by the PME grid tile that holds their B-spline stencil's
+// origin: perm lists source indices tile by tile, chunk = (tile, begin, end)
+// with at most SPREAD_CHUNK sources per chunk.
+struct SpreadPlan {
+  DBuf<int> perm;
+  DBuf<int4> chunk;
+  int n = 0, nchunk = 0;
+  bool valid = false;
+};
+
 struct PmeState {
+  SpreadPlan cplan, wplan;  // cell and wall sources
+  DBuf<int2> sched;         // stencil-node schedule of the tiled spread
+  int sched_P = 0;
   int N1 = 0, N2 = 0, N3 = 0, NH = 0;
   size_t G = 0, GC = 0;
   DBuf<float> grid32;      // 12*G real grids

@@ -484,6 +484,7 @@ rbc3d_status build_source_list(rbc3d_ctx* ctx) {
                                                    ctx->a3.p, ctx->s_x.p, ctx->s_a3.p, ctx->s_meta.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   ctx->src_sorted = true;
+  ctx->pme.cplan.valid = false;  // the PME tiles follow the source positions
   // tlist_rbc shares the source order
   TargetSet& t = ctx->tl[RBC3D_TLIST_RBC];
   t.sorted = false;

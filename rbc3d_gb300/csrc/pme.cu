@@ -1,8 +1,11 @@
 // pme.cu -- smooth-particle-mesh Ewald of ModPME.F90 on one GPU.
 //
 //   PME_Distrib_Source (ModPME.F90:58-133, 405-443): B-spline spreading of
-//     c1*f (3 grids) and c2*g (x) Bcoef*a3 (9 grids) with global atomics;
-//     walls spread one centroid source per triangle.
+//     c1*f (3 grids) and c2*g (x) Bcoef*a3 (9 grids); walls spread one
+//     centroid source per triangle.  Sources are binned by 8^3 grid tiles
+//     (once per position update); a CTA accumulates one tile's sources into
+//     a (8+P-1)^3 box in shared memory and adds the box to the grids with
+//     one global atomic per touched node.
 //   PME_Transform (ModPME.F90:137-222): batched 3-D R2C FFTs (cuFFT), one
 //     fused kernel for the Stokeslet / stresslet influence and the B-spline
 //     factor bb, 3 C2R FFTs.  Unnormalised, as Get_That / Get_R.
@@ -17,6 +20,7 @@
 // the y and z passes; that equals replacing those planes by their Hermitian
 // part, which the influence kernel does explicitly so any C2R algorithm
 // reproduces the reference.
+#include <cub/cub.cuh>
 #include <cufft.h>
 
 #include <algorithm>
@@ -60,46 +64,151 @@ __device__ __forceinline__ void weights(double x, double ih, int P, int& imin, R
   w[0] = (R)1;
 #pragma unroll
   for (int j = 1; j < 8; ++j) w[j] = (R)0;
-  for (int pp = 2; pp <= P; ++pp) {
+  // fixed trip counts (guarded by P) keep w[] in registers
+#pragma unroll
+  for (int pp = 2; pp <= 8; ++pp) {
+    if (pp > P) break;
     R inv = (R)1 / (R)(pp - 1);
+#pragma unroll
     for (int j = pp; j >= 2; --j) w[j - 1] = u[j - 1] * inv * w[j - 1] + ((R)pp - u[j - 1]) * inv * w[j - 2];
     w[0] = u[0] * inv * w[0];
   }
 }
 
-template <typename R>
-__global__ void k_spread(SpreadArgs a, R* __restrict__ grid) {
+constexpr int SPREAD_TILE = 8;     // grid nodes per tile edge
+constexpr int SPREAD_CHUNK = 256;  // sources per CTA at most
+
+struct TileArgs {
+  int ntile[3];        // tiles per axis
+  int B;               // box edge, SPREAD_TILE + P - 1
+  int cg;              // grid planes per warp (3)
+  const int2* sched;   // [rounds][32] stencil-node schedule
+  int c0;              // first grid plane of the launch (3 per warp from there)
+};
+
+// Tile of each source's stencil origin (the stencil is x*ih - (P-1) .. x*ih).
+__global__ void k_tile_keys(int n, const double* __restrict__ x, SpreadArgs a, TileArgs t, int* __restrict__ key,
+                            int* __restrict__ idx) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= a.n) return;
-  R wx[8], wy[8], wz[8];
-  int imin, jmin, kmin;
-  weights<R>(a.x[p], a.ih[0], a.P, imin, wx);
-  weights<R>(a.x[p + a.n], a.ih[1], a.P, jmin, wy);
-  weights<R>(a.x[p + 2 * (size_t)a.n], a.ih[2], a.P, kmin, wz);
-  R fv[3] = {0, 0, 0}, tv[9];
-  if (a.sl)
-    for (int k = 0; k < 3; ++k) fv[k] = (R)(a.c1 * a.f[p + (size_t)k * a.n]);
-  if (a.dl) {
-    double gg[3], aa[3];
-    for (int k = 0; k < 3; ++k) { gg[k] = a.g[p + (size_t)k * a.n]; aa[k] = a.a3[p + (size_t)k * a.n]; }
-    for (int ii = 0; ii < 3; ++ii)
-      for (int jj = 0; jj < 3; ++jj) tv[ii + 3 * jj] = (R)(a.c2 * (gg[ii] * aa[jj]));
+  if (p >= n) return;
+  int tc[3];
+  for (int d = 0; d < 3; ++d) {
+    int m = (int)floor(x[p + (size_t)d * n] * a.ih[d]) - (a.P - 1);
+    tc[d] = imod(m, a.N[d]) / SPREAD_TILE;
   }
-  for (int k0 = 0; k0 < a.P; ++k0) {
-    int k = imod(kmin + k0, a.N[2]);
-    for (int j0 = 0; j0 < a.P; ++j0) {
-      int j = imod(jmin + j0, a.N[1]);
-      R wyz = wy[j0] * wz[k0];
-      size_t row = (size_t)a.N[0] * (j + (size_t)a.N[1] * k);
-      for (int i0 = 0; i0 < a.P; ++i0) {
-        int i = imod(imin + i0, a.N[0]);
-        R wxyz = wx[i0] * wyz;
-        size_t q = row + i;
-        if (a.sl)
-          for (int c = 0; c < 3; ++c) atomicAdd(grid + q + c * a.G, wxyz * fv[c]);
-        if (a.dl)
-          for (int c = 0; c < 9; ++c) atomicAdd(grid + (3 + c) * a.G + q, wxyz * tv[c]);
+  key[p] = tc[0] + t.ntile[0] * (tc[1] + t.ntile[1] * tc[2]);
+  idx[p] = p;
+}
+
+// Stencil-node schedule of the spread: lane l handles, in round r, the r-th
+// stencil node whose box offset i0 + B j0 + B^2 k0 falls in shared-memory
+// bank l, so the 32 lanes of one round never share a bank.  The number of
+// rounds is the largest count of nodes per bank (7 for P = 6, B = 13: the
+// 216 nodes in 7 conflict-free rounds).
+__host__ __device__ constexpr int spread_rounds(int P) {
+  int B = SPREAD_TILE + P - 1, cnt[32] = {}, mx = 0;
+  for (int k = 0; k < P; ++k)
+    for (int j = 0; j < P; ++j)
+      for (int i = 0; i < P; ++i) {
+        int b = (i + B * j + B * B * k) % 32;
+        if (++cnt[b] > mx) mx = cnt[b];
       }
+  return mx;
+}
+
+// Shared-memory bytes of k_spread_tile: the box (3 planes per warp) and one
+// batch of 32 staged sources (24 weights, 3 values per warp, box offset).
+inline size_t spread_smem_bytes(int B, int nw, size_t elem) {
+  return (size_t)3 * nw * B * B * B * elem + 32 * ((24 + 3 * nw) * elem + sizeof(int));
+}
+
+// One CTA per chunk of a tile, warp w owning grid planes c0+3w..+2 (one
+// vector quantity: c1 f, or one column of c2 g (x) a3).  Sources are staged
+// 32 at a time (weights, values, box offset); then every warp adds them one
+// after another into its planes of a shared-memory box, lanes over the
+// stencil nodes in the bank-conflict-free schedule.  A warp alone owns its
+// planes, so plain read-modify-writes suffice.  Finally the box goes to the
+// grids with one global atomic per nonzero node and plane.
+template <typename R, int PT>  // PT: the B-spline order, 2..8
+__global__ void __launch_bounds__(128) k_spread_tile(SpreadArgs a, TileArgs t, const int* __restrict__ perm,
+                                                     const int4* __restrict__ chunk, R* __restrict__ grid) {
+  constexpr int P = PT, NR = spread_rounds(PT);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int4 ch = chunk[blockIdx.x];
+  const int nw = blockDim.x >> 5;
+  const int B = t.B, B2 = B * B, B3 = B2 * B;
+  R* box = reinterpret_cast<R*>(smem_raw);  // [3 nw][B3]
+  R* sw = box + (size_t)3 * nw * B3;         // [32][24]
+  R* sv = sw + 32 * 24;                      // [32][3 nw]
+  int* sb = reinterpret_cast<int*>(sv + 32 * 3 * nw);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int tx = ch.x % t.ntile[0], ty = (ch.x / t.ntile[0]) % t.ntile[1], tz = ch.x / (t.ntile[0] * t.ntile[1]);
+  const int o[3] = {tx * SPREAD_TILE, ty * SPREAD_TILE, tz * SPREAD_TILE};
+  const int cfirst = t.c0;
+  // this lane's nodes: box offset and (i0, j0, k0) packed, offset -1 if none
+  int noff[NR], nidx[NR];
+#pragma unroll
+  for (int q = 0; q < NR; ++q) {
+    const int2 e = t.sched[q * 32 + lane];
+    noff[q] = e.x;
+    nidx[q] = e.y;
+  }
+  for (int i = threadIdx.x; i < 3 * nw * B3; i += blockDim.x) box[i] = (R)0;
+  const int nsrc = ch.z - ch.y;
+  for (int s0 = 0; s0 < nsrc; s0 += 32) {
+    const int nb = min(32, nsrc - s0);
+    __syncthreads();
+    if (lane < nb) {
+      const int p = perm[ch.y + s0 + lane];
+      if (wid == 0) {
+        R w[8];
+        int m[3];
+        for (int d = 0; d < 3; ++d) {
+          weights<R>(a.x[p + (size_t)d * a.n], a.ih[d], P, m[d], w);
+#pragma unroll
+          for (int q = 0; q < 8; ++q) sw[lane * 24 + d * 8 + q] = w[q];
+        }
+        sb[lane] = imod(m[0] - o[0], a.N[0]) + B * (imod(m[1] - o[1], a.N[1]) + B * imod(m[2] - o[2], a.N[2]));
+      }
+      for (int c = 0; c < 3; ++c) {
+        const int gc = cfirst + 3 * wid + c;
+        R v;
+        if (gc < 3) v = (R)(a.c1 * a.f[p + (size_t)gc * a.n]);
+        else {
+          const int ii = (gc - 3) % 3, jj = (gc - 3) / 3;
+          v = (R)(a.c2 * (a.g[p + (size_t)ii * a.n] * a.a3[p + (size_t)jj * a.n]));
+        }
+        sv[lane * 3 * nw + 3 * wid + c] = v;
+      }
+    }
+    __syncthreads();
+    R* wbox = box + (size_t)3 * wid * B3;
+    for (int s = 0; s < nb; ++s) {
+      const R* ws = sw + s * 24;
+      const R v0 = sv[s * 3 * nw + 3 * wid], v1 = sv[s * 3 * nw + 3 * wid + 1], v2 = sv[s * 3 * nw + 3 * wid + 2];
+      R* bs = wbox + sb[s];
+#pragma unroll
+      for (int r = 0; r < NR; ++r) {
+        if (noff[r] >= 0) {
+          const R w = ws[nidx[r] & 15] * ws[8 + ((nidx[r] >> 4) & 15)] * ws[16 + (nidx[r] >> 8)];
+          R* q = bs + noff[r];
+          const R o0 = q[0], o1 = q[B3], o2 = q[2 * B3];
+          q[0] = o0 + w * v0;
+          q[B3] = o1 + w * v1;
+          q[2 * B3] = o2 + w * v2;
+        }
+      }
+      __syncwarp();  // the next source may touch the same nodes
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < B3; i += blockDim.x) {
+    const int bx = i % B, by = (i / B) % B, bz = i / B2;
+    const int gx = (o[0] + bx) % a.N[0], gy = (o[1] + by) % a.N[1], gz = (o[2] + bz) % a.N[2];
+    const size_t q = gx + (size_t)a.N[0] * (gy + (size_t)a.N[1] * gz);
+    for (int c = 0; c < 3 * nw; ++c) {
+      const R v = box[i + (size_t)c * B3];
+      if (v != (R)0) atomicAdd(grid + q + (size_t)(cfirst + c) * a.G, v);
     }
   }
 }
@@ -328,6 +437,102 @@ rbc3d_status pme_release(rbc3d_ctx* ctx) {
   return RBC3D_OK;
 }
 
+TileArgs tile_args(const rbc3d_ctx* ctx, size_t elem) {
+  TileArgs t;
+  for (int d = 0; d < 3; ++d) t.ntile[d] = (ctx->prm.Nb[d] + SPREAD_TILE - 1) / SPREAD_TILE;
+  t.B = SPREAD_TILE + ctx->prm.P - 1;
+  t.cg = 3;
+  return t;
+}
+
+// Bin n sources (SoA positions on the device) by tile; chunks built on the host.
+rbc3d_status build_spread_plan(rbc3d_ctx* ctx, int n, const double* x, SpreadArgs a, SpreadPlan& pl) {
+  pl.n = n;
+  pl.nchunk = 0;
+  pl.valid = true;
+  if (n == 0) return RBC3D_OK;
+  TileArgs t = tile_args(ctx, 4);
+  DBuf<int> key, key2, idx;
+  CUDA_TRY(key.alloc(n)); CUDA_TRY(key2.alloc(n)); CUDA_TRY(idx.alloc(n)); CUDA_TRY(pl.perm.alloc(n));
+  { k_tile_keys<<<nblk(n, 256), 256, 0, ctx->st>>>(n, x, a, t, key.p, idx.p); ++ctx->launches; }
+  CUDA_TRY(cudaGetLastError());
+  const int ntiles = t.ntile[0] * t.ntile[1] * t.ntile[2];
+  int bits = 1;
+  while ((1 << bits) < ntiles) ++bits;
+  size_t tmp = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, tmp, key.p, key2.p, idx.p, pl.perm.p, n, 0, bits, ctx->st);
+  DBuf<char> tb;
+  CUDA_TRY(tb.alloc(tmp + 1));
+  CUDA_TRY(cub::DeviceRadixSort::SortPairs(tb.p, tmp, key.p, key2.p, idx.p, pl.perm.p, n, 0, bits, ctx->st));
+  std::vector<int> hk(n);
+  CUDA_TRY(cudaMemcpyAsync(hk.data(), key2.p, sizeof(int) * n, cudaMemcpyDeviceToHost, ctx->st));
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  std::vector<int4> ch;
+  for (int b = 0; b < n;) {
+    int e = b;
+    while (e < n && hk[e] == hk[b]) ++e;
+    for (int c = b; c < e; c += SPREAD_CHUNK) ch.push_back(make_int4(hk[b], c, std::min(e, c + SPREAD_CHUNK), 0));
+    b = e;
+  }
+  pl.nchunk = (int)ch.size();
+  CUDA_TRY(pl.chunk.upload(ch.data(), ch.size(), ctx->st));
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  return RBC3D_OK;
+}
+
+// The node schedule of k_spread_tile for order P (see spread_rounds).
+rbc3d_status spread_schedule(rbc3d_ctx* ctx, int P, TileArgs& t) {
+  PmeState& S = ctx->pme;
+  if (S.sched_P != P) {
+    const int B = SPREAD_TILE + P - 1, NR = spread_rounds(P);
+    std::vector<int2> tab((size_t)NR * 32, make_int2(-1, 0));
+    std::vector<int> cnt(32, 0);
+    for (int k = 0; k < P; ++k)
+      for (int j = 0; j < P; ++j)
+        for (int i = 0; i < P; ++i) {
+          const int off = i + B * j + B * B * k, b = off % 32;
+          tab[(size_t)cnt[b]++ * 32 + b] = make_int2(off, i | (j << 4) | (k << 8));
+        }
+    CUDA_TRY(S.sched.upload(tab.data(), tab.size(), ctx->st));
+    S.sched_P = P;
+  }
+  t.sched = S.sched.p;
+  return RBC3D_OK;
+}
+
+template <typename R, int PT>
+rbc3d_status launch_spread_p(rbc3d_ctx* ctx, const SpreadArgs& a, const SpreadPlan& pl, R* grid) {
+  TileArgs t = tile_args(ctx, sizeof(R));
+  rbc3d_status st = spread_schedule(ctx, PT, t);
+  if (st) return st;
+  // warps (3-plane groups) per launch: as many as the 227 KB of shared memory hold
+  const int gfirst = a.sl ? 0 : 1, glast = a.dl ? 4 : 1;
+  int per = glast - gfirst;
+  while (per > 1 && spread_smem_bytes(t.B, per, sizeof(R)) > 227 * 1024) --per;
+  for (int g = gfirst; g < glast; g += per) {
+    const int nw = std::min(per, glast - g);
+    t.c0 = 3 * g;
+    const size_t bytes = spread_smem_bytes(t.B, nw, sizeof(R));
+    CUDA_TRY(cudaFuncSetAttribute(k_spread_tile<R, PT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    { k_spread_tile<R, PT><<<pl.nchunk, 32 * nw, bytes, ctx->st>>>(a, t, pl.perm.p, pl.chunk.p, grid); ++ctx->launches; }
+    CUDA_TRY(cudaGetLastError());
+  }
+  return RBC3D_OK;
+}
+template <typename R>
+rbc3d_status launch_spread(rbc3d_ctx* ctx, const SpreadArgs& a, const SpreadPlan& pl, R* grid) {
+  if (pl.nchunk == 0) return RBC3D_OK;
+  switch (a.P) {
+    case 2: return launch_spread_p<R, 2>(ctx, a, pl, grid);
+    case 3: return launch_spread_p<R, 3>(ctx, a, pl, grid);
+    case 4: return launch_spread_p<R, 4>(ctx, a, pl, grid);
+    case 5: return launch_spread_p<R, 5>(ctx, a, pl, grid);
+    case 6: return launch_spread_p<R, 6>(ctx, a, pl, grid);
+    case 7: return launch_spread_p<R, 7>(ctx, a, pl, grid);
+    default: return launch_spread_p<R, 8>(ctx, a, pl, grid);  // P <= 8 checked at rbc3d_create
+  }
+}
+
 rbc3d_status pme_spread(rbc3d_ctx* ctx, double c1, double c2, int cells, int walls, int prec) {
   PmeState& P = ctx->pme;
   if (prec != RBC3D_FP64) prec = RBC3D_FP32C;  // FP32C and FP32M share the FP32 PME
@@ -351,9 +556,11 @@ rbc3d_status pme_spread(rbc3d_ctx* ctx, double c1, double c2, int cells, int wal
     a.n = ctx->npt; a.x = ctx->s_x.p; a.f = ctx->s_f.p; a.g = ctx->s_g.p; a.a3 = ctx->s_a3.p;
     a.sl = P.sl && ctx->has_f; a.dl = P.dl && ctx->has_g;
     if (a.sl || a.dl) {
-      if (prec == RBC3D_FP32C) { k_spread<float><<<nblk(a.n, 128), 128, 0, ctx->st>>>(a, P.grid32.p); ++ctx->launches; }
-      else { k_spread<double><<<nblk(a.n, 128), 128, 0, ctx->st>>>(a, P.grid64.p); ++ctx->launches; }
-      CUDA_TRY(cudaGetLastError());
+      rbc3d_status s;
+      if (!P.cplan.valid && (s = build_spread_plan(ctx, a.n, a.x, a, P.cplan))) return s;
+      s = prec == RBC3D_FP32C ? launch_spread<float>(ctx, a, P.cplan, P.grid32.p)
+                              : launch_spread<double>(ctx, a, P.cplan, P.grid64.p);
+      if (s) return s;
     }
   }
   if (walls && ctx->wall.nele > 0 && P.sl) {
@@ -362,9 +569,11 @@ rbc3d_status pme_spread(rbc3d_ctx* ctx, double c1, double c2, int cells, int wal
     CUDA_TRY(W.src_f.alloc(3 * (size_t)W.nele));
     { k_wall_sources<<<nblk(W.nele, 256), 256, 0, ctx->st>>>(W.nele, W.nvert, W.e2v.p, W.x.p, W.f.p, W.area.p, W.src_x.p, W.src_f.p); ++ctx->launches; }
     a.n = W.nele; a.x = W.src_x.p; a.f = W.src_f.p; a.g = nullptr; a.a3 = nullptr; a.sl = 1; a.dl = 0;
-    if (prec == RBC3D_FP32C) { k_spread<float><<<nblk(a.n, 128), 128, 0, ctx->st>>>(a, P.grid32.p); ++ctx->launches; }
-    else { k_spread<double><<<nblk(a.n, 128), 128, 0, ctx->st>>>(a, P.grid64.p); ++ctx->launches; }
-    CUDA_TRY(cudaGetLastError());
+    rbc3d_status s;
+    if (!P.wplan.valid && (s = build_spread_plan(ctx, a.n, a.x, a, P.wplan))) return s;
+    s = prec == RBC3D_FP32C ? launch_spread<float>(ctx, a, P.wplan, P.grid32.p)
+                            : launch_spread<double>(ctx, a, P.wplan, P.grid64.p);
+    if (s) return s;
   }
   return RBC3D_OK;
 }
