@@ -145,6 +145,15 @@ struct rbc3d_ctx {
   DBuf<int> s_order, s_cstart, s_cend;
   DBuf<double> s_x, s_f, s_g, s_a3;  // sorted, SoA 3*npt; s_g carries Bcoef
   DBuf<int4> s_meta;                 // (surf, ilat, ilon, original index)
+  // FP32 pair-sum records of the sorted sources: hi/lo coordinates relative
+  // to the source's hash-cell centre (+ surf / id bits), unit-sphere point,
+  // a3; c1 f and c2 g of the current call; per-cell tile offsets and boxes
+  DBuf<float4> s_p0, s_p1, s_u4, s_a4, s_F4, s_G4;
+  DBuf<int> s_toff;
+  DBuf<float4> s_tbox;
+  int s_ntiles = 0;
+  float erfcx_q[16] = {0};   // FP32 erfc fit of the pair kernel
+  double erfcx_X = -1.0;
   bool src_sorted = false, src_density = false;
 
   TargetSet tl[3];
@@ -205,6 +214,11 @@ rbc3d_status run_near_corr(rbc3d_ctx* ctx, int tlist, double c1, double c2, int 
 rbc3d_status pme_setup(rbc3d_ctx* ctx);
 rbc3d_status pme_release(rbc3d_ctx* ctx);
 rbc3d_status pme_spread(rbc3d_ctx* ctx, double c1, double c2, int cells, int walls, int prec);
+// FP32 erfc of the pair and self kernels: erfc(x) = exp(-x^2) t Q(t),
+// t = 1/(1 + x/2), Q of degree ERFCX_DEG fitted on [0, rc sqrt(pi/alpha)]
+constexpr int ERFCX_DEG = 8;
+void fit_erfcx(double X, float* q);
+void erfcx_coeffs(rbc3d_ctx* ctx);  // fills ctx->erfcx_q for the context's rc, alpha
 rbc3d_status pme_transform(rbc3d_ctx* ctx);
 rbc3d_status pme_gather(rbc3d_ctx* ctx, int tlist);
 // walls.cu

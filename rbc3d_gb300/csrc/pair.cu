@@ -6,12 +6,17 @@
 // [start, end) ranges per cell.  The same Nc = max(floor(L/rc), 3) cells are
 // used, so a target visits its 27 neighbour cells exactly as the reference.
 //
-// Pair kernel: one CTA per (target cell, chunk of <= 128 targets); the 27
-// neighbour cells are streamed through shared memory in tiles of 128 sources;
-// each thread owns one target.  Positions are taken relative to the centre of
-// the target cell in FP64 and split into FP32 hi/lo parts, so the FP32
-// difference x_j - x_i is exact to ~1e-14 regardless of the box size.  The
-// FP32 variant accumulates each target with Kahan compensation.
+// Pair kernels: one CTA per unit (target cell, <= 128 targets; units of a
+// cell equal-sized, heaviest units launched first); the 27 neighbour cells
+// are streamed through shared memory in tiles of 128 sources, each thread
+// owning one target.  Tiles whose bounding box lies farther than rc from the
+// CTA's (or a warp's) targets are skipped.  FP32: sources carry hi/lo FP32
+// coordinates relative to their own cell centre (from FP64, once per
+// position update) and the targets are shifted into each neighbour cell's
+// frame with an error-free difference, so x_j - x_i keeps full FP32 accuracy
+// regardless of the box size; each target accumulates with Kahan
+// compensation.  FP64 (the plain form): positions relative to the target
+// cell centre, reference table arithmetic.
 #include <cub/cub.cuh>
 
 #include <algorithm>
@@ -59,6 +64,76 @@ __global__ void k_gather_src(int n, int nlat, int nv, const int* __restrict__ or
   meta[q] = make_int4(cell + 1, r % nlat, r / nlat, p);
 }
 
+__device__ __forceinline__ double min_image(double d, double L, double iL) { return d - round(d * iL) * L; }
+
+// FP32 pair-sum records of the sorted sources (see PairArgs).
+__global__ void k_src_records(int n, const double* __restrict__ sx, const double* __restrict__ sa3,
+                              const int4* __restrict__ meta, const float4* __restrict__ usph, int nlat, int Nc0,
+                              int Nc1, int Nc2, double h0, double h1, double h2, double L0, double L1, double L2,
+                              float4* __restrict__ p0, float4* __restrict__ p1, float4* __restrict__ u4,
+                              float4* __restrict__ a4) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int Nc[3] = {Nc0, Nc1, Nc2};
+  const double h[3] = {h0, h1, h2}, L[3] = {L0, L1, L2};
+  float hi[3], lo[3];
+  for (int k = 0; k < 3; ++k) {
+    const double x = sx[q + (size_t)k * n];
+    const int c = imod((int)floor(x * (Nc[k] / L[k])), Nc[k]);  // HashTable_Index
+    const double r = min_image(x - (c + 0.5) * h[k], L[k], 1.0 / L[k]);
+    hi[k] = (float)r;
+    lo[k] = (float)(r - (double)hi[k]);
+  }
+  const int4 m = meta[q];
+  p0[q] = make_float4(hi[0], hi[1], hi[2], __int_as_float(m.x));
+  p1[q] = make_float4(lo[0], lo[1], lo[2], __int_as_float(m.y | (m.z << 16)));
+  u4[q] = usph[m.y + nlat * m.z];
+  a4[q] = make_float4((float)sa3[q], (float)sa3[q + n], (float)sa3[q + 2 * (size_t)n], 0.f);
+}
+
+// Bounding box of each tile (TILE consecutive sources of one cell), from the
+// hi coordinates; tiles listed as (first source, count).
+__global__ void k_tile_boxes(const int2* __restrict__ tiles, const float4* __restrict__ p0, float4* __restrict__ box) {
+  const int2 t = tiles[blockIdx.x];
+  const float big = 3.0e38f;
+  float3 lo = make_float3(big, big, big), hi = make_float3(-big, -big, -big);
+  for (int i = threadIdx.x; i < t.y; i += blockDim.x) {
+    const float4 p = p0[t.x + i];
+    lo.x = fminf(lo.x, p.x); lo.y = fminf(lo.y, p.y); lo.z = fminf(lo.z, p.z);
+    hi.x = fmaxf(hi.x, p.x); hi.y = fmaxf(hi.y, p.y); hi.z = fmaxf(hi.z, p.z);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lo.x = fminf(lo.x, __shfl_xor_sync(0xffffffffu, lo.x, o));
+    lo.y = fminf(lo.y, __shfl_xor_sync(0xffffffffu, lo.y, o));
+    lo.z = fminf(lo.z, __shfl_xor_sync(0xffffffffu, lo.z, o));
+    hi.x = fmaxf(hi.x, __shfl_xor_sync(0xffffffffu, hi.x, o));
+    hi.y = fmaxf(hi.y, __shfl_xor_sync(0xffffffffu, hi.y, o));
+    hi.z = fmaxf(hi.z, __shfl_xor_sync(0xffffffffu, hi.z, o));
+  }
+  __shared__ float3 red[32][2];
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) { red[w][0] = lo; red[w][1] = hi; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
+      lo.x = fminf(lo.x, red[k][0].x); lo.y = fminf(lo.y, red[k][0].y); lo.z = fminf(lo.z, red[k][0].z);
+      hi.x = fmaxf(hi.x, red[k][1].x); hi.y = fmaxf(hi.y, red[k][1].y); hi.z = fmaxf(hi.z, red[k][1].z);
+    }
+    box[2 * blockIdx.x] = make_float4(lo.x, lo.y, lo.z, 0.f);
+    box[2 * blockIdx.x + 1] = make_float4(hi.x, hi.y, hi.z, 0.f);
+  }
+}
+
+// c1 f dS and c2 g dS Bcoef of the sorted sources in FP32 (per call).
+__global__ void k_src_dens4(int n, double c1, double c2, const double* __restrict__ sf, const double* __restrict__ sg,
+                            int do_g, float4* __restrict__ F, float4* __restrict__ Gv) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  F[q] = make_float4((float)(c1 * sf[q]), (float)(c1 * sf[q + n]), (float)(c1 * sf[q + 2 * (size_t)n]), 0.f);
+  if (do_g)
+    Gv[q] = make_float4((float)(c2 * sg[q]), (float)(c2 * sg[q + n]), (float)(c2 * sg[q + 2 * (size_t)n]), 0.f);
+}
+
 // SourceList_UpdateDensity (ModSourceList.F90:160-189): f*dS, g*dS with
 // dS = detJ*w(ilat); the sorted copy of g also carries Bcoef of the cell type.
 __global__ void k_density(int n, int nlat, int nv, const double* __restrict__ f, const double* __restrict__ detJ,
@@ -101,6 +176,15 @@ struct PairArgs {
   const int4* smeta;
   const int* cs;
   const int* ce;
+  // FP32 source records (sorted order) and tile boxes
+  const float4* sp0;   // (x, y, z) hi relative to the source's hash-cell centre, surf bits
+  const float4* sp1;   // (x, y, z) lo, id bits (ilat | ilon << 16)
+  const float4* su;    // unit-sphere coordinates of the grid point
+  const float4* sa4;   // a3
+  const float4* sF4;   // c1 f dS
+  const float4* sG4;   // c2 g dS Bcoef
+  const int* toff;     // per hash cell: first tile (TILE consecutive sources per tile)
+  const float4* tbox;  // per tile: lo, hi (relative to the cell centre)
   // grid
   int Nc[3];
   double h[3], L[3], iL[3];
@@ -116,6 +200,7 @@ struct PairArgs {
   float rc2_f, reps2_f;
   float rthr2_f;  // FP32 path: cross-surface pairs closer than this are left to the FP64 near-singular pass
   float sqpa_f, two_isqa_f, m8_ispi_f, q75_spi_f;  // sqrt(pi/alpha), 2/sqrt(alpha), -8/sqrt(pi), 0.75 sqrt(pi)
+  float erfcx_q[ERFCX_DEG + 1];  // erfc(x) exp(x^2) = t Q(t), t = 1/(1 + x/2), on [0, rc sqrt(pi/alpha)]
   Tables T;
   // near-singular work list
   int collect;
@@ -124,7 +209,6 @@ struct PairArgs {
   unsigned long long* cnt;  // [0] items, [1] pairs, [2] overflow
 };
 
-__device__ __forceinline__ double min_image(double d, double L, double iL) { return d - round(d * iL) * L; }
 
 struct NbrList {
   int n;
@@ -158,9 +242,74 @@ struct TileD {
   int surf[TILE], ilat[TILE], ilon[TILE];
 };
 
+// Box-to-box distance test of the tile culling: true if every point of box
+// [alo, ahi] is farther than sqrt(rc2) from every point of [blo, bhi].  The
+// boxes hold FP32 coordinates; the margin absorbs their rounding.
+__device__ __forceinline__ bool boxes_apart(float3 alo, float3 ahi, float3 blo, float3 bhi, float rc2) {
+  float gx = fmaxf(0.f, fmaxf(alo.x - bhi.x, blo.x - ahi.x));
+  float gy = fmaxf(0.f, fmaxf(alo.y - bhi.y, blo.y - ahi.y));
+  float gz = fmaxf(0.f, fmaxf(alo.z - bhi.z, blo.z - ahi.z));
+  float g = sqrtf(gx * gx + gy * gy + gz * gz) - 1e-3f;
+  return g > 0.f && g * g > rc2;
+}
+
+__device__ __forceinline__ void warp_minmax(float3& lo, float3& hi) {
+  for (int o = 16; o > 0; o >>= 1) {
+    lo.x = fminf(lo.x, __shfl_xor_sync(0xffffffffu, lo.x, o));
+    lo.y = fminf(lo.y, __shfl_xor_sync(0xffffffffu, lo.y, o));
+    lo.z = fminf(lo.z, __shfl_xor_sync(0xffffffffu, lo.z, o));
+    hi.x = fmaxf(hi.x, __shfl_xor_sync(0xffffffffu, hi.x, o));
+    hi.y = fmaxf(hi.y, __shfl_xor_sync(0xffffffffu, hi.y, o));
+    hi.z = fmaxf(hi.z, __shfl_xor_sync(0xffffffffu, hi.z, o));
+  }
+}
+
+// Error-free a - b = s + e (Knuth TwoSum).
+__device__ __forceinline__ void two_diff(float a, float b, float& s, float& e) {
+  s = a - b;
+  float bb = a - s;
+  e = (a - (s + bb)) + (bb - b);
+}
+
+// Target and tile bounding boxes of the culling, shared by both precisions.
+struct CullBoxes {
+  float3 wlo, whi;  // this warp's targets
+  float3 clo, chi;  // the CTA's targets
+};
+
+__device__ __forceinline__ CullBoxes cull_boxes(bool active, float tx, float ty, float tz, float3 (*wb)[2]) {
+  const float big = 3.0e38f;
+  CullBoxes b;
+  b.wlo = active ? make_float3(tx, ty, tz) : make_float3(big, big, big);
+  b.whi = active ? make_float3(tx, ty, tz) : make_float3(-big, -big, -big);
+  warp_minmax(b.wlo, b.whi);
+  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if ((threadIdx.x & 31) == 0) { wb[w][0] = b.wlo; wb[w][1] = b.whi; }
+  __syncthreads();
+  b.clo = wb[0][0]; b.chi = wb[0][1];
+  for (int k = 1; k < nw; ++k) {
+    b.clo.x = fminf(b.clo.x, wb[k][0].x); b.clo.y = fminf(b.clo.y, wb[k][0].y); b.clo.z = fminf(b.clo.z, wb[k][0].z);
+    b.chi.x = fmaxf(b.chi.x, wb[k][1].x); b.chi.y = fmaxf(b.chi.y, wb[k][1].y); b.chi.z = fmaxf(b.chi.z, wb[k][1].z);
+  }
+  return b;
+}
+
+__device__ __forceinline__ float3 f3sub(float3 a, float3 d) { return make_float3(a.x - d.x, a.y - d.y, a.z - d.z); }
+
+// FP32 real-space pair sums (EwaldCoeff_SL / EwaldCoeff_DL of ModEwaldFunc
+// over the 27 neighbour hash cells, AddIntOnRbcs ModIntOnRbcs.F90:25-160).
+// One CTA per (hash cell, up to TILE targets).  Sources carry FP32 hi/lo
+// coordinates relative to their own cell centre; per neighbour cell the
+// targets are shifted into that frame with an error-free difference, so the
+// pair vector keeps full FP32 accuracy however far from the origin the cells
+// are.  Source tiles (TILE consecutive sources of a cell) whose bounding box
+// is farther than rc from the CTA's targets are not loaded, and a warp skips
+// a loaded tile that is out of its own targets' reach.
 template <bool DL>
 __global__ void __launch_bounds__(TILE) k_pair32(PairArgs a) {
-  __shared__ TileF sm;
+  __shared__ float4 s_p0[TILE], s_p1[TILE], s_f[TILE];
+  __shared__ float4 s_g[DL ? TILE : 1], s_a[DL ? TILE : 1];
+  __shared__ float3 wb[TILE / 32][2];
   const int4 unit = a.units[blockIdx.x];
   const int cell = unit.x;
   const int tid = threadIdx.x;
@@ -181,6 +330,7 @@ __global__ void __launch_bounds__(TILE) k_pair32(PairArgs a) {
     surf_i = m.x;
     if (m.y >= 0) ui = a.usph[m.y + a.nlat * m.z];
   }
+  const CullBoxes cb = cull_boxes(active, th_[0], th_[1], th_[2], wb);
   Kahan3 acc;
   acc.zero();
   NbrList L;
@@ -190,100 +340,113 @@ __global__ void __launch_bounds__(TILE) k_pair32(PairArgs a) {
   unsigned long long npairs = 0;
 
   for (int nb = 0; nb < 27; ++nb) {
-    int dx = nb % 3 - 1, dy = (nb / 3) % 3 - 1, dz = nb / 9 - 1;
-    int ni = imod(ci + dx, a.Nc[0]), nj = imod(cj + dy, a.Nc[1]), nk = imod(ck + dz, a.Nc[2]);
-    int ncell = ni + a.Nc[0] * (nj + a.Nc[1] * nk);
-    int sbeg = a.cs[ncell], send = a.ce[ncell];
-    for (int base = sbeg; base < send; base += TILE) {
-      int cnt = min(TILE, send - base);
+    const int dx = nb % 3 - 1, dy = (nb / 3) % 3 - 1, dz = nb / 9 - 1;
+    const int ni = imod(ci + dx, a.Nc[0]), nj = imod(cj + dy, a.Nc[1]), nk = imod(ck + dz, a.Nc[2]);
+    const int ncell = ni + a.Nc[0] * (nj + a.Nc[1] * nk);
+    const int sbeg = a.cs[ncell], send = a.ce[ncell];
+    if (sbeg >= send) continue;
+    // the neighbour cell's centre relative to ours, hi/lo
+    const double d64[3] = {dx * a.h[0], dy * a.h[1], dz * a.h[2]};
+    const float3 dh = make_float3((float)d64[0], (float)d64[1], (float)d64[2]);
+    const float3 dl = make_float3((float)(d64[0] - (double)dh.x), (float)(d64[1] - (double)dh.y),
+                                  (float)(d64[2] - (double)dh.z));
+    // targets in the neighbour cell's frame: t - d = tsh + tsl
+    float tsh[3], tsl[3];
+    {
+      float e;
+      two_diff(th_[0], dh.x, tsh[0], e); tsl[0] = (tl_[0] - dl.x) + e;
+      two_diff(th_[1], dh.y, tsh[1], e); tsl[1] = (tl_[1] - dl.y) + e;
+      two_diff(th_[2], dh.z, tsh[2], e); tsl[2] = (tl_[2] - dl.z) + e;
+    }
+    const float3 wlo = f3sub(cb.wlo, dh), whi = f3sub(cb.whi, dh);
+    const float3 clo = f3sub(cb.clo, dh), chi = f3sub(cb.chi, dh);
+    const int t0 = a.toff[ncell];
+    for (int base = sbeg, tt = t0; base < send; base += TILE, ++tt) {
+      const float4 blo = a.tbox[2 * tt], bhi = a.tbox[2 * tt + 1];
+      const float3 bl = make_float3(blo.x, blo.y, blo.z), bh = make_float3(bhi.x, bhi.y, bhi.z);
+      if (boxes_apart(clo, chi, bl, bh, a.rc2_f)) continue;  // uniform over the CTA
+      const int cnt = min(TILE, send - base);
       __syncthreads();
       if (tid < cnt) {
-        int q = base + tid;
-        double r[3];
-        for (int k = 0; k < 3; ++k) r[k] = min_image(a.sx[q + (size_t)k * a.ns] - c0[k], a.L[k], a.iL[k]);
-        float hx = (float)r[0], hy = (float)r[1], hz = (float)r[2];
-        sm.hx[tid] = hx; sm.hy[tid] = hy; sm.hz[tid] = hz;
-        sm.lx[tid] = (float)(r[0] - (double)hx); sm.ly[tid] = (float)(r[1] - (double)hy); sm.lz[tid] = (float)(r[2] - (double)hz);
-        sm.fx[tid] = (float)(a.c1 * a.sf[q]); sm.fy[tid] = (float)(a.c1 * a.sf[q + a.ns]); sm.fz[tid] = (float)(a.c1 * a.sf[q + 2 * (size_t)a.ns]);
-        if (DL) {
-          sm.gx[tid] = (float)(a.c2 * a.sg[q]); sm.gy[tid] = (float)(a.c2 * a.sg[q + a.ns]); sm.gz[tid] = (float)(a.c2 * a.sg[q + 2 * (size_t)a.ns]);
-          sm.ax[tid] = (float)a.sa3[q]; sm.ay[tid] = (float)a.sa3[q + a.ns]; sm.az[tid] = (float)a.sa3[q + 2 * (size_t)a.ns];
-        }
-        int4 m = a.smeta[q];
-        float4 u = a.usph[m.y + a.nlat * m.z];
-        sm.ux[tid] = u.x; sm.uy[tid] = u.y; sm.uz[tid] = u.z;
-        sm.surf[tid] = m.x;
-        sm.id[tid] = m.y | (m.z << 16);
+        const int q = base + tid;
+        s_p0[tid] = a.sp0[q];
+        s_p1[tid] = a.sp1[q];
+        s_f[tid] = a.sF4[q];
+        if (DL) { s_g[tid] = a.sG4[q]; s_a[tid] = a.sa4[q]; }
       }
       __syncthreads();
-      if (active) {
-        for (int j = 0; j < cnt; ++j) {
-          const int sj = sm.surf[j];
-          if (a.collect && sj != run_surf) {
-            if (run_id >= 0) L.insert(run_surf, run_id, run_d2);
-            run_surf = sj; run_id = -1; run_d2 = 3.4e38f;
-          }
-          float xx = __fadd_rn(sm.hx[j] - th_[0], sm.lx[j] - tl_[0]);
-          float yy = __fadd_rn(sm.hy[j] - th_[1], sm.ly[j] - tl_[1]);
-          float zz = __fadd_rn(sm.hz[j] - th_[2], sm.lz[j] - tl_[2]);
-          float r2 = xx * xx + yy * yy + zz * zz;
-          if (r2 > a.rc2_f) continue;
-          ++npairs;
-          float wgt = 1.f;
-          if (sj == surf_i) {
-            float ex = ui.x - sm.ux[j], ey = ui.y - sm.uy[j], ez = ui.z - sm.uz[j];
-            float ch2 = ex * ex + ey * ey + ez * ez;
-            if (ch2 < a.chord2_max) {
-              // dth = 2 asin(chord/2); MaskFunc lerp on the reference table
-              float t = 2.f * asinf(0.5f * sqrtf(ch2)) * a.inv_radius_f;
-              float s = t * (float)MASK_NTAB;
-              int i = (int)s;
-              if (i < MASK_NTAB) {
-                float2 e = __ldg(a.T.mask32 + i);
-                wgt = 1.f - (e.x + (s - (float)i) * e.y);
-              } else wgt = 1.f;
-            }
-          } else {
-            if (a.collect && r2 < run_d2) { run_d2 = r2; run_id = sm.id[j]; }
-            // A pair this close to another surface is re-evaluated in FP64 by
-            // the near-singular pass (its FP32 rounding would survive the
-            // cancellation with the FP64 subtraction).
-            if (a.collect && r2 < a.rthr2_f) continue;
-          }
-          if (r2 < a.reps2_f) continue;
-          float rinv = rsqrtf(r2);
-          float r = r2 * rinv;
-          // Ewald coefficients evaluated directly (erfc / exp in FP32) rather
-          // than by per-lane gathers into the 8193-entry tables: the tables'
-          // lerp differs from the exact functions by ~2e-8 relative, below
-          // FP32 resolution (the FP64 plain form keeps the tables).
-          float st = r * a.sqpa_f;  // r*sqrt(pi/alpha)
-          float ex = expf(-st * st);
-          float c1 = erfcf(st), c2 = a.two_isqa_f * ex;
-          float ir2 = rinv * rinv;
-          float A = (c1 * rinv + c2) * ir2;
-          float B = c1 * rinv - c2;
-          float dotf = xx * sm.fx[j] + yy * sm.fy[j] + zz * sm.fz[j];
-          float Ad = A * dotf;
-          float vx = Ad * xx + B * sm.fx[j];
-          float vy = Ad * yy + B * sm.fy[j];
-          float vz = Ad * zz + B * sm.fz[j];
-          if (DL) {
-            // -8/sqrt(pi) [exp(-t^2)(1.5 t + t^3) + 0.75 sqrt(pi) erfc(t)] / r^5
-            float cdl = a.m8_ispi_f * (ex * (st * (1.5f + st * st)) + a.q75_spi_f * c1);
-            float Adl = cdl * ir2 * ir2 * rinv;
-            float dg = xx * sm.gx[j] + yy * sm.gy[j] + zz * sm.gz[j];
-            float da = xx * sm.ax[j] + yy * sm.ay[j] + zz * sm.az[j];
-            float t = Adl * dg * da;
-            vx += t * xx; vy += t * yy; vz += t * zz;
-          }
-          acc.add(0, wgt * vx);
-          acc.add(1, wgt * vy);
-          acc.add(2, wgt * vz);
+      if (!active || boxes_apart(wlo, whi, bl, bh, a.rc2_f)) continue;
+      for (int j = 0; j < cnt; ++j) {
+        const float4 p0 = s_p0[j], p1 = s_p1[j];
+        const int sj = __float_as_int(p0.w);
+        if (a.collect && sj != run_surf) {
+          if (run_id >= 0) L.insert(run_surf, run_id, run_d2);
+          run_surf = sj; run_id = -1; run_d2 = 3.4e38f;
         }
-        if (a.collect && run_id >= 0) { L.insert(run_surf, run_id, run_d2); }
-        run_surf = -3; run_id = -1; run_d2 = 3.4e38f;
+        const float xx = __fadd_rn(p0.x - tsh[0], p1.x - tsl[0]);
+        const float yy = __fadd_rn(p0.y - tsh[1], p1.y - tsl[1]);
+        const float zz = __fadd_rn(p0.z - tsh[2], p1.z - tsl[2]);
+        const float r2 = xx * xx + yy * yy + zz * zz;
+        if (r2 > a.rc2_f) continue;
+        ++npairs;
+        float wgt = 1.f;
+        if (sj == surf_i) {
+          const float4 u = a.su[base + j];
+          const float ex = ui.x - u.x, ey = ui.y - u.y, ez = ui.z - u.z;
+          const float ch2 = ex * ex + ey * ey + ez * ez;
+          if (ch2 < a.chord2_max) {
+            // dth = 2 asin(chord/2); MaskFunc lerp on the reference table
+            const float t = 2.f * asinf(0.5f * sqrtf(ch2)) * a.inv_radius_f;
+            const float sx = t * (float)MASK_NTAB;
+            const int i = (int)sx;
+            if (i < MASK_NTAB) {
+              const float2 e = __ldg(a.T.mask32 + i);
+              wgt = 1.f - (e.x + (sx - (float)i) * e.y);
+            }
+          }
+        } else {
+          if (a.collect && r2 < run_d2) { run_d2 = r2; run_id = __float_as_int(p1.w); }
+          // A pair this close to another surface is re-evaluated in FP64 by
+          // the near-singular pass (its FP32 rounding would survive the
+          // cancellation with the FP64 subtraction).
+          if (a.collect && r2 < a.rthr2_f) continue;
+        }
+        if (r2 < a.reps2_f) continue;
+        const float rinv = rsqrtf(r2);
+        const float r = r2 * rinv;
+        // Ewald coefficients evaluated directly in FP32 rather than by
+        // per-lane gathers into the 8193-entry tables (the FP64 plain form
+        // keeps the tables)
+        const float st = r * a.sqpa_f;  // r*sqrt(pi/alpha)
+        const float ex = expf(-st * st);
+        // erfc(st) = exp(-st^2) t Q(t), t = 1/(1 + st/2) (fit_erfcx)
+        const float tq = __frcp_rn(fmaf(0.5f, st, 1.f));
+        float Q = a.erfcx_q[ERFCX_DEG];
+#pragma unroll
+        for (int k = ERFCX_DEG - 1; k >= 0; --k) Q = fmaf(Q, tq, a.erfcx_q[k]);
+        const float c1 = ex * (tq * Q), c2 = a.two_isqa_f * ex;
+        const float ir2 = rinv * rinv;
+        const float A = (c1 * rinv + c2) * ir2;
+        const float B = c1 * rinv - c2;
+        const float4 f = s_f[j];
+        const float Ad = A * (xx * f.x + yy * f.y + zz * f.z);
+        float vx = Ad * xx + B * f.x;
+        float vy = Ad * yy + B * f.y;
+        float vz = Ad * zz + B * f.z;
+        if (DL) {
+          // -8/sqrt(pi) [exp(-t^2)(1.5 t + t^3) + 0.75 sqrt(pi) erfc(t)] / r^5
+          const float cdl = a.m8_ispi_f * (ex * (st * (1.5f + st * st)) + a.q75_spi_f * c1);
+          const float Adl = cdl * ir2 * ir2 * rinv;
+          const float4 g = s_g[j], an = s_a[j];
+          const float t = Adl * (xx * g.x + yy * g.y + zz * g.z) * (xx * an.x + yy * an.y + zz * an.z);
+          vx += t * xx; vy += t * yy; vz += t * zz;
+        }
+        acc.add(0, wgt * vx);
+        acc.add(1, wgt * vy);
+        acc.add(2, wgt * vz);
       }
+      if (a.collect && run_id >= 0) { L.insert(run_surf, run_id, run_d2); }
+      run_surf = -3; run_id = -1; run_d2 = 3.4e38f;
     }
   }
   if (active) {
@@ -306,6 +469,7 @@ __global__ void __launch_bounds__(TILE) k_pair32(PairArgs a) {
 template <bool DL>
 __global__ void __launch_bounds__(TILE) k_pair64(PairArgs a) {
   __shared__ TileD sm;
+  __shared__ float3 wb[TILE / 32][2];
   const int4 unit = a.units[blockIdx.x];
   const int cell = unit.x;
   const int tid = threadIdx.x;
@@ -322,20 +486,27 @@ __global__ void __launch_bounds__(TILE) k_pair64(PairArgs a) {
     surf_i = m.x;
     if (m.y >= 0) { th_i = a.th[m.y]; phi_i = a.phi[m.z]; }
   }
+  // the same tile culling as the FP32 form (boxes in FP32 with a margin)
+  const CullBoxes cb = cull_boxes(active, (float)t_[0], (float)t_[1], (float)t_[2], wb);
   double acc[3] = {0, 0, 0};
   NbrList L;
   L.n = 0; L.overflow = 0;
   int run_surf = -3, run_id = -1;
   double run_d = 1e300;
   unsigned long long npairs = 0;
-  const double rc = a.T.rc;
 
   for (int nb = 0; nb < 27; ++nb) {
     int dx = nb % 3 - 1, dy = (nb / 3) % 3 - 1, dz = nb / 9 - 1;
     int ni = imod(ci + dx, a.Nc[0]), nj = imod(cj + dy, a.Nc[1]), nk = imod(ck + dz, a.Nc[2]);
     int ncell = ni + a.Nc[0] * (nj + a.Nc[1] * nk);
     int sbeg = a.cs[ncell], send = a.ce[ncell];
-    for (int base = sbeg; base < send; base += TILE) {
+    const float3 dh = make_float3((float)(dx * a.h[0]), (float)(dy * a.h[1]), (float)(dz * a.h[2]));
+    const float3 wlo = f3sub(cb.wlo, dh), whi = f3sub(cb.whi, dh);
+    const float3 clo = f3sub(cb.clo, dh), chi = f3sub(cb.chi, dh);
+    for (int base = sbeg, tt = a.toff[ncell]; base < send; base += TILE, ++tt) {
+      const float4 blo = a.tbox[2 * tt], bhi = a.tbox[2 * tt + 1];
+      const float3 bl = make_float3(blo.x, blo.y, blo.z), bh = make_float3(bhi.x, bhi.y, bhi.z);
+      if (boxes_apart(clo, chi, bl, bh, a.rc2_f)) continue;  // uniform over the CTA
       int cnt = min(TILE, send - base);
       __syncthreads();
       if (tid < cnt) {
@@ -352,7 +523,7 @@ __global__ void __launch_bounds__(TILE) k_pair64(PairArgs a) {
         sm.surf[tid] = m.x; sm.ilat[tid] = m.y; sm.ilon[tid] = m.z;
       }
       __syncthreads();
-      if (active) {
+      if (active && !boxes_apart(wlo, whi, bl, bh, a.rc2_f)) {
         for (int j = 0; j < cnt; ++j) {
           const int sj = sm.surf[j];
           if (a.collect && sj != run_surf) {
@@ -360,8 +531,9 @@ __global__ void __launch_bounds__(TILE) k_pair64(PairArgs a) {
             run_surf = sj; run_id = -1; run_d = 1e300;
           }
           double xx = sm.x[j] - t_[0], yy = sm.y[j] - t_[1], zz = sm.z[j] - t_[2];
-          double rr = sqrt(xx * xx + yy * yy + zz * zz);
-          if (rr > rc) continue;
+          const double r2 = xx * xx + yy * yy + zz * zz;
+          if (r2 > a.rc2) continue;  // the square root only for pairs inside the cutoff
+          double rr = sqrt(r2);
           ++npairs;
           double mask = 0.;
           if (sj == surf_i) {
@@ -457,17 +629,83 @@ rbc3d_status make_units(rbc3d_ctx* ctx, TargetSet& t, const DBuf<int>& cs, const
   std::vector<int> hs(nc), he(nc);
   CUDA_TRY(cudaMemcpy(hs.data(), cs.p, sizeof(int) * nc, cudaMemcpyDeviceToHost));
   CUDA_TRY(cudaMemcpy(he.data(), ce.p, sizeof(int) * nc, cudaMemcpyDeviceToHost));
-  std::vector<int4> u;
-  for (int c = 0; c < nc; ++c)
-    for (int b = hs[c]; b < he[c]; b += TILE) u.push_back(make_int4(c, b, std::min(TILE, he[c] - b), 0));
-  // heaviest cells first: cells are visited in decreasing neighbourhood load
-  t.nunits = (int)u.size();
-  if (t.nunits) CUDA_TRY(t.units.upload(u.data(), u.size(), ctx->st));
+  // sources per cell (the pair work of a unit is its targets x the sources
+  // of the 27 neighbour cells)
+  std::vector<long long> src(nc, 0);
+  if (ctx->npt > 0 && ctx->s_cstart.p) {
+    std::vector<int> ss(nc), se(nc);
+    CUDA_TRY(cudaMemcpy(ss.data(), ctx->s_cstart.p, sizeof(int) * nc, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(se.data(), ctx->s_cend.p, sizeof(int) * nc, cudaMemcpyDeviceToHost));
+    for (int c = 0; c < nc; ++c) src[c] = se[c] - ss[c];
+  }
+  const int* N = ctx->hg.Nc;
+  std::vector<std::pair<long long, int4>> u;
+  for (int c = 0; c < nc; ++c) {
+    const int cnt = he[c] - hs[c];
+    if (cnt <= 0) continue;
+    const int ci = c % N[0], cj = (c / N[0]) % N[1], ck = c / (N[0] * N[1]);
+    long long nsrc = 0;
+    for (int nb = 0; nb < 27; ++nb) {
+      const int ni = (ci + nb % 3 - 1 + N[0]) % N[0], nj = (cj + (nb / 3) % 3 - 1 + N[1]) % N[1];
+      const int nk = (ck + nb / 9 - 1 + N[2]) % N[2];
+      nsrc += src[ni + N[0] * (nj + N[1] * nk)];
+    }
+    // equal-sized units of at most TILE targets
+    const int k = (cnt + TILE - 1) / TILE, per = (cnt + k - 1) / k;
+    for (int b = 0; b < cnt; b += per) {
+      const int m = std::min(per, cnt - b);
+      u.push_back({nsrc * m, make_int4(c, hs[c] + b, m, 0)});
+    }
+  }
+  // heaviest units first, so the last wave holds the light ones
+  std::stable_sort(u.begin(), u.end(), [](const std::pair<long long, int4>& x, const std::pair<long long, int4>& y) {
+    return x.first > y.first;
+  });
+  std::vector<int4> uu(u.size());
+  for (size_t i = 0; i < u.size(); ++i) uu[i] = u[i].second;
+  t.nunits = (int)uu.size();
+  if (t.nunits) CUDA_TRY(t.units.upload(uu.data(), uu.size(), ctx->st));
   CUDA_TRY(cudaStreamSynchronize(ctx->st));
   return RBC3D_OK;
 }
 
 }  // namespace
+
+
+// erfc(x) exp(x^2) on [0, X] as t Q(t) with t = 1/(1 + x/2) (the variable of
+// the Chebyshev erfc fit of Press et al., Numerical Recipes, sec. 6.2) and Q
+// a degree-ERFCX_DEG polynomial: the truncated Chebyshev series of Q over the
+// t-interval (projection on 64 Chebyshev nodes, FP64 std::erfc), converted to
+// monomial coefficients in t.  Max relative error ~3e-7 in FP32 Horner for
+// X = 4.24 (eps = 1e-6 at rc = 3), against ~1e-9 of the series itself.
+void fit_erfcx(double X, float* q) {  // declared in ctx.hpp
+  const int N = 64, D = ERFCX_DEG;
+  const double tlo = 1.0 / (1.0 + 0.5 * X);
+  const double a = 2.0 / (1.0 - tlo), b = -(1.0 + tlo) / (1.0 - tlo);  // s = a t + b in [-1, 1]
+  double c[D + 1] = {0};
+  for (int j = 0; j < N; ++j) {
+    const double th = RBC3D_PI * (j + 0.5) / N, sj = std::cos(th), t = (sj - b) / a, x = 2.0 * (1.0 / t - 1.0);
+    const double g = std::erfc(x) * std::exp(x * x) / t;
+    for (int k = 0; k <= D; ++k) c[k] += 2.0 / N * g * std::cos(k * th);
+  }
+  c[0] *= 0.5;
+  // sum c_k T_k(s), s = a t + b, as a polynomial in t: T_{k+1} = 2 s T_k - T_{k-1}
+  double Tm[D + 1] = {0}, Tk[D + 1] = {0}, out[D + 1] = {0};
+  Tm[0] = 1.0;                  // T_0
+  Tk[0] = b; Tk[1] = a;         // T_1 = s
+  for (int i = 0; i <= D; ++i) out[i] += c[0] * Tm[i];
+  for (int k = 1; k <= D; ++k) {
+    for (int i = 0; i <= D; ++i) out[i] += c[k] * Tk[i];
+    double Tn[D + 1] = {0};
+    for (int i = 0; i <= D; ++i) {
+      Tn[i] += 2.0 * b * Tk[i] - Tm[i];
+      if (i + 1 <= D) Tn[i + 1] += 2.0 * a * Tk[i];
+    }
+    for (int i = 0; i <= D; ++i) { Tm[i] = Tk[i]; Tk[i] = Tn[i]; }
+  }
+  for (int i = 0; i <= D; ++i) q[i] = (float)out[i];
+}
+
 
 rbc3d_status sort_points_by_cell(rbc3d_ctx* ctx, int n, const double* x_dev, DBuf<int>& order, DBuf<int>& cs,
                                 DBuf<int>& ce) {
@@ -483,6 +721,37 @@ rbc3d_status build_source_list(rbc3d_ctx* ctx) {
   { k_gather_src<<<nblk(n, 256), 256, 0, ctx->st>>>(n, ctx->nlat, ctx->nlat * ctx->nlon, ctx->s_order.p, ctx->x.p,
                                                    ctx->a3.p, ctx->s_x.p, ctx->s_a3.p, ctx->s_meta.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
+  // FP32 pair-sum records and tile boxes
+  CUDA_TRY(ctx->s_p0.alloc(n)); CUDA_TRY(ctx->s_p1.alloc(n)); CUDA_TRY(ctx->s_u4.alloc(n)); CUDA_TRY(ctx->s_a4.alloc(n));
+  {
+    const HashGrid& hg = ctx->hg;
+    k_src_records<<<nblk(n, 256), 256, 0, ctx->st>>>(n, ctx->s_x.p, ctx->s_a3.p, ctx->s_meta.p, ctx->usph.p, ctx->nlat,
+                                                     hg.Nc[0], hg.Nc[1], hg.Nc[2], hg.h[0], hg.h[1], hg.h[2], hg.L[0],
+                                                     hg.L[1], hg.L[2], ctx->s_p0.p, ctx->s_p1.p, ctx->s_u4.p,
+                                                     ctx->s_a4.p);
+    ++ctx->launches;
+    CUDA_TRY(cudaGetLastError());
+    const int nc = hg.ncells;
+    std::vector<int> hs(nc), he(nc), toff(nc + 1, 0);
+    CUDA_TRY(cudaMemcpy(hs.data(), ctx->s_cstart.p, sizeof(int) * nc, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(he.data(), ctx->s_cend.p, sizeof(int) * nc, cudaMemcpyDeviceToHost));
+    std::vector<int2> tiles;
+    for (int c = 0; c < nc; ++c) {
+      toff[c] = (int)tiles.size();
+      for (int b = hs[c]; b < he[c]; b += TILE) tiles.push_back(make_int2(b, std::min(TILE, he[c] - b)));
+    }
+    toff[nc] = (int)tiles.size();
+    ctx->s_ntiles = (int)tiles.size();
+    CUDA_TRY(ctx->s_toff.upload(toff.data(), toff.size(), ctx->st));
+    CUDA_TRY(ctx->s_tbox.alloc(2 * tiles.size() + 2));
+    if (!tiles.empty()) {
+      DBuf<int2> dt;
+      CUDA_TRY(dt.upload(tiles.data(), tiles.size(), ctx->st));
+      { k_tile_boxes<<<(int)tiles.size(), TILE, 0, ctx->st>>>(dt.p, ctx->s_p0.p, ctx->s_tbox.p); ++ctx->launches; }
+      CUDA_TRY(cudaGetLastError());
+      CUDA_TRY(cudaStreamSynchronize(ctx->st));
+    }
+  }
   ctx->src_sorted = true;
   ctx->pme.cplan.valid = false;  // the PME tiles follow the source positions
   // tlist_rbc shares the source order
@@ -534,6 +803,8 @@ rbc3d_status run_pair_sum(rbc3d_ctx* ctx, int tlist, double c1, double c2, int p
   a.nt = t.n; a.tx = t.x.p; a.tA = t.Acoef.p; a.tmeta = t.meta.p; a.torder = t.order.p; a.units = t.units.p; a.v = t.v.p;
   a.ns = ctx->npt; a.sx = ctx->s_x.p; a.sf = ctx->s_f.p; a.sg = ctx->s_g.p; a.sa3 = ctx->s_a3.p; a.smeta = ctx->s_meta.p;
   a.cs = ctx->s_cstart.p; a.ce = ctx->s_cend.p;
+  a.sp0 = ctx->s_p0.p; a.sp1 = ctx->s_p1.p; a.su = ctx->s_u4.p; a.sa4 = ctx->s_a4.p;
+  a.sF4 = ctx->s_F4.p; a.sG4 = ctx->s_G4.p; a.toff = ctx->s_toff.p; a.tbox = ctx->s_tbox.p;
   for (int d = 0; d < 3; ++d) { a.Nc[d] = ctx->hg.Nc[d]; a.h[d] = ctx->hg.h[d]; a.L[d] = ctx->hg.L[d]; a.iL[d] = ctx->iLb[d]; }
   a.th = ctx->th.p; a.phi = ctx->phi.p; a.usph = ctx->usph.p; a.nlat = ctx->nlat;
   a.radius = ctx->radius; a.inv_radius = 1.0 / ctx->radius; a.inv_radius_f = (float)(1.0 / ctx->radius);
@@ -546,11 +817,18 @@ rbc3d_status run_pair_sum(rbc3d_ctx* ctx, int tlist, double c1, double c2, int p
   a.two_isqa_f = (float)(2.0 / sqrt(ctx->prm.alpha));
   a.m8_ispi_f = (float)(-8.0 / sqrt(RBC3D_PI));
   a.q75_spi_f = (float)(0.75 * sqrt(RBC3D_PI));
+  erfcx_coeffs(ctx);
+  for (int k = 0; k <= ERFCX_DEG; ++k) a.erfcx_q[k] = ctx->erfcx_q[k];
   a.T = ctx->T;
   a.collect = collect_nbr ? 1 : 0;
   a.items = ctx->items.p; a.cap = ctx->items_cap; a.cnt = ctx->dcnt.p;
   bool dl = (c2 != 0.0) && ctx->has_g;
   if (prec != RBC3D_FP64) {
+    CUDA_TRY(ctx->s_F4.alloc(ctx->npt));
+    if (dl) CUDA_TRY(ctx->s_G4.alloc(ctx->npt));
+    a.sF4 = ctx->s_F4.p; a.sG4 = ctx->s_G4.p;
+    { k_src_dens4<<<nblk(ctx->npt, 256), 256, 0, ctx->st>>>(ctx->npt, c1, c2, ctx->s_f.p, ctx->s_g.p, dl ? 1 : 0,
+                                                             ctx->s_F4.p, ctx->s_G4.p); ++ctx->launches; }
     if (dl) { k_pair32<true><<<t.nunits, TILE, 0, ctx->st>>>(a); ++ctx->launches; }
     else { k_pair32<false><<<t.nunits, TILE, 0, ctx->st>>>(a); ++ctx->launches; }
   } else {
@@ -575,4 +853,12 @@ rbc3d_status run_linear(rbc3d_ctx* ctx, int tlist, double c2) {
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaStreamSynchronize(ctx->st));
   return RBC3D_OK;
+}
+
+void erfcx_coeffs(rbc3d_ctx* ctx) {
+  const double X = ctx->prm.rc * std::sqrt(RBC3D_PI / ctx->prm.alpha);
+  if (ctx->erfcx_X != X) {
+    ctx->erfcx_X = X;
+    fit_erfcx(X, ctx->erfcx_q);
+  }
 }

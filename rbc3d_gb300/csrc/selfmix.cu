@@ -9,8 +9,10 @@
 // target, (X_hi - t_hi) + (X_lo - t_lo), is formed before the bicubic
 // weights are applied, so xx carries ~1e-7 relative error instead of the
 // ~1e-5 of plain FP32 positions.  Densities, normals, weights and the Ewald
-// kernel are FP32 (erfc / exp evaluated directly), accumulated with Kahan
-// compensation per target.
+// kernel are FP32 (erfc as exp(-x^2) t Q(t), the fit of fit_erfcx),
+// accumulated with Kahan compensation per target.  Node records are read
+// as float4.  erfc is exp(-x^2) t Q(t) with the fitted
+// polynomial of fit_erfcx (pair.cu).
 //
 // Patch geometry: the bicubic weights of patch point q of a target at
 // latitude ilat0 depend only on (ilat0, q); longitudes shift the stencil by
@@ -112,10 +114,25 @@ struct MixArgs {
   double B[RBC3D_MAX_CELLTYPES];
   float c1, c2;
   float rc2, sqpa, two_isqa, m8_ispi, q75_spi;
+  float erfcx_q[ERFCX_DEG + 1];
 };
+
+// The 13 float4 of a node record in registers (only those the terms need).
+template <bool DL>
+__device__ __forceinline__ void load_rec(const float* r, float* v) {
+  const float4* r4 = reinterpret_cast<const float4*>(r);
+#pragma unroll
+  for (int i = 0; i < REC / 4; ++i) {
+    // SL needs x (floats 0-14) and F (27-38): float4 0-3 and 6-9
+    if (!DL && (i == 4 || i == 5 || i >= 10)) continue;
+    const float4 q = __ldg(r4 + i);
+    v[4 * i] = q.x; v[4 * i + 1] = q.y; v[4 * i + 2] = q.z; v[4 * i + 3] = q.w;
+  }
+}
 
 // one warp per target; warps of a block walk one latitude ring so that
 // neighbouring warps share most stencil nodes in L1
+template <bool DL>
 __global__ void __launch_bounds__(256) k_self_mix(MixArgs a) {
   const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
@@ -125,7 +142,7 @@ __global__ void __launch_bounds__(256) k_self_mix(MixArgs a) {
   const int ilon0 = rr % a.nlon, ilat0 = rr / a.nlon;
   const int p = cell * nv + ilon0 * a.nlat + ilat0;
   const float c1 = a.c1;
-  const float c2m = (float)(a.c2 * a.B[a.celltype[cell]]);
+  const float c2m = DL ? (float)(a.c2 * a.B[a.celltype[cell]]) : 0.f;
   const float4 th4 = a.thi[p], tl4 = a.tlo[p];
   const float th_[3] = {th4.x, th4.y, th4.z}, tl_[3] = {tl4.x, tl4.y, tl4.z};
   const float* base = a.rec + (size_t)cell * a.m * a.nlon * REC;
@@ -147,29 +164,31 @@ __global__ void __launch_bounds__(256) k_self_mix(MixArgs a) {
     float xx[3] = {0, 0, 0}, F[3] = {0, 0, 0}, G[3] = {0, 0, 0}, A3[3] = {0, 0, 0};
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      const float* r = base + (size_t)nodes[k] * REC;
+      float v[REC];
+      load_rec<DL>(base + (size_t)nodes[k] * REC, v);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        float d = __fadd_rn(__fsub_rn(__ldg(r + OFF_X + c), th_[c]), __fsub_rn(__ldg(r + OFF_X + 3 + c), tl_[c]));
-        xx[c] += wu[k] * d + w1[k] * __ldg(r + OFF_X + 6 + c) + w2[k] * __ldg(r + OFF_X + 9 + c) +
-                 w12[k] * __ldg(r + OFF_X + 12 + c);
-        F[c] += wu[k] * __ldg(r + OFF_F + c) + w1[k] * __ldg(r + OFF_F + 3 + c) + w2[k] * __ldg(r + OFF_F + 6 + c) +
-                w12[k] * __ldg(r + OFF_F + 9 + c);
-      }
-      if (c2m != 0.f) {
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          G[c] += wu[k] * __ldg(r + OFF_G + c) + w1[k] * __ldg(r + OFF_G + 3 + c) + w2[k] * __ldg(r + OFF_G + 6 + c) +
-                  w12[k] * __ldg(r + OFF_G + 9 + c);
-          A3[c] += wu[k] * __ldg(r + OFF_A3 + c) + w1[k] * __ldg(r + OFF_A3 + 3 + c) +
-                   w2[k] * __ldg(r + OFF_A3 + 6 + c) + w12[k] * __ldg(r + OFF_A3 + 9 + c);
+        const float d = __fadd_rn(__fsub_rn(v[OFF_X + c], th_[c]), __fsub_rn(v[OFF_X + 3 + c], tl_[c]));
+        xx[c] += wu[k] * d + w1[k] * v[OFF_X + 6 + c] + w2[k] * v[OFF_X + 9 + c] + w12[k] * v[OFF_X + 12 + c];
+        F[c] += wu[k] * v[OFF_F + c] + w1[k] * v[OFF_F + 3 + c] + w2[k] * v[OFF_F + 6 + c] + w12[k] * v[OFF_F + 9 + c];
+        if (DL) {
+          G[c] += wu[k] * v[OFF_G + c] + w1[k] * v[OFF_G + 3 + c] + w2[k] * v[OFF_G + 6 + c] +
+                  w12[k] * v[OFF_G + 9 + c];
+          A3[c] += wu[k] * v[OFF_A3 + c] + w1[k] * v[OFF_A3 + 3 + c] + w2[k] * v[OFF_A3 + 6 + c] +
+                   w12[k] * v[OFF_A3 + 9 + c];
         }
       }
     }
     const float r2 = xx[0] * xx[0] + xx[1] * xx[1] + xx[2] * xx[2];
     if (r2 >= a.rc2) continue;  // rr >= rc (ModRbcSingInt.F90:65)
     const float rinv = rsqrtf(r2), rv = r2 * rinv, ir2 = rinv * rinv;
-    const float st = rv * a.sqpa, ex = expf(-st * st), e1 = erfcf(st), e2 = a.two_isqa * ex;
+    const float st = rv * a.sqpa, ex = expf(-st * st);
+    // erfc(st) = exp(-st^2) t Q(t), t = 1/(1 + st/2) (fit_erfcx)
+    const float tq = __frcp_rn(fmaf(0.5f, st, 1.f));
+    float Qp = a.erfcx_q[ERFCX_DEG];
+#pragma unroll
+    for (int k = ERFCX_DEG - 1; k >= 0; --k) Qp = fmaf(Qp, tq, a.erfcx_q[k]);
+    const float e1 = ex * (tq * Qp), e2 = a.two_isqa * ex;
     const float wq = a.pw[irad];
     float v0 = 0.f, v1 = 0.f, v2 = 0.f;
     if (c1 != 0.f) {
@@ -180,7 +199,7 @@ __global__ void __launch_bounds__(256) k_self_mix(MixArgs a) {
       v1 = c1 * (A * xx[1] * d + Bc * f1);
       v2 = c1 * (A * xx[2] * d + Bc * f2);
     }
-    if (c2m != 0.f) {
+    if (DL) {
       const float cdl = a.m8_ispi * (ex * (st * (1.5f + st * st)) + a.q75_spi * e1);
       const float Ad = cdl * ir2 * ir2 * rinv;
       const float dg = wq * (xx[0] * G[0] + xx[1] * G[1] + xx[2] * G[2]);
@@ -282,8 +301,11 @@ rbc3d_status run_self_mixed(rbc3d_ctx* ctx, int tlist, double c1, double c2) {
   a.two_isqa = (float)(2.0 / std::sqrt(ctx->prm.alpha));
   a.m8_ispi = (float)(-8.0 / std::sqrt(RBC3D_PI));
   a.q75_spi = (float)(0.75 * std::sqrt(RBC3D_PI));
+  erfcx_coeffs(ctx);
+  for (int k = 0; k <= ERFCX_DEG; ++k) a.erfcx_q[k] = ctx->erfcx_q[k];
   long long threads = (long long)t.n * 32;
-  { k_self_mix<<<(int)((threads + 255) / 256), 256, 0, ctx->st>>>(a); ++ctx->launches; }
+  if (a.c2 != 0.f) { k_self_mix<true><<<(int)((threads + 255) / 256), 256, 0, ctx->st>>>(a); ++ctx->launches; }
+  else { k_self_mix<false><<<(int)((threads + 255) / 256), 256, 0, ctx->st>>>(a); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   return RBC3D_OK;
 }
