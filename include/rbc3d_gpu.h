@@ -213,6 +213,25 @@ rbc3d_status rbc3d_compute_wall_residual_vel(rbc3d_ctx* ctx, int prec,
  * (two of them back to back for guess mode 3). */
 rbc3d_status rbc3d_no_slip_wall(rbc3d_ctx* ctx, const rbc3d_solve_opts* opt,
                                 const double* guess, rbc3d_solve_stats* st);
+/* Solve_RBC_Vel, ModVelSolver.F90:44-132 (Deflate off): GMRES (FP64 matvec
+ * and Arnoldi, opt->prec ignored) on the spherical-harmonic coefficients of
+ * the cell surface velocities, degree < nlat0 (the layout of Glob_Sph_Trans,
+ * ModVelSolver.F90:641-719: per cell a(m,n) for m < nlat0, n >= m, then
+ * b(m,n) for 1 <= m < nlat0, three components each; rbc3d_cell_dof values).
+ * The right-hand side is Compute_Rhs (single layer of cells and walls, PME,
+ * 2 vBkg/Acoef), the operator MyMatMult (g from the coefficients, its spline
+ * rebuilt as Rbc_BuildSurfaceSource, double layer with c2 = -1/(4 pi), plus
+ * g).  sol: NULL, or the solution vector, used as the initial guess when
+ * opt->guess != 0 (KSPSetInitialGuessNonzero) and overwritten with the
+ * solution.  v: surface velocities (npt x 3) out.  With every viscRat = 1
+ * the solution is the right-hand side (no GMRES).  Needs even nlon and
+ * 2 (nlat0 - 1) < nlon.  The cells' g (and its spline) are left at the
+ * solution. */
+rbc3d_status rbc3d_solve_rbc_vel(rbc3d_ctx* ctx, const rbc3d_solve_opts* opt,
+                                 int nlat0, double* sol, double* v,
+                                 rbc3d_solve_stats* st);
+/* Length of the coefficient vector of rbc3d_solve_rbc_vel: 3 nlat0^2 ncell. */
+int rbc3d_cell_dof(const rbc3d_ctx* ctx, int nlat0);
 /* MyMatMult of ModNoSlip.F90:255 on a dof-length vector: y = A u. */
 rbc3d_status rbc3d_wall_matmult(rbc3d_ctx* ctx, int prec, const double* u,
                                 double* y);

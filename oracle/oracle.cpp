@@ -970,6 +970,126 @@ static int gmres(int n, MV&& A, const std::vector<double>& b, std::vector<double
 
 // ---------------------------------------------------------------------------
 // C ABI
+// ---------------------------------------------------------------------------
+// Cell velocity solve (Solve_RBC_Vel, ModVelSolver.F90:44-132): spherical
+// harmonic transforms on the Gauss grid (Glob_Sph_Trans :641-719 through
+// Spherepack shags / shsgs, restated from their documented definitions with
+// pbar_table) and the g spline rebuild of Rbc_BuildSurfaceSource
+// (ModRbc.F90:716-807: analysis, ShFilter to degree < nlat0, synthesis on the
+// equiangular grid with both poles, Spline_Build_On_Sphere).
+struct ShTab {
+  int L = 0, nlat = 0, nlon = 0;
+  std::vector<double> PG, PE;  // [row][m][n], Gauss rows and equiangular rows (nlat+1)
+  std::vector<double> cs, sn;  // cos(m phi_j), sin(m phi_j): [m * nlon + j]
+};
+static void sh_setup(const Ctx* c, int L, ShTab& T) {
+  T.L = L; T.nlat = c->nlat; T.nlon = c->nlon;
+  T.PG.assign((size_t)c->nlat * L * L, 0.);
+  T.PE.assign((size_t)(c->nlat + 1) * L * L, 0.);
+  for (int i = 0; i < c->nlat; ++i) pbar_table(L, c->th[i], &T.PG[(size_t)i * L * L]);
+  for (int i = 0; i <= c->nlat; ++i) pbar_table(L, i * PI / c->nlat, &T.PE[(size_t)i * L * L]);
+  T.cs.resize((size_t)L * c->nlon); T.sn.resize((size_t)L * c->nlon);
+  for (int m = 0; m < L; ++m)
+    for (int j = 0; j < c->nlon; ++j) { T.cs[m * c->nlon + j] = std::cos(m * c->phi[j]); T.sn[m * c->nlon + j] = std::sin(m * c->phi[j]); }
+}
+// shags restricted to m, n < L: v[ilat + nlat*ilon] -> a, b [m*L + n]
+static void sh_anal(const Ctx* c, const ShTab& T, const double* v, double* a, double* b) {
+  const int L = T.L, nlat = T.nlat, nlon = T.nlon;
+  std::fill(a, a + L * L, 0.); std::fill(b, b + L * L, 0.);
+  for (int i = 0; i < nlat; ++i)
+    for (int m = 0; m < L; ++m) {
+      double C = 0, S = 0;
+      for (int j = 0; j < nlon; ++j) { C += v[i + nlat * j] * T.cs[m * nlon + j]; S += v[i + nlat * j] * T.sn[m * nlon + j]; }
+      // Gauss weight x 2/nlon; the grid's w is the Gauss weight x 2 pi/nlon (RBC_Create, ModRbc.F90:94)
+      const double wf = c->w[i] / PI;
+      for (int n = m; n < L; ++n) {
+        const double P = T.PG[((size_t)i * L + m) * L + n];
+        a[m * L + n] += wf * P * C;
+        b[m * L + n] -= wf * P * S;
+      }
+    }
+}
+// shsgs / shses restricted to m, n < L on the rows of P: out[i + nrow*j]
+static void sh_synth(const ShTab& T, const std::vector<double>& P, int nrow, const double* a, const double* b, double* out) {
+  const int L = T.L, nlon = T.nlon;
+  for (int i = 0; i < nrow; ++i) {
+    std::vector<double> G(L, 0.), H(L, 0.);
+    for (int m = 0; m < L; ++m)
+      for (int n = m; n < L; ++n) {
+        const double p = P[((size_t)i * L + m) * L + n];
+        G[m] += p * a[m * L + n];
+        H[m] += p * b[m * L + n];
+      }
+    for (int j = 0; j < nlon; ++j) {
+      double s = 0.5 * G[0];
+      for (int m = 1; m < L; ++m) s += G[m] * T.cs[m * nlon + j] - H[m] * T.sn[m * nlon + j];
+      out[i + nrow * j] = s;
+    }
+  }
+}
+// Glob_Sph_Trans layout of one cell's coefficients: a(m, n) for m < L, n >= m,
+// then b(m, n) for 1 <= m < L, n >= m; 3 components each.
+static void sh_pack(int L, const double* a /*3 x L*L*/, const double* b, double* cvec) {
+  size_t pc = 0;
+  for (int m = 0; m < L; ++m)
+    for (int n = m; n < L; ++n)
+      for (int k = 0; k < 3; ++k) cvec[pc++] = a[(size_t)k * L * L + m * L + n];
+  for (int m = 1; m < L; ++m)
+    for (int n = m; n < L; ++n)
+      for (int k = 0; k < 3; ++k) cvec[pc++] = b[(size_t)k * L * L + m * L + n];
+}
+static void sh_unpack(int L, const double* cvec, double* a, double* b) {
+  std::fill(a, a + 3 * L * L, 0.); std::fill(b, b + 3 * L * L, 0.);
+  size_t pc = 0;
+  for (int m = 0; m < L; ++m)
+    for (int n = m; n < L; ++n)
+      for (int k = 0; k < 3; ++k) a[(size_t)k * L * L + m * L + n] = cvec[pc++];
+  for (int m = 1; m < L; ++m)
+    for (int n = m; n < L; ++n)
+      for (int k = 0; k < 3; ++k) b[(size_t)k * L * L + m * L + n] = cvec[pc++];
+}
+// Glob_Sph_Trans over all cells: v (N x 3, point layout) <-> c (3 L^2 per cell)
+static void glob_sph_trans(const Ctx* c, const ShTab& T, double* v, double* cv, bool to_four) {
+  const int L = T.L, nv = c->nlat * c->nlon;
+  const size_t N = c->npt;
+  std::vector<double> a(3 * L * L), b(3 * L * L);
+  for (int cell = 0; cell < c->ncell; ++cell) {
+    double* cc = cv + (size_t)cell * 3 * L * L;
+    if (to_four) {
+      for (int k = 0; k < 3; ++k) sh_anal(c, T, v + (size_t)cell * nv + k * N, &a[(size_t)k * L * L], &b[(size_t)k * L * L]);
+      sh_pack(L, a.data(), b.data(), cc);
+    } else {
+      sh_unpack(L, cc, a.data(), b.data());
+      for (int k = 0; k < 3; ++k)
+        sh_synth(T, T.PG, c->nlat, &a[(size_t)k * L * L], &b[(size_t)k * L * L], v + (size_t)cell * nv + k * N);
+    }
+  }
+}
+// rbc%g <- g, Rbc_BuildSurfaceSource(gFlag), SourceList_UpdateDensity(updateG)
+static void set_g_from_grid(Ctx* c, const ShTab& T, const double* g) {
+  const int L = T.L, nlat = c->nlat, nlon = c->nlon, nv = nlat * nlon;
+  const size_t N = c->npt, S = (size_t)4 * 2 * nlat * nlon;  // per cell and variable
+  c->g.assign(g, g + 3 * N);
+  c->sg.resize(3 * N);
+  c->spl_G.resize(3 * S * c->ncell);
+  std::vector<double> gd(nv), a(L * L), b(L * L), fe((size_t)(nlat + 1) * nlon * 3), tab(3 * S);
+  for (int cell = 0; cell < c->ncell; ++cell) {
+    for (int k = 0; k < 3; ++k) {
+      for (int r = 0; r < nv; ++r) gd[r] = g[(size_t)cell * nv + r + k * N] * c->detJ[(size_t)cell * nv + r];
+      sh_anal(c, T, gd.data(), a.data(), b.data());  // ShAnalGau + ShFilter (degree < nlat0)
+      sh_synth(T, T.PE, nlat + 1, a.data(), b.data(), &fe[(size_t)(nlat + 1) * nlon * k]);
+    }
+    spline_build_on_sphere(nlat, nlon, 3, fe.data(), tab.data());
+    std::copy(tab.begin(), tab.end(), c->spl_G.begin() + (size_t)cell * 3 * S);
+  }
+  for (size_t p = 0; p < N; ++p) {
+    const int ilat = (int)((p % nv) % nlat);
+    const double ds = c->detJ[p] * c->w[ilat];
+    for (int k = 0; k < 3; ++k) c->sg[p + k * N] = c->g[p + k * N] * ds;
+  }
+  c->has_g = true;
+}
+
 extern "C" {
 
 int API(abi_version)(void) { return RBC3D_ABI_VERSION; }
@@ -1188,6 +1308,65 @@ rbc3d_status API(no_slip_wall)(Ctx* c, const rbc3d_solve_opts* o, const double* 
 
 rbc3d_status API(get_counts)(const Ctx* c, rbc3d_counts* out) { *out = c->counts; return RBC3D_OK; }
 
+int API(cell_dof)(const Ctx* c, int nlat0) { return 3 * nlat0 * nlat0 * c->ncell; }
+
+// Solve_RBC_Vel, ModVelSolver.F90:44-132 (Deflate off)
+rbc3d_status API(solve_rbc_vel)(Ctx* c, const rbc3d_solve_opts* o, int nlat0, double* sol, double* v,
+                                rbc3d_solve_stats* st) {
+  if (!o || !v || nlat0 < 1 || nlat0 > c->nlat || 2 * (nlat0 - 1) >= c->nlon) return fail(c, RBC3D_ERR_ARG, "bad nlat0");
+  if (c->npt == 0) return RBC3D_OK;
+  auto t0 = std::chrono::steady_clock::now();
+  rbc3d_solve_stats s{};
+  ShTab T;
+  sh_setup(c, nlat0, T);
+  TView t;
+  make_tlist(c, RBC3D_TLIST_RBC, t);
+  const size_t N = c->npt;
+  const int dof = 3 * nlat0 * nlat0 * c->ncell;
+  const double ip4 = 1.0 / (4. * PI);
+  rbc3d_status err;
+  // Compute_Rhs (:455-515)
+  std::vector<double> vv(3 * N, 0.), rhs(dof), x(dof, 0.);
+  if ((err = add_int_on_rbcs(c, t, ip4, 0., vv.data()))) return err;
+  if ((err = add_int_on_walls(c, RBC3D_TLIST_RBC, t, ip4, vv.data()))) return err;
+  if ((err = pme_distrib_source(c, ip4, 0., 1, 1))) return err;
+  pme_transform(c);
+  pme_add_interp_vel(c, t, vv.data());
+  for (int k = 0; k < 3; ++k)
+    for (size_t i = 0; i < N; ++i) vv[i + k * N] += 2. * c->prm.vBkg[k] / t.Acoef[i];
+  glob_sph_trans(c, T, vv.data(), rhs.data(), true);
+  bool all_one = true;
+  for (int l = 0; l < c->prm.ncelltypes; ++l) all_one = all_one && c->prm.viscRat[l] == 1.0;
+  if (all_one) {
+    x = rhs;
+    s.converged = 1;
+  } else {
+    if (o->guess && sol) x.assign(sol, sol + dof);
+    // MyMatMult (:523-601)
+    std::vector<double> g(3 * N);
+    auto A = [&](const double* u, double* y) -> rbc3d_status {
+      glob_sph_trans(c, T, g.data(), const_cast<double*>(u), false);
+      set_g_from_grid(c, T, g.data());
+      std::fill(vv.begin(), vv.end(), 0.);
+      rbc3d_status e;
+      if ((e = add_int_on_rbcs(c, t, 0., -ip4, vv.data()))) return e;
+      if ((e = pme_distrib_source(c, 0., -ip4, 1, 0))) return e;
+      pme_transform(c);
+      pme_add_interp_vel(c, t, vv.data());
+      for (size_t i = 0; i < 3 * N; ++i) vv[i] += g[i];
+      glob_sph_trans(c, T, vv.data(), y, true);
+      return RBC3D_OK;
+    };
+    int r = gmres(dof, A, rhs, x, o->rtol, o->max_it, o->restart > 0 ? o->restart : 30, &s, &err);
+    if (r < 0) return err;
+  }
+  if (sol) std::copy(x.begin(), x.end(), sol);
+  glob_sph_trans(c, T, v, x.data(), false);
+  s.ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  if (st) *st = s;
+  return s.converged ? RBC3D_OK : fail(c, RBC3D_ERR_NOCONV, "GMRES reached max_it");
+}
+
 // Test hooks for the known-answer tests of the building blocks.
 void API(kat_ewald_sl)(double alpha, double rc, int n, const double* r, double* A, double* B, int exact) {
   EwaldTables E;
@@ -1245,6 +1424,17 @@ void API(kat_find_projection)(int m, int n, const double* tab, const double* xta
 }
 // PME grid after PME_Transform (3 x G, x fastest) for white-box tests.
 void API(pme_velocity_grid)(const Ctx* c, double* out) { std::copy(c->vv.begin(), c->vv.end(), out); }
+void API(kat_pbar)(int L, double theta, double* P) { pbar_table(L, theta, P); }
+void API(kat_spline_build)(int nlat, int nlon, int nvar, const double* f, double* tab) {
+  spline_build_on_sphere(nlat, nlon, nvar, f, tab);
+}
+// Glob_Sph_Trans of the context's cells (to_four = 1: v -> c, else c -> v)
+rbc3d_status API(kat_sph_trans)(Ctx* c, int nlat0, double* v, double* cv, int to_four) {
+  ShTab T;
+  sh_setup(c, nlat0, T);
+  glob_sph_trans(c, T, v, cv, to_four != 0);
+  return RBC3D_OK;
+}
 int API(set_threads)(int n) { if (n > 0) omp_set_num_threads(n); return omp_get_max_threads(); }
 
 }  // extern "C"

@@ -472,4 +472,66 @@ void tri_int_duffy(const EwaldTables& E, const double* x, const double* f, const
   }
 }
 
+
+void pbar_table(int L, double theta, double* P) {
+  const double x = std::cos(theta), sn = std::sin(theta);
+  for (int i = 0; i < L * L; ++i) P[i] = 0.;
+  double pmm = std::sqrt(0.5);  // pbar(0, 0)
+  for (int m = 0; m < L; ++m) {
+    if (m > 0) pmm *= std::sqrt((2.0 * m + 1.0) / (2.0 * m)) * sn;
+    P[m * L + m] = pmm;
+    if (m + 1 < L) P[m * L + m + 1] = std::sqrt(2.0 * m + 3.0) * x * pmm;
+    for (int n = m + 2; n < L; ++n) {
+      const double a = std::sqrt((4.0 * n * n - 1.0) / ((double)n * n - (double)m * m));
+      const double b = std::sqrt(((n - 1.0) * (n - 1.0) - (double)m * m) / (4.0 * (n - 1.0) * (n - 1.0) - 1.0));
+      P[m * L + n] = a * (x * P[m * L + n - 1] - b * P[m * L + n - 2]);
+    }
+  }
+}
+
+void fft_diff(const double* u, int M, int stride, double* du) {
+  std::vector<std::complex<double>> a(M);
+  for (int i = 0; i < M; ++i) a[i] = u[(size_t)i * stride];
+  fft_c2c(a.data(), M, 1, -1);
+  // half spectrum k = 0 .. M/2: k < M/2 times i k / M, k = M/2 zeroed
+  const int H = M / 2;
+  std::vector<std::complex<double>> h(H + 1);
+  for (int k = 0; k < H; ++k) h[k] = a[k] * std::complex<double>(0.0, (double)k / M);
+  h[H] = 0.;
+  // c2r: the Hermitian extension, imaginary parts of k = 0 (and M/2) ignored
+  std::vector<std::complex<double>> b(M);
+  b[0] = h[0].real();
+  for (int k = 1; k <= H; ++k) {
+    if (2 * k == M) { b[k] = h[k].real(); continue; }
+    b[k] = h[k];
+    b[M - k] = std::conj(h[k]);
+  }
+  fft_c2c(b.data(), M, 1, +1);
+  for (int i = 0; i < M; ++i) du[(size_t)i * stride] = b[i].real();
+}
+
+void spline_build_on_sphere(int nlat, int nlon, int nvar, const double* f, double* tab) {
+  const int m = 2 * nlat, n = nlon;
+  const size_t per = (size_t)m * n * nvar;
+  double* u = tab;
+  double* u1 = tab + per;
+  double* u2 = tab + 2 * per;
+  double* u12 = tab + 3 * per;
+  for (int l = 0; l < nvar; ++l)
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < nlat; ++i) {
+        u[i + (size_t)m * (j + (size_t)n * l)] = f[i + (size_t)(nlat + 1) * (j + (size_t)n * l)];
+        u[nlat + i + (size_t)m * (j + (size_t)n * l)] =
+            f[(nlat - i) + (size_t)(nlat + 1) * ((j + n / 2) % n + (size_t)n * l)];
+      }
+  for (int l = 0; l < nvar; ++l) {
+    for (int j = 0; j < n; ++j) fft_diff(u + (size_t)m * (j + (size_t)n * l), m, 1, u1 + (size_t)m * (j + (size_t)n * l));
+    for (int i = 0; i < m; ++i) {
+      fft_diff(u + i + (size_t)m * n * l, n, m, u2 + i + (size_t)m * n * l);
+      // u12 from u1 along the second axis (FFT_Diff(u1, u2=u12))
+    }
+  }
+  for (int l = 0; l < nvar; ++l)
+    for (int i = 0; i < m; ++i) fft_diff(u1 + i + (size_t)m * n * l, n, m, u12 + i + (size_t)m * n * l);
+}
 }  // namespace orc

@@ -170,6 +170,21 @@ void spline_find_projection(const Spline& s, const double* xtar, double& th0, do
 // other factors).  sign = -1 forward, +1 backward; unnormalised.
 void fft_c2c(std::complex<double>* a, int n, int stride, int sign);
 
+// Spherepack's normalised associated Legendre functions pbar(m, n, theta)
+// (documentation of shags/shsgs: sqrt((2n+1)/2 (n-m)!/(n+m)!) sin^m(theta)
+// d^m P_n / dx^m at x = cos(theta), no Condon-Shortley phase, so that
+// int_{-1}^{1} pbar^2 dx = 1), for 0 <= m <= n < L, by the standard
+// three-term recurrence in n.  P[m*L + n].
+void pbar_table(int L, double theta, double* P);
+// FFT_Diff, ModFFT.F90:25-93, along one axis of length M (stride in the
+// array): the r2c transform, modes k < M/2 times i k / M, mode M/2 zeroed,
+// the unnormalised c2r back (FFTW semantics).
+void fft_diff(const double* u, int M, int stride, double* du);
+// Spline_Build_On_Sphere, ModSpline.F90:121-143: f on the equiangular grid
+// (nlat+1 rows with both poles, nlon columns, nvar; f[i + (nlat+1)*(j + nlon*l)])
+// to the table u | u1 | u2 | u12, each (2 nlat, nlon, nvar) column-major.
+void spline_build_on_sphere(int nlat, int nlon, int nvar, const double* f, double* tab);
+
 // MinDistToTri (Eberly), ModIntOnWalls.F90:480-577.  x(3,3) col-major:
 // x[l + 3*c] is vertex l component c.
 double min_dist_to_tri(const double* xtar, const double* x, double& s0, double& t0);

@@ -96,6 +96,8 @@ SIGNATURES = [
     ("wall_matmult", C.c_int, [_vp, C.c_int, _dp, _dp]),
     ("calc_velocity_field", C.c_int, [_vp, C.c_int, C.c_int, _dp]),
     ("get_counts", C.c_int, [_vp, C.POINTER(Counts)]),
+    ("cell_dof", C.c_int, [_vp, C.c_int]),
+    ("solve_rbc_vel", C.c_int, [_vp, C.POINTER(SolveOpts), C.c_int, _dp, _dp, C.POINTER(SolveStats)]),
 ]
 # Device-timing entry points of the GPU library only.
 GPU_SIGNATURES = [
@@ -314,6 +316,21 @@ class Context:
         if check and code not in (0, 4):
             self._check(code)
         return st, code
+
+    def solve_rbc_vel(self, nlat0, rtol=1e-11, max_it=200, restart=30, sol=None, check=True):
+        """Solve_RBC_Vel: returns (sol, v (N,3) as (3,N) SoA, stats, code).  sol, when
+        given, is the warm start (the reference keeps its solution vector
+        between calls, KSPSetInitialGuessNonzero)."""
+        n = self.L.fn["cell_dof"](self.h, nlat0)
+        x = np.zeros(n) if sol is None else f64(sol).copy()
+        o = SolveOpts(rtol=rtol, max_it=max_it, restart=restart, prec=FP64, guess=0 if sol is None else 1)
+        st = SolveStats()
+        N = self.L.fn["num_targets"](self.h, 0)
+        v = np.zeros(3 * N)
+        code = self.L.fn["solve_rbc_vel"](self.h, C.byref(o), nlat0, _ptr(x), _ptr(v), C.byref(st))
+        if check and code not in (0, 4):
+            self._check(code)
+        return x, v.reshape(3, N), st, code
 
     def counts(self):
         c = Counts()

@@ -1,0 +1,153 @@
+// gmres.cuh -- restarted GMRES on the device (FP64), the KSPGMRES defaults
+// the reference configures in NoSlipWall (ModNoSlip.F90:69-87) and
+// Solve_RBC_Vel (ModVelSolver.F90:74-90): classical Gram-Schmidt without
+// refinement, Givens rotations, PCNONE, converged when the true residual
+// ||b - A x|| < rtol ||b|| (KSPConvergedDefault); a cycle ends on the Givens
+// estimate and the true residual after the update decides.  The Krylov basis,
+// Hessenberg matrix and rotations stay on the device; one scalar per
+// iteration is read back for the convergence test.
+#pragma once
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "ctx.hpp"
+
+namespace {
+
+// ---- GMRES kernels (FP64)
+__global__ void k_dots(int n, int nv, const double* __restrict__ V, size_t ld, const double* __restrict__ w,
+                       double* __restrict__ out) {
+  // block j computes V_j . w
+  int j = blockIdx.x;
+  if (j >= nv) return;
+  const double* vj = V + (size_t)j * ld;
+  double s = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += vj[i] * w[i];
+  __shared__ double red[32];
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double t = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.;
+    t = warp_sum(t);
+    if (threadIdx.x == 0) out[j] = t;
+  }
+}
+__global__ void k_orth(int n, int nv, const double* __restrict__ V, size_t ld, const double* __restrict__ h,
+                       double* __restrict__ w) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = w[i];
+  for (int j = 0; j < nv; ++j) s -= h[j] * V[(size_t)j * ld + i];
+  w[i] = s;
+}
+__global__ void k_axpby(int n, double a, const double* __restrict__ x, double b, double* __restrict__ y) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = a * x[i] + b * y[i];
+}
+// Givens / Hessenberg step for column k (single thread).  H column-major with
+// leading dimension ldh = restart+1.  Writes |g_{k+1}| to res.
+__global__ void k_givens(int k, int ldh, double* H, const double* hcol, double hn, double* cs, double* sn,
+                         double* g, double* res) {
+  if (threadIdx.x || blockIdx.x) return;
+  double* c = H + (size_t)ldh * k;
+  for (int j = 0; j <= k; ++j) c[j] = hcol[j];
+  c[k + 1] = hn;
+  for (int j = 0; j < k; ++j) {
+    double a = c[j], b = c[j + 1];
+    c[j] = cs[j] * a + sn[j] * b;
+    c[j + 1] = -sn[j] * a + cs[j] * b;
+  }
+  double a = c[k], b = c[k + 1];
+  double den = sqrt(a * a + b * b);
+  cs[k] = den > 0 ? a / den : 1.;
+  sn[k] = den > 0 ? b / den : 0.;
+  c[k] = den;
+  c[k + 1] = 0.;
+  g[k + 1] = -sn[k] * g[k];
+  g[k] = cs[k] * g[k];
+  *res = fabs(g[k + 1]);
+}
+__global__ void k_backsolve(int k, int ldh, const double* H, const double* g, double* y) {
+  if (threadIdx.x || blockIdx.x) return;
+  for (int i = k - 1; i >= 0; --i) {
+    double s = g[i];
+    for (int j = i + 1; j < k; ++j) s -= H[i + (size_t)ldh * j] * y[j];
+    y[i] = s / H[i + (size_t)ldh * i];
+  }
+}
+__global__ void k_xupdate(int n, int k, const double* __restrict__ V, size_t ld, const double* __restrict__ y,
+                          double* __restrict__ x) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = x[i];
+  for (int j = 0; j < k; ++j) s += y[j] * V[(size_t)j * ld + i];
+  x[i] = s;
+}
+
+
+inline int gm_nblk(long long n, int b) { return (int)((n + b - 1) / b); }
+
+inline double dev_norm(rbc3d_ctx* ctx, int n, const double* v, double* tmp) {
+  { k_dots<<<1, 512, 0, ctx->st>>>(n, 1, v, 0, v, tmp); ++ctx->launches; }
+  double h = 0;
+  cudaMemcpyAsync(&h, tmp, sizeof(double), cudaMemcpyDeviceToHost, ctx->st);
+  cudaStreamSynchronize(ctx->st);
+  return std::sqrt(h);
+}
+
+// GMRES cycles from x (device, in/out) for A x = b (device).  On entry r must
+// hold b - A x and beta its norm; ttol is the absolute tolerance.  Counts go
+// to S (iterations, converged, rnorm; matvecs through the functor).
+template <class MV>
+rbc3d_status gmres_cycles(rbc3d_ctx* ctx, int n, MV&& matvec, const double* b, double* x, double* r, double beta,
+                          double ttol, int max_it, int R, rbc3d_solve_stats& S) {
+  const size_t ld = (size_t)n;
+  DBuf<double> V, w, H, cs, sn, g, hcol, yv, tmp;
+  CUDA_TRY(V.alloc((size_t)(R + 1) * ld)); CUDA_TRY(w.alloc(n));
+  CUDA_TRY(H.alloc((size_t)(R + 1) * R)); CUDA_TRY(cs.alloc(R)); CUDA_TRY(sn.alloc(R)); CUDA_TRY(g.alloc(R + 1));
+  CUDA_TRY(hcol.alloc(R + 1)); CUDA_TRY(yv.alloc(R)); CUDA_TRY(tmp.alloc(R + 2));
+  rbc3d_status s;
+  auto residual = [&]() -> rbc3d_status {  // r = b - A x
+    rbc3d_status e = matvec(x, w.p);
+    if (e) return e;
+    CUDA_TRY(cudaMemcpyAsync(r, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->st));
+    { k_axpby<<<gm_nblk(n, 256), 256, 0, ctx->st>>>(n, -1.0, w.p, 1.0, r); ++ctx->launches; }
+    return RBC3D_OK;
+  };
+  int its = 0;
+  bool conv = beta <= ttol;
+  while (!conv && its < max_it) {
+    { k_axpby<<<gm_nblk(n, 256), 256, 0, ctx->st>>>(n, 1.0 / beta, r, 0.0, V.p); ++ctx->launches; }
+    std::vector<double> gh(R + 1, 0.);
+    gh[0] = beta;
+    CUDA_TRY(cudaMemcpyAsync(g.p, gh.data(), sizeof(double) * (R + 1), cudaMemcpyHostToDevice, ctx->st));
+    int k;
+    for (k = 0; k < R && its < max_it; ++k) {
+      if ((s = matvec(V.p + k * ld, w.p))) return s;
+      { k_dots<<<k + 1, 512, 0, ctx->st>>>(n, k + 1, V.p, ld, w.p, hcol.p); ++ctx->launches; }
+      { k_orth<<<gm_nblk(n, 256), 256, 0, ctx->st>>>(n, k + 1, V.p, ld, hcol.p, w.p); ++ctx->launches; }
+      double hn = dev_norm(ctx, n, w.p, tmp.p);
+      if (hn > 0) { k_axpby<<<gm_nblk(n, 256), 256, 0, ctx->st>>>(n, 1.0 / hn, w.p, 0.0, V.p + (k + 1) * ld); ++ctx->launches; }
+      { k_givens<<<1, 1, 0, ctx->st>>>(k, R + 1, H.p, hcol.p, hn, cs.p, sn.p, g.p, tmp.p + R + 1); ++ctx->launches; }
+      double res = 0;
+      CUDA_TRY(cudaMemcpyAsync(&res, tmp.p + R + 1, sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+      CUDA_TRY(cudaStreamSynchronize(ctx->st));
+      ++its;
+      if (res <= ttol || hn == 0) { ++k; conv = true; break; }
+    }
+    { k_backsolve<<<1, 1, 0, ctx->st>>>(k, R + 1, H.p, g.p, yv.p); ++ctx->launches; }
+    { k_xupdate<<<gm_nblk(n, 256), 256, 0, ctx->st>>>(n, k, V.p, ld, yv.p, x); ++ctx->launches; }
+    if ((s = residual())) return s;
+    beta = dev_norm(ctx, n, r, tmp.p);
+    conv = beta <= ttol;  // the true residual decides, not the Givens estimate
+  }
+  S.iterations = its;
+  S.converged = conv ? 1 : 0;
+  S.rnorm = beta;
+  CUDA_TRY(cudaGetLastError());
+  return RBC3D_OK;
+}
+
+}  // namespace

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "ctx.hpp"
+#include "gmres.cuh"
 
 namespace {
 
@@ -348,77 +349,6 @@ __global__ void k_add_const(int n, double a0, double a1, double a2, double* v) {
   v[i] += a0; v[i + n] += a1; v[i + 2 * (size_t)n] += a2;
 }
 
-// ---- GMRES kernels (FP64)
-__global__ void k_dots(int n, int nv, const double* __restrict__ V, size_t ld, const double* __restrict__ w,
-                       double* __restrict__ out) {
-  // block j computes V_j . w
-  int j = blockIdx.x;
-  if (j >= nv) return;
-  const double* vj = V + (size_t)j * ld;
-  double s = 0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) s += vj[i] * w[i];
-  __shared__ double red[32];
-  s = warp_sum(s);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    double t = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.;
-    t = warp_sum(t);
-    if (threadIdx.x == 0) out[j] = t;
-  }
-}
-__global__ void k_orth(int n, int nv, const double* __restrict__ V, size_t ld, const double* __restrict__ h,
-                       double* __restrict__ w) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  double s = w[i];
-  for (int j = 0; j < nv; ++j) s -= h[j] * V[(size_t)j * ld + i];
-  w[i] = s;
-}
-__global__ void k_axpby(int n, double a, const double* __restrict__ x, double b, double* __restrict__ y) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) y[i] = a * x[i] + b * y[i];
-}
-// Givens / Hessenberg step for column k (single thread).  H column-major with
-// leading dimension ldh = restart+1.  Writes |g_{k+1}| to res.
-__global__ void k_givens(int k, int ldh, double* H, const double* hcol, double hn, double* cs, double* sn,
-                         double* g, double* res) {
-  if (threadIdx.x || blockIdx.x) return;
-  double* c = H + (size_t)ldh * k;
-  for (int j = 0; j <= k; ++j) c[j] = hcol[j];
-  c[k + 1] = hn;
-  for (int j = 0; j < k; ++j) {
-    double a = c[j], b = c[j + 1];
-    c[j] = cs[j] * a + sn[j] * b;
-    c[j + 1] = -sn[j] * a + cs[j] * b;
-  }
-  double a = c[k], b = c[k + 1];
-  double den = sqrt(a * a + b * b);
-  cs[k] = den > 0 ? a / den : 1.;
-  sn[k] = den > 0 ? b / den : 0.;
-  c[k] = den;
-  c[k + 1] = 0.;
-  g[k + 1] = -sn[k] * g[k];
-  g[k] = cs[k] * g[k];
-  *res = fabs(g[k + 1]);
-}
-__global__ void k_backsolve(int k, int ldh, const double* H, const double* g, double* y) {
-  if (threadIdx.x || blockIdx.x) return;
-  for (int i = k - 1; i >= 0; --i) {
-    double s = g[i];
-    for (int j = i + 1; j < k; ++j) s -= H[i + (size_t)ldh * j] * y[j];
-    y[i] = s / H[i + (size_t)ldh * i];
-  }
-}
-__global__ void k_xupdate(int n, int k, const double* __restrict__ V, size_t ld, const double* __restrict__ y,
-                          double* __restrict__ x) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  double s = x[i];
-  for (int j = 0; j < k; ++j) s += y[j] * V[(size_t)j * ld + i];
-  x[i] = s;
-}
-
 WallArgs wall_args(rbc3d_ctx* ctx) {
   WallState& W = ctx->wall;
   WallArgs a;
@@ -430,13 +360,6 @@ WallArgs wall_args(rbc3d_ctx* ctx) {
   return a;
 }
 
-double dev_norm(rbc3d_ctx* ctx, int n, const double* v, double* tmp) {
-  { k_dots<<<1, 512, 0, ctx->st>>>(n, 1, v, 0, v, tmp); ++ctx->launches; }
-  double h = 0;
-  cudaMemcpyAsync(&h, tmp, sizeof(double), cudaMemcpyDeviceToHost, ctx->st);
-  cudaStreamSynchronize(ctx->st);
-  return std::sqrt(h);
-}
 
 }  // namespace
 
@@ -613,13 +536,9 @@ rbc3d_status wall_solve(rbc3d_ctx* ctx, const rbc3d_solve_opts* o, const double*
   rbc3d_solve_stats S{};
   const int n = W.ndof, R = o->restart > 0 ? o->restart : 30;
   const int prec = o->prec;
-  const size_t ld = (size_t)n;
-  // device storage: V (R+1 vectors), b, x, r, w, f0, small arrays
-  DBuf<double> V, b, x, r, w, f0, H, cs, sn, g, hcol, yv, tmp;
-  CUDA_TRY(V.alloc((size_t)(R + 1) * ld)); CUDA_TRY(b.alloc(n)); CUDA_TRY(x.alloc(n)); CUDA_TRY(r.alloc(n));
-  CUDA_TRY(w.alloc(n)); CUDA_TRY(f0.alloc(3 * (size_t)W.nvert));
-  CUDA_TRY(H.alloc((size_t)(R + 1) * R)); CUDA_TRY(cs.alloc(R)); CUDA_TRY(sn.alloc(R)); CUDA_TRY(g.alloc(R + 1));
-  CUDA_TRY(hcol.alloc(R + 1)); CUDA_TRY(yv.alloc(R)); CUDA_TRY(tmp.alloc(R + 2));
+  DBuf<double> b, x, r, w, f0, tmp;
+  CUDA_TRY(b.alloc(n)); CUDA_TRY(x.alloc(n)); CUDA_TRY(r.alloc(n)); CUDA_TRY(w.alloc(n));
+  CUDA_TRY(f0.alloc(3 * (size_t)W.nvert)); CUDA_TRY(tmp.alloc(8));
   CUDA_TRY(cudaMemcpyAsync(f0.p, W.f.p, sizeof(double) * 3 * W.nvert, cudaMemcpyDeviceToDevice, ctx->st));
   rbc3d_status s;
   // rhs = -assemble(residual velocity)
@@ -638,14 +557,10 @@ rbc3d_status wall_solve(rbc3d_ctx* ctx, const rbc3d_solve_opts* o, const double*
     S.matvecs++;
     return wall_matmult_dev(ctx, prec, in, out);
   };
-  auto residual = [&]() -> rbc3d_status {  // r = b - A x
-    rbc3d_status e = matvec(x.p, w.p);
-    if (e) return e;
-    CUDA_TRY(cudaMemcpyAsync(r.p, b.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->st));
-    { k_axpby<<<nblk(n, 256), 256, 0, ctx->st>>>(n, -1.0, w.p, 1.0, r.p); ++ctx->launches; }
-    return RBC3D_OK;
-  };
-  if ((s = residual())) return s;
+  // r = b - A x
+  if ((s = matvec(x.p, w.p))) return s;
+  CUDA_TRY(cudaMemcpyAsync(r.p, b.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->st));
+  { k_axpby<<<nblk(n, 256), 256, 0, ctx->st>>>(n, -1.0, w.p, 1.0, r.p); ++ctx->launches; }
   if (o->guess == 2 && guess) {
     // minimum-residual scaling of the guess: x0 <- a x0, a = <b, A x0> / ||A x0||^2,
     // so that ||b - A x0|| <= ||b|| whatever the guess (w holds A x0)
@@ -684,41 +599,12 @@ rbc3d_status wall_solve(rbc3d_ctx* ctx, const rbc3d_solve_opts* o, const double*
     { k_axpby<<<nblk(n, 256), 256, 0, ctx->st>>>(n, -p, w.p, 1.0, r.p); ++ctx->launches; }
     { k_axpby<<<nblk(n, 256), 256, 0, ctx->st>>>(n, -q, w2.p, 1.0, r.p); ++ctx->launches; }
   }
-  double beta = dev_norm(ctx, n, r.p, tmp.p);
+  const double beta = dev_norm(ctx, n, r.p, tmp.p);
   S.rnorm0 = beta;
   S.bnorm = dev_norm(ctx, n, b.p, tmp.p);
   // KSPConvergedDefault: ||r|| < max(rtol * ||b||, abstol), ||b|| of the right-hand side
-  double ttol = std::max(o->rtol * S.bnorm, 1e-50);
-  int its = 0;
-  bool conv = beta <= ttol;
-  while (!conv && its < o->max_it) {
-    { k_axpby<<<nblk(n, 256), 256, 0, ctx->st>>>(n, 1.0 / beta, r.p, 0.0, V.p); ++ctx->launches; }
-    std::vector<double> gh(R + 1, 0.);
-    gh[0] = beta;
-    CUDA_TRY(cudaMemcpyAsync(g.p, gh.data(), sizeof(double) * (R + 1), cudaMemcpyHostToDevice, ctx->st));
-    int k;
-    for (k = 0; k < R && its < o->max_it; ++k) {
-      if ((s = matvec(V.p + k * ld, w.p))) return s;
-      { k_dots<<<k + 1, 512, 0, ctx->st>>>(n, k + 1, V.p, ld, w.p, hcol.p); ++ctx->launches; }
-      { k_orth<<<nblk(n, 256), 256, 0, ctx->st>>>(n, k + 1, V.p, ld, hcol.p, w.p); ++ctx->launches; }
-      double hn = dev_norm(ctx, n, w.p, tmp.p);
-      if (hn > 0) { k_axpby<<<nblk(n, 256), 256, 0, ctx->st>>>(n, 1.0 / hn, w.p, 0.0, V.p + (k + 1) * ld); ++ctx->launches; }
-      { k_givens<<<1, 1, 0, ctx->st>>>(k, R + 1, H.p, hcol.p, hn, cs.p, sn.p, g.p, tmp.p + R + 1); ++ctx->launches; }
-      double res = 0;
-      CUDA_TRY(cudaMemcpyAsync(&res, tmp.p + R + 1, sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
-      CUDA_TRY(cudaStreamSynchronize(ctx->st));
-      ++its;
-      if (res <= ttol || hn == 0) { ++k; conv = true; break; }
-    }
-    { k_backsolve<<<1, 1, 0, ctx->st>>>(k, R + 1, H.p, g.p, yv.p); ++ctx->launches; }
-    { k_xupdate<<<nblk(n, 256), 256, 0, ctx->st>>>(n, k, V.p, ld, yv.p, x.p); ++ctx->launches; }
-    if ((s = residual())) return s;
-    beta = dev_norm(ctx, n, r.p, tmp.p);
-    conv = beta <= ttol;  // the true residual decides, not the Givens estimate
-  }
-  S.iterations = its;
-  S.converged = conv ? 1 : 0;
-  S.rnorm = beta;
+  const double ttol = std::max(o->rtol * S.bnorm, 1e-50);
+  if ((s = gmres_cycles(ctx, n, matvec, b.p, x.p, r.p, beta, ttol, o->max_it, R, S))) return s;
   // wall f = f0 + expand(x)
   { k_expand<<<nblk(W.nvert, 256), 256, 0, ctx->st>>>(W.nvert, W.glb.p, x.p, W.f.p); ++ctx->launches; }
   { k_axpby<<<nblk(3 * W.nvert, 256), 256, 0, ctx->st>>>(3 * W.nvert, 1.0, f0.p, 1.0, W.f.p); ++ctx->launches; }
@@ -726,7 +612,7 @@ rbc3d_status wall_solve(rbc3d_ctx* ctx, const rbc3d_solve_opts* o, const double*
   CUDA_TRY(cudaStreamSynchronize(ctx->st));
   S.ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   if (st) *st = S;
-  return conv ? RBC3D_OK : ctx_fail(ctx, RBC3D_ERR_NOCONV, "GMRES reached max_it");
+  return S.converged ? RBC3D_OK : ctx_fail(ctx, RBC3D_ERR_NOCONV, "GMRES reached max_it");
 }
 
 // b = -AssembleArray(Compute_Wall_Residual_Vel) (ModNoSlip.F90:110-113), host copy

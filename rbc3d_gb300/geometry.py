@@ -197,12 +197,12 @@ def sh_eval(coeffs, th, phi):
 # ---------------------------------------------------------------------------
 # Splines
 def fft_diff(u, axis):
-    """FFT_Diff of ModFFT.F90:25-93 along one axis (domain mapped to 2*pi,
-    Nyquist mode zeroed)."""
+    """FFT_Diff of ModFFT.F90:25-93 along one axis (domain mapped to 2*pi):
+    modes k < n/2 times i k, mode n/2 (integer division, odd n too) zeroed."""
     n = u.shape[axis]
     U = np.fft.rfft(u, axis=axis)
     k = np.arange(n // 2 + 1, dtype=np.float64)
-    k[-1] = 0.0 if n % 2 == 0 else k[-1]
+    k[-1] = 0.0
     shape = [1] * u.ndim
     shape[axis] = k.size
     U = U * (1j * k).reshape(shape)
