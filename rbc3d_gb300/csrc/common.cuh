@@ -43,6 +43,30 @@ __device__ __forceinline__ void ewald_sl64(const Tables& T, double r, double& A,
   A = c1 * ir * ir2 + c2 * ir2;
   B = c1 * ir - c2;
 }
+// The same with 1/r supplied (from rsqrt of r^2, 1 ulp) and the table index as
+// r * (NTAB/rc): no FP64 division.
+// Callers pass r = r2 * rsqrt(r2), which is NaN for r2 = 0 (a target that is
+// its own source): !(r >= r_eps) catches it, and the index is range-checked.
+__device__ __forceinline__ void ewald_sl64r(const Tables& T, double r, double ir, double& A, double& B) {
+  if (!(r >= T.r_eps)) { A = 0.; B = 0.; return; }
+  double s = r * T.ntab_over_rc;
+  int i = (int)floor(s);
+  if (i < 0 || i >= EWALD_NTAB) { A = 0.; B = 0.; return; }
+  double c1 = __ldg(T.sl_c1 + i) * (i + 1 - s) + __ldg(T.sl_c1 + i + 1) * (s - i);
+  double c2 = __ldg(T.sl_c2 + i) * (i + 1 - s) + __ldg(T.sl_c2 + i + 1) * (s - i);
+  double ir2 = ir * ir;
+  A = c1 * ir * ir2 + c2 * ir2;
+  B = c1 * ir - c2;
+}
+__device__ __forceinline__ double ewald_dl64r(const Tables& T, double r, double ir) {
+  if (!(r >= T.r_eps)) return 0.;
+  double s = r * T.ntab_over_rc;
+  int i = (int)floor(s);
+  if (i < 0 || i >= EWALD_NTAB) return 0.;
+  double c1 = __ldg(T.dl_c1 + i) * (i + 1 - s) + __ldg(T.dl_c1 + i + 1) * (s - i);
+  double ir2 = ir * ir;
+  return c1 * (ir2 * ir2 * ir);
+}
 __device__ __forceinline__ double ewald_dl64(const Tables& T, double r) {
   if (r < T.r_eps) return 0.;
   double s = EWALD_NTAB * r / T.rc;
@@ -75,6 +99,33 @@ struct SplW {
 };
 __device__ __forceinline__ int imod(int a, int b) { int r = a % b; return r < 0 ? r + b : r; }
 
+// Spline_Create constants of the periodic (m, n) grid: h = 2 pi / m, ih = 1 / h.
+struct SplGrid {
+  int m, n;
+  double hx, hy, ihx, ihy;
+};
+inline SplGrid spl_grid(int m, int n) {
+  SplGrid g;
+  g.m = m; g.n = n;
+  g.hx = RBC3D_TWO_PI / m; g.hy = RBC3D_TWO_PI / n;
+  g.ihx = 1. / g.hx; g.ihy = 1. / g.hy;
+  return g;
+}
+// Spline_Interp weights (ModSpline.F90:150-191) with the grid constants
+// precomputed (bitwise the same values as computing them here).
+__device__ __forceinline__ void spline_weights_g(double x, double y, const SplGrid& G, SplW& W) {
+  const int m = G.m, n = G.n;
+  const double hx = G.hx, hy = G.hy, ihx = G.ihx, ihy = G.ihy;
+  int i1 = (int)floor(x * ihx), j1 = (int)floor(y * ihy);
+  double s = x * ihx - i1, t = y * ihy - j1;
+  i1 = imod(i1, m); j1 = imod(j1, n);
+  int i2 = imod(i1 + 1, m), j2 = imod(j1 + 1, n);
+  W.cx[0] = 1 + s * s * (-3. + 2. * s); W.cx[1] = s * s * (3. - 2. * s);
+  W.cx[2] = hx * s * (1. + s * (-2. + s)); W.cx[3] = hx * s * s * (-1. + s);
+  W.cy[0] = 1 + t * t * (-3. + 2. * t); W.cy[1] = t * t * (3. - 2. * t);
+  W.cy[2] = hy * t * (1. + t * (-2. + t)); W.cy[3] = hy * t * t * (-1. + t);
+  W.n11 = i1 + m * j1; W.n12 = i1 + m * j2; W.n21 = i2 + m * j1; W.n22 = i2 + m * j2;
+}
 __device__ __forceinline__ void spline_weights(double x, double y, int m, int n, SplW& W) {
   const double hx = RBC3D_TWO_PI / m, hy = RBC3D_TWO_PI / n;
   const double ihx = 1. / hx, ihy = 1. / hy;

@@ -21,6 +21,8 @@ struct CorrArgs {
   const int4* tmeta;
   double* v;
   int ncell, nlat, nlon, m;
+  SplGrid G;  // Spline_Create constants of the (2 nlat, nlon) spline grid
+  double rc2;
   const double* th;
   const double* phi;
   const double* w;
@@ -87,18 +89,19 @@ __global__ void __launch_bounds__(256) k_self(CorrArgs a) {
     double th_j = a.thG[(size_t)ilat0 * NQ + q];
     double p = a.phiA[(size_t)ilat0 * NQ + q] + phi0;  // PolarPatch_Build: atan2(...) + phi0
     double phi_j = p - floor(p * RBC3D_I_2PI) * RBC3D_TWO_PI;
-    spline_weights(th_j, phi_j, a.m, a.nlon, W);
+    spline_weights_g(th_j, phi_j, a.G, W);
     double xj[3], xx[3];
     spline_eval(sx, W, 3, xj);
     for (int k = 0; k < 3; ++k) xx[k] = xj[k] - xi[k];
-    double rr = sqrt(xx[0] * xx[0] + xx[1] * xx[1] + xx[2] * xx[2]);
-    if (rr >= a.T.rc) continue;
+    const double r2 = xx[0] * xx[0] + xx[1] * xx[1] + xx[2] * xx[2];
+    if (r2 >= a.rc2) continue;  // rr >= rc (ModRbcSingInt.F90:65)
+    const double ir = rsqrt(r2), rr = r2 > 0. ? r2 * ir : 0.;
     double wq = a.pw[irad];
     if (c1 != 0.) {
       double fj[3], EA, EB;
       spline_eval(sF, W, 3, fj);
       for (int k = 0; k < 3; ++k) fj[k] = wq * fj[k];
-      ewald_sl64(a.T, rr, EA, EB);
+      ewald_sl64r(a.T, rr, ir, EA, EB);
       double d = xx[0] * fj[0] + xx[1] * fj[1] + xx[2] * fj[2];
       for (int k = 0; k < 3; ++k) dv[k] += c1 * (EA * xx[k] * d + EB * fj[k]);
     }
@@ -107,7 +110,7 @@ __global__ void __launch_bounds__(256) k_self(CorrArgs a) {
       spline_eval(sG, W, 3, gj);
       for (int k = 0; k < 3; ++k) gj[k] = wq * gj[k];
       spline_eval(sA, W, 3, aj);
-      double EA = ewald_dl64(a.T, rr);
+      double EA = ewald_dl64r(a.T, rr, ir);
       double dg = xx[0] * gj[0] + xx[1] * gj[1] + xx[2] * gj[2];
       double da = xx[0] * aj[0] + xx[1] * aj[1] + xx[2] * aj[2];
       for (int k = 0; k < 3; ++k) dv[k] += c2m * (EA * xx[k] * dg * da);
@@ -347,17 +350,18 @@ __device__ void near_readd(const CorrArgs& a, int cell, double c1, double c2, co
     double thG, phG;
     patch_point(st0, ct0, phi0, sin(thP), cos(thP), cph, sph, thG, phG);
     SplW W;
-    spline_weights(thG, phG, a.m, a.nlon, W);
+    spline_weights_g(thG, phG, a.G, W);
     double xj[3], xx[3];
     spline_eval(sx, W, 3, xj);
     for (int k = 0; k < 3; ++k) xx[k] = xj[k] - xi[k];
-    double rr = sqrt(xx[0] * xx[0] + xx[1] * xx[1] + xx[2] * xx[2]);
-    if (rr > a.T.rc) continue;
+    const double r2 = xx[0] * xx[0] + xx[1] * xx[1] + xx[2] * xx[2];
+    if (r2 > a.rc2) continue;  // rr > rc
+    const double ir = rsqrt(r2), rr = r2 > 0. ? r2 * ir : 0.;
     if (c1 != 0.) {
       double fj[3], EA, EB;
       spline_eval(sF, W, 3, fj);
       for (int k = 0; k < 3; ++k) fj[k] = wt * fj[k];
-      ewald_sl64(a.T, rr, EA, EB);
+      ewald_sl64r(a.T, rr, ir, EA, EB);
       double dd = xx[0] * fj[0] + xx[1] * fj[1] + xx[2] * fj[2];
       for (int k = 0; k < 3; ++k) acc[k] += c1 * (EA * xx[k] * dd + EB * fj[k]);
     }
@@ -366,7 +370,7 @@ __device__ void near_readd(const CorrArgs& a, int cell, double c1, double c2, co
       spline_eval(sA, W, 3, aj);
       spline_eval(sG, W, 3, gj);
       for (int k = 0; k < 3; ++k) gj[k] = wt * gj[k];
-      double EA = ewald_dl64(a.T, rr);
+      double EA = ewald_dl64r(a.T, rr, ir);
       double dg = xx[0] * gj[0] + xx[1] * gj[1] + xx[2] * gj[2];
       double da = xx[0] * aj[0] + xx[1] * aj[1] + xx[2] * aj[2];
       for (int k = 0; k < 3; ++k) acc[k] += c2 * (EA * xx[k] * dg * da);
@@ -588,6 +592,8 @@ void fill_args(rbc3d_ctx* ctx, int tlist, double c1, double c2, CorrArgs& a, con
   TargetSet& t = ctx->tl[tlist];
   a.nt = t.n; a.tx = t.x.p; a.tA = t.Acoef.p; a.tmeta = t.meta.p; a.v = t.v.p;
   a.ncell = ctx->ncell; a.nlat = ctx->nlat; a.nlon = ctx->nlon; a.m = ctx->m;
+  a.G = spl_grid(ctx->m, ctx->nlon);
+  a.rc2 = ctx->prm.rc * ctx->prm.rc;
   a.th = ctx->th.p; a.phi = ctx->phi.p; a.w = ctx->w.p;
   a.x = ctx->x.p; a.a3 = ctx->a3.p; a.detJ = ctx->detJ.p; a.f = ctx->f.p; a.g = ctx->g.p;
   a.area = ctx->area.p; a.meshSize = ctx->meshSize.p; a.celltype = ctx->celltype.p; a.Bc = Bc;

@@ -307,12 +307,13 @@ __device__ __forceinline__ float3 f3sub(float3 a, float3 d) { return make_float3
 // a loaded tile that is out of its own targets' reach.
 template <bool DL>
 __global__ void __launch_bounds__(TILE) k_pair32(PairArgs a) {
-  __shared__ float4 s_p0[TILE], s_p1[TILE], s_f[TILE];
-  __shared__ float4 s_g[DL ? TILE : 1], s_a[DL ? TILE : 1];
-  __shared__ float3 wb[TILE / 32][2];
+  // per-warp source chunks: the warps of a unit run independently (no block barrier)
+  __shared__ float4 s_p0[TILE / 32][32], s_p1[TILE / 32][32], s_f[TILE / 32][32];
+  __shared__ float4 s_g[TILE / 32][DL ? 32 : 1], s_a[TILE / 32][DL ? 32 : 1];
   const int4 unit = a.units[blockIdx.x];
   const int cell = unit.x;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  if (wid * 32 >= unit.z) return;  // no targets for this warp
   const bool active = tid < unit.z;
   const int ci = cell % a.Nc[0], cj = (cell / a.Nc[0]) % a.Nc[1], ck = cell / (a.Nc[0] * a.Nc[1]);
   const double c0[3] = {(ci + 0.5) * a.h[0], (cj + 0.5) * a.h[1], (ck + 0.5) * a.h[2]};
@@ -330,7 +331,19 @@ __global__ void __launch_bounds__(TILE) k_pair32(PairArgs a) {
     surf_i = m.x;
     if (m.y >= 0) ui = a.usph[m.y + a.nlat * m.z];
   }
-  const CullBoxes cb = cull_boxes(active, th_[0], th_[1], th_[2], wb);
+  // this warp's target box
+  float3 wlo0, whi0;
+  {
+    const float big = 3.0e38f;
+    wlo0 = active ? make_float3(th_[0], th_[1], th_[2]) : make_float3(big, big, big);
+    whi0 = active ? make_float3(th_[0], th_[1], th_[2]) : make_float3(-big, -big, -big);
+    warp_minmax(wlo0, whi0);
+  }
+  float4* w_p0 = s_p0[wid];
+  float4* w_p1 = s_p1[wid];
+  float4* w_f = s_f[wid];
+  float4* w_g = s_g[wid];
+  float4* w_a = s_a[wid];
   Kahan3 acc;
   acc.zero();
   NbrList L;
@@ -358,95 +371,97 @@ __global__ void __launch_bounds__(TILE) k_pair32(PairArgs a) {
       two_diff(th_[1], dh.y, tsh[1], e); tsl[1] = (tl_[1] - dl.y) + e;
       two_diff(th_[2], dh.z, tsh[2], e); tsl[2] = (tl_[2] - dl.z) + e;
     }
-    const float3 wlo = f3sub(cb.wlo, dh), whi = f3sub(cb.whi, dh);
-    const float3 clo = f3sub(cb.clo, dh), chi = f3sub(cb.chi, dh);
+    const float3 wlo = f3sub(wlo0, dh), whi = f3sub(whi0, dh);
     const int t0 = a.toff[ncell];
     for (int base = sbeg, tt = t0; base < send; base += TILE, ++tt) {
       const float4 blo = a.tbox[2 * tt], bhi = a.tbox[2 * tt + 1];
       const float3 bl = make_float3(blo.x, blo.y, blo.z), bh = make_float3(bhi.x, bhi.y, bhi.z);
-      if (boxes_apart(clo, chi, bl, bh, a.rc2_f)) continue;  // uniform over the CTA
-      const int cnt = min(TILE, send - base);
-      __syncthreads();
-      if (tid < cnt) {
-        const int q = base + tid;
-        s_p0[tid] = a.sp0[q];
-        s_p1[tid] = a.sp1[q];
-        s_f[tid] = a.sF4[q];
-        if (DL) { s_g[tid] = a.sG4[q]; s_a[tid] = a.sa4[q]; }
-      }
-      __syncthreads();
-      if (!active || boxes_apart(wlo, whi, bl, bh, a.rc2_f)) continue;
-      for (int j = 0; j < cnt; ++j) {
-        const float4 p0 = s_p0[j], p1 = s_p1[j];
-        const int sj = __float_as_int(p0.w);
-        if (a.collect && sj != run_surf) {
-          if (run_id >= 0) L.insert(run_surf, run_id, run_d2);
-          run_surf = sj; run_id = -1; run_d2 = 3.4e38f;
+      if (boxes_apart(wlo, whi, bl, bh, a.rc2_f)) continue;  // uniform over the warp
+      const int tend = min(base + TILE, send);
+      for (int cb = base; cb < tend; cb += 32) {
+        const int cnt = min(32, tend - cb);
+        __syncwarp();
+        if (lane < cnt) {
+          const int q = cb + lane;
+          w_p0[lane] = a.sp0[q];
+          w_p1[lane] = a.sp1[q];
+          w_f[lane] = a.sF4[q];
+          if (DL) { w_g[lane] = a.sG4[q]; w_a[lane] = a.sa4[q]; }
         }
-        const float xx = __fadd_rn(p0.x - tsh[0], p1.x - tsl[0]);
-        const float yy = __fadd_rn(p0.y - tsh[1], p1.y - tsl[1]);
-        const float zz = __fadd_rn(p0.z - tsh[2], p1.z - tsl[2]);
-        const float r2 = xx * xx + yy * yy + zz * zz;
-        if (r2 > a.rc2_f) continue;
-        ++npairs;
-        float wgt = 1.f;
-        if (sj == surf_i) {
-          const float4 u = a.su[base + j];
-          const float ex = ui.x - u.x, ey = ui.y - u.y, ez = ui.z - u.z;
-          const float ch2 = ex * ex + ey * ey + ez * ez;
-          if (ch2 < a.chord2_max) {
-            // dth = 2 asin(chord/2); MaskFunc lerp on the reference table
-            const float t = 2.f * asinf(0.5f * sqrtf(ch2)) * a.inv_radius_f;
-            const float sx = t * (float)MASK_NTAB;
-            const int i = (int)sx;
-            if (i < MASK_NTAB) {
-              const float2 e = __ldg(a.T.mask32 + i);
-              wgt = 1.f - (e.x + (sx - (float)i) * e.y);
-            }
+        __syncwarp();
+        if (!active) continue;
+        for (int j = 0; j < cnt; ++j) {
+          const float4 p0 = w_p0[j], p1 = w_p1[j];
+          const int sj = __float_as_int(p0.w);
+          if (a.collect && sj != run_surf) {
+            if (run_id >= 0) L.insert(run_surf, run_id, run_d2);
+            run_surf = sj; run_id = -1; run_d2 = 3.4e38f;
           }
-        } else {
-          if (a.collect && r2 < run_d2) { run_d2 = r2; run_id = __float_as_int(p1.w); }
-          // A pair this close to another surface is re-evaluated in FP64 by
-          // the near-singular pass (its FP32 rounding would survive the
-          // cancellation with the FP64 subtraction).
-          if (a.collect && r2 < a.rthr2_f) continue;
+          const float xx = __fadd_rn(p0.x - tsh[0], p1.x - tsl[0]);
+          const float yy = __fadd_rn(p0.y - tsh[1], p1.y - tsl[1]);
+          const float zz = __fadd_rn(p0.z - tsh[2], p1.z - tsl[2]);
+          const float r2 = xx * xx + yy * yy + zz * zz;
+          if (r2 > a.rc2_f) continue;
+          ++npairs;
+          float wgt = 1.f;
+          if (sj == surf_i) {
+            const float4 u = a.su[cb + j];
+            const float ex = ui.x - u.x, ey = ui.y - u.y, ez = ui.z - u.z;
+            const float ch2 = ex * ex + ey * ey + ez * ez;
+            if (ch2 < a.chord2_max) {
+              // dth = 2 asin(chord/2); MaskFunc lerp on the reference table
+              const float t = 2.f * asinf(0.5f * sqrtf(ch2)) * a.inv_radius_f;
+              const float sx = t * (float)MASK_NTAB;
+              const int i = (int)sx;
+              if (i < MASK_NTAB) {
+                const float2 e = __ldg(a.T.mask32 + i);
+                wgt = 1.f - (e.x + (sx - (float)i) * e.y);
+              }
+            }
+          } else {
+            if (a.collect && r2 < run_d2) { run_d2 = r2; run_id = __float_as_int(p1.w); }
+            // A pair this close to another surface is re-evaluated in FP64 by
+            // the near-singular pass (its FP32 rounding would survive the
+            // cancellation with the FP64 subtraction).
+            if (a.collect && r2 < a.rthr2_f) continue;
+          }
+          if (r2 < a.reps2_f) continue;
+          const float rinv = rsqrtf(r2);
+          const float r = r2 * rinv;
+          // Ewald coefficients evaluated directly in FP32 rather than by
+          // per-lane gathers into the 8193-entry tables (the FP64 plain form
+          // keeps the tables)
+          const float st = r * a.sqpa_f;  // r*sqrt(pi/alpha)
+          const float ex = expf(-st * st);
+          // erfc(st) = exp(-st^2) t Q(t), t = 1/(1 + st/2) (fit_erfcx)
+          const float tq = __frcp_rn(fmaf(0.5f, st, 1.f));
+          float Q = a.erfcx_q[ERFCX_DEG];
+  #pragma unroll
+          for (int k = ERFCX_DEG - 1; k >= 0; --k) Q = fmaf(Q, tq, a.erfcx_q[k]);
+          const float c1 = ex * (tq * Q), c2 = a.two_isqa_f * ex;
+          const float ir2 = rinv * rinv;
+          const float A = (c1 * rinv + c2) * ir2;
+          const float B = c1 * rinv - c2;
+          const float4 f = w_f[j];
+          const float Ad = A * (xx * f.x + yy * f.y + zz * f.z);
+          float vx = Ad * xx + B * f.x;
+          float vy = Ad * yy + B * f.y;
+          float vz = Ad * zz + B * f.z;
+          if (DL) {
+            // -8/sqrt(pi) [exp(-t^2)(1.5 t + t^3) + 0.75 sqrt(pi) erfc(t)] / r^5
+            const float cdl = a.m8_ispi_f * (ex * (st * (1.5f + st * st)) + a.q75_spi_f * c1);
+            const float Adl = cdl * ir2 * ir2 * rinv;
+            const float4 g = w_g[j], an = w_a[j];
+            const float t = Adl * (xx * g.x + yy * g.y + zz * g.z) * (xx * an.x + yy * an.y + zz * an.z);
+            vx += t * xx; vy += t * yy; vz += t * zz;
+          }
+          acc.add(0, wgt * vx);
+          acc.add(1, wgt * vy);
+          acc.add(2, wgt * vz);
         }
-        if (r2 < a.reps2_f) continue;
-        const float rinv = rsqrtf(r2);
-        const float r = r2 * rinv;
-        // Ewald coefficients evaluated directly in FP32 rather than by
-        // per-lane gathers into the 8193-entry tables (the FP64 plain form
-        // keeps the tables)
-        const float st = r * a.sqpa_f;  // r*sqrt(pi/alpha)
-        const float ex = expf(-st * st);
-        // erfc(st) = exp(-st^2) t Q(t), t = 1/(1 + st/2) (fit_erfcx)
-        const float tq = __frcp_rn(fmaf(0.5f, st, 1.f));
-        float Q = a.erfcx_q[ERFCX_DEG];
-#pragma unroll
-        for (int k = ERFCX_DEG - 1; k >= 0; --k) Q = fmaf(Q, tq, a.erfcx_q[k]);
-        const float c1 = ex * (tq * Q), c2 = a.two_isqa_f * ex;
-        const float ir2 = rinv * rinv;
-        const float A = (c1 * rinv + c2) * ir2;
-        const float B = c1 * rinv - c2;
-        const float4 f = s_f[j];
-        const float Ad = A * (xx * f.x + yy * f.y + zz * f.z);
-        float vx = Ad * xx + B * f.x;
-        float vy = Ad * yy + B * f.y;
-        float vz = Ad * zz + B * f.z;
-        if (DL) {
-          // -8/sqrt(pi) [exp(-t^2)(1.5 t + t^3) + 0.75 sqrt(pi) erfc(t)] / r^5
-          const float cdl = a.m8_ispi_f * (ex * (st * (1.5f + st * st)) + a.q75_spi_f * c1);
-          const float Adl = cdl * ir2 * ir2 * rinv;
-          const float4 g = s_g[j], an = s_a[j];
-          const float t = Adl * (xx * g.x + yy * g.y + zz * g.z) * (xx * an.x + yy * an.y + zz * an.z);
-          vx += t * xx; vy += t * yy; vz += t * zz;
-        }
-        acc.add(0, wgt * vx);
-        acc.add(1, wgt * vy);
-        acc.add(2, wgt * vz);
+        if (a.collect && run_id >= 0) { L.insert(run_surf, run_id, run_d2); }
+        run_surf = -3; run_id = -1; run_d2 = 3.4e38f;
       }
-      if (a.collect && run_id >= 0) { L.insert(run_surf, run_id, run_d2); }
-      run_surf = -3; run_id = -1; run_d2 = 3.4e38f;
     }
   }
   if (active) {
@@ -533,7 +548,7 @@ __global__ void __launch_bounds__(TILE) k_pair64(PairArgs a) {
           double xx = sm.x[j] - t_[0], yy = sm.y[j] - t_[1], zz = sm.z[j] - t_[2];
           const double r2 = xx * xx + yy * yy + zz * zz;
           if (r2 > a.rc2) continue;  // the square root only for pairs inside the cutoff
-          double rr = sqrt(r2);
+          const double ir = rsqrt(r2), rr = r2 > 0. ? r2 * ir : 0.;
           ++npairs;
           double mask = 0.;
           if (sj == surf_i) {
@@ -543,14 +558,14 @@ __global__ void __launch_bounds__(TILE) k_pair64(PairArgs a) {
             if (rr < run_d) { run_d = rr; run_id = sm.ilat[j] | (sm.ilon[j] << 16); }
           }
           double EA, EB;
-          ewald_sl64(a.T, rr, EA, EB);
+          ewald_sl64r(a.T, rr, ir, EA, EB);
           double s1 = (1. - mask) * a.c1;
           double d = xx * sm.fx[j] + yy * sm.fy[j] + zz * sm.fz[j];
           acc[0] += s1 * (EA * xx * d + EB * sm.fx[j]);
           acc[1] += s1 * (EA * yy * d + EB * sm.fy[j]);
           acc[2] += s1 * (EA * zz * d + EB * sm.fz[j]);
           if (DL) {
-            double EAd = ewald_dl64(a.T, rr);
+            double EAd = ewald_dl64r(a.T, rr, ir);
             double dg = xx * sm.gx[j] + yy * sm.gy[j] + zz * sm.gz[j];
             double da = xx * sm.ax[j] + yy * sm.ay[j] + zz * sm.az[j];
             double s2 = (1. - mask) * a.c2;
