@@ -3,11 +3,10 @@
 //
 // Layers: nin -> width (SiLU) -> ... -> width (SiLU) -> nout, "depth" hidden
 // layers.  GEMM operands are BF16 (inputs, activations, weights, gradients),
-// products accumulate in FP32 on the tensor cores through
-// mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32; master weights, Adam
-// moments and the loss are FP32.  One tiled GEMM kernel (64x64x32 tiles, four
-// warps of 32x32, operands staged in shared memory with generic strides so the
-// same kernel serves x W^T, dz^T a and dz W) plus small element-wise kernels.
+// products accumulate in FP32 in tensor memory through tcgen05.mma (k_umma);
+// master weights, Adam moments and the loss are FP32.  One GEMM kernel
+// (operands gathered with generic strides, so it serves x W^T, dz^T a and
+// dz W) plus small element-wise kernels.
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -21,7 +20,6 @@ namespace {
 
 inline int nblk(long long n, int b) { return (int)((n + b - 1) / b); }
 
-constexpr int BM = 64, BN = 64, BK = 32, PADK = BK + 8;
 
 struct GemmArgs {
   int M, N, K;
@@ -35,85 +33,179 @@ struct GemmArgs {
   __nv_bfloat16* Abf;      // EPI 1: SiLU(z) in BF16, row-major ldc
 };
 
-__device__ __forceinline__ unsigned pack2(const __nv_bfloat16* p) { return *reinterpret_cast<const unsigned*>(p); }
+__device__ __forceinline__ float silu(float z) { return z / (1.f + expf(-z)); }
 
-__device__ __forceinline__ void mma_bf16(float* c, const unsigned* a, const unsigned* b) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+// ---------------------------------------------------------------------------
+// tcgen05 GEMM: 128 x 128 output tile per CTA, K staged 64 at a time into a
+// double-buffered shared-memory ring in the canonical no-swizzle K-major
+// layout (8-row x 16-byte core matrices: element (r, k) at byte
+// ((r/8)*8 + k/8)*128 + (r%8)*16 + (k%8)*2, so core matrices adjacent in K are
+// 128 B apart and 8-row groups 1024 B apart), one elected thread issuing
+// tcgen05.mma.cta_group::1.kind::f16 (M 128, N 128, K 16, BF16 in, FP32
+// accumulate in 128 TMEM columns) and committing each stage to an mbarrier;
+// the four warps read their 32 accumulator rows back with tcgen05.ld and run
+// the epilogue.  Operands are gathered with generic strides (16-byte vectors
+// when k or m is contiguous), so one kernel serves x W^T, dz^T a and dz W.
+constexpr int UBM = 128, UBN = 128, UBK = 64;
+constexpr int USTAGE = UBM * UBK * 2;  // bytes per operand per stage (16 KB)
+constexpr unsigned UMMA_IDESC = (1u << 4)              // D: FP32
+                                | (1u << 7)            // A: BF16
+                                | (1u << 10)           // B: BF16
+                                | ((UBN >> 3) << 17)   // N / 8
+                                | ((UBM >> 4) << 24);  // M / 16  (A, B K-major)
+constexpr long long UMMA_WAIT_LIMIT = 1ll << 26;       // bounded mbarrier waits
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: start >> 4, LBO >> 4 (K-adjacent core
+// matrices), SBO >> 4 (8-row groups), version 1, no swizzle
+__device__ __forceinline__ unsigned long long umma_desc(unsigned addr) {
+  return (unsigned long long)((addr >> 4) & 0x3FFF) | ((unsigned long long)(128 >> 4) << 16) |
+         ((unsigned long long)(1024 >> 4) << 32) | (1ull << 46);
 }
 
-__device__ __forceinline__ float silu(float z) { return z / (1.f + expf(-z)); }
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+  for (long long it = 0; it < UMMA_WAIT_LIMIT; ++it) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// stage rows [r0, r0+128) x k [k0, k0+64) of X (element (r, k) at X[r*sr + k*sk],
+// zero outside rows x K) into the core-matrix layout at dst
+__device__ __forceinline__ void umma_stage(unsigned char* dst, const __nv_bfloat16* X, long long sr, long long sk,
+                                           int rows, int K, int r0, int k0) {
+  const int tid = threadIdx.x;
+  const __nv_bfloat16 zero = __float2bfloat16(0.f);
+  if (sk == 1 && (sr % 8) == 0 && ((reinterpret_cast<size_t>(X) & 15) == 0)) {
+    // k contiguous: one 16-byte vector = one core-matrix row
+    for (int e = tid; e < UBM * (UBK / 8); e += blockDim.x) {
+      const int r = e / (UBK / 8), k8 = e % (UBK / 8);
+      const int gr = r0 + r, gk = k0 + 8 * k8;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (gr < rows && gk + 8 <= K) v = *reinterpret_cast<const uint4*>(X + (long long)gr * sr + gk);
+      else if (gr < rows)
+        for (int q = 0; q < 8; ++q)
+          reinterpret_cast<__nv_bfloat16*>(&v)[q] = gk + q < K ? X[(long long)gr * sr + gk + q] : zero;
+      *reinterpret_cast<uint4*>(dst + ((r >> 3) * 8 + k8) * 128 + (r & 7) * 16) = v;
+    }
+  } else if (sr == 1 && (sk % 8) == 0 && ((reinterpret_cast<size_t>(X) & 15) == 0)) {
+    // rows contiguous: 8 consecutive rows of one k per vector, transposed into place
+    for (int e = tid; e < (UBM / 8) * UBK; e += blockDim.x) {
+      const int r8 = e % (UBM / 8), k = e / (UBM / 8);
+      const int gr = r0 + 8 * r8, gk = k0 + k;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (gk < K && gr + 8 <= rows) v = *reinterpret_cast<const uint4*>(X + gr + (long long)gk * sk);
+      else if (gk < K)
+        for (int q = 0; q < 8; ++q)
+          reinterpret_cast<__nv_bfloat16*>(&v)[q] = gr + q < rows ? X[gr + q + (long long)gk * sk] : zero;
+      const __nv_bfloat16* h = reinterpret_cast<const __nv_bfloat16*>(&v);
+      unsigned char* base = dst + (r8 * 8 + (k >> 3)) * 128 + (k & 7) * 2;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) *reinterpret_cast<__nv_bfloat16*>(base + q * 16) = h[q];
+    }
+  } else {
+    for (int e = tid; e < UBM * UBK; e += blockDim.x) {
+      const int r = e / UBK, k = e % UBK;
+      const int gr = r0 + r, gk = k0 + k;
+      const __nv_bfloat16 v = (gr < rows && gk < K) ? X[(long long)gr * sr + (long long)gk * sk] : zero;
+      *reinterpret_cast<__nv_bfloat16*>(dst + ((r >> 3) * 8 + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2) = v;
+    }
+  }
+}
 
 // EPI 0: C = A B;  EPI 1: z = A B + bias -> C, SiLU(z) -> Abf;  EPI 2: C = A B + bias
 template <int EPI>
-__global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
-  __shared__ __align__(16) __nv_bfloat16 As[BM][PADK];
-  __shared__ __align__(16) __nv_bfloat16 Bs[BN][PADK];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int wm = warp >> 1, wn = warp & 1;
-  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-  const int gq = lane >> 2, tq = lane & 3;
-  float acc[2][4][4];
-#pragma unroll
-  for (int i = 0; i < 2; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-      for (int k = 0; k < 4; ++k) acc[i][j][k] = 0.f;
-  const __nv_bfloat16 zero = __float2bfloat16(0.f);
-  for (int k0 = 0; k0 < g.K; k0 += BK) {
-    // stage A (BM x BK) and B^T (BN x BK), k contiguous in shared memory
-    for (int e = tid; e < BM * BK; e += 128) {
-      int r = e / BK, kk = e % BK;
-      int m = m0 + r, k = k0 + kk;
-      As[r][kk] = (m < g.M && k < g.K) ? g.A[(long long)m * g.sam + (long long)k * g.sak] : zero;
-      int n = n0 + r;
-      Bs[r][kk] = (n < g.N && k < g.K) ? g.B[(long long)k * g.sbk + (long long)n * g.sbn] : zero;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int ks = 0; ks < BK; ks += 16) {
-      unsigned af[2][4], bf[4][2];
-#pragma unroll
-      for (int mt = 0; mt < 2; ++mt) {
-        int r = wm * 32 + mt * 16 + gq;
-        af[mt][0] = pack2(&As[r][ks + 2 * tq]);
-        af[mt][1] = pack2(&As[r + 8][ks + 2 * tq]);
-        af[mt][2] = pack2(&As[r][ks + 2 * tq + 8]);
-        af[mt][3] = pack2(&As[r + 8][ks + 2 * tq + 8]);
-      }
-#pragma unroll
-      for (int nt = 0; nt < 4; ++nt) {
-        int c = wn * 32 + nt * 8 + gq;
-        bf[nt][0] = pack2(&Bs[c][ks + 2 * tq]);
-        bf[nt][1] = pack2(&Bs[c][ks + 2 * tq + 8]);
-      }
-#pragma unroll
-      for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-        for (int nt = 0; nt < 4; ++nt) mma_bf16(acc[mt][nt], af[mt], bf[nt]);
-    }
-    __syncthreads();
+__global__ void __launch_bounds__(128) k_umma(GemmArgs g, int* err) {
+  extern __shared__ __align__(1024) unsigned char usm[];
+  unsigned char* As = usm;                 // 2 stages
+  unsigned char* Bs = usm + 2 * USTAGE;    // 2 stages
+  __shared__ __align__(8) unsigned long long mbar[2];
+  __shared__ unsigned tmem_slot;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int m0 = blockIdx.y * UBM, n0 = blockIdx.x * UBN;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(UBN));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
   }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[0])));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[1])));
+    asm volatile("fence.mbarrier_init.release.cluster;\n");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n");
+  const unsigned taddr = tmem_slot;
+  const int nk = (g.K + UBK - 1) / UBK;
+  bool ok = true;
+  for (int kc = 0; kc < nk; ++kc) {
+    const int buf = kc & 1;
+    // the stage's previous MMAs (chunk kc - 2) must be done before it is overwritten
+    if (kc >= 2 && !mbar_wait(smem_u32(&mbar[buf]), ((kc - 2) >> 1) & 1)) ok = false;
+    // A: rows m (sam), k (sak);  B as [n][k]: rows n (sbn), k (sbk)
+    umma_stage(As + buf * USTAGE, g.A, g.sam, g.sak, g.M, g.K, m0, kc * UBK);
+    umma_stage(Bs + buf * USTAGE, g.B, g.sbn, g.sbk, g.N, g.K, n0, kc * UBK);
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;\n");
+      const unsigned a0 = smem_u32(As + buf * USTAGE), b0 = smem_u32(Bs + buf * USTAGE);
 #pragma unroll
-  for (int mt = 0; mt < 2; ++mt)
+      for (int j = 0; j < UBK / 16; ++j) {
+        const unsigned long long da = umma_desc(a0 + j * 256), db = umma_desc(b0 + j * 256);
+        const unsigned acc = (kc > 0 || j > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(taddr),
+            "l"(da), "l"(db), "r"(UMMA_IDESC), "r"(acc));
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+          smem_u32(&mbar[buf])));
+    }
+  }
+  // all MMAs done: the last commit tracks every earlier MMA of the thread
+  if (nk > 0 && !mbar_wait(smem_u32(&mbar[(nk - 1) & 1]), ((nk - 1) >> 1) & 1)) ok = false;
+  asm volatile("tcgen05.fence::after_thread_sync;\n");
+  if (!ok) {
+    if (tid == 0) atomicExch(err, 1);
+  } else {
+    const int row = m0 + warp * 32 + (tid & 31);
+#pragma unroll 1
+    for (int c0 = 0; c0 < UBN; c0 += 32) {
+      unsigned r[32];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+          "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+            "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+            "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+          : "r"(taddr + ((unsigned)(warp * 32) << 16) + (unsigned)c0));
+      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+      if (row < g.M) {
 #pragma unroll
-    for (int nt = 0; nt < 4; ++nt)
-#pragma unroll
-      for (int h = 0; h < 2; ++h)
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-          int m = m0 + wm * 32 + mt * 16 + gq + 8 * h;
-          int n = n0 + wn * 32 + nt * 8 + 2 * tq + q;
-          if (m >= g.M || n >= g.N) continue;
-          float v = acc[mt][nt][2 * h + q];
+        for (int q = 0; q < 32; ++q) {
+          const int n = n0 + c0 + q;
+          if (n >= g.N) break;
+          float v = __uint_as_float(r[q]);
           if (EPI != 0) v += g.bias[n];
-          g.C[(long long)m * g.ldc + n] = v;
-          if (EPI == 1) g.Abf[(long long)m * g.ldc + n] = __float2bfloat16(silu(v));
+          g.C[(long long)row * g.ldc + n] = v;
+          if (EPI == 1) g.Abf[(long long)row * g.ldc + n] = __float2bfloat16(silu(v));
         }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(UBN));
 }
 
 __global__ void k_to_bf16(long long n, const float* __restrict__ x, __nv_bfloat16* __restrict__ y) {
@@ -186,6 +278,7 @@ struct rbc3d_mlp {
   long long step = 0;
   cudaStream_t st = nullptr;
   long long launches = 0;
+  DBuf<int> err;  // set by a GEMM whose mbarrier wait ran out
 };
 
 namespace {
@@ -210,11 +303,27 @@ void gemm(rbc3d_mlp* m, int epi, int M, int N, int K, const __nv_bfloat16* A, lo
           const __nv_bfloat16* B, long long sbk, long long sbn, float* C, int ldc, const float* bias,
           __nv_bfloat16* Abf) {
   GemmArgs g{M, N, K, A, sam, sak, B, sbk, sbn, C, ldc, bias, Abf};
-  dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
-  if (epi == 0) k_gemm<0><<<grid, 128, 0, m->st>>>(g);
-  else if (epi == 1) k_gemm<1><<<grid, 128, 0, m->st>>>(g);
-  else k_gemm<2><<<grid, 128, 0, m->st>>>(g);
+  dim3 grid((N + UBN - 1) / UBN, (M + UBM - 1) / UBM);
+  const int smem = 4 * USTAGE;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_umma<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_umma<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_umma<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    attr = true;
+  }
+  if (epi == 0) k_umma<0><<<grid, 128, smem, m->st>>>(g, m->err.p);
+  else if (epi == 1) k_umma<1><<<grid, 128, smem, m->st>>>(g, m->err.p);
+  else k_umma<2><<<grid, 128, smem, m->st>>>(g, m->err.p);
   ++m->launches;
+}
+
+// a GEMM whose mbarrier wait ran out left err set (read after a synchronisation)
+rbc3d_status gemm_status(rbc3d_mlp* m) {
+  int e = 0;
+  if (cudaMemcpyAsync(&e, m->err.p, sizeof(int), cudaMemcpyDeviceToHost, m->st) || cudaStreamSynchronize(m->st))
+    return RBC3D_ERR_CUDA;
+  return e ? RBC3D_ERR_TIMEOUT : RBC3D_OK;
 }
 
 // forward pass on n rows already in m->X; output in m->Y
@@ -285,10 +394,11 @@ rbc3d_status rbc3d_mlp_create(int nin, int width, int depth, int nout, unsigned 
     for (size_t i = 0; i < (size_t)m->din[l] * m->dout[l]; ++i) h[m->woff[l] + i] = U(rng);
   }
   if (cudaStreamCreateWithFlags(&m->st, cudaStreamNonBlocking) || m->P.upload(h.data(), off, m->st) ||
-      m->G.alloc(off) || m->Mo.alloc(off) || m->Vo.alloc(off) || m->Wb.alloc(off)) {
+      m->G.alloc(off) || m->Mo.alloc(off) || m->Vo.alloc(off) || m->Wb.alloc(off) || m->err.alloc(1)) {
     delete m;
     return RBC3D_ERR_CUDA;
   }
+  cudaMemsetAsync(m->err.p, 0, sizeof(int), m->st);
   cudaMemsetAsync(m->Mo.p, 0, off * sizeof(float), m->st);
   cudaMemsetAsync(m->Vo.p, 0, off * sizeof(float), m->st);
   { k_to_bf16<<<nblk(off, 256), 256, 0, m->st>>>(off, m->P.p, m->Wb.p); ++m->launches; }
@@ -329,7 +439,7 @@ rbc3d_status rbc3d_mlp_forward(rbc3d_mlp* m, int n, const float* x, float* y) {
   rbc3d_status s = mlp_fwd(m, n);
   if (s) return s;
   if (cudaMemcpyAsync(y, m->Y.p, sizeof(float) * n * m->nout, cudaMemcpyDeviceToHost, m->st)) return RBC3D_ERR_CUDA;
-  return cudaStreamSynchronize(m->st) ? RBC3D_ERR_CUDA : RBC3D_OK;
+  return gemm_status(m);
 }
 
 // Loss (mean squared error) and packed FP32 gradients (for checks).
@@ -342,6 +452,7 @@ rbc3d_status rbc3d_mlp_gradients(rbc3d_mlp* m, int n, const float* x, const floa
   rbc3d_status s = mlp_fwd(m, n);
   if (s) return s;
   if ((s = mlp_bwd(m, n, loss))) return s;
+  if ((s = gemm_status(m))) return s;
   if (grads && cudaMemcpy(grads, m->G.p, m->nparam * sizeof(float), cudaMemcpyDeviceToHost)) return RBC3D_ERR_CUDA;
   return RBC3D_OK;
 }

@@ -96,7 +96,7 @@ def run(ncell=64, warm_steps=30, test_steps=10, rtol=1e-8, restart=100, max_it=8
     res["train_ms_per_step"] = float(np.mean(train_ms))
     res["speedup_learned_incl_training"] = res["plain"]["ms"] / (res["learned"]["ms"] + res["train_ms_per_step"])
     res["final_loss"] = float(losses[-1]) if losses else None
-    res["mlp"] = {"layers": f"{guess.mlp.dims[0]} -> {width} x {depth} (SiLU) -> 3", "weights": "bf16",
+    res["mlp"] = {"layers": f"{guess.mlp.dims[0]} -> {width} x {depth} (SiLU) -> 3", "weights": "bf16 (tcgen05.mma kind::f16)",
                   "accumulation": "fp32", "params": int(guess.mlp.nparam)}
     guess.mlp.close()
     ctx.close()
