@@ -191,14 +191,35 @@ __global__ void __launch_bounds__(128) k_umma(GemmArgs g, int* err) {
           : "r"(taddr + ((unsigned)(warp * 32) << 16) + (unsigned)c0));
       asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
       if (row < g.M) {
+        float v[32];
 #pragma unroll
-        for (int q = 0; q < 32; ++q) {
-          const int n = n0 + c0 + q;
-          if (n >= g.N) break;
-          float v = __uint_as_float(r[q]);
-          if (EPI != 0) v += g.bias[n];
-          g.C[(long long)row * g.ldc + n] = v;
-          if (EPI == 1) g.Abf[(long long)row * g.ldc + n] = __float2bfloat16(silu(v));
+        for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]) + ((EPI != 0 && n0 + c0 + q < g.N) ? g.bias[n0 + c0 + q] : 0.f);
+        float* crow = g.C + (long long)row * g.ldc + n0 + c0;
+        const bool vec = n0 + c0 + 32 <= g.N && (g.ldc % 8) == 0 && ((reinterpret_cast<size_t>(crow) & 15) == 0) &&
+                         (EPI != 1 || ((reinterpret_cast<size_t>(g.Abf + (long long)row * g.ldc + n0 + c0) & 15) == 0));
+        if (vec) {
+          // a row segment of 32: 8 float4 (and 4 x 8 bf16) stores
+#pragma unroll
+          for (int q = 0; q < 8; ++q)
+            reinterpret_cast<float4*>(crow)[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+          if (EPI == 1) {
+            __nv_bfloat16* arow = g.Abf + (long long)row * g.ldc + n0 + c0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              __nv_bfloat16 h[8];
+#pragma unroll
+              for (int e = 0; e < 8; ++e) h[e] = __float2bfloat16(silu(v[8 * q + e]));
+              reinterpret_cast<uint4*>(arow)[q] = *reinterpret_cast<const uint4*>(h);
+            }
+          }
+        } else {
+#pragma unroll
+          for (int q = 0; q < 32; ++q) {
+            const int n = n0 + c0 + q;
+            if (n >= g.N) break;
+            crow[q] = v[q];
+            if (EPI == 1) g.Abf[(long long)row * g.ldc + n] = __float2bfloat16(silu(v[q]));
+          }
         }
       }
     }
@@ -237,13 +258,36 @@ __global__ void k_silu_back(long long n, const float* __restrict__ da, const flo
   dzb[i] = __float2bfloat16(da[i] * s * (1.f + z[i] * (1.f - s)));
 }
 
-// column sums of a row-major rows x cols matrix (bias gradient)
+// column sums of a row-major rows x cols matrix (bias gradient): 32 columns
+// per block, its 8 warps over the rows, a shared-memory reduction
 __global__ void k_colsum(int rows, int cols, const __nv_bfloat16* __restrict__ dz, float* __restrict__ out) {
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= cols) return;
+  __shared__ float part[8][32];
+  const int c = blockIdx.x * 32 + (threadIdx.x & 31), w = threadIdx.x >> 5;
   float s = 0.f;
-  for (int r = 0; r < rows; ++r) s += __bfloat162float(dz[(long long)r * cols + c]);
-  out[c] = s;
+  if (c < cols)
+    for (int r = w; r < rows; r += 8) s += __bfloat162float(dz[(long long)r * cols + c]);
+  part[w][threadIdx.x & 31] = s;
+  __syncthreads();
+  if (w == 0 && c < cols) {
+    float t = 0.f;
+    for (int k = 0; k < 8; ++k) t += part[k][threadIdx.x & 31];
+    out[c] = t;
+  }
+}
+
+// out[c][r] = in[r][c] for a row-major rows x cols BF16 matrix (32 x 32 tiles)
+__global__ void k_transpose(int rows, int cols, const __nv_bfloat16* __restrict__ in, __nv_bfloat16* __restrict__ out) {
+  __shared__ __nv_bfloat16 t[32][33];
+  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const int r = r0 + i, c = c0 + threadIdx.x;
+    if (r < rows && c < cols) t[i][threadIdx.x] = in[(long long)r * cols + c];
+  }
+  __syncthreads();
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const int c = c0 + i, r = r0 + threadIdx.x;
+    if (r < rows && c < cols) out[(long long)c * rows + r] = t[threadIdx.x][i];
+  }
 }
 
 __global__ void k_adam(long long n, float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
@@ -275,6 +319,7 @@ struct rbc3d_mlp {
   std::vector<DBuf<__nv_bfloat16>> A;  // layer inputs (bf16), A[0] = x
   DBuf<float> X, T, Y, DY, DA, loss;
   DBuf<__nv_bfloat16> DZ, DZ2;
+  DBuf<__nv_bfloat16> TA, TB;       // transposed GEMM operands of the backward pass
   long long step = 0;
   cudaStream_t st = nullptr;
   long long launches = 0;
@@ -294,7 +339,8 @@ rbc3d_status mlp_ensure(rbc3d_mlp* m, int n) {
   int wmax = std::max(m->width, std::max(m->nin, m->nout));
   if (m->X.alloc((size_t)n * m->nin) || m->T.alloc((size_t)n * m->nout) || m->Y.alloc((size_t)n * m->nout) ||
       m->DY.alloc((size_t)n * m->nout) || m->DA.alloc((size_t)n * wmax) || m->DZ.alloc((size_t)n * wmax) ||
-      m->DZ2.alloc((size_t)n * wmax) || m->loss.alloc(1))
+      m->DZ2.alloc((size_t)n * wmax) || m->loss.alloc(1) || m->TA.alloc((size_t)n * wmax) ||
+      m->TB.alloc((size_t)std::max((size_t)n * wmax, (size_t)wmax * wmax)))
     return RBC3D_ERR_NOMEM;
   return RBC3D_OK;
 }
@@ -315,6 +361,12 @@ void gemm(rbc3d_mlp* m, int epi, int M, int N, int K, const __nv_bfloat16* A, lo
   if (epi == 0) k_umma<0><<<grid, 128, smem, m->st>>>(g, m->err.p);
   else if (epi == 1) k_umma<1><<<grid, 128, smem, m->st>>>(g, m->err.p);
   else k_umma<2><<<grid, 128, smem, m->st>>>(g, m->err.p);
+  ++m->launches;
+}
+
+void transpose(rbc3d_mlp* m, int rows, int cols, const __nv_bfloat16* in, __nv_bfloat16* out) {
+  dim3 grid((cols + 31) / 32, (rows + 31) / 32), block(32, 8);
+  k_transpose<<<grid, block, 0, m->st>>>(rows, cols, in, out);
   ++m->launches;
 }
 
@@ -349,13 +401,16 @@ rbc3d_status mlp_bwd(rbc3d_mlp* m, int n, float* loss_out) {
   __nv_bfloat16* dzn = m->DZ2.p;
   for (int l = m->nl - 1; l >= 0; --l) {
     int di = m->din[l], dd = m->dout[l];
-    // dW[dd, di] = dz^T[dd, n] a[n, di]
-    gemm(m, 0, dd, di, n, dz, 1, dd, m->A[l].p, di, 1, m->G.p + m->woff[l], di, nullptr, nullptr);
-    { k_colsum<<<nblk(dd, 128), 128, 0, m->st>>>(n, dd, dz, m->G.p + m->boff[l]); ++m->launches; }
+    // dW[dd, di] = dz^T[dd, n] a[n, di], from K-major copies dz^T [dd][n] and a^T [di][n]
+    transpose(m, n, dd, dz, m->TA.p);
+    transpose(m, n, di, m->A[l].p, m->TB.p);
+    gemm(m, 0, dd, di, n, m->TA.p, n, 1, m->TB.p, 1, n, m->G.p + m->woff[l], di, nullptr, nullptr);
+    { k_colsum<<<nblk(dd, 32), 256, 0, m->st>>>(n, dd, dz, m->G.p + m->boff[l]); ++m->launches; }
     if (l == 0) break;
-    // da[n, di] = dz[n, dd] W[dd, di]
+    // da[n, di] = dz[n, dd] W[dd, di], from W^T [di][dd]
     const __nv_bfloat16* W = m->Wb.p + m->woff[l];
-    gemm(m, 0, n, di, dd, dz, dd, 1, W, di, 1, m->DA.p, di, nullptr, nullptr);
+    transpose(m, dd, di, W, m->TB.p);
+    gemm(m, 0, n, di, dd, dz, dd, 1, m->TB.p, 1, dd, m->DA.p, di, nullptr, nullptr);
     long long na = (long long)n * di;
     { k_silu_back<<<nblk(na, 256), 256, 0, m->st>>>(na, m->DA.p, m->Z[l - 1].p, dzn); ++m->launches; }
     std::swap(dz, dzn);
