@@ -397,7 +397,7 @@ def main():
                     "ms_per_step": te * 1e3},
             "stages_ms_per_step": st_ms,
             "counts": {k: counts[k] for k in ("pairs_within_rc", "nbr_items", "nearsing_items", "self_items",
-                                              "screen_misses")},
+                                              "screen_misses", "near_replays", "near_projections")},
             "roofline": roof,
             "wall_gmres": wall,
             "fma_peaks_tflops": {"fp32": peak32, "fp64": peak64},

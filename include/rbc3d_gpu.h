@@ -98,6 +98,8 @@ typedef struct rbc3d_counts {
   long long kernel_launches;  /* kernels of this library launched so far on the context */
   long long screen_misses;    /* FP32C near-singular screen: screened items the FP64
                                  test would correct (counted with RBC3D_VERIFY_SCREEN=1) */
+  long long near_replays;     /* FP32 modes: candidates given the FP32 projection replay */
+  long long near_projections; /* candidates given the FP64 projection */
 } rbc3d_counts;
 
 typedef struct rbc3d_solve_opts {

@@ -32,7 +32,8 @@ class Counts(C.Structure):
                 ("nearsing_items", C.c_longlong), ("self_items", C.c_longlong),
                 ("wall_pairs", C.c_longlong), ("wall_duffy", C.c_longlong),
                 ("nbr_overflow", C.c_int), ("kernel_launches", C.c_longlong),
-                ("screen_misses", C.c_longlong)]
+                ("screen_misses", C.c_longlong), ("near_replays", C.c_longlong),
+                ("near_projections", C.c_longlong)]
 
 
 class SolveOpts(C.Structure):

@@ -185,6 +185,7 @@ rbc3d_status rbcs_dev(rbc3d_ctx* ctx, int which, double c1, double c2, int prec,
   if (corr) {
     CUDA_TRY(cudaMemsetAsync(ctx->dcnt.p + 3, 0, sizeof(unsigned long long), ctx->st));
     CUDA_TRY(cudaMemsetAsync(ctx->dcnt.p + 6, 0, sizeof(unsigned long long), ctx->st));
+    CUDA_TRY(cudaMemsetAsync(ctx->dcnt.p + 8, 0, sizeof(unsigned long long) * 3, ctx->st));
     {
       StageScope sc(ctx, 1);
       if (prec == RBC3D_FP32M) {
@@ -201,7 +202,7 @@ rbc3d_status rbcs_dev(rbc3d_ctx* ctx, int which, double c1, double c2, int prec,
     StageScope sc(ctx, 3);
     if ((s = run_linear(ctx, which, c2))) return s;
   }
-  unsigned long long h[7];
+  unsigned long long h[10];
   CUDA_TRY(cudaMemcpyAsync(h, ctx->dcnt.p, sizeof(h), cudaMemcpyDeviceToHost, ctx->st));
   CUDA_TRY(cudaStreamSynchronize(ctx->st));
   ctx->counts.pairs_within_rc = (long long)h[1];
@@ -209,6 +210,8 @@ rbc3d_status rbcs_dev(rbc3d_ctx* ctx, int which, double c1, double c2, int prec,
     ctx->counts.nbr_items = (long long)h[0];
     ctx->counts.nearsing_items = (long long)h[3];
     ctx->counts.screen_misses = (long long)h[6];
+    ctx->counts.near_replays = (long long)h[8];
+    ctx->counts.near_projections = (long long)h[9];
     ctx->counts.self_items = (which == RBC3D_TLIST_RBC) ? t.n : 0;
   }
   ctx->counts.nbr_overflow = (int)h[2];
@@ -314,7 +317,7 @@ rbc3d_status rbc3d_create(const rbc3d_params* prm, rbc3d_ctx** out) {
   if (ctx->t_sl1.upload(c1.data(), c1.size(), ctx->st) || ctx->t_sl2.upload(c2.data(), c2.size(), ctx->st) ||
       ctx->t_dl.upload(dl.data(), dl.size(), ctx->st) || ctx->t_mask.upload(mk.data(), mk.size(), ctx->st) ||
       ctx->t_sl32.upload(sl32.data(), sl32.size(), ctx->st) || ctx->t_dl32.upload(dl32.data(), dl32.size(), ctx->st) ||
-      ctx->t_mask32.upload(mk32.data(), mk32.size(), ctx->st) || ctx->dcnt.alloc(8) || ctx->xvint.alloc(3))
+      ctx->t_mask32.upload(mk32.data(), mk32.size(), ctx->st) || ctx->dcnt.alloc(16) || ctx->xvint.alloc(3))
     return bail(RBC3D_ERR_CUDA);
   Tables& T = ctx->T;
   T.sl_c1 = ctx->t_sl1.p; T.sl_c2 = ctx->t_sl2.p; T.dl_c1 = ctx->t_dl.p; T.mask = ctx->t_mask.p;

@@ -23,6 +23,9 @@ struct CorrArgs {
   int ncell, nlat, nlon, m;
   SplGrid G;  // Spline_Create constants of the (2 nlat, nlon) spline grid
   double rc2;
+  unsigned long long* queue;  // k_near's item counter
+  const int* list;            // k_near: items to process (indices), or null for all
+  const unsigned long long* nlist;
   const double* th;
   const double* phi;
   const double* w;
@@ -332,23 +335,31 @@ __device__ void near_readd(const CorrArgs& a, int cell, double c1, double c2, co
   const double st0 = sin(th0), ct0 = cos(th0);
   const double phL = lane * RBC3D_TWO_PI / nazm;
   const double cph = cos(phL), sph = sin(phL);
+  // the radial rule and its weights depend on irad only: lane irad (< 16)
+  // evaluates them once and the loop takes them by shuffle
+  double rth = 0, rwt = 0, rs = 0, rc = 1;
+  if (lane < nrad) {
+    if (sinh_rule) {
+      double s = a.rd_s[lane];
+      rth = a0 + b0 * sinh(mu * s - eta);
+      rwt = a.rd_w[lane] * b0 * mu * cosh(mu * s - eta);
+      rwt = xl * rwt;
+      rth = xm + xl * rth;
+    } else {
+      rth = a.rd_x0[lane];
+      rwt = a.rd_w0[lane];
+    }
+    rs = sin(rth);
+    rc = cos(rth);
+    rwt = rwt * rs * (RBC3D_TWO_PI / nazm);
+    rwt = rwt * mask64(a.T, rth / radPat);
+  }
   double acc[3] = {0, 0, 0};
   for (int irad = 0; irad < nrad; ++irad) {
-    double thP, wt;
-    if (sinh_rule) {
-      double s = a.rd_s[irad];
-      thP = a0 + b0 * sinh(mu * s - eta);
-      wt = a.rd_w[irad] * b0 * mu * cosh(mu * s - eta);
-      wt = xl * wt;
-      thP = xm + xl * thP;
-    } else {
-      thP = a.rd_x0[irad];
-      wt = a.rd_w0[irad];
-    }
-    wt = wt * sin(thP) * (RBC3D_TWO_PI / nazm);
-    wt = wt * mask64(a.T, thP / radPat);
+    const double wt = __shfl_sync(0xffffffffu, rwt, irad);
+    const double sthP = __shfl_sync(0xffffffffu, rs, irad), cthP = __shfl_sync(0xffffffffu, rc, irad);
     double thG, phG;
-    patch_point(st0, ct0, phi0, sin(thP), cos(thP), cph, sph, thG, phG);
+    patch_point(st0, ct0, phi0, sthP, cthP, cph, sph, thG, phG);
     SplW W;
     spline_weights_g(thG, phG, a.G, W);
     double xj[3], xx[3];
@@ -514,14 +525,84 @@ __device__ float projection_dist32(const double* sx, const double* sa, int m, in
 }
 
 // RBC_NearSingInt over the work list (persistent warps)
-__global__ void __launch_bounds__(128) k_near(CorrArgs a) {
-  const int lane = threadIdx.x & 31;
-  const int wpb = blockDim.x >> 5;
+// Target position in the item's cell frame (minimum image about the closest
+// mesh point x0), as RBC_NearSingInt receives it.
+__device__ __forceinline__ void item_geometry(const CorrArgs& a, int4 item, double* x0, double* xt, size_t& q0) {
+  const int t = item.x, cell = item.y - 1, ilat0 = item.z, ilon0 = item.w;
+  q0 = (size_t)cell * a.nlat * a.nlon + (size_t)ilon0 * a.nlat + ilat0;
+  for (int k = 0; k < 3; ++k) {
+    x0[k] = a.x[q0 + (size_t)k * a.npt];
+    double xx = a.tx[t + (size_t)k * a.nt] - x0[k];
+    xx = xx - round(xx * a.iL[k]) * a.L[k];
+    xt[k] = x0[k] + xx;
+  }
+}
+
+// FP32 modes, stage 1 (one thread per candidate): screen (1) -- a target
+// farther than 6*meshSize from its closest mesh point, on its outer side,
+// projects farther than 2*meshSize -- and the survivors listed for stage 2.
+__global__ void k_near_screen(CorrArgs a, int* __restrict__ out, unsigned long long* __restrict__ nout) {
   unsigned long long nitem = *a.nitems;
   if (nitem > (unsigned long long)a.cap) nitem = a.cap;
-  for (long long it = (long long)blockIdx.x * wpb + (threadIdx.x >> 5); it < (long long)nitem;
-       it += (long long)gridDim.x * wpb) {
-    int4 item = a.items[it];
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long long)nitem) return;
+  const int4 item = a.items[i];
+  const int cell = item.y - 1;
+  if (cell < 0 || cell >= a.ncell) return;
+  double x0[3], xt[3];
+  size_t q0;
+  item_geometry(a, item, x0, xt, q0);
+  const double msz = a.meshSize[cell];
+  const double dx0 = xt[0] - x0[0], dx1 = xt[1] - x0[1], dx2 = xt[2] - x0[2];
+  const double d = sqrt(dx0 * dx0 + dx1 * dx1 + dx2 * dx2);
+  const double nd = a.a3[q0] * dx0 + a.a3[q0 + a.npt] * dx1 + a.a3[q0 + 2 * (size_t)a.npt] * dx2;
+  if (d > 6.0 * msz && nd > 0.9 * d) return;
+  out[atomicAdd(nout, 1ull)] = (int)i;
+}
+
+// stage 2 (one warp per listed candidate): the FP32 replay of the projection;
+// candidates within 2.3*meshSize are listed for the FP64 stage.
+__global__ void __launch_bounds__(128) k_near_replay(CorrArgs a, const int* __restrict__ in,
+                                                     const unsigned long long* __restrict__ nin,
+                                                     int* __restrict__ out, unsigned long long* __restrict__ nout) {
+  const int lane = threadIdx.x & 31;
+  const long long n = (long long)*nin;
+  const long long nw = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long w = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < n; w += nw) {
+    const int idx = in[w];
+    const int4 item = a.items[idx];
+    const int cell = item.y - 1;
+    double x0[3], xt[3];
+    size_t q0;
+    item_geometry(a, item, x0, xt, q0);
+    const double msz = a.meshSize[cell];
+    const float d32 = projection_dist32(set_ptr(a, cell, SPL_X), set_ptr(a, cell, SPL_A3), a.m, a.nlon, xt,
+                                        a.th[item.z], a.phi[item.w]);
+    if ((double)d32 > 2.3 * msz) continue;
+    if (lane == 0) out[atomicAdd(nout, 1ull)] = idx;
+  }
+}
+
+__global__ void __launch_bounds__(128) k_near(CorrArgs a) {
+  const int lane = threadIdx.x & 31;
+  unsigned long long nitem = a.list ? *a.nlist : *a.nitems;
+  if (nitem > (unsigned long long)a.cap) nitem = a.cap;
+  // warps take items from a shared counter (the grid is one resident wave):
+  // corrected items cost ~100x screened ones, so a static split leaves a tail
+  // items per counter update: 4 over the full candidate list; 1 over the short
+  // list of the FP32 modes, so its few expensive items spread over all SMs
+  const int GRAB = a.list ? 1 : 4;
+  long long it = 0, it_end = 0;
+  for (;;) {
+    if (it == it_end) {
+      unsigned long long g0 = 0;
+      if (lane == 0) g0 = atomicAdd(a.queue, (unsigned long long)GRAB);
+      it = (long long)__shfl_sync(0xffffffffu, g0, 0);
+      it_end = it + GRAB;
+    }
+    if (it >= (long long)nitem) break;
+    const long long cur = it++;
+    int4 item = a.items[a.list ? a.list[cur] : cur];
     int t = item.x, cell = item.y - 1, ilat0 = item.z, ilon0 = item.w;
     if (cell < 0 || cell >= a.ncell) continue;
     double th0 = a.th[ilat0], phi0 = a.phi[ilon0];
@@ -544,10 +625,14 @@ __global__ void __launch_bounds__(128) k_near(CorrArgs a) {
       double nd = a.a3[q0] * dx0 + a.a3[q0 + a.npt] * dx1 + a.a3[q0 + 2 * (size_t)a.npt] * dx2;
       if (d > 6.0 * msz && nd > 0.9 * d) skip = true;
       // (2) FP32 replay of the projection, margin 0.3*meshSize
-      else if ((double)projection_dist32(sx, set_ptr(a, cell, SPL_A3), a.m, a.nlon, xt, th0, phi0) > 2.3 * msz)
-        skip = true;
+      else {
+        if (lane == 0) atomicAdd(a.cnt + 8, 1ull);
+        if ((double)projection_dist32(sx, set_ptr(a, cell, SPL_A3), a.m, a.nlon, xt, th0, phi0) > 2.3 * msz)
+          skip = true;
+      }
       if (skip && !a.verify) continue;
     }
+    if (lane == 0) atomicAdd(a.cnt + 9, 1ull);
     find_projection(sx, a.m, a.nlon, xt, th0, phi0, x0);
     const double c1 = a.c1, c2 = a.c2 * a.Bc[a.celltype[cell]];
     SplW W;
@@ -563,7 +648,7 @@ __global__ void __launch_bounds__(128) k_near(CorrArgs a) {
     double sizePat = a.radius * sqrt(a.area[cell] / (4 * RBC3D_PI));
     double dist1 = copysign(fabs(0.01 * sizePat), dist);
     double dv[3], tmp[3];
-    near_subtract(a, cell, c1, c2, xt, th0, phi0, a.radius, a.screen ? a.rthr : -1.0, dv);
+    near_subtract(a, cell, c1, c2, xt, th0, phi0, a.radius, a.rthr, dv);
     if (fabs(dist) >= fabs(dist1)) {
       near_readd(a, cell, c1, c2, xt, x0, th0, phi0, a.radius, tmp);
       for (int k = 0; k < 3; ++k) dv[k] += tmp[k];
@@ -632,11 +717,31 @@ rbc3d_status run_near_corr(rbc3d_ctx* ctx, int tlist, double c1, double c2, int 
   fill_args(ctx, tlist, c1, (c2 != 0 && ctx->has_g) ? c2 : 0.0, a, Bc.p);
   if (c1 != 0 && !ctx->has_f) a.c1 = 0;
   a.screen = (prec != RBC3D_FP64) ? 1 : 0;
-  a.rthr = ctx->near_rthr;
+  // FP32 modes: pairs closer than rthr were left out of the FP32 pair sum and
+  // are added back by the FP64 pass (-1: the FP64 plain form left nothing out)
+  a.rthr = (prec != RBC3D_FP64) ? ctx->near_rthr : -1.0;
   a.verify = ctx->verify_screen ? 1 : 0;
-  int nsm = 0;
+  a.list = nullptr;
+  a.nlist = nullptr;
+  int nsm = 0, per_sm = 0;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);
-  { k_near<<<nsm * 8, 128, 0, ctx->st>>>(a); ++ctx->launches; }
+  if (a.screen && !a.verify) {
+    // FP32 modes: geometric screen per thread, FP32 replay per warp, then the
+    // FP64 pass on what is left (counters: dcnt[8] replays, dcnt[10] listed)
+    CUDA_TRY(ctx->near_l1.alloc(std::max(ctx->items_cap, 1)));
+    CUDA_TRY(ctx->near_l2.alloc(std::max(ctx->items_cap, 1)));
+    { k_near_screen<<<(ctx->items_cap + 255) / 256, 256, 0, ctx->st>>>(a, ctx->near_l1.p, ctx->dcnt.p + 8); ++ctx->launches; }
+    { k_near_replay<<<nsm * 8, 128, 0, ctx->st>>>(a, ctx->near_l1.p, ctx->dcnt.p + 8, ctx->near_l2.p,
+                                                   ctx->dcnt.p + 10); ++ctx->launches; }
+    a.screen = 0;
+    a.list = ctx->near_l2.p;
+    a.nlist = ctx->dcnt.p + 10;
+  }
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_near, 128, 0));
+  CUDA_TRY(ctx->near_queue.alloc(1));
+  CUDA_TRY(cudaMemsetAsync(ctx->near_queue.p, 0, sizeof(unsigned long long), ctx->st));
+  a.queue = ctx->near_queue.p;
+  { k_near<<<nsm * std::max(per_sm, 1), 128, 0, ctx->st>>>(a); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaStreamSynchronize(ctx->st));
   return RBC3D_OK;

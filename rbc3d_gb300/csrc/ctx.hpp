@@ -152,6 +152,8 @@ struct rbc3d_ctx {
   DBuf<int> s_toff;
   DBuf<float4> s_tbox;
   int s_ntiles = 0;
+  DBuf<unsigned long long> near_queue;  // work counter of the near-singular kernel
+  DBuf<int> near_l1, near_l2;           // near-singular candidates after the screen / the FP32 replay
   float erfcx_q[16] = {0};   // FP32 erfc fit of the pair kernel
   double erfcx_X = -1.0;
   bool src_sorted = false, src_density = false;
