@@ -317,7 +317,8 @@ rbc3d_status rbc3d_create(const rbc3d_params* prm, rbc3d_ctx** out) {
   if (ctx->t_sl1.upload(c1.data(), c1.size(), ctx->st) || ctx->t_sl2.upload(c2.data(), c2.size(), ctx->st) ||
       ctx->t_dl.upload(dl.data(), dl.size(), ctx->st) || ctx->t_mask.upload(mk.data(), mk.size(), ctx->st) ||
       ctx->t_sl32.upload(sl32.data(), sl32.size(), ctx->st) || ctx->t_dl32.upload(dl32.data(), dl32.size(), ctx->st) ||
-      ctx->t_mask32.upload(mk32.data(), mk32.size(), ctx->st) || ctx->dcnt.alloc(16) || ctx->xvint.alloc(3))
+      ctx->t_mask32.upload(mk32.data(), mk32.size(), ctx->st) || ctx->dcnt.alloc(16) || ctx->xvint.alloc(3) ||
+      ctx->dBcoef.upload(ctx->Bcoef, RBC3D_MAX_CELLTYPES, ctx->st))
     return bail(RBC3D_ERR_CUDA);
   Tables& T = ctx->T;
   T.sl_c1 = ctx->t_sl1.p; T.sl_c2 = ctx->t_sl2.p; T.dl_c1 = ctx->t_dl.p; T.mask = ctx->t_mask.p;

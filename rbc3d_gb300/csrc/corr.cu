@@ -696,25 +696,22 @@ void fill_args(rbc3d_ctx* ctx, int tlist, double c1, double c2, CorrArgs& a, con
 rbc3d_status run_self_corr(rbc3d_ctx* ctx, int tlist, double c1, double c2) {
   TargetSet& t = ctx->tl[tlist];
   if (tlist != RBC3D_TLIST_RBC || t.n == 0 || ctx->ncell == 0) return RBC3D_OK;
-  DBuf<double> Bc;
-  CUDA_TRY(Bc.upload(ctx->Bcoef, RBC3D_MAX_CELLTYPES, ctx->st));
+  const double* Bc = ctx->dBcoef.p;
   CorrArgs a;
-  fill_args(ctx, tlist, c1, (c2 != 0 && ctx->has_g) ? c2 : 0.0, a, Bc.p);
+  fill_args(ctx, tlist, c1, (c2 != 0 && ctx->has_g) ? c2 : 0.0, a, Bc);
   if (c1 != 0 && !ctx->has_f) a.c1 = 0;
   long long threads = (long long)t.n * 32;
   { k_self<<<(int)((threads + 255) / 256), 256, 0, ctx->st>>>(a); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
-  CUDA_TRY(cudaStreamSynchronize(ctx->st));
   return RBC3D_OK;
 }
 
 rbc3d_status run_near_corr(rbc3d_ctx* ctx, int tlist, double c1, double c2, int prec) {
   TargetSet& t = ctx->tl[tlist];
   if (t.n == 0 || ctx->ncell == 0) return RBC3D_OK;
-  DBuf<double> Bc;
-  CUDA_TRY(Bc.upload(ctx->Bcoef, RBC3D_MAX_CELLTYPES, ctx->st));
+  const double* Bc = ctx->dBcoef.p;
   CorrArgs a;
-  fill_args(ctx, tlist, c1, (c2 != 0 && ctx->has_g) ? c2 : 0.0, a, Bc.p);
+  fill_args(ctx, tlist, c1, (c2 != 0 && ctx->has_g) ? c2 : 0.0, a, Bc);
   if (c1 != 0 && !ctx->has_f) a.c1 = 0;
   a.screen = (prec != RBC3D_FP64) ? 1 : 0;
   // FP32 modes: pairs closer than rthr were left out of the FP32 pair sum and
@@ -743,6 +740,5 @@ rbc3d_status run_near_corr(rbc3d_ctx* ctx, int tlist, double c1, double c2, int 
   a.queue = ctx->near_queue.p;
   { k_near<<<nsm * std::max(per_sm, 1), 128, 0, ctx->st>>>(a); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
-  CUDA_TRY(cudaStreamSynchronize(ctx->st));
   return RBC3D_OK;
 }

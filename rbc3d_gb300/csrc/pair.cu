@@ -198,6 +198,7 @@ struct PairArgs {
   float c1f, c2f;
   double rc2;
   float rc2_f, reps2_f;
+  float rc2_loose;  // (rc + 1e-3)^2: hi-part reject threshold of the FP32 pair kernel
   float rthr2_f;  // FP32 path: cross-surface pairs closer than this are left to the FP64 near-singular pass
   float sqpa_f, two_isqa_f, m8_ispi_f, q75_spi_f;  // sqrt(pi/alpha), 2/sqrt(alpha), -8/sqrt(pi), 0.75 sqrt(pi)
   float erfcx_q[ERFCX_DEG + 1];  // erfc(x) exp(x^2) = t Q(t), t = 1/(1 + x/2), on [0, rc sqrt(pi/alpha)]
@@ -350,7 +351,7 @@ __global__ void __launch_bounds__(TILE) k_pair32(PairArgs a) {
   L.n = 0; L.overflow = 0;
   int run_surf = -3, run_id = -1;
   float run_d2 = 3.4e38f;
-  unsigned long long npairs = 0;
+  unsigned npairs = 0;  // < 2^32 pairs per target
 
   for (int nb = 0; nb < 27; ++nb) {
     const int dx = nb % 3 - 1, dy = (nb / 3) % 3 - 1, dz = nb / 9 - 1;
@@ -390,6 +391,9 @@ __global__ void __launch_bounds__(TILE) k_pair32(PairArgs a) {
         }
         __syncwarp();
         if (!active) continue;
+        // plain FP32 sums over the (at most 32) sources of the chunk, then one
+        // compensated (Kahan) addition per chunk into the target's total
+        float cx = 0.f, cy = 0.f, cz = 0.f;
         for (int j = 0; j < cnt; ++j) {
           const float4 p0 = w_p0[j], p1 = w_p1[j];
           const int sj = __float_as_int(p0.w);
@@ -397,9 +401,12 @@ __global__ void __launch_bounds__(TILE) k_pair32(PairArgs a) {
             if (run_id >= 0) L.insert(run_surf, run_id, run_d2);
             run_surf = sj; run_id = -1; run_d2 = 3.4e38f;
           }
-          const float xx = __fadd_rn(p0.x - tsh[0], p1.x - tsl[0]);
-          const float yy = __fadd_rn(p0.y - tsh[1], p1.y - tsl[1]);
-          const float zz = __fadd_rn(p0.z - tsh[2], p1.z - tsl[2]);
+          // reject on the hi parts (a margin covers the lo parts), then the exact test
+          const float hx = p0.x - tsh[0], hy = p0.y - tsh[1], hz = p0.z - tsh[2];
+          if (hx * hx + hy * hy + hz * hz > a.rc2_loose) continue;
+          const float xx = __fadd_rn(hx, p1.x - tsl[0]);
+          const float yy = __fadd_rn(hy, p1.y - tsl[1]);
+          const float zz = __fadd_rn(hz, p1.z - tsl[2]);
           const float r2 = xx * xx + yy * yy + zz * zz;
           if (r2 > a.rc2_f) continue;
           ++npairs;
@@ -455,10 +462,13 @@ __global__ void __launch_bounds__(TILE) k_pair32(PairArgs a) {
             const float t = Adl * (xx * g.x + yy * g.y + zz * g.z) * (xx * an.x + yy * an.y + zz * an.z);
             vx += t * xx; vy += t * yy; vz += t * zz;
           }
-          acc.add(0, wgt * vx);
-          acc.add(1, wgt * vy);
-          acc.add(2, wgt * vz);
+          cx = fmaf(wgt, vx, cx);
+          cy = fmaf(wgt, vy, cy);
+          cz = fmaf(wgt, vz, cz);
         }
+        acc.add(0, cx);
+        acc.add(1, cy);
+        acc.add(2, cz);
         if (a.collect && run_id >= 0) { L.insert(run_surf, run_id, run_d2); }
         run_surf = -3; run_id = -1; run_d2 = 3.4e38f;
       }
@@ -476,8 +486,9 @@ __global__ void __launch_bounds__(TILE) k_pair32(PairArgs a) {
     }
   }
   // pair count
-  for (int o = 16; o > 0; o >>= 1) npairs += __shfl_xor_sync(0xffffffffu, npairs, o);
-  if ((tid & 31) == 0 && npairs) atomicAdd(a.cnt + 1, npairs);
+  unsigned long long np = npairs;
+  for (int o = 16; o > 0; o >>= 1) np += __shfl_xor_sync(0xffffffffu, np, o);
+  if ((tid & 31) == 0 && np) atomicAdd(a.cnt + 1, np);
 }
 
 // FP64 plain form: the same traversal with the reference arithmetic.
@@ -778,14 +789,12 @@ rbc3d_status build_source_list(rbc3d_ctx* ctx) {
 rbc3d_status build_source_density(rbc3d_ctx* ctx) {
   int n = ctx->npt, nv = ctx->nlat * ctx->nlon;
   if (n == 0) return RBC3D_OK;
-  DBuf<double> Bc;
-  CUDA_TRY(Bc.upload(ctx->Bcoef, RBC3D_MAX_CELLTYPES, ctx->st));
+  const double* Bc = ctx->dBcoef.p;
   if (ctx->has_f) { k_density<<<nblk(n, 256), 256, 0, ctx->st>>>(n, ctx->nlat, nv, ctx->f.p, ctx->detJ.p, ctx->w.p, ctx->sf.p); ++ctx->launches; }
   if (ctx->has_g) { k_density<<<nblk(n, 256), 256, 0, ctx->st>>>(n, ctx->nlat, nv, ctx->g.p, ctx->detJ.p, ctx->w.p, ctx->sg.p); ++ctx->launches; }
   { k_gather_density<<<nblk(n, 256), 256, 0, ctx->st>>>(n, nv, ctx->s_order.p, ctx->sf.p, ctx->sg.p, ctx->celltype.p,
-                                                       Bc.p, ctx->s_f.p, ctx->s_g.p, ctx->has_f, ctx->has_g); ++ctx->launches; }
+                                                       Bc, ctx->s_f.p, ctx->s_g.p, ctx->has_f, ctx->has_g); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
-  CUDA_TRY(cudaStreamSynchronize(ctx->st));
   ctx->src_density = true;
   return RBC3D_OK;
 }
@@ -826,7 +835,8 @@ rbc3d_status run_pair_sum(rbc3d_ctx* ctx, int tlist, double c1, double c2, int p
   double cm = 2.0 * sin(0.5 * ctx->radius) * (1.0 + 1e-6);
   a.chord2_max = (float)(cm * cm);
   a.c1 = c1; a.c2 = c2; a.c1f = (float)c1; a.c2f = (float)c2;
-  a.rc2 = ctx->prm.rc * ctx->prm.rc; a.rc2_f = (float)a.rc2; a.reps2_f = (float)(ctx->T.r_eps * ctx->T.r_eps);
+  a.rc2 = ctx->prm.rc * ctx->prm.rc; a.rc2_f = (float)a.rc2;
+  a.rc2_loose = (float)((ctx->prm.rc + 1e-3) * (ctx->prm.rc + 1e-3)); a.reps2_f = (float)(ctx->T.r_eps * ctx->T.r_eps);
   a.rthr2_f = (float)(ctx->near_rthr * ctx->near_rthr);
   a.sqpa_f = (float)sqrt(RBC3D_PI / ctx->prm.alpha);
   a.two_isqa_f = (float)(2.0 / sqrt(ctx->prm.alpha));
@@ -857,16 +867,14 @@ rbc3d_status run_pair_sum(rbc3d_ctx* ctx, int tlist, double c1, double c2, int p
 rbc3d_status run_linear(rbc3d_ctx* ctx, int tlist, double c2) {
   if (c2 == 0.0 || ctx->npt == 0 || !ctx->has_g) return RBC3D_OK;
   TargetSet& t = ctx->tl[tlist];
-  DBuf<double> Bc;
-  CUDA_TRY(Bc.upload(ctx->Bcoef, RBC3D_MAX_CELLTYPES, ctx->st));
+  const double* Bc = ctx->dBcoef.p;
   CUDA_TRY(ctx->xvint.alloc(3));
   CUDA_TRY(cudaMemsetAsync(ctx->xvint.p, 0, 3 * sizeof(double), ctx->st));
   { k_linear_reduce<<<304, 256, 0, ctx->st>>>(ctx->npt, ctx->nlat * ctx->nlon, ctx->x.p, ctx->sg.p, ctx->a3.p,
-                                            ctx->celltype.p, Bc.p, ctx->xvint.p); ++ctx->launches; }
+                                            ctx->celltype.p, Bc, ctx->xvint.p); ++ctx->launches; }
   double pil = ctx->iLb[0] * ctx->iLb[1] * ctx->iLb[2];
   if (t.n) { k_linear_add<<<nblk(t.n, 256), 256, 0, ctx->st>>>(t.n, t.Acoef.p, ctx->xvint.p, c2 * (-8 * RBC3D_PI * pil), t.v.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
-  CUDA_TRY(cudaStreamSynchronize(ctx->st));
   return RBC3D_OK;
 }
 
