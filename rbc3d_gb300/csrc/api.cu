@@ -410,6 +410,28 @@ rbc3d_status rbc3d_set_cell_grid(rbc3d_ctx* ctx, const double* th, const double*
     rbc3d_status s = self_mixed_grid(ctx, thG, phiA, pw);
     if (s) return s;
   }
+  {
+    // FP64 Spline_Interp weights per (latitude, patch point) for k_self: with
+    // phi(j) = j 2 pi / nlon, phiG = atan2(...) + phi0 moves the stencil by
+    // whole columns, so only the column offset depends on the target's longitude
+    const int m = 2 * nlat;
+    const double hx = RBC3D_TWO_PI / m, hy = RBC3D_TWO_PI / nlon, ihx = 1. / hx, ihy = 1. / hy;
+    std::vector<SelfW64> W((size_t)nlat * NQ);
+    for (size_t i = 0; i < W.size(); ++i) {
+      const double x = thG[i] * ihx, y = phiA[i] * ihy;
+      const int i1 = (int)std::floor(x), j1 = (int)std::floor(y);
+      const double s = x - i1, t = y - j1;
+      SelfW64 e;
+      e.i1 = ((i1 % m) + m) % m;
+      e.j1b = j1;
+      e.cx[0] = 1 + s * s * (-3. + 2. * s); e.cx[1] = s * s * (3. - 2. * s);
+      e.cx[2] = hx * s * (1. + s * (-2. + s)); e.cx[3] = hx * s * s * (-1. + s);
+      e.cy[0] = 1 + t * t * (-3. + 2. * t); e.cy[1] = t * t * (3. - 2. * t);
+      e.cy[2] = hy * t * (1. + t * (-2. + t)); e.cy[3] = hy * t * t * (-1. + t);
+      W[i] = e;
+    }
+    CUDA_TRY(ctx->self_w64.upload(reinterpret_cast<const char*>(W.data()), W.size() * sizeof(SelfW64), ctx->st));
+  }
   CUDA_TRY(ctx->thG.upload(thG.data(), thG.size(), ctx->st));
   CUDA_TRY(ctx->phiA.upload(phiA.data(), phiA.size(), ctx->st));
   std::vector<double> x0(16), w0(16);

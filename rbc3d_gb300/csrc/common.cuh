@@ -93,6 +93,12 @@ __device__ __forceinline__ double dist_on_sphere(double th0, double phi0, double
 // ---------------------------------------------------------------------------
 // Bicubic Hermite interpolation on the doubled-sphere grid (Spline_Interp,
 // ModSpline.F90:150-191).  Node layout: spl[node*SPL_NODE + kind*3 + var].
+// Spline_Interp weights of one patch point for a target latitude: row i1,
+// column offset j1b (before adding the target's longitude index), cx, cy.
+struct SelfW64 {
+  int i1, j1b;
+  double cx[4], cy[4];
+};
 struct SplW {
   int n11, n12, n21, n22;  // node ids (i1,j1) (i1,j2) (i2,j1) (i2,j2)
   double cx[4], cy[4];
@@ -154,6 +160,39 @@ __device__ __forceinline__ void spline_eval(const double* __restrict__ spl, cons
     double r2 = __ldg(a + 3 + l) * W.cy[0] + __ldg(b + 3 + l) * W.cy[1] + __ldg(a + 9 + l) * W.cy[2] + __ldg(b + 9 + l) * W.cy[3];
     double r3 = __ldg(c + 3 + l) * W.cy[0] + __ldg(d + 3 + l) * W.cy[1] + __ldg(c + 9 + l) * W.cy[2] + __ldg(d + 9 + l) * W.cy[3];
     f[l] = W.cx[0] * r0 + W.cx[1] * r1 + W.cx[2] * r2 + W.cx[3] * r3;
+  }
+}
+
+// The 16 products cx[.] cy[.] of Spline_Interp's weights, in record order:
+// per node (n11, n12, n21, n22) the weights of (u, u1, u2, u12).
+__device__ __forceinline__ void spline_w16(const SplW& W, double* w) {
+  const double* cx = W.cx;
+  const double* cy = W.cy;
+  // node n11 = (i1, j1): u cx0 cy0, u1 cx2 cy0, u2 cx0 cy2, u12 cx2 cy2
+  w[0] = cx[0] * cy[0]; w[1] = cx[2] * cy[0]; w[2] = cx[0] * cy[2]; w[3] = cx[2] * cy[2];
+  // n12 = (i1, j2)
+  w[4] = cx[0] * cy[1]; w[5] = cx[2] * cy[1]; w[6] = cx[0] * cy[3]; w[7] = cx[2] * cy[3];
+  // n21 = (i2, j1)
+  w[8] = cx[1] * cy[0]; w[9] = cx[3] * cy[0]; w[10] = cx[1] * cy[2]; w[11] = cx[3] * cy[2];
+  // n22 = (i2, j2)
+  w[12] = cx[1] * cy[1]; w[13] = cx[3] * cy[1]; w[14] = cx[1] * cy[3]; w[15] = cx[3] * cy[3];
+}
+// Spline_Interp with the products precomputed: 16 FMA per variable.
+__device__ __forceinline__ void spline_eval16(const double* __restrict__ spl, const SplW& W, const double* w, int nvar,
+                                              double* f) {
+  const double* nd[4] = {spl + (size_t)W.n11 * SPL_NODE, spl + (size_t)W.n12 * SPL_NODE,
+                         spl + (size_t)W.n21 * SPL_NODE, spl + (size_t)W.n22 * SPL_NODE};
+#pragma unroll
+  for (int l = 0; l < 3; ++l) {
+    if (l >= nvar) break;
+    double s = 0.;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const double* p = nd[k];
+      s += w[4 * k] * __ldg(p + l) + w[4 * k + 1] * __ldg(p + 3 + l) + w[4 * k + 2] * __ldg(p + 6 + l) +
+           w[4 * k + 3] * __ldg(p + 9 + l);
+    }
+    f[l] = s;
   }
 }
 

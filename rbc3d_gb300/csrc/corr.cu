@@ -24,6 +24,7 @@ struct CorrArgs {
   SplGrid G;  // Spline_Create constants of the (2 nlat, nlon) spline grid
   double rc2;
   unsigned long long* queue;  // k_near's item counter
+  const SelfW64* W64;         // k_self: tabulated patch weights (uniform longitudes), or null
   const int* list;            // k_near: items to process (indices), or null for all
   const unsigned long long* nlist;
   const double* th;
@@ -92,9 +93,20 @@ __global__ void __launch_bounds__(256) k_self(CorrArgs a) {
     double th_j = a.thG[(size_t)ilat0 * NQ + q];
     double p = a.phiA[(size_t)ilat0 * NQ + q] + phi0;  // PolarPatch_Build: atan2(...) + phi0
     double phi_j = p - floor(p * RBC3D_I_2PI) * RBC3D_TWO_PI;
-    spline_weights_g(th_j, phi_j, a.G, W);
+    if (a.W64) {
+      // weights tabulated per (latitude, patch point); longitudes shift the stencil
+      const SelfW64 e = a.W64[(size_t)ilat0 * NQ + q];
+      const int j1 = imod(e.j1b + ilon0, a.nlon), j2 = (j1 + 1 == a.nlon) ? 0 : j1 + 1;
+      const int i2 = (e.i1 + 1 == a.m) ? 0 : e.i1 + 1;
+      W.n11 = e.i1 + a.m * j1; W.n12 = e.i1 + a.m * j2; W.n21 = i2 + a.m * j1; W.n22 = i2 + a.m * j2;
+      for (int k = 0; k < 4; ++k) { W.cx[k] = e.cx[k]; W.cy[k] = e.cy[k]; }
+    } else {
+      spline_weights_g(th_j, phi_j, a.G, W);
+    }
+    double w16[16];
+    spline_w16(W, w16);
     double xj[3], xx[3];
-    spline_eval(sx, W, 3, xj);
+    spline_eval16(sx, W, w16, 3, xj);
     for (int k = 0; k < 3; ++k) xx[k] = xj[k] - xi[k];
     const double r2 = xx[0] * xx[0] + xx[1] * xx[1] + xx[2] * xx[2];
     if (r2 >= a.rc2) continue;  // rr >= rc (ModRbcSingInt.F90:65)
@@ -102,7 +114,7 @@ __global__ void __launch_bounds__(256) k_self(CorrArgs a) {
     double wq = a.pw[irad];
     if (c1 != 0.) {
       double fj[3], EA, EB;
-      spline_eval(sF, W, 3, fj);
+      spline_eval16(sF, W, w16, 3, fj);
       for (int k = 0; k < 3; ++k) fj[k] = wq * fj[k];
       ewald_sl64r(a.T, rr, ir, EA, EB);
       double d = xx[0] * fj[0] + xx[1] * fj[1] + xx[2] * fj[2];
@@ -110,9 +122,9 @@ __global__ void __launch_bounds__(256) k_self(CorrArgs a) {
     }
     if (c2m != 0.) {
       double gj[3], aj[3];
-      spline_eval(sG, W, 3, gj);
+      spline_eval16(sG, W, w16, 3, gj);
       for (int k = 0; k < 3; ++k) gj[k] = wq * gj[k];
-      spline_eval(sA, W, 3, aj);
+      spline_eval16(sA, W, w16, 3, aj);
       double EA = ewald_dl64r(a.T, rr, ir);
       double dg = xx[0] * gj[0] + xx[1] * gj[1] + xx[2] * gj[2];
       double da = xx[0] * aj[0] + xx[1] * aj[1] + xx[2] * aj[2];
@@ -678,6 +690,7 @@ void fill_args(rbc3d_ctx* ctx, int tlist, double c1, double c2, CorrArgs& a, con
   a.nt = t.n; a.tx = t.x.p; a.tA = t.Acoef.p; a.tmeta = t.meta.p; a.v = t.v.p;
   a.ncell = ctx->ncell; a.nlat = ctx->nlat; a.nlon = ctx->nlon; a.m = ctx->m;
   a.G = spl_grid(ctx->m, ctx->nlon);
+  a.W64 = ctx->phi_uniform ? reinterpret_cast<const SelfW64*>(ctx->self_w64.p) : nullptr;
   a.rc2 = ctx->prm.rc * ctx->prm.rc;
   a.th = ctx->th.p; a.phi = ctx->phi.p; a.w = ctx->w.p;
   a.x = ctx->x.p; a.a3 = ctx->a3.p; a.detJ = ctx->detJ.p; a.f = ctx->f.p; a.g = ctx->g.p;

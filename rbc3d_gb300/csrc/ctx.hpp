@@ -154,6 +154,7 @@ struct rbc3d_ctx {
   int s_ntiles = 0;
   DBuf<unsigned long long> near_queue;  // work counter of the near-singular kernel
   DBuf<double> dBcoef;                  // Bcoef per cell type on the device
+  DBuf<char> self_w64;                  // FP64 patch weights per (latitude, patch point)
   DBuf<int> near_l1, near_l2;           // near-singular candidates after the screen / the FP32 replay
   float erfcx_q[16] = {0};   // FP32 erfc fit of the pair kernel
   double erfcx_X = -1.0;
