@@ -201,6 +201,7 @@ def main():
     ap.add_argument("--cells", type=int, default=None, help="smaller workload (profiling)")
     ap.add_argument("--quick", action="store_true", help="FP32C timing only (profiling)")
     ap.add_argument("--no-wall", action="store_true", help="skip the learned-guess wall GMRES comparison")
+    ap.add_argument("--no-scaleup", action="store_true", help="skip the 2048-cell (PME 256^3) scale-up line")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     dist = dist_init()
@@ -354,6 +355,44 @@ def main():
         except Exception:
             pass
 
+    # ---- scale-up: 2048 cells, L = 80, PME 256^3 (2.56 M targets), all three modes
+    scale = None
+    if not args.quick and not args.no_scaleup:
+        from rbc3d_gb300 import geometry as G
+        t1 = time.perf_counter()
+        prm5, cells5, _ = G.config("C5", seed=args.seed + rank)
+        N5 = cells5.x.shape[1]
+        ctx5 = Context(lib, prm5)
+        ctx5.set_cells(cells5)
+        ctx5.set_cell_density(f=cells5.f, g=cells5.g, spl_F=cells5.spl_F, spl_G=cells5.spl_G)
+
+        def timed(prec, warm, steps):
+            for _ in range(warm):
+                ctx5.matvec(TLIST_RBC, c, c, TERM_ALL, prec, device_only=True)
+            ctx5.timer_start()
+            for _ in range(steps):
+                ctx5.matvec(TLIST_RBC, c, c, TERM_ALL, prec, device_only=True)
+            return dist_max(dist, ctx5.timer_stop()) / steps
+
+        m32c = timed(FP32C, 2, 3)
+        m32m = timed(FP32M, 2, 3)
+        m64 = timed(FP64, 1, 1)
+        v64 = ctx5.matvec(TLIST_RBC, c, c, TERM_ALL, FP64)
+        e32c = float(np.linalg.norm(ctx5.matvec(TLIST_RBC, c, c, TERM_ALL, FP32C) - v64) / np.linalg.norm(v64))
+        e32m = float(np.linalg.norm(ctx5.matvec(TLIST_RBC, c, c, TERM_ALL, FP32M) - v64) / np.linalg.norm(v64))
+        cnt5 = ctx5.counts()
+        ctx5.close()
+        log(f"scale-up in {time.perf_counter() - t1:.1f}s")
+        scale = {"workload": "2048 biconcave cells, 25x50 grid (2,560,000 targets), periodic L=80, rc=3, "
+                             "PME 256^3 P=6, SL+DL, viscRat=5 (C5)",
+                 "targets": N5,
+                 "fp32c": {"ms_per_step": m32c, "value": ws * N5 / (m32c * 1e-3), "rel_l2_vs_fp64_plain": e32c},
+                 "fp32m": {"ms_per_step": m32m, "value": ws * N5 / (m32m * 1e-3), "rel_l2_vs_fp64_plain": e32m},
+                 "fp64_plain": {"ms_per_step": m64, "value": ws * N5 / (m64 * 1e-3)},
+                 "fp32c_over_fp64": m64 / m32c, "fp32m_over_fp64": m64 / m32m,
+                 "pairs_within_rc": cnt5["pairs_within_rc"], "nearsing_items": cnt5["nearsing_items"],
+                 "steps": "fp32c, fp32m: 2 warm-up + 3 timed; fp64: 1 + 1"}
+
     # ---- wall no-slip GMRES on the tube workload: plain vs history vs learned guess
     wall = None
     if not args.quick and not args.no_wall:
@@ -399,6 +438,11 @@ def main():
             "counts": {k: counts[k] for k in ("pairs_within_rc", "nbr_items", "nearsing_items", "self_items",
                                               "screen_misses", "near_replays", "near_projections")},
             "roofline": roof,
+            "fp32_over_fp64_plain": {"fp32c": value / fp64_value, "fp32m": fp32m_value / fp64_value,
+                                     "target": 20.0,
+                                     "note": "fp32c keeps the self patch in FP64 (GB300 FP64 is 1/74 of FP32); "
+                                             "fp32m does it in FP32 with hi/lo geometry"},
+            "scaleup_c5": scale,
             "wall_gmres": wall,
             "fma_peaks_tflops": {"fp32": peak32, "fp64": peak64},
             "cpu_baseline": cpu,

@@ -178,20 +178,35 @@ def random_sh_coeffs(rng, lmax=6, lmin=1):
     return out
 
 
+_SH_BASIS = {}
+
+
+def _sh_basis(keys, th, phi):
+    """Y_lm on the (th, phi) grid for the ordered (l, m) keys, cached per grid."""
+    ck = (tuple(keys), th.size, phi.size, float(th[0]), float(th[-1]), float(phi[-1]))
+    B = _SH_BASIS.get(ck)
+    if B is None:
+        lmax = max(l for l, _ in keys)
+        P = _assoc_legendre(lmax, np.cos(th))
+        B = np.empty((len(keys), th.size, phi.size))
+        for i, (l, m) in enumerate(keys):
+            am = abs(m)
+            if m == 0:
+                ang = np.ones_like(phi)
+            elif m > 0:
+                ang = math.sqrt(2) * np.cos(m * phi)
+            else:
+                ang = math.sqrt(2) * np.sin(am * phi)
+            B[i] = P[(l, am)][:, None] * ang[None, :]
+        _SH_BASIS[ck] = B
+    return B
+
+
 def sh_eval(coeffs, th, phi):
-    lmax = max(l for l, _ in coeffs)
-    P = _assoc_legendre(lmax, np.cos(th))
-    out = np.zeros((th.size, phi.size))
-    for (l, m), a in coeffs.items():
-        am = abs(m)
-        if m == 0:
-            ang = np.ones_like(phi)
-        elif m > 0:
-            ang = math.sqrt(2) * np.cos(m * phi)
-        else:
-            ang = math.sqrt(2) * np.sin(am * phi)
-        out += a * P[(l, am)][:, None] * ang[None, :]
-    return out
+    keys = list(coeffs)
+    B = _sh_basis(keys, th, phi)
+    a = np.array([coeffs[k] for k in keys])
+    return np.tensordot(a, B, axes=(0, 0))
 
 
 # ---------------------------------------------------------------------------
@@ -228,6 +243,22 @@ def spline_on_sphere(v):
     u12 = fft_diff(u1, 1)
     tab = np.stack([u, u1, u2, u12])          # (4, m, n, nvar)
     return np.ascontiguousarray(tab.transpose(0, 3, 2, 1))  # (4, nvar, n, m)
+
+
+def spline_on_sphere_batch(V):
+    """spline_on_sphere over a stack of cells: V (ncell, nlat+1, nlon, nvar)
+    -> (ncell, 4, nvar, nlon, 2*nlat)."""
+    ncell, nl1, nlon, nvar = V.shape
+    nlat = nl1 - 1
+    m = 2 * nlat
+    u = np.empty((ncell, m, nlon, nvar))
+    u[:, :nlat] = V[:, :nlat]
+    u[:, nlat:] = np.roll(V[:, nlat:0:-1], -(nlon // 2), axis=2)
+    u1 = fft_diff(u, 1)
+    u2 = fft_diff(u, 2)
+    u12 = fft_diff(u1, 2)
+    tab = np.stack([u, u1, u2, u12], axis=1)  # (ncell, 4, m, n, nvar)
+    return np.ascontiguousarray(tab.transpose(0, 1, 4, 3, 2))
 
 
 def equi_theta(nlat):
@@ -273,6 +304,10 @@ def place_cells(rng, ncell, L, min_dist, inside=None, max_tries=2_000_000):
     L = np.asarray(L, dtype=np.float64)
     C = []
     tries = 0
+    nb = np.maximum(1, np.floor(L / max(min_dist, 1e-12)).astype(int))
+    bs = L / nb
+    offs = [np.array((i, j, k)) for i in (-1, 0, 1) for j in (-1, 0, 1) for k in (-1, 0, 1)]
+    bins = {}
     while len(C) < ncell:
         tries += 1
         if tries > max_tries:
@@ -281,14 +316,21 @@ def place_cells(rng, ncell, L, min_dist, inside=None, max_tries=2_000_000):
         if inside is not None and not inside(c):
             continue
         ok = True
-        for d in C:
-            dd = c - d
-            dd -= np.round(dd / L) * L
-            if np.dot(dd, dd) < min_dist ** 2:
-                ok = False
+        # the accepted centres in the neighbouring bins (bin edge >= min_dist)
+        # are the only ones that can be closer than min_dist
+        b = np.floor(c / bs).astype(int) % nb
+        for off in offs:
+            for d in bins.get(tuple((b + off) % nb), ()):
+                dd = c - d
+                dd -= np.round(dd / L) * L
+                if np.dot(dd, dd) < min_dist ** 2:
+                    ok = False
+                    break
+            if not ok:
                 break
         if ok:
             C.append(c)
+            bins.setdefault(tuple(b), []).append(c)
     return np.array(C)
 
 
@@ -307,33 +349,32 @@ def make_cells(rng, ncell, L, min_dist, nlat=25, nlon=50, celltype=0, rc=1.0,
         x, n, dj = biconcave_surface(th, phi, R, centres[ic], rc)
         xe, ne, dje = biconcave_surface(the, phi, R, centres[ic], rc)
         X.append(x); A3.append(n); DJ.append(dj[..., None])
-        SX.append(spline_on_sphere(xe)); SA.append(spline_on_sphere(ne))
-        SD.append(spline_on_sphere(dje[..., None]))
+        SX.append(xe); SA.append(ne); SD.append(dje[..., None])
         area = float(np.sum(dj * w[:, None]))
         areas.append(area)
         msz.append(math.sqrt(area / nlat ** 2))
         coeff = [random_sh_coeffs(rng) for _ in range(3)]
         f = np.stack([sh_eval(cf, th, phi) for cf in coeff], axis=-1)
         fe = np.stack([sh_eval(cf, the, phi) for cf in coeff], axis=-1)
-        F.append(f); SF.append(spline_on_sphere(fe * dje[..., None]))
+        F.append(f); SF.append(fe * dje[..., None])
         if with_g:
             coeffg = [random_sh_coeffs(rng) for _ in range(3)]
             g = np.stack([sh_eval(cf, th, phi) for cf in coeffg], axis=-1)
             ge = np.stack([sh_eval(cf, the, phi) for cf in coeffg], axis=-1)
-            G.append(g); SG.append(spline_on_sphere(ge * dje[..., None]))
+            G.append(g); SG.append(ge * dje[..., None])
     cells = Cells(
         nlat=nlat, nlon=nlon, th=th, phi=phi, w=w, ncell=ncell,
         celltype=np.full(ncell, celltype, dtype=np.int32),
         x=_to_points(np.array(X)), a3=_to_points(np.array(A3)),
         detJ=_to_points(np.array(DJ))[0].copy(),
         area=np.array(areas), meshSize=np.array(msz),
-        spl_x=np.ascontiguousarray(np.array(SX)), spl_a3=np.ascontiguousarray(np.array(SA)),
-        spl_detJ=np.ascontiguousarray(np.array(SD)),
-        f=_to_points(np.array(F)), spl_F=np.ascontiguousarray(np.array(SF)),
+        spl_x=spline_on_sphere_batch(np.array(SX)), spl_a3=spline_on_sphere_batch(np.array(SA)),
+        spl_detJ=spline_on_sphere_batch(np.array(SD)),
+        f=_to_points(np.array(F)), spl_F=spline_on_sphere_batch(np.array(SF)),
         centres=centres, rotations=rots)
     if with_g:
         cells.g = _to_points(np.array(G))
-        cells.spl_G = np.ascontiguousarray(np.array(SG))
+        cells.spl_G = spline_on_sphere_batch(np.array(SG))
     else:
         cells.g = np.zeros_like(cells.f)
         cells.spl_G = np.zeros_like(cells.spl_F)

@@ -196,3 +196,21 @@ def test_wall_solve_error_codes(gpu):
     ctx.prepare_sing_int_on_wall()
     st, code = ctx.no_slip_wall(1e-12, 2, check=False)
     assert code == 4 and st.iterations == 2 and st.converged == 0  # NOCONV, bounded
+
+
+@pytest.mark.gpu
+def test_fp32_modes_vs_fp64_full_size_c5(gpu):
+    # the 2048-cell, PME 256^3 workload (2.56 M targets): both FP32 modes
+    # within 1e-6 of the FP64 plain form, identical pair counts
+    prm, cells, _ = G.config("C5")
+    ctx = Context(gpu, prm)
+    ctx.set_cells(cells)
+    ctx.set_cell_density(f=cells.f, g=cells.g, spl_F=cells.spl_F, spl_G=cells.spl_G)
+    c = 1 / (4 * np.pi)
+    v64 = ctx.matvec(TLIST_RBC, c, c, TERM_ALL, FP64)
+    n64 = ctx.counts()["pairs_within_rc"]
+    for prec in (FP32C, FP32M):
+        v = ctx.matvec(TLIST_RBC, c, c, TERM_ALL, prec)
+        assert np.linalg.norm(v - v64) <= 1e-6 * np.linalg.norm(v64)
+        assert abs(ctx.counts()["pairs_within_rc"] - n64) <= 1e-6 * n64  # only pairs at r = rc may differ
+    ctx.close()
