@@ -439,9 +439,9 @@ __global__ void __launch_bounds__(TILE) k_pair32(PairArgs a) {
           // per-lane gathers into the 8193-entry tables (the FP64 plain form
           // keeps the tables)
           const float st = r * a.sqpa_f;  // r*sqrt(pi/alpha)
-          const float ex = expf(-st * st);
+          const float ex = __expf(-st * st);  // ex2.approx: ~2 ulp where it matters (small st)
           // erfc(st) = exp(-st^2) t Q(t), t = 1/(1 + st/2) (fit_erfcx)
-          const float tq = __frcp_rn(fmaf(0.5f, st, 1.f));
+          const float tq = __fdividef(1.f, fmaf(0.5f, st, 1.f));
           float Q = a.erfcx_q[ERFCX_DEG];
   #pragma unroll
           for (int k = ERFCX_DEG - 1; k >= 0; --k) Q = fmaf(Q, tq, a.erfcx_q[k]);

@@ -182,9 +182,9 @@ __global__ void __launch_bounds__(256) k_self_mix(MixArgs a) {
     const float r2 = xx[0] * xx[0] + xx[1] * xx[1] + xx[2] * xx[2];
     if (r2 >= a.rc2) continue;  // rr >= rc (ModRbcSingInt.F90:65)
     const float rinv = rsqrtf(r2), rv = r2 * rinv, ir2 = rinv * rinv;
-    const float st = rv * a.sqpa, ex = expf(-st * st);
+    const float st = rv * a.sqpa, ex = __expf(-st * st);
     // erfc(st) = exp(-st^2) t Q(t), t = 1/(1 + st/2) (fit_erfcx)
-    const float tq = __frcp_rn(fmaf(0.5f, st, 1.f));
+    const float tq = __fdividef(1.f, fmaf(0.5f, st, 1.f));
     float Qp = a.erfcx_q[ERFCX_DEG];
 #pragma unroll
     for (int k = ERFCX_DEG - 1; k >= 0; --k) Qp = fmaf(Qp, tq, a.erfcx_q[k]);
