@@ -373,6 +373,7 @@ rbc3d_status rbc3d_set_cell_grid(rbc3d_ctx* ctx, const double* th, const double*
   // polar patch
   std::vector<double> mk(MASK_NTAB + 1);
   for (int i = 0; i <= MASK_NTAB; ++i) mk[i] = mask_exact((double)i / MASK_NTAB);
+  const std::vector<double>& mk_tab = mk;
   ctx->radius = RBC3D_PI / std::sqrt((double)nlat);
   double h = RBC3D_PI / nlat;
   ctx->nrad = 2 * (int)std::round(ctx->radius / h);
@@ -406,6 +407,25 @@ rbc3d_status rbc3d_set_cell_grid(rbc3d_ctx* ctx, const double* th, const double*
   ctx->phi_uniform = true;
   for (int j = 0; j < nlon; ++j)
     if (std::fabs(phi[j] - j * RBC3D_TWO_PI / nlon) > 1e-12) ctx->phi_uniform = false;
+  if (ctx->phi_uniform) {
+    // MaskFunc(DistOnSphere / radius) of every pair of grid points of one cell
+    // (ModIntOnRbcs.F90:77-80): with phi(j) = j 2 pi / nlon it depends on the two
+    // latitudes and the longitude difference d (and d ~ nlon - d) only
+    const int nh = nlon / 2 + 1;
+    std::vector<double> m64((size_t)nlat * nlat * nh);
+    std::vector<float> w32(m64.size());
+    for (int i0 = 0; i0 < nlat; ++i0)
+      for (int i1 = 0; i1 < nlat; ++i1)
+        for (int d = 0; d < nh; ++d) {
+          double c = std::cos(th[i0] - th[i1]) - std::sin(th[i0]) * std::sin(th[i1]) * (1. - std::cos(phi[0] - phi[d]));
+          c = std::fmin(1., std::fmax(-1., c));
+          const double mk = mask_lerp(mk_tab, std::acos(c) / ctx->radius);
+          m64[((size_t)i0 * nlat + i1) * nh + d] = mk;
+          w32[((size_t)i0 * nlat + i1) * nh + d] = (float)(1.0 - mk);
+        }
+    CUDA_TRY(ctx->mtab64.upload(m64.data(), m64.size(), ctx->st));
+    CUDA_TRY(ctx->mtab32.upload(w32.data(), w32.size(), ctx->st));
+  }
   {
     rbc3d_status s = self_mixed_grid(ctx, thG, phiA, pw);
     if (s) return s;

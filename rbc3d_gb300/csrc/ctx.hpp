@@ -155,6 +155,8 @@ struct rbc3d_ctx {
   DBuf<unsigned long long> near_queue;  // work counter of the near-singular kernel
   DBuf<double> dBcoef;                  // Bcoef per cell type on the device
   DBuf<char> self_w64;                  // FP64 patch weights per (latitude, patch point)
+  DBuf<double> mtab64;                  // same-cell mask per (latitude, latitude, longitude gap)
+  DBuf<float> mtab32;                   // 1 - mask, FP32
   DBuf<int> near_l1, near_l2;           // near-singular candidates after the screen / the FP32 replay
   float erfcx_q[16] = {0};   // FP32 erfc fit of the pair kernel
   double erfcx_X = -1.0;

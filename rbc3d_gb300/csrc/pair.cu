@@ -191,7 +191,9 @@ struct PairArgs {
   const double* th;
   const double* phi;
   const float4* usph;
-  int nlat;
+  int nlat, nlon, nhalf;
+  const double* mtab64;  // MaskFunc of same-cell grid pairs, (ilat_i, ilat_j, |dlon|), or null
+  const float* mtab32;   // 1 - mask in FP32
   double radius, inv_radius;
   float inv_radius_f, chord2_max;
   double c1, c2;
@@ -321,7 +323,7 @@ __global__ void __launch_bounds__(TILE) k_pair32(PairArgs a) {
   int ti = active ? a.torder[unit.y + tid] : 0;
   float th_[3] = {0, 0, 0}, tl_[3] = {0, 0, 0};
   float4 ui = make_float4(0, 0, 0, 0);
-  int surf_i = -2;
+  int surf_i = -2, tlat = 0, tlon = 0;
   if (active) {
     for (int k = 0; k < 3; ++k) {
       double r = min_image(a.tx[ti + (size_t)k * a.nt] - c0[k], a.L[k], a.iL[k]);
@@ -330,8 +332,9 @@ __global__ void __launch_bounds__(TILE) k_pair32(PairArgs a) {
     }
     int4 m = a.tmeta[ti];
     surf_i = m.x;
-    if (m.y >= 0) ui = a.usph[m.y + a.nlat * m.z];
+    if (m.y >= 0) { ui = a.usph[m.y + a.nlat * m.z]; tlat = m.y; tlon = m.z; }
   }
+  const float* mrow = a.mtab32 ? a.mtab32 + (size_t)tlat * a.nlat * a.nhalf : nullptr;
   // this warp's target box
   float3 wlo0, whi0;
   {
@@ -411,7 +414,13 @@ __global__ void __launch_bounds__(TILE) k_pair32(PairArgs a) {
           if (r2 > a.rc2_f) continue;
           ++npairs;
           float wgt = 1.f;
-          if (sj == surf_i) {
+          if (sj == surf_i && mrow) {
+            // tabulated 1 - MaskFunc(DistOnSphere / radius) of the grid pair
+            const int idj = __float_as_int(p1.w);
+            int dl = abs((idj >> 16) - tlon);
+            dl = min(dl, a.nlon - dl);
+            wgt = __ldg(mrow + (idj & 0xffff) * a.nhalf + dl);
+          } else if (sj == surf_i) {
             const float4 u = a.su[cb + j];
             const float ex = ui.x - u.x, ey = ui.y - u.y, ez = ui.z - u.z;
             const float ch2 = ex * ex + ey * ey + ez * ez;
@@ -504,13 +513,13 @@ __global__ void __launch_bounds__(TILE) k_pair64(PairArgs a) {
   const double c0[3] = {(ci + 0.5) * a.h[0], (cj + 0.5) * a.h[1], (ck + 0.5) * a.h[2]};
   int ti = active ? a.torder[unit.y + tid] : 0;
   double t_[3] = {0, 0, 0};
-  int surf_i = -2;
+  int surf_i = -2, tlat = 0, tlon = 0;
   double th_i = 0, phi_i = 0;
   if (active) {
     for (int k = 0; k < 3; ++k) t_[k] = min_image(a.tx[ti + (size_t)k * a.nt] - c0[k], a.L[k], a.iL[k]);
     int4 m = a.tmeta[ti];
     surf_i = m.x;
-    if (m.y >= 0) { th_i = a.th[m.y]; phi_i = a.phi[m.z]; }
+    if (m.y >= 0) { th_i = a.th[m.y]; phi_i = a.phi[m.z]; tlat = m.y; tlon = m.z; }
   }
   // the same tile culling as the FP32 form (boxes in FP32 with a margin)
   const CullBoxes cb = cull_boxes(active, (float)t_[0], (float)t_[1], (float)t_[2], wb);
@@ -562,7 +571,11 @@ __global__ void __launch_bounds__(TILE) k_pair64(PairArgs a) {
           const double ir = rsqrt(r2), rr = r2 > 0. ? r2 * ir : 0.;
           ++npairs;
           double mask = 0.;
-          if (sj == surf_i) {
+          if (sj == surf_i && a.mtab64) {
+            int dl = abs(sm.ilon[j] - tlon);
+            dl = min(dl, a.nlon - dl);
+            mask = __ldg(a.mtab64 + ((size_t)tlat * a.nlat + sm.ilat[j]) * a.nhalf + dl);
+          } else if (sj == surf_i) {
             double dth = dist_on_sphere(th_i, phi_i, a.th[sm.ilat[j]], a.phi[sm.ilon[j]]);
             mask = mask64(a.T, dth * a.inv_radius);
           } else if (a.collect) {
@@ -831,6 +844,9 @@ rbc3d_status run_pair_sum(rbc3d_ctx* ctx, int tlist, double c1, double c2, int p
   a.sF4 = ctx->s_F4.p; a.sG4 = ctx->s_G4.p; a.toff = ctx->s_toff.p; a.tbox = ctx->s_tbox.p;
   for (int d = 0; d < 3; ++d) { a.Nc[d] = ctx->hg.Nc[d]; a.h[d] = ctx->hg.h[d]; a.L[d] = ctx->hg.L[d]; a.iL[d] = ctx->iLb[d]; }
   a.th = ctx->th.p; a.phi = ctx->phi.p; a.usph = ctx->usph.p; a.nlat = ctx->nlat;
+  a.nlon = ctx->nlon; a.nhalf = ctx->nlon / 2 + 1;
+  a.mtab64 = ctx->phi_uniform ? ctx->mtab64.p : nullptr;
+  a.mtab32 = ctx->phi_uniform ? ctx->mtab32.p : nullptr;
   a.radius = ctx->radius; a.inv_radius = 1.0 / ctx->radius; a.inv_radius_f = (float)(1.0 / ctx->radius);
   double cm = 2.0 * sin(0.5 * ctx->radius) * (1.0 + 1e-6);
   a.chord2_max = (float)(cm * cm);
