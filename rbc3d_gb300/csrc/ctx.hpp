@@ -149,8 +149,8 @@ struct rbc3d_ctx {
   // to the source's hash-cell centre (+ surf / id bits), unit-sphere point,
   // a3; c1 f and c2 g of the current call; per-cell tile offsets and boxes
   DBuf<float4> s_p0, s_p1, s_u4, s_a4, s_F4, s_G4;
-  DBuf<int> s_toff;
-  DBuf<float4> s_tbox;
+  DBuf<int> s_toff, s_coff;
+  DBuf<float4> s_tbox, s_cbox;  // per 128-source tile and per 32-source chunk
   int s_ntiles = 0;
   DBuf<unsigned long long> near_queue;  // work counter of the near-singular kernel
   DBuf<double> dBcoef;                  // Bcoef per cell type on the device

@@ -185,6 +185,8 @@ struct PairArgs {
   const float4* sG4;   // c2 g dS Bcoef
   const int* toff;     // per hash cell: first tile (TILE consecutive sources per tile)
   const float4* tbox;  // per tile: lo, hi (relative to the cell centre)
+  const int* coff;     // per hash cell: first 32-source chunk
+  const float4* cbox;  // per chunk: lo, hi
   // grid
   int Nc[3];
   double h[3], L[3], iL[3];
@@ -382,7 +384,12 @@ __global__ void __launch_bounds__(TILE) k_pair32(PairArgs a) {
       const float3 bl = make_float3(blo.x, blo.y, blo.z), bh = make_float3(bhi.x, bhi.y, bhi.z);
       if (boxes_apart(wlo, whi, bl, bh, a.rc2_f)) continue;  // uniform over the warp
       const int tend = min(base + TILE, send);
-      for (int cb = base; cb < tend; cb += 32) {
+      for (int cb = base, cc = a.coff[ncell] + (base - sbeg) / 32; cb < tend; cb += 32, ++cc) {
+        {
+          const float4 clo4 = a.cbox[2 * cc], chi4 = a.cbox[2 * cc + 1];
+          if (boxes_apart(wlo, whi, make_float3(clo4.x, clo4.y, clo4.z), make_float3(chi4.x, chi4.y, chi4.z), a.rc2_f))
+            continue;  // uniform over the warp
+        }
         const int cnt = min(32, tend - cb);
         __syncwarp();
         if (lane < cnt) {
@@ -774,12 +781,25 @@ rbc3d_status build_source_list(rbc3d_ctx* ctx) {
     std::vector<int> hs(nc), he(nc), toff(nc + 1, 0);
     CUDA_TRY(cudaMemcpy(hs.data(), ctx->s_cstart.p, sizeof(int) * nc, cudaMemcpyDeviceToHost));
     CUDA_TRY(cudaMemcpy(he.data(), ctx->s_cend.p, sizeof(int) * nc, cudaMemcpyDeviceToHost));
-    std::vector<int2> tiles;
+    std::vector<int2> tiles, chunks;
+    std::vector<int> coff(nc + 1, 0);
     for (int c = 0; c < nc; ++c) {
       toff[c] = (int)tiles.size();
+      coff[c] = (int)chunks.size();
       for (int b = hs[c]; b < he[c]; b += TILE) tiles.push_back(make_int2(b, std::min(TILE, he[c] - b)));
+      for (int b = hs[c]; b < he[c]; b += 32) chunks.push_back(make_int2(b, std::min(32, he[c] - b)));
     }
     toff[nc] = (int)tiles.size();
+    coff[nc] = (int)chunks.size();
+    CUDA_TRY(ctx->s_coff.upload(coff.data(), coff.size(), ctx->st));
+    CUDA_TRY(ctx->s_cbox.alloc(2 * chunks.size() + 2));
+    if (!chunks.empty()) {
+      DBuf<int2> dc;
+      CUDA_TRY(dc.upload(chunks.data(), chunks.size(), ctx->st));
+      { k_tile_boxes<<<(int)chunks.size(), 32, 0, ctx->st>>>(dc.p, ctx->s_p0.p, ctx->s_cbox.p); ++ctx->launches; }
+      CUDA_TRY(cudaGetLastError());
+      CUDA_TRY(cudaStreamSynchronize(ctx->st));
+    }
     ctx->s_ntiles = (int)tiles.size();
     CUDA_TRY(ctx->s_toff.upload(toff.data(), toff.size(), ctx->st));
     CUDA_TRY(ctx->s_tbox.alloc(2 * tiles.size() + 2));
@@ -842,6 +862,7 @@ rbc3d_status run_pair_sum(rbc3d_ctx* ctx, int tlist, double c1, double c2, int p
   a.cs = ctx->s_cstart.p; a.ce = ctx->s_cend.p;
   a.sp0 = ctx->s_p0.p; a.sp1 = ctx->s_p1.p; a.su = ctx->s_u4.p; a.sa4 = ctx->s_a4.p;
   a.sF4 = ctx->s_F4.p; a.sG4 = ctx->s_G4.p; a.toff = ctx->s_toff.p; a.tbox = ctx->s_tbox.p;
+  a.coff = ctx->s_coff.p; a.cbox = ctx->s_cbox.p;
   for (int d = 0; d < 3; ++d) { a.Nc[d] = ctx->hg.Nc[d]; a.h[d] = ctx->hg.h[d]; a.L[d] = ctx->hg.L[d]; a.iL[d] = ctx->iLb[d]; }
   a.th = ctx->th.p; a.phi = ctx->phi.p; a.usph = ctx->usph.p; a.nlat = ctx->nlat;
   a.nlon = ctx->nlon; a.nhalf = ctx->nlon / 2 + 1;
