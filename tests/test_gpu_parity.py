@@ -214,3 +214,19 @@ def test_fp32_modes_vs_fp64_full_size_c5(gpu):
         assert np.linalg.norm(v - v64) <= 1e-6 * np.linalg.norm(v64)
         assert abs(ctx.counts()["pairs_within_rc"] - n64) <= 1e-6 * n64  # only pairs at r = rc may differ
     ctx.close()
+
+
+@pytest.mark.parametrize("P", [4, 8])
+def test_pme_spline_orders(gpu, oracle, c1_case, P):
+    # the tiled spread is instantiated per spline order; each order against the
+    # oracle (even orders: with an odd order the SPME factor b(k) of the
+    # reference's PME_Init is singular at the Nyquist frequency)
+    prm, cells = c1_case
+    prm = dict(prm, P=P)
+    out = {}
+    for name, lib in (("o", oracle), ("g", gpu)):
+        ctx = setup(lib, prm, cells, dl=False)
+        out[name] = [ctx.matvec(TLIST_RBC, C, 0.0, TERM_PME, prec) for prec in ((FP64,) if name == "o" else (FP64, FP32C))]
+        ctx.close()
+    assert rel(out["g"][0], out["o"][0]) < 1e-12
+    assert rel(out["g"][1], out["o"][0]) < 1e-6
