@@ -202,6 +202,7 @@ def main():
     ap.add_argument("--quick", action="store_true", help="FP32C timing only (profiling)")
     ap.add_argument("--no-wall", action="store_true", help="skip the learned-guess wall GMRES comparison")
     ap.add_argument("--no-scaleup", action="store_true", help="skip the 2048-cell (PME 256^3) scale-up line")
+    ap.add_argument("--no-cellsolve", action="store_true", help="skip the cell velocity GMRES line")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     dist = dist_init()
@@ -398,14 +399,44 @@ def main():
     if not args.quick and not args.no_wall:
         from rbc3d_gb300.learned_run import run as wall_run
         t1 = time.perf_counter()
-        w = wall_run(ncell=64, warm_steps=12, test_steps=4, rtol=1e-8, restart=300, max_it=900, train_iters=30,
-                     seed=args.seed + rank)
+        w = wall_run(ncell=64, warm_steps=50, test_steps=6, rtol=1e-8, restart=300, max_it=900, train_iters=30,
+                     history=48, seed=args.seed + rank)
         log(f"wall GMRES comparison in {time.perf_counter() - t1:.1f}s")
         wall = {"workload": "C3 tube (R=8, L=48, 64 cells), FP64 matvec + FP64 Arnoldi, ||r|| < 1e-8 ||b||",
                 **{k: w[k] for k in ("wall_dof", "restart", "history", "plain", "history_only", "learned",
                                      "speedup_learned", "speedup_history_only", "train_ms_per_step",
                                      "speedup_learned_incl_training", "mlp")},
-                "steps": "12 warm-up steps (plain solves, history + online training), 4 compared steps"}
+                "steps": "50 warm-up steps (plain solves, history + online training), 6 compared steps"}
+        # the same run with mixed-precision solves (FP32M operator inside FP64 refinement, FP64 residual)
+        t1 = time.perf_counter()
+        wm = wall_run(ncell=64, warm_steps=50, test_steps=6, rtol=1e-8, restart=300, max_it=900, train_iters=30,
+                      history=48, seed=args.seed + rank, prec=FP32M)
+        log(f"mixed-precision wall GMRES comparison in {time.perf_counter() - t1:.1f}s")
+        wall["mixed_fp32m"] = {k: wm[k] for k in ("plain", "history_only", "learned", "speedup_learned",
+                                                  "speedup_history_only", "speedup_learned_incl_training")}
+        wall["mixed_fp32m"]["learned_over_fp64_plain"] = w["plain"]["ms"] / wm["learned"]["ms"]
+
+    # ---- cell velocity GMRES (Solve_RBC_Vel, degree 12, rtol 1e-11 as the reference
+    # sets it) on the same 256 cells: FP64 solve vs the mixed-precision solves
+    cellsolve = None
+    if not args.quick and not args.no_cellsolve:
+        t1 = time.perf_counter()
+        arms = {}
+        for name, p in (("fp64", FP64), ("fp32m", FP32M), ("fp32c", FP32C)):
+            sol, v, st, code = ctx.solve_rbc_vel(12, rtol=1e-11, max_it=300, restart=30, prec=p, check=False)
+            arms[name] = (sol, v, st, code)
+        s64, v64 = arms["fp64"][0], arms["fp64"][1]
+        cellsolve = {"workload": "Solve_RBC_Vel on the 256-cell workload (viscRat 5, SH degree 12, "
+                                 f"{3 * 144 * 256} unknowns), restart 30, ||r|| < 1e-11 ||b|| (FP64 residual)"}
+        for name, (sol, v, st, code) in arms.items():
+            cellsolve[name] = {"ms": st.ms, "iterations": st.iterations, "matvecs": st.matvecs,
+                               "refinements": st.refinements, "status": code,
+                               "final_rel_residual": st.rnorm / st.bnorm if st.bnorm > 0 else 0.0,
+                               "rel_l2_vs_fp64_solution": float(np.linalg.norm(sol - s64) / np.linalg.norm(s64)),
+                               "rel_l2_vs_fp64_velocity": float(np.linalg.norm(v - v64) / np.linalg.norm(v64))}
+        for name in ("fp32m", "fp32c"):
+            cellsolve[name]["speedup_vs_fp64"] = arms["fp64"][2].ms / arms[name][2].ms
+        log(f"cell solve comparison in {time.perf_counter() - t1:.1f}s")
 
     # ---- CPU baseline (rank 0, N = 1 only): oracle, all host threads
     cpu = None
@@ -444,6 +475,7 @@ def main():
                                              "fp32m does it in FP32 with hi/lo geometry"},
             "scaleup_c5": scale,
             "wall_gmres": wall,
+            "cell_gmres": cellsolve,
             "fma_peaks_tflops": {"fp32": peak32, "fp64": peak64},
             "cpu_baseline": cpu,
             "gpu_launches": launches,

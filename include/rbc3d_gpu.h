@@ -107,7 +107,11 @@ typedef struct rbc3d_solve_opts {
                     (KSPSetTolerances rtol, KSPConvergedDefault) */
   int max_it;    /* KSPSetTolerances max_it */
   int restart;   /* GMRES restart (PETSc default 30) */
-  int prec;      /* matvec arithmetic, RBC3D_FP64 or RBC3D_FP32C */
+  int prec;      /* matvec arithmetic: RBC3D_FP64, or an FP32 mode
+                    (RBC3D_FP32C, RBC3D_FP32M) for a mixed-precision solve:
+                    inner GMRES cycles with the FP32 operator correct x
+                    against the FP64 residual b - A x (iterative refinement),
+                    and convergence is judged on that FP64 residual */
   int guess;     /* 0: zero increment (reference); 1: caller-supplied guess;
                     2: caller-supplied guess scaled by a = <b,Ax0>/||Ax0||^2
                     (never a larger initial residual than 0);
@@ -123,7 +127,8 @@ typedef struct rbc3d_solve_stats {
   double rnorm;        /* final residual norm (true residual, recomputed) */
   double bnorm;
   double ms;           /* wall time of the solve */
-  int matvecs;
+  int matvecs;         /* operator applications, FP64 and FP32 */
+  int refinements;     /* mixed-precision solves: FP32 corrections applied (0 for FP64) */
 } rbc3d_solve_stats;
 
 typedef struct rbc3d_ctx rbc3d_ctx;

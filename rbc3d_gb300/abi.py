@@ -44,7 +44,7 @@ class SolveOpts(C.Structure):
 class SolveStats(C.Structure):
     _fields_ = [("iterations", C.c_int), ("converged", C.c_int), ("rnorm0", C.c_double),
                 ("rnorm", C.c_double), ("bnorm", C.c_double), ("ms", C.c_double),
-                ("matvecs", C.c_int)]
+                ("matvecs", C.c_int), ("refinements", C.c_int)]
 
 
 class RBC3DError(RuntimeError):
@@ -318,13 +318,14 @@ class Context:
             self._check(code)
         return st, code
 
-    def solve_rbc_vel(self, nlat0, rtol=1e-11, max_it=200, restart=30, sol=None, check=True):
+    def solve_rbc_vel(self, nlat0, rtol=1e-11, max_it=200, restart=30, sol=None, check=True, prec=FP64):
         """Solve_RBC_Vel: returns (sol, v (N,3) as (3,N) SoA, stats, code).  sol, when
         given, is the warm start (the reference keeps its solution vector
-        between calls, KSPSetInitialGuessNonzero)."""
+        between calls, KSPSetInitialGuessNonzero).  prec FP32C / FP32M: the
+        mixed-precision solve (FP32 operator inside, FP64 residual)."""
         n = self.L.fn["cell_dof"](self.h, nlat0)
         x = np.zeros(n) if sol is None else f64(sol).copy()
-        o = SolveOpts(rtol=rtol, max_it=max_it, restart=restart, prec=FP64, guess=0 if sol is None else 1)
+        o = SolveOpts(rtol=rtol, max_it=max_it, restart=restart, prec=prec, guess=0 if sol is None else 1)
         st = SolveStats()
         N = self.L.fn["num_targets"](self.h, 0)
         v = np.zeros(3 * N)

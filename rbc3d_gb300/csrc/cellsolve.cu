@@ -295,7 +295,9 @@ extern "C" rbc3d_status rbc3d_solve_rbc_vel(rbc3d_ctx* ctx, const rbc3d_solve_op
   if (!ctx || !o || !v) return RBC3D_ERR_ARG;
   if (nlat0 < 1 || nlat0 > ctx->nlat || 2 * (nlat0 - 1) >= ctx->nlon || (ctx->nlon % 2) != 0)
     return ctx_fail(ctx, RBC3D_ERR_ARG, "solve_rbc_vel: need 1 <= nlat0 <= nlat, 2 (nlat0 - 1) < nlon, even nlon");
-  if (o->rtol < 0 || o->max_it < 0 || (o->guess && !sol)) return ctx_fail(ctx, RBC3D_ERR_ARG, "solve_rbc_vel: bad options");
+  if (o->rtol < 0 || o->max_it < 0 || (o->guess && !sol) || !valid_prec(o->prec))
+    return ctx_fail(ctx, RBC3D_ERR_ARG, "solve_rbc_vel: bad options");
+  const bool mixed = o->prec != RBC3D_FP64;  // FP32 operator inside an FP64 refinement loop
   if (ctx->npt == 0) return RBC3D_OK;
   auto t0 = std::chrono::steady_clock::now();
   rbc3d_solve_stats S{};
@@ -325,15 +327,17 @@ extern "C" rbc3d_status rbc3d_solve_rbc_vel(rbc3d_ctx* ctx, const rbc3d_solve_op
     else CUDA_TRY(cudaMemsetAsync(x.p, 0, sizeof(double) * n, ctx->st));
     // MyMatMult (:523-601)
     const unsigned dl_terms = RBC3D_TERM_REAL | RBC3D_TERM_CORR | RBC3D_TERM_LINEAR | RBC3D_TERM_PME;
-    auto matvec = [&](const double* u, double* y) -> rbc3d_status {
+    auto matvec_p = [&](const double* u, double* y, int prec) -> rbc3d_status {
       S.matvecs++;
       rbc3d_status e;
       if ((e = sh_synth(ctx, T, u, g.p, false))) return e;
       if ((e = set_g_device(ctx, T, g.p, cg, fe))) return e;
-      if ((e = matvec_dev(ctx, RBC3D_TLIST_RBC, 0.0, -ip4, dl_terms, RBC3D_FP64))) return e;
+      if ((e = matvec_dev(ctx, RBC3D_TLIST_RBC, 0.0, -ip4, dl_terms, prec))) return e;
       { k_axpby<<<cs_nblk(3 * N, 256), 256, 0, ctx->st>>>((int)(3 * N), 1.0, g.p, 1.0, t.v.p); ++ctx->launches; }
       return sh_anal(ctx, T, t.v.p, nullptr, y);
     };
+    auto matvec = [&](const double* u, double* y) { return matvec_p(u, y, RBC3D_FP64); };
+    auto matvec32 = [&](const double* u, double* y) { return matvec_p(u, y, o->prec); };
     DBuf<double> w;
     CUDA_TRY(w.alloc(n));
     if ((s = matvec(x.p, w.p))) return s;
@@ -343,7 +347,11 @@ extern "C" rbc3d_status rbc3d_solve_rbc_vel(rbc3d_ctx* ctx, const rbc3d_solve_op
     S.rnorm0 = beta;
     S.bnorm = dev_norm(ctx, n, b.p, tmp.p);
     const double ttol = std::max(o->rtol * S.bnorm, 1e-50);
-    if ((s = gmres_cycles(ctx, n, matvec, b.p, x.p, r.p, beta, ttol, o->max_it, R, S))) return s;
+    if (mixed) {
+      if ((s = gmres_ir(ctx, n, matvec, matvec32, b.p, x.p, r.p, beta, ttol, o->max_it, R, RBC3D_IR_ETA, S))) return s;
+    } else if ((s = gmres_cycles(ctx, n, matvec, b.p, x.p, r.p, beta, ttol, o->max_it, R, S))) {
+      return s;
+    }
   }
   // the surface velocities; rbc%g and its spline are left at the solution
   if ((s = sh_synth(ctx, T, x.p, g.p, false))) return s;

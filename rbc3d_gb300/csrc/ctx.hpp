@@ -243,6 +243,9 @@ rbc3d_status self_mixed_geom(rbc3d_ctx* ctx, const double* x_host);
 rbc3d_status self_mixed_density(rbc3d_ctx* ctx, bool f, bool g);
 rbc3d_status run_self_mixed(rbc3d_ctx* ctx, int tlist, double c1, double c2);
 inline bool valid_prec(int p) { return p == RBC3D_FP64 || p == RBC3D_FP32C || p == RBC3D_FP32M; }
+// mixed-precision solves: relative residual reduction asked of each inner
+// FP32 GMRES solve (well above the FP32 operators' ~3e-7 relative error)
+constexpr double RBC3D_IR_ETA = 1e-5;
 
 // peak.cu
 rbc3d_status fma_peak(int prec, double* tflops);

@@ -150,4 +150,50 @@ rbc3d_status gmres_cycles(rbc3d_ctx* ctx, int n, MV&& matvec, const double* b, d
   return RBC3D_OK;
 }
 
+// Mixed-precision solve (GMRES with iterative refinement): the residual
+// r = b - A x is formed with the FP64 operator (mv64) and the correction
+// A d = r is solved by inner GMRES cycles on the FP32 operator (mv32, FP64
+// Arnoldi and Hessenberg) to a relative reduction eta, then x += d.  Each
+// refinement lowers the FP64 residual by about max(eta, the FP32 operator's
+// relative error), so the solve reaches the same ||b - A x|| < ttol as the FP64
+// solve, judged by the FP64 residual.  On entry r and beta hold the FP64
+// residual of x.  S.iterations counts the inner iterations, S.refinements the
+// corrections.
+template <class MV64, class MV32>
+rbc3d_status gmres_ir(rbc3d_ctx* ctx, int n, MV64&& mv64, MV32&& mv32, const double* b, double* x, double* r,
+                      double beta, double ttol, int max_it, int R, double eta, rbc3d_solve_stats& S) {
+  DBuf<double> rhs, d, ri, w;
+  CUDA_TRY(rhs.alloc(n)); CUDA_TRY(d.alloc(n)); CUDA_TRY(ri.alloc(n)); CUDA_TRY(w.alloc(n));
+  rbc3d_status s;
+  int its = 0, refinements = 0;
+  const int max_refine = 32;
+  bool conv = beta <= ttol;
+  while (!conv && its < max_it && refinements < max_refine) {
+    // inner: A32 d = r from d = 0, to max(eta ||r||, ttol / 2)
+    CUDA_TRY(cudaMemcpyAsync(rhs.p, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->st));
+    CUDA_TRY(cudaMemcpyAsync(ri.p, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->st));
+    CUDA_TRY(cudaMemsetAsync(d.p, 0, sizeof(double) * n, ctx->st));
+    rbc3d_solve_stats Si{};
+    if ((s = gmres_cycles(ctx, n, mv32, rhs.p, d.p, ri.p, beta, std::max(eta * beta, 0.5 * ttol), max_it - its, R, Si)))
+      return s;
+    its += Si.iterations;
+    ++refinements;
+    { k_axpby<<<gm_nblk(n, 256), 256, 0, ctx->st>>>(n, 1.0, d.p, 1.0, x); ++ctx->launches; }
+    // FP64 residual of the corrected x
+    if ((s = mv64(x, w.p))) return s;
+    CUDA_TRY(cudaMemcpyAsync(r, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->st));
+    { k_axpby<<<gm_nblk(n, 256), 256, 0, ctx->st>>>(n, -1.0, w.p, 1.0, r); ++ctx->launches; }
+    const double nb = dev_norm(ctx, n, r, w.p);
+    if (!(nb < beta) && Si.iterations == 0) { beta = nb; break; }  // no progress possible
+    beta = nb;
+    conv = beta <= ttol;
+  }
+  S.iterations = its;
+  S.refinements = refinements;
+  S.converged = conv ? 1 : 0;
+  S.rnorm = beta;
+  CUDA_TRY(cudaGetLastError());
+  return RBC3D_OK;
+}
+
 }  // namespace

@@ -31,22 +31,28 @@ struct GemmArgs {
   int ldc;
   const float* bias;       // per column n (EPI 1, 2)
   __nv_bfloat16* Abf;      // EPI 1: SiLU(z) in BF16, row-major ldc
+  int ksplit;              // EPI 0: K split over gridDim.z; partial tiles to ws[z][M][N]
+  float* ws;
 };
 
 __device__ __forceinline__ float silu(float z) { return z / (1.f + expf(-z)); }
 
 // ---------------------------------------------------------------------------
 // tcgen05 GEMM: 128 x 128 output tile per CTA, K staged 64 at a time into a
-// double-buffered shared-memory ring in the canonical no-swizzle K-major
-// layout (8-row x 16-byte core matrices: element (r, k) at byte
+// UNST-deep shared-memory ring (cp.async 16-byte copies, UNST - 1 stages in
+// flight while the tensor core works on the oldest) in the canonical no-swizzle
+// K-major layout (8-row x 16-byte core matrices: element (r, k) at byte
 // ((r/8)*8 + k/8)*128 + (r%8)*16 + (k%8)*2, so core matrices adjacent in K are
 // 128 B apart and 8-row groups 1024 B apart), one elected thread issuing
 // tcgen05.mma.cta_group::1.kind::f16 (M 128, N 128, K 16, BF16 in, FP32
 // accumulate in 128 TMEM columns) and committing each stage to an mbarrier;
 // the four warps read their 32 accumulator rows back with tcgen05.ld and run
-// the epilogue.  Operands are gathered with generic strides (16-byte vectors
-// when k or m is contiguous), so one kernel serves x W^T, dz^T a and dz W.
-constexpr int UBM = 128, UBN = 128, UBK = 64;
+// the epilogue.  Operands are gathered with generic strides (asynchronous
+// 16-byte copies when k is contiguous, else synchronous gathers), so one kernel
+// serves x W^T, dz^T a and dz W.  GEMMs with few output tiles and a long K (the
+// weight gradients, K = batch rows) split K over gridDim.z; the partial tiles
+// are summed in a fixed order by k_splitk_sum.
+constexpr int UBM = 128, UBN = 128, UBK = 64, UNST = 4;
 constexpr int USTAGE = UBM * UBK * 2;  // bytes per operand per stage (16 KB)
 constexpr unsigned UMMA_IDESC = (1u << 4)              // D: FP32
                                 | (1u << 7)            // A: BF16
@@ -75,6 +81,25 @@ __device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
     if (done) return true;
   }
   return false;
+}
+
+__device__ __forceinline__ bool umma_async_ok(const __nv_bfloat16* X, long long sr, long long sk, int K) {
+  return sk == 1 && (sr % 8) == 0 && (K % 8) == 0 && ((reinterpret_cast<size_t>(X) & 15) == 0);
+}
+
+// asynchronous form of the k-contiguous stage (umma_async_ok): one 16-byte
+// cp.async per core-matrix row, zero-filled outside rows x K
+__device__ __forceinline__ void umma_stage_async(unsigned dst, const __nv_bfloat16* X, long long sr, int rows, int K,
+                                                 int r0, int k0) {
+  for (int e = threadIdx.x; e < UBM * (UBK / 8); e += blockDim.x) {
+    const int r = e / (UBK / 8), k8 = e % (UBK / 8);
+    const int gr = r0 + r, gk = k0 + 8 * k8;
+    const bool in = gr < rows && gk < K;  // K % 8 == 0: a vector is wholly in or out
+    const __nv_bfloat16* src = in ? X + (long long)gr * sr + gk : X;
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst + ((r >> 3) * 8 + k8) * 128 + (r & 7) * 16),
+                 "l"(src), "r"(in ? 16 : 0)
+                 : "memory");
+  }
 }
 
 // stage rows [r0, r0+128) x k [k0, k0+64) of X (element (r, k) at X[r*sr + k*sk],
@@ -124,9 +149,9 @@ __device__ __forceinline__ void umma_stage(unsigned char* dst, const __nv_bfloat
 template <int EPI>
 __global__ void __launch_bounds__(128) k_umma(GemmArgs g, int* err) {
   extern __shared__ __align__(1024) unsigned char usm[];
-  unsigned char* As = usm;                 // 2 stages
-  unsigned char* Bs = usm + 2 * USTAGE;    // 2 stages
-  __shared__ __align__(8) unsigned long long mbar[2];
+  unsigned char* As = usm;                    // UNST stages
+  unsigned char* Bs = usm + UNST * USTAGE;    // UNST stages
+  __shared__ __align__(8) unsigned long long mbar[UNST];
   __shared__ unsigned tmem_slot;
   const int tid = threadIdx.x, warp = tid >> 5;
   const int m0 = blockIdx.y * UBM, n0 = blockIdx.x * UBN;
@@ -136,23 +161,34 @@ __global__ void __launch_bounds__(128) k_umma(GemmArgs g, int* err) {
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
   }
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[0])));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[1])));
+    for (int b = 0; b < UNST; ++b) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[b])));
     asm volatile("fence.mbarrier_init.release.cluster;\n");
   }
   asm volatile("tcgen05.fence::before_thread_sync;\n");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n");
   const unsigned taddr = tmem_slot;
-  const int nk = (g.K + UBK - 1) / UBK;
+  // this CTA's K chunks [kb, ke)
+  const int nkall = (g.K + UBK - 1) / UBK;
+  const int kb = (int)((long long)nkall * blockIdx.z / gridDim.z), ke = (int)((long long)nkall * (blockIdx.z + 1) / gridDim.z);
+  const int nk = ke - kb;
+  const bool asyncA = umma_async_ok(g.A, g.sam, g.sak, g.K), asyncB = umma_async_ok(g.B, g.sbn, g.sbk, g.K);
+  // A: rows m (sam), k (sak);  B as [n][k]: rows n (sbn), k (sbk)
+  auto issue = [&](int c) {
+    const int buf = c % UNST, k0 = (kb + c) * UBK;
+    if (asyncA) umma_stage_async(smem_u32(As + buf * USTAGE), g.A, g.sam, g.M, g.K, m0, k0);
+    else umma_stage(As + buf * USTAGE, g.A, g.sam, g.sak, g.M, g.K, m0, k0);
+    if (asyncB) umma_stage_async(smem_u32(Bs + buf * USTAGE), g.B, g.sbn, g.N, g.K, n0, k0);
+    else umma_stage(Bs + buf * USTAGE, g.B, g.sbn, g.sbk, g.N, g.K, n0, k0);
+  };
   bool ok = true;
-  for (int kc = 0; kc < nk; ++kc) {
-    const int buf = kc & 1;
-    // the stage's previous MMAs (chunk kc - 2) must be done before it is overwritten
-    if (kc >= 2 && !mbar_wait(smem_u32(&mbar[buf]), ((kc - 2) >> 1) & 1)) ok = false;
-    // A: rows m (sam), k (sak);  B as [n][k]: rows n (sbn), k (sbk)
-    umma_stage(As + buf * USTAGE, g.A, g.sam, g.sak, g.M, g.K, m0, kc * UBK);
-    umma_stage(Bs + buf * USTAGE, g.B, g.sbn, g.sbk, g.N, g.K, n0, kc * UBK);
+  for (int c = 0; c < UNST - 1; ++c) {
+    if (c < nk) issue(c);
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+  }
+  for (int c = 0; c < nk; ++c) {
+    const int buf = c % UNST;
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(UNST - 2) : "memory");  // chunk c has landed
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     __syncthreads();
     if (tid == 0) {
@@ -161,7 +197,7 @@ __global__ void __launch_bounds__(128) k_umma(GemmArgs g, int* err) {
 #pragma unroll
       for (int j = 0; j < UBK / 16; ++j) {
         const unsigned long long da = umma_desc(a0 + j * 256), db = umma_desc(b0 + j * 256);
-        const unsigned acc = (kc > 0 || j > 0) ? 1u : 0u;
+        const unsigned acc = (c > 0 || j > 0) ? 1u : 0u;
         asm volatile(
             "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
             " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(taddr),
@@ -170,9 +206,17 @@ __global__ void __launch_bounds__(128) k_umma(GemmArgs g, int* err) {
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
           smem_u32(&mbar[buf])));
     }
+    // refill the buffer of chunk c - 1 with chunk c + UNST - 1 once chunk c - 1's MMAs are done
+    const int nx = c + UNST - 1;
+    if (nx < nk) {
+      if (c >= 1 && !mbar_wait(smem_u32(&mbar[(c - 1) % UNST]), ((c - 1) / UNST) & 1)) ok = false;
+      issue(nx);
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
   }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
   // all MMAs done: the last commit tracks every earlier MMA of the thread
-  if (nk > 0 && !mbar_wait(smem_u32(&mbar[(nk - 1) & 1]), ((nk - 1) >> 1) & 1)) ok = false;
+  if (nk > 0 && !mbar_wait(smem_u32(&mbar[(nk - 1) % UNST]), ((nk - 1) / UNST) & 1)) ok = false;
   asm volatile("tcgen05.fence::after_thread_sync;\n");
   if (!ok) {
     if (tid == 0) atomicExch(err, 1);
@@ -194,8 +238,10 @@ __global__ void __launch_bounds__(128) k_umma(GemmArgs g, int* err) {
         float v[32];
 #pragma unroll
         for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]) + ((EPI != 0 && n0 + c0 + q < g.N) ? g.bias[n0 + c0 + q] : 0.f);
-        float* crow = g.C + (long long)row * g.ldc + n0 + c0;
-        const bool vec = n0 + c0 + 32 <= g.N && (g.ldc % 8) == 0 && ((reinterpret_cast<size_t>(crow) & 15) == 0) &&
+        const bool part = EPI == 0 && g.ksplit > 1;
+        const int ldc = part ? g.N : g.ldc;
+        float* crow = (part ? g.ws + (long long)blockIdx.z * g.M * g.N : g.C) + (long long)row * ldc + n0 + c0;
+        const bool vec = n0 + c0 + 32 <= g.N && (ldc % 8) == 0 && ((reinterpret_cast<size_t>(crow) & 15) == 0) &&
                          (EPI != 1 || ((reinterpret_cast<size_t>(g.Abf + (long long)row * g.ldc + n0 + c0) & 15) == 0));
         if (vec) {
           // a row segment of 32: 8 float4 (and 4 x 8 bf16) stores
@@ -227,6 +273,15 @@ __global__ void __launch_bounds__(128) k_umma(GemmArgs g, int* err) {
   asm volatile("tcgen05.fence::before_thread_sync;\n");
   __syncthreads();
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(UBN));
+}
+
+// C[m][n] = sum over z of ws[z][m][n] (the split-K partial tiles, fixed order)
+__global__ void k_splitk_sum(int M, int N, int S, const float* __restrict__ ws, float* __restrict__ C, int ldc) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x, MN = (long long)M * N;
+  if (i >= MN) return;
+  float s = 0.f;
+  for (int z = 0; z < S; ++z) s += ws[z * MN + i];
+  C[(i / N) * ldc + i % N] = s;
 }
 
 __global__ void k_to_bf16(long long n, const float* __restrict__ x, __nv_bfloat16* __restrict__ y) {
@@ -324,6 +379,7 @@ struct rbc3d_mlp {
   cudaStream_t st = nullptr;
   long long launches = 0;
   DBuf<int> err;  // set by a GEMM whose mbarrier wait ran out
+  DBuf<float> WS;  // split-K partial tiles
 };
 
 namespace {
@@ -348,9 +404,22 @@ rbc3d_status mlp_ensure(rbc3d_mlp* m, int n) {
 void gemm(rbc3d_mlp* m, int epi, int M, int N, int K, const __nv_bfloat16* A, long long sam, long long sak,
           const __nv_bfloat16* B, long long sbk, long long sbn, float* C, int ldc, const float* bias,
           __nv_bfloat16* Abf) {
-  GemmArgs g{M, N, K, A, sam, sak, B, sbk, sbn, C, ldc, bias, Abf};
+  GemmArgs g{M, N, K, A, sam, sak, B, sbk, sbn, C, ldc, bias, Abf, 1, nullptr};
   dim3 grid((N + UBN - 1) / UBN, (M + UBM - 1) / UBM);
-  const int smem = 4 * USTAGE;
+  // weight gradients (few tiles, K = batch rows): split K to fill the SMs
+  const int tiles = grid.x * grid.y, nk = (K + UBK - 1) / UBK;
+  if (epi == 0 && tiles < 76 && nk >= 4) {
+    int sm = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev);
+    const int S = std::min(nk, std::max(1, sm / tiles));
+    if (S > 1 && !m->WS.alloc((size_t)S * M * N)) {
+      g.ksplit = S;
+      g.ws = m->WS.p;
+      grid.z = S;
+    }
+  }
+  const int smem = 2 * UNST * USTAGE;
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_umma<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -362,6 +431,10 @@ void gemm(rbc3d_mlp* m, int epi, int M, int N, int K, const __nv_bfloat16* A, lo
   else if (epi == 1) k_umma<1><<<grid, 128, smem, m->st>>>(g, m->err.p);
   else k_umma<2><<<grid, 128, smem, m->st>>>(g, m->err.p);
   ++m->launches;
+  if (g.ksplit > 1) {
+    k_splitk_sum<<<nblk((long long)M * N, 256), 256, 0, m->st>>>(M, N, g.ksplit, g.ws, C, ldc);
+    ++m->launches;
+  }
 }
 
 void transpose(rbc3d_mlp* m, int rows, int cols, const __nv_bfloat16* in, __nv_bfloat16* out) {

@@ -536,13 +536,15 @@ rbc3d_status wall_solve(rbc3d_ctx* ctx, const rbc3d_solve_opts* o, const double*
   rbc3d_solve_stats S{};
   const int n = W.ndof, R = o->restart > 0 ? o->restart : 30;
   const int prec = o->prec;
+  if (!valid_prec(prec)) return ctx_fail(ctx, RBC3D_ERR_ARG, "no_slip_wall: bad precision mode");
+  const bool mixed = prec != RBC3D_FP64;  // FP32 operator inside an FP64 refinement loop
   DBuf<double> b, x, r, w, f0, tmp;
   CUDA_TRY(b.alloc(n)); CUDA_TRY(x.alloc(n)); CUDA_TRY(r.alloc(n)); CUDA_TRY(w.alloc(n));
   CUDA_TRY(f0.alloc(3 * (size_t)W.nvert)); CUDA_TRY(tmp.alloc(8));
   CUDA_TRY(cudaMemcpyAsync(f0.p, W.f.p, sizeof(double) * 3 * W.nvert, cudaMemcpyDeviceToDevice, ctx->st));
   rbc3d_status s;
-  // rhs = -assemble(residual velocity)
-  if ((s = wall_residual_dev(ctx, prec))) return s;
+  // rhs = -assemble(residual velocity), FP64 in the mixed-precision solve
+  if ((s = wall_residual_dev(ctx, mixed ? RBC3D_FP64 : prec))) return s;
   { k_assemble<<<nblk(W.nvert, 256), 256, 0, ctx->st>>>(W.nvert, W.glb.p, W.writer.p, ctx->tl[RBC3D_TLIST_WALL].v.p, -1.0,
                                                        b.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
@@ -599,12 +601,25 @@ rbc3d_status wall_solve(rbc3d_ctx* ctx, const rbc3d_solve_opts* o, const double*
     { k_axpby<<<nblk(n, 256), 256, 0, ctx->st>>>(n, -p, w.p, 1.0, r.p); ++ctx->launches; }
     { k_axpby<<<nblk(n, 256), 256, 0, ctx->st>>>(n, -q, w2.p, 1.0, r.p); ++ctx->launches; }
   }
+  auto matvec64 = [&](const double* in, double* out) -> rbc3d_status {
+    S.matvecs++;
+    return wall_matmult_dev(ctx, RBC3D_FP64, in, out);
+  };
+  if (mixed) {  // the initial residual of the guess with the FP64 operator
+    if ((s = matvec64(x.p, w.p))) return s;
+    CUDA_TRY(cudaMemcpyAsync(r.p, b.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->st));
+    { k_axpby<<<nblk(n, 256), 256, 0, ctx->st>>>(n, -1.0, w.p, 1.0, r.p); ++ctx->launches; }
+  }
   const double beta = dev_norm(ctx, n, r.p, tmp.p);
   S.rnorm0 = beta;
   S.bnorm = dev_norm(ctx, n, b.p, tmp.p);
   // KSPConvergedDefault: ||r|| < max(rtol * ||b||, abstol), ||b|| of the right-hand side
   const double ttol = std::max(o->rtol * S.bnorm, 1e-50);
-  if ((s = gmres_cycles(ctx, n, matvec, b.p, x.p, r.p, beta, ttol, o->max_it, R, S))) return s;
+  if (mixed) {
+    if ((s = gmres_ir(ctx, n, matvec64, matvec, b.p, x.p, r.p, beta, ttol, o->max_it, R, RBC3D_IR_ETA, S))) return s;
+  } else if ((s = gmres_cycles(ctx, n, matvec, b.p, x.p, r.p, beta, ttol, o->max_it, R, S))) {
+    return s;
+  }
   // wall f = f0 + expand(x)
   { k_expand<<<nblk(W.nvert, 256), 256, 0, ctx->st>>>(W.nvert, W.glb.p, x.p, W.f.p); ++ctx->launches; }
   { k_axpby<<<nblk(3 * W.nvert, 256), 256, 0, ctx->st>>>(3 * W.nvert, 1.0, f0.p, 1.0, W.f.p); ++ctx->launches; }

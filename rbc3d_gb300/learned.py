@@ -28,7 +28,7 @@ import time
 
 import numpy as np
 
-from .abi import RBC3DError, _ptr
+from .abi import FP64, RBC3DError, _ptr
 
 _fp = C.POINTER(C.c_float)
 _dp = C.POINTER(C.c_double)
@@ -156,7 +156,7 @@ class WallGuess:
     """Online-trained initial guess for rbc3d_no_slip_wall (history
     projection + MLP correction of the remainder)."""
 
-    def __init__(self, lib, wall, width=512, depth=4, seed=0, history=6, buffer_steps=32, nlap=2):
+    def __init__(self, lib, wall, width=512, depth=4, seed=0, history=48, buffer_steps=32, nlap=2):
         self.nlap = nlap
         self.mlp = MLP(lib, 3 * (nlap + 2), width, depth, 3, seed)
         self.fn = self.mlp.fn
@@ -245,8 +245,10 @@ class WallGuess:
         return xh, np.ascontiguousarray(self._to_global(y.astype(np.float64) * (self.k * sr)).reshape(-1))
 
     def rhs(self, ctx, prec):
+        # the solves' right-hand side is FP64 in every mode (the mixed-precision
+        # solves form b and their residuals with the FP64 operator)
         b = np.empty(3 * self.nv)
-        st = self.fn["rbc3d_wall_rhs"](ctx.h, prec, b.ctypes.data_as(_dp))
+        st = self.fn["rbc3d_wall_rhs"](ctx.h, FP64, b.ctypes.data_as(_dp))
         if st:
             raise RBC3DError(st, "rbc3d_wall_rhs")
         return b

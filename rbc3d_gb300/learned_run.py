@@ -11,7 +11,7 @@ plain, history guess only, history + network guess -- and iterations, times
 and final residuals are compared.  The plain solution continues the run and
 is recorded for the guess, so all arms see the same states.
 
-    python -m rbc3d_gb300.learned_run --cells 64 --warm 30 --test 10
+    python -m rbc3d_gb300.learned_run --cells 64 --warm 50 --test 10
 """
 from __future__ import annotations
 
@@ -23,7 +23,7 @@ import numpy as np
 
 from . import geometry as G
 from . import library
-from .abi import FP64, Context
+from .abi import FP32C, FP32M, FP64, Context
 from .learned import WallGuess
 
 
@@ -34,7 +34,7 @@ def _unique_increment(wall, f1, f0):
 
 
 def run(ncell=64, warm_steps=30, test_steps=10, rtol=1e-8, restart=100, max_it=800, dt=5e-3, umax=8.0,
-        train_iters=10, width=512, depth=4, history=6, seed=20261203, prec=FP64, log=None):
+        train_iters=10, width=512, depth=4, history=48, seed=20261203, prec=FP64, log=None):
     prm, cells, wall = G.config("C3", seed=seed, ncell=ncell)
     lib = library()
     ctx = Context(lib, prm)
@@ -106,9 +106,14 @@ def run(ncell=64, warm_steps=30, test_steps=10, rtol=1e-8, restart=100, max_it=8
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--cells", type=int, default=64)
-    ap.add_argument("--warm", type=int, default=30)
+    ap.add_argument("--warm", type=int, default=50)
     ap.add_argument("--test", type=int, default=10)
-    ap.add_argument("--restart", type=int, default=100)
-    ap.add_argument("--train-iters", type=int, default=10)
+    ap.add_argument("--restart", type=int, default=300)
+    ap.add_argument("--train-iters", type=int, default=30)
+    ap.add_argument("--history", type=int, default=48)
+    ap.add_argument("--prec", choices=("fp64", "fp32c", "fp32m"), default="fp64",
+                    help="operator arithmetic of every arm (FP32 modes: mixed-precision solves)")
     a = ap.parse_args()
-    print(json.dumps(run(a.cells, a.warm, a.test, restart=a.restart, train_iters=a.train_iters, log=print)))
+    prec = {"fp64": FP64, "fp32c": FP32C, "fp32m": FP32M}[a.prec]
+    print(json.dumps(run(a.cells, a.warm, a.test, restart=a.restart, train_iters=a.train_iters, history=a.history,
+                         prec=prec, log=print)))

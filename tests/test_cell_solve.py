@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from rbc3d_gb300 import geometry as G
-from rbc3d_gb300.abi import Context
+from rbc3d_gb300.abi import FP32C, FP32M, FP64, Context
 
 _dp = ctypes.POINTER(ctypes.c_double)
 NLAT0 = 12  # spherical-harmonic degree < 12 on the 25 x 50 grid
@@ -130,3 +130,22 @@ def test_gpu_cell_solve_matches_oracle(gpu, oracle, visc):
     assert abs(stg.iterations - sto.iterations) <= 1
     assert np.linalg.norm(vg - vo) <= 1e-9 * np.linalg.norm(vo)
     assert np.linalg.norm(sg - so) <= 1e-9 * np.linalg.norm(so)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [FP32C, FP32M])
+def test_gpu_cell_solve_mixed_precision(gpu, prec):
+    # FP32 double-layer operator inside FP64 refinement, to the reference's 1e-11
+    prm, cells = _small(ncell=3, visc=5.0)
+    out = {}
+    for p in (FP64, prec):
+        ctx = Context(gpu, prm)
+        ctx.set_cells(cells)
+        ctx.set_cell_density(f=cells.f, spl_F=cells.spl_F)
+        out[p] = ctx.solve_rbc_vel(NLAT0, rtol=1e-11, max_it=200, restart=30, prec=p)
+        ctx.close()
+    (s, v, st, c), (s64, v64, st64, c64) = out[prec], out[FP64]
+    assert c == 0 and c64 == 0 and st.converged == 1 and st.refinements >= 1
+    assert st.rnorm < 1e-11 * st.bnorm
+    assert np.linalg.norm(v - v64) <= 1e-9 * np.linalg.norm(v64)
+    assert np.linalg.norm(s - s64) <= 1e-9 * np.linalg.norm(s64)

@@ -171,6 +171,27 @@ def test_walls_and_no_slip_solve(gpu, oracle):
     assert g[7]["wall_pairs"] == o[7]["wall_pairs"]
 
 
+@pytest.mark.parametrize("prec", [FP32C, FP32M])
+def test_mixed_precision_wall_solve(gpu, prec):
+    # FP32 operator inside FP64 refinement: the FP64 residual meets the FP64 solve's tolerance
+    prm, cells, wall = _tube_case()
+    out = {}
+    for p in (FP64, prec):
+        ctx = setup(gpu, prm, cells, False)
+        ctx.set_walls(wall)
+        ctx.prepare_sing_int_on_wall()
+        ctx.set_wall_density(np.zeros((3, wall.nvert)))
+        st, code = ctx.no_slip_wall(1e-8, 300, 100, prec=p)
+        out[p] = (st, code, ctx.get_wall_density(wall.nvert))
+        ctx.close()
+    (st, code, f), (st64, code64, f64) = out[prec], out[FP64]
+    assert code == 0 and code64 == 0 and st.converged == 1
+    assert st.refinements >= 1 and st64.refinements == 0
+    assert st.rnorm / st.bnorm <= 1e-8
+    assert abs(st.bnorm - st64.bnorm) <= 1e-12 * st64.bnorm  # the same FP64 right-hand side
+    assert rel(f, f64) < 1e-4
+
+
 def test_error_paths(gpu, c1_case):
     prm, cells = c1_case
     g = setup(gpu, prm, cells, False)

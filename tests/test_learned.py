@@ -45,9 +45,12 @@ def test_vertex_frames_orthonormal():
 
 
 @pytest.mark.gpu
-def test_mlp_gradients_match_restatement(gpu):
+@pytest.mark.parametrize("nin,width,depth,nout,n", [
+    (6, 96, 3, 3, 700),     # ragged vs the 128-wide tiles, K not a multiple of 8: synchronous staging
+    (16, 200, 2, 3, 2056),  # asynchronous staging, ragged tiles, weight gradients split over K
+])
+def test_mlp_gradients_match_restatement(gpu, nin, width, depth, nout, n):
     from rbc3d_gb300.learned import MLP
-    nin, width, depth, nout, n = 6, 96, 3, 3, 700  # ragged vs the 64-wide tiles
     m = MLP(gpu, nin, width, depth, nout, seed=7)
     rng = np.random.default_rng(3)
     x = rng.standard_normal((n, nin)).astype(np.float32)
