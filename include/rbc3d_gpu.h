@@ -239,6 +239,32 @@ rbc3d_status rbc3d_solve_rbc_vel(rbc3d_ctx* ctx, const rbc3d_solve_opts* opt,
                                  rbc3d_solve_stats* st);
 /* Length of the coefficient vector of rbc3d_solve_rbc_vel: 3 nlat0^2 ncell. */
 int rbc3d_cell_dof(const rbc3d_ctx* ctx, int nlat0);
+
+/* ---- membrane mechanics (FP64) ------------------------------------------
+ * Positions are on the cell grid of rbc3d_set_cell_grid, SoA 3 x (ncell nlat
+ * nlon), point index cell*nlat*nlon + ilon*nlat + ilat.  Surface derivatives
+ * are those of the degree < nlat spherical-harmonic expansion on the Gauss
+ * grid (ShAnalGau + ShGradGau, ModSphpk.F90:74-105, 377-417). */
+
+/* Reference cells (rbcRefs), one per cell type: their positions xref
+ * (3 x ntypes nlat nlon) and the moduli of Shell_ElasStrs / Shell_Bend
+ * (ES shear, ED area dilation, EB bending; t_rbc%ES/ED/EB).  Replaces the
+ * reference-cell set-up of the drivers (RBC_Create + RBC_ComputeGeometry on
+ * rbcRefs, e.g. examples/case/tube.F90). */
+rbc3d_status rbc3d_set_ref_cells(rbc3d_ctx* ctx, int ntypes, const double* xref,
+                                 const double* ES, const double* ED, const double* EB);
+
+/* RBC_ComputeGeometry (ModRbc.F90:404-509) of ncell cells at positions x:
+ * unit normals a3 (3 x N), detJ = |x_th x x_phi| / sin(th) (N), area and
+ * volume per cell; any output may be NULL. */
+rbc3d_status rbc3d_cell_geometry(rbc3d_ctx* ctx, int ncell, const double* x, double* a3,
+                                 double* detJ, double* area, double* vol);
+
+/* Shell_ResForce (ModRbc.F90:815-899) of every cell at positions x against
+ * the reference cell of its type: f (3 x N, Cartesian), the residual force
+ * whose negative Compute_Rbc_Vel (ModTimeInt.F90:747-752) takes as traction. */
+rbc3d_status rbc3d_shell_res_force(rbc3d_ctx* ctx, int ncell, const int* celltype,
+                                   const double* x, double* f);
 /* MyMatMult of ModNoSlip.F90:255 on a dof-length vector: y = A u. */
 rbc3d_status rbc3d_wall_matmult(rbc3d_ctx* ctx, int prec, const double* u,
                                 double* y);

@@ -93,6 +93,10 @@ struct rbc3d_oracle_ctx {
   std::vector<double> bbx, bby, bbz;
   bool flag_sl = false, flag_dl = false;
   rbc3d_counts counts{};
+  // membrane mechanics: reference cells (rbcRefs) per cell type
+  int nref = 0;
+  std::vector<double> ref_ar, ref_b;  // a_rcp and b of each reference cell, [type][4][nv]
+  std::vector<double> ES, ED, EB;
 };
 typedef rbc3d_oracle_ctx Ctx;
 
@@ -1090,6 +1094,243 @@ static void set_g_from_grid(Ctx* c, const ShTab& T, const double* g) {
   c->has_g = true;
 }
 
+// ---------------------------------------------------------------------------
+// Membrane mechanics: RBC_ComputeGeometry (ModRbc.F90:404-509),
+// RBC_CovarGrad_Vec / RBC_CovarGrad_Tensor (:527-658), Shell_ResForce,
+// Shell_ElasStrs, Shell_Bend (:815-963).  Surface derivatives through
+// ShAnalGau + ShGradGau (ModSphpk.F90:74-105, 377-417: Spherepack gradgs
+// with the sin(theta) factor restored, so v = d/dtheta and w = d/dphi of the
+// degree < nlat expansion).  Per-cell fields are [k][nv], r = ilat + nlat*ilon;
+// 2x2 tensors [ij][nv] with ij = 2*(i-1) + (j-1).
+
+// d pbar(m, n, theta) / d theta from (1 - x^2) dP_n^m/dx = (n + m) P_{n-1}^m - n x P_n^m
+// in the orthonormal normalisation (sin(theta) > 0 on the Gauss rows)
+static void dpbar_table(int L, double theta, const double* P, double* dP) {
+  const double x = std::cos(theta), s = std::sin(theta);
+  for (int i = 0; i < L * L; ++i) dP[i] = 0.;
+  for (int m = 0; m < L; ++m)
+    for (int n = m; n < L; ++n) {
+      const double q = n > m ? std::sqrt((2.0 * n + 1.0) * (n + m) * (n - m) / (2.0 * n - 1.0)) * P[m * L + n - 1] : 0.0;
+      dP[m * L + n] = (n * x * P[m * L + n] - q) / s;
+    }
+}
+struct MbTab {
+  ShTab T;                 // degree < nlat (no ShFilter in the geometry and force)
+  std::vector<double> DG;  // dpbar at the Gauss rows, [i][m][n]
+};
+static void mb_setup(const Ctx* c, MbTab& M) {
+  const int L = c->nlat;
+  sh_setup(c, L, M.T);
+  M.DG.assign((size_t)c->nlat * L * L, 0.);
+  for (int i = 0; i < c->nlat; ++i) dpbar_table(L, c->th[i], &M.T.PG[(size_t)i * L * L], &M.DG[(size_t)i * L * L]);
+}
+// ShAnalGau + ShGradGau of one field: vt = d/dtheta, vp = d/dphi at the Gauss points
+static void sh_grad(const Ctx* c, const MbTab& M, const double* v, double* vt, double* vp) {
+  const int L = M.T.L, nlat = c->nlat, nlon = c->nlon;
+  std::vector<double> a(L * L), b(L * L), G(L), H(L), Gt(L), Ht(L);
+  sh_anal(c, M.T, v, a.data(), b.data());
+  for (int i = 0; i < nlat; ++i) {
+    for (int m = 0; m < L; ++m) {
+      G[m] = H[m] = Gt[m] = Ht[m] = 0.;
+      for (int n = m; n < L; ++n) {
+        const size_t q = ((size_t)i * L + m) * L + n;
+        G[m] += M.T.PG[q] * a[m * L + n]; H[m] += M.T.PG[q] * b[m * L + n];
+        Gt[m] += M.DG[q] * a[m * L + n]; Ht[m] += M.DG[q] * b[m * L + n];
+      }
+    }
+    for (int j = 0; j < nlon; ++j) {
+      double st = 0.5 * Gt[0], sp = 0.;
+      for (int m = 1; m < L; ++m) {
+        const double cm = M.T.cs[m * nlon + j], sm = M.T.sn[m * nlon + j];
+        st += Gt[m] * cm - Ht[m] * sm;
+        sp += -m * (G[m] * sm + H[m] * cm);
+      }
+      vt[i + nlat * j] = st;
+      vp[i + nlat * j] = sp;
+    }
+  }
+}
+struct CellGeom {
+  std::vector<double> a1, a2, a3, a1r, a2r;  // [k][nv]
+  std::vector<double> a, ar, b;              // [ij][nv]
+  std::vector<double> detJ;                  // [nv]
+  double area = 0, vol = 0, xc[3] = {0, 0, 0}, meshSize = 0;
+};
+static inline double dot3(const double* u, const double* v, int nv, int r) {
+  return u[r] * v[r] + u[r + nv] * v[r + nv] + u[r + 2 * nv] * v[r + 2 * nv];
+}
+// RBC_ComputeGeometry of one cell, x [k][nv]
+static void compute_geometry(const Ctx* c, const MbTab& M, const double* x, CellGeom& G) {
+  const int nlat = c->nlat, nlon = c->nlon, nv = nlat * nlon;
+  G.a1.assign(3 * nv, 0.); G.a2.assign(3 * nv, 0.); G.a3.assign(3 * nv, 0.);
+  G.a1r.assign(3 * nv, 0.); G.a2r.assign(3 * nv, 0.);
+  G.a.assign(4 * nv, 0.); G.ar.assign(4 * nv, 0.); G.b.assign(4 * nv, 0.); G.detJ.assign(nv, 0.);
+  for (int k = 0; k < 3; ++k) sh_grad(c, M, x + (size_t)k * nv, &G.a1[(size_t)k * nv], &G.a2[(size_t)k * nv]);
+  for (int r = 0; r < nv; ++r) {
+    const int ilat = r % nlat;
+    const double* a1 = G.a1.data();
+    const double* a2 = G.a2.data();
+    const double a11 = dot3(a1, a1, nv, r), a12 = dot3(a1, a2, nv, r), a22 = dot3(a2, a2, nv, r);
+    const double detA = a11 * a22 - a12 * a12, idet = 1. / detA;
+    const double r11 = idet * a22, r12 = -idet * a12, r21 = -idet * a12, r22 = idet * a11;
+    G.a[r] = a11; G.a[nv + r] = a12; G.a[2 * nv + r] = a12; G.a[3 * nv + r] = a22;
+    G.ar[r] = r11; G.ar[nv + r] = r12; G.ar[2 * nv + r] = r21; G.ar[3 * nv + r] = r22;
+    double n[3];
+    for (int k = 0; k < 3; ++k) {
+      G.a1r[k * nv + r] = r11 * a1[k * nv + r] + r12 * a2[k * nv + r];
+      G.a2r[k * nv + r] = r21 * a1[k * nv + r] + r22 * a2[k * nv + r];
+    }
+    n[0] = a1[nv + r] * a2[2 * nv + r] - a1[2 * nv + r] * a2[nv + r];
+    n[1] = a1[2 * nv + r] * a2[r] - a1[r] * a2[2 * nv + r];
+    n[2] = a1[r] * a2[nv + r] - a1[nv + r] * a2[r];
+    const double nn = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    for (int k = 0; k < 3; ++k) G.a3[k * nv + r] = n[k] / nn;
+    G.detJ[r] = std::sqrt(detA) / std::sin(c->th[ilat]);
+  }
+  // curvature tensor b = -(a_i . d a3 / d theta_j)
+  std::vector<double> a31(3 * nv), a32(3 * nv);
+  for (int k = 0; k < 3; ++k) sh_grad(c, M, &G.a3[(size_t)k * nv], &a31[(size_t)k * nv], &a32[(size_t)k * nv]);
+  for (int r = 0; r < nv; ++r) {
+    G.b[r] = -dot3(G.a1.data(), a31.data(), nv, r);
+    G.b[nv + r] = -dot3(G.a1.data(), a32.data(), nv, r);
+    G.b[2 * nv + r] = -dot3(G.a2.data(), a31.data(), nv, r);
+    G.b[3 * nv + r] = -dot3(G.a2.data(), a32.data(), nv, r);
+  }
+  // centroid and area (ilat outer, ilon inner), then volume
+  G.area = 0; G.xc[0] = G.xc[1] = G.xc[2] = 0;
+  for (int i = 0; i < nlat; ++i)
+    for (int j = 0; j < nlon; ++j) {
+      const int r = i + nlat * j;
+      const double ds = G.detJ[r] * c->w[i];
+      G.area += ds;
+      for (int k = 0; k < 3; ++k) G.xc[k] += ds * x[(size_t)k * nv + r];
+    }
+  for (int k = 0; k < 3; ++k) G.xc[k] /= G.area;
+  G.vol = 0;
+  for (int j = 0; j < nlon; ++j)
+    for (int i = 0; i < nlat; ++i) {
+      const int r = i + nlat * j;
+      const double ds = G.detJ[r] * c->w[i];
+      double d = 0;
+      for (int k = 0; k < 3; ++k) d += G.a3[(size_t)k * nv + r] * (x[(size_t)k * nv + r] - G.xc[k]);
+      G.vol += ds * d;
+    }
+  G.vol *= THRD;
+  G.meshSize = std::sqrt(G.area / ((double)nlat * nlat));
+}
+// RBC_CovarGrad_Tensor: t [ij][nv] (contravariant) -> dt [ij][kd][nv], kd = derivative direction
+static void covar_grad_tensor(const Ctx* c, const MbTab& M, const CellGeom& G, const double* t, double* dt) {
+  const int nv = c->nlat * c->nlon;
+  std::vector<double> tc(9 * (size_t)nv), t1(9 * (size_t)nv), t2(9 * (size_t)nv);
+  for (int r = 0; r < nv; ++r)
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        const double a1i = G.a1[i * nv + r], a2i = G.a2[i * nv + r], a1j = G.a1[j * nv + r], a2j = G.a2[j * nv + r];
+        tc[(size_t)(3 * i + j) * nv + r] = t[r] * a1i * a1j + t[nv + r] * a1i * a2j + t[2 * nv + r] * a2i * a1j +
+                                          t[3 * nv + r] * a2i * a2j;
+      }
+  for (int q = 0; q < 9; ++q) sh_grad(c, M, &tc[(size_t)q * nv], &t1[(size_t)q * nv], &t2[(size_t)q * nv]);
+  for (int r = 0; r < nv; ++r) {
+    double u[2][3];
+    for (int k = 0; k < 3; ++k) { u[0][k] = G.a1r[k * nv + r]; u[1][k] = G.a2r[k * nv + r]; }
+    for (int kd = 0; kd < 2; ++kd) {
+      const std::vector<double>& td = kd == 0 ? t1 : t2;
+      for (int al = 0; al < 2; ++al)
+        for (int be = 0; be < 2; ++be) {
+          double s = 0;
+          for (int i = 0; i < 3; ++i) {
+            double mv = 0;
+            for (int j = 0; j < 3; ++j) mv += td[(size_t)(3 * i + j) * nv + r] * u[be][j];
+            s += u[al][i] * mv;
+          }
+          dt[(size_t)((2 * al + be) * 2 + kd) * nv + r] = s;
+        }
+    }
+  }
+}
+// RBC_CovarGrad_Vec: v [i][nv] (contravariant) -> dv [ij][nv], dv(i, j) = dv^i_j
+static void covar_grad_vec(const Ctx* c, const MbTab& M, const CellGeom& G, const double* v, double* dv) {
+  const int nv = c->nlat * c->nlon;
+  std::vector<double> vc(3 * (size_t)nv), v1(3 * (size_t)nv), v2(3 * (size_t)nv);
+  for (int r = 0; r < nv; ++r)
+    for (int k = 0; k < 3; ++k) vc[(size_t)k * nv + r] = v[r] * G.a1[k * nv + r] + v[nv + r] * G.a2[k * nv + r];
+  for (int k = 0; k < 3; ++k) sh_grad(c, M, &vc[(size_t)k * nv], &v1[(size_t)k * nv], &v2[(size_t)k * nv]);
+  for (int r = 0; r < nv; ++r) {
+    dv[r] = dot3(G.a1r.data(), v1.data(), nv, r);
+    dv[nv + r] = dot3(G.a1r.data(), v2.data(), nv, r);
+    dv[2 * nv + r] = dot3(G.a2r.data(), v1.data(), nv, r);
+    dv[3 * nv + r] = dot3(G.a2r.data(), v2.data(), nv, r);
+  }
+}
+static inline void mm2(const double* A, const double* B, double* C) {  // 2x2 row-major products
+  C[0] = A[0] * B[0] + A[1] * B[2]; C[1] = A[0] * B[1] + A[1] * B[3];
+  C[2] = A[2] * B[0] + A[3] * B[2]; C[3] = A[2] * B[1] + A[3] * B[3];
+}
+// Shell_ResForce of one cell (geometry G) against its reference (ar_ref, b_ref
+// [ij][nv]): f [k][nv], Cartesian
+static void shell_res_force(const Ctx* c, const MbTab& M, const CellGeom& G, const double* ar_ref, const double* b_ref,
+                            double ES, double ED, double EB, double* f) {
+  const int nlat = c->nlat, nlon = c->nlon, nv = nlat * nlon;
+  std::vector<double> tau(4 * (size_t)nv), bnd(4 * (size_t)nv), dtau(8 * (size_t)nv), dbnd(8 * (size_t)nv);
+  std::vector<double> taun(2 * (size_t)nv), dtaun(4 * (size_t)nv), fl(3 * (size_t)nv);
+  for (int r = 0; r < nv; ++r) {
+    double a[4], ar[4], arr[4], b[4], brf[4], V2[4];
+    for (int q = 0; q < 4; ++q) {
+      a[q] = G.a[q * nv + r]; ar[q] = G.ar[q * nv + r]; arr[q] = ar_ref[q * nv + r];
+      b[q] = G.b[q * nv + r]; brf[q] = b_ref[q * nv + r];
+    }
+    // Shell_ElasStrs (:906-942)
+    mm2(a, arr, V2);
+    const double lbd1 = V2[0] + V2[3] - 2.0;
+    const double lbd2 = V2[0] * V2[3] - V2[1] * V2[2] - 1.0;
+    const double JS = std::sqrt(V2[0] * V2[3] - V2[1] * V2[2]);
+    for (int q = 0; q < 4; ++q) tau[q * nv + r] = 0.5 * ES / JS * (lbd1 + 1.0) * arr[q] + 0.5 * JS * (ED * lbd2 - ES) * ar[q];
+    // Shell_Bend (:949-963)
+    double bm[4], bmr[4], d[4], o[4];
+    mm2(ar, b, bm);
+    mm2(arr, brf, bmr);
+    for (int q = 0; q < 4; ++q) d[q] = bm[q] - bmr[q];
+    mm2(d, ar, o);
+    for (int q = 0; q < 4; ++q) bnd[q * nv + r] = -EB * o[q];
+  }
+  covar_grad_tensor(c, M, G, bnd.data(), dbnd.data());
+  auto D = [&](const std::vector<double>& t, int i, int j, int kd, int r) { return t[(size_t)((2 * i + j) * 2 + kd) * nv + r]; };
+  for (int r = 0; r < nv; ++r) {
+    taun[r] = D(dbnd, 0, 0, 0, r) + D(dbnd, 1, 0, 1, r);
+    taun[nv + r] = D(dbnd, 0, 1, 0, r) + D(dbnd, 1, 1, 1, r);
+  }
+  covar_grad_tensor(c, M, G, tau.data(), dtau.data());
+  for (int r = 0; r < nv; ++r) {
+    double f1 = -D(dtau, 0, 0, 0, r) - D(dtau, 1, 0, 1, r);
+    double f2 = -D(dtau, 0, 1, 0, r) - D(dtau, 1, 1, 1, r);
+    const double b11 = G.b[r], b12 = G.b[nv + r], b21 = G.b[2 * nv + r], b22 = G.b[3 * nv + r];
+    const double bt1 = b11 * taun[r] + b12 * taun[nv + r], bt2 = b21 * taun[r] + b22 * taun[nv + r];
+    f1 += G.ar[r] * bt1 + G.ar[nv + r] * bt2;
+    f2 += G.ar[2 * nv + r] * bt1 + G.ar[3 * nv + r] * bt2;
+    fl[r] = f1;
+    fl[nv + r] = f2;
+  }
+  covar_grad_vec(c, M, G, taun.data(), dtaun.data());
+  for (int r = 0; r < nv; ++r) {
+    double tb = 0;
+    for (int q = 0; q < 4; ++q) tb += tau[q * nv + r] * G.b[q * nv + r];
+    fl[2 * nv + r] = -dtaun[r] - dtaun[3 * nv + r] - tb;
+  }
+  // subtract the average normal force (ilon outer, ilat inner)
+  double fnTot = 0;
+  for (int j = 0; j < nlon; ++j)
+    for (int i = 0; i < nlat; ++i) fnTot += fl[2 * nv + i + nlat * j] * G.detJ[i + nlat * j] * c->w[i];
+  for (int r = 0; r < nv; ++r) fl[2 * nv + r] -= fnTot / G.area;
+  for (int r = 0; r < nv; ++r)
+    for (int k = 0; k < 3; ++k)
+      f[(size_t)k * nv + r] = fl[r] * G.a1[k * nv + r] + fl[nv + r] * G.a2[k * nv + r] + fl[2 * nv + r] * G.a3[k * nv + r];
+}
+// gather cell `cell` of an SoA point array (3 x n) into [k][nv]
+static void gather_cell(const double* x, size_t n, int cell, int nv, double* out) {
+  for (int k = 0; k < 3; ++k)
+    for (int r = 0; r < nv; ++r) out[(size_t)k * nv + r] = x[(size_t)cell * nv + r + k * n];
+}
+
 extern "C" {
 
 int API(abi_version)(void) { return RBC3D_ABI_VERSION; }
@@ -1309,6 +1550,74 @@ rbc3d_status API(no_slip_wall)(Ctx* c, const rbc3d_solve_opts* o, const double* 
 rbc3d_status API(get_counts)(const Ctx* c, rbc3d_counts* out) { *out = c->counts; return RBC3D_OK; }
 
 int API(cell_dof)(const Ctx* c, int nlat0) { return 3 * nlat0 * nlat0 * c->ncell; }
+
+rbc3d_status API(set_ref_cells)(Ctx* c, int ntypes, const double* xref, const double* ES, const double* ED,
+                                const double* EB) {
+  if (!c || ntypes < 1 || ntypes > RBC3D_MAX_CELLTYPES || !xref || !ES || !ED || !EB) return fail(c, RBC3D_ERR_ARG, "set_ref_cells");
+  if (c->th.empty()) return fail(c, RBC3D_ERR_STATE, "cell grid not set");
+  const int nv = c->nlat * c->nlon;
+  MbTab M;
+  mb_setup(c, M);
+  c->nref = ntypes;
+  c->ref_ar.assign((size_t)ntypes * 4 * nv, 0.);
+  c->ref_b.assign((size_t)ntypes * 4 * nv, 0.);
+  c->ES.assign(ES, ES + ntypes); c->ED.assign(ED, ED + ntypes); c->EB.assign(EB, EB + ntypes);
+  std::vector<double> xc(3 * (size_t)nv);
+  for (int t = 0; t < ntypes; ++t) {
+    gather_cell(xref, (size_t)ntypes * nv, t, nv, xc.data());
+    CellGeom G;
+    compute_geometry(c, M, xc.data(), G);
+    std::copy(G.ar.begin(), G.ar.end(), c->ref_ar.begin() + (size_t)t * 4 * nv);
+    std::copy(G.b.begin(), G.b.end(), c->ref_b.begin() + (size_t)t * 4 * nv);
+  }
+  return RBC3D_OK;
+}
+
+rbc3d_status API(cell_geometry)(Ctx* c, int ncell, const double* x, double* a3, double* detJ, double* area, double* vol) {
+  if (!c || ncell < 0 || (ncell > 0 && !x)) return fail(c, RBC3D_ERR_ARG, "cell_geometry");
+  if (c->th.empty()) return fail(c, RBC3D_ERR_STATE, "cell grid not set");
+  const int nv = c->nlat * c->nlon;
+  const size_t n = (size_t)ncell * nv;
+  MbTab M;
+  mb_setup(c, M);
+  std::vector<double> xc(3 * (size_t)nv);
+  for (int cell = 0; cell < ncell; ++cell) {
+    gather_cell(x, n, cell, nv, xc.data());
+    CellGeom G;
+    compute_geometry(c, M, xc.data(), G);
+    for (int r = 0; r < nv; ++r) {
+      const size_t p = (size_t)cell * nv + r;
+      if (a3) for (int k = 0; k < 3; ++k) a3[p + k * n] = G.a3[(size_t)k * nv + r];
+      if (detJ) detJ[p] = G.detJ[r];
+    }
+    if (area) area[cell] = G.area;
+    if (vol) vol[cell] = G.vol;
+  }
+  return RBC3D_OK;
+}
+
+rbc3d_status API(shell_res_force)(Ctx* c, int ncell, const int* celltype, const double* x, double* f) {
+  if (!c || ncell < 0 || (ncell > 0 && (!celltype || !x || !f))) return fail(c, RBC3D_ERR_ARG, "shell_res_force");
+  if (c->nref == 0) return fail(c, RBC3D_ERR_STATE, "reference cells not set");
+  const int nv = c->nlat * c->nlon;
+  const size_t n = (size_t)ncell * nv;
+  for (int cell = 0; cell < ncell; ++cell)
+    if (celltype[cell] < 0 || celltype[cell] >= c->nref) return fail(c, RBC3D_ERR_ARG, "bad celltype");
+  MbTab M;
+  mb_setup(c, M);
+  std::vector<double> xc(3 * (size_t)nv), fc(3 * (size_t)nv);
+  for (int cell = 0; cell < ncell; ++cell) {
+    gather_cell(x, n, cell, nv, xc.data());
+    CellGeom G;
+    compute_geometry(c, M, xc.data(), G);
+    const int t = celltype[cell];
+    shell_res_force(c, M, G, &c->ref_ar[(size_t)t * 4 * nv], &c->ref_b[(size_t)t * 4 * nv], c->ES[t], c->ED[t], c->EB[t],
+                    fc.data());
+    for (int k = 0; k < 3; ++k)
+      for (int r = 0; r < nv; ++r) f[(size_t)cell * nv + r + k * n] = fc[(size_t)k * nv + r];
+  }
+  return RBC3D_OK;
+}
 
 // Solve_RBC_Vel, ModVelSolver.F90:44-132 (Deflate off)
 rbc3d_status API(solve_rbc_vel)(Ctx* c, const rbc3d_solve_opts* o, int nlat0, double* sol, double* v,

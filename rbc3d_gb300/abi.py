@@ -99,6 +99,9 @@ SIGNATURES = [
     ("get_counts", C.c_int, [_vp, C.POINTER(Counts)]),
     ("cell_dof", C.c_int, [_vp, C.c_int]),
     ("solve_rbc_vel", C.c_int, [_vp, C.POINTER(SolveOpts), C.c_int, _dp, _dp, C.POINTER(SolveStats)]),
+    ("set_ref_cells", C.c_int, [_vp, C.c_int, _dp, _dp, _dp, _dp]),
+    ("cell_geometry", C.c_int, [_vp, C.c_int, _dp, _dp, _dp, _dp, _dp]),
+    ("shell_res_force", C.c_int, [_vp, C.c_int, _ip, _dp, _dp]),
 ]
 # Device-timing entry points of the GPU library only.
 GPU_SIGNATURES = [
@@ -333,6 +336,30 @@ class Context:
         if check and code not in (0, 4):
             self._check(code)
         return x, v.reshape(3, N), st, code
+
+    def set_ref_cells(self, xref, ES, ED, EB):
+        """Reference cells (one per cell type, positions 3 x ntypes*nlat*nlon) and
+        their moduli for Shell_ResForce."""
+        xref = f64(xref)
+        ES, ED, EB = (f64(np.atleast_1d(v)) for v in (ES, ED, EB))
+        nt = ES.size
+        self._check(self.L.fn["set_ref_cells"](self.h, nt, _ptr(xref), _ptr(ES), _ptr(ED), _ptr(EB)))
+
+    def cell_geometry(self, x, ncell):
+        """RBC_ComputeGeometry: (a3 (3,N), detJ (N,), area (ncell,), vol (ncell,))."""
+        x = f64(x)
+        N = x.shape[1]
+        a3, dj, ar, vo = np.zeros((3, N)), np.zeros(N), np.zeros(ncell), np.zeros(ncell)
+        self._check(self.L.fn["cell_geometry"](self.h, ncell, _ptr(x), _ptr(a3), _ptr(dj), _ptr(ar), _ptr(vo)))
+        return a3, dj, ar, vo
+
+    def shell_res_force(self, x, celltype):
+        """Shell_ResForce of every cell at positions x: f (3, N), Cartesian."""
+        x = f64(x)
+        ct = i32(celltype)
+        f = np.zeros_like(x)
+        self._check(self.L.fn["shell_res_force"](self.h, int(ct.size), _ptr(ct, np.int32), _ptr(x), _ptr(f)))
+        return f
 
     def counts(self):
         c = Counts()

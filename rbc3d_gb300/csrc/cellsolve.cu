@@ -30,10 +30,6 @@
 #include "ctx.hpp"
 #include "gmres.cuh"
 
-namespace {
-
-inline int cs_nblk(long long n, int b) { return (int)((n + b - 1) / b); }
-
 // Spherepack pbar(m, n, theta) for 0 <= m <= n < L, P[m*L + n]: the standard
 // recurrences for orthonormal associated Legendre functions.
 void pbar_table(int L, double theta, double* P) {
@@ -51,6 +47,10 @@ void pbar_table(int L, double theta, double* P) {
     }
   }
 }
+
+namespace {
+
+inline int cs_nblk(long long n, int b) { return (int)((n + b - 1) / b); }
 
 // FFT_Diff (ModFFT.F90:25-93) on a periodic axis of M points as a matrix:
 // modes k < M/2 times i k (domain 2 pi), mode M/2 zeroed, so

@@ -180,6 +180,16 @@ struct rbc3d_ctx {
   DBuf<float4> mix_thi, mix_tlo;
   bool phi_uniform = false;
 
+  // membrane mechanics (membrane.cu): transform tables of the degree < nlat
+  // expansion and the reference cells' a_rcp and b, [type][4][nv]
+  struct MbState {
+    int L = 0;
+    DBuf<double> P, DP, wf, cs, sn, sinth;
+    int nref = 0;
+    DBuf<double> ref_ar, ref_b;
+    std::vector<double> ES, ED, EB;
+  } mb;
+
   DBuf<double> scratch;           // GMRES basis / temporaries
   rbc3d_counts counts{};
 
@@ -246,6 +256,9 @@ inline bool valid_prec(int p) { return p == RBC3D_FP64 || p == RBC3D_FP32C || p 
 // mixed-precision solves: relative residual reduction asked of each inner
 // FP32 GMRES solve (well above the FP32 operators' ~3e-7 relative error)
 constexpr double RBC3D_IR_ETA = 1e-5;
+
+// cellsolve.cu: Spherepack pbar(m, n, theta), P[m*L + n] for 0 <= m <= n < L
+void pbar_table(int L, double theta, double* P);
 
 // peak.cu
 rbc3d_status fma_peak(int prec, double* tflops);

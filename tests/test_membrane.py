@@ -1,0 +1,140 @@
+"""Membrane mechanics (RBC_ComputeGeometry, Shell_ResForce with the Skalak
+law and bending, ModRbc.F90:404-963): the oracle against analytic geometry
+and the equilibrium identities, and the GPU against the oracle."""
+import math
+
+import numpy as np
+import pytest
+
+from rbc3d_gb300 import geometry as G
+from rbc3d_gb300.abi import Context
+
+MODULI = (1.0, 50.0, 5.4e-3)  # ES (shear), ED (area dilation), EB (bending)
+
+
+def _ctx(lib, ncell=2):
+    prm, cells, _ = G.config("C1", ncell=ncell)
+    ctx = Context(lib, prm)
+    ctx.set_cells(cells)
+    return ctx, cells
+
+
+def _reference():
+    th, phi, _ = G.gauss_grid(25, 50)
+    x0, _, _ = G.biconcave_surface(th, phi, np.eye(3), np.zeros(3))
+    return G._to_points(x0[None]), x0
+
+
+def _deformed(ncell, seed=4, amp=0.08):
+    """Rotated, translated biconcave cells with a smooth random deformation (degree <= 4)."""
+    rng = np.random.default_rng(seed)
+    th, phi, _ = G.gauss_grid(25, 50)
+    X = []
+    for c in range(ncell):
+        x, _, _ = G.biconcave_surface(th, phi, G.random_rotation(rng), rng.uniform(-2, 2, 3))
+        d = np.stack([G.sh_eval(G.random_sh_coeffs(rng, lmax=4), th, phi) for _ in range(3)], axis=-1)
+        X.append(x + amp * d)
+    return G._to_points(np.array(X))
+
+
+def test_oracle_geometry_matches_analytic(oracle):
+    ctx, cells = _ctx(oracle)
+    a3, dj, area, vol = ctx.cell_geometry(cells.x, cells.ncell)
+    # the biconcave surface is a degree-5 expansion: the Gauss-grid derivatives are exact
+    assert np.abs(a3 - cells.a3).max() < 1e-10
+    assert np.abs(dj - cells.detJ).max() < 1e-10
+    assert np.allclose(area, cells.area, rtol=1e-12, atol=0)
+    sph = G.make_sphere_cells([np.array([1.0, -2.0, 0.5])], radius=1.3)
+    a3s, djs, ars, vos = ctx.cell_geometry(sph.x, 1)
+    assert np.abs(a3s - sph.a3).max() < 1e-10 and np.abs(djs - 1.3 ** 2).max() < 1e-10
+    assert abs(ars[0] - 4 * math.pi * 1.3 ** 2) < 1e-11 and abs(vos[0] - 4 / 3 * math.pi * 1.3 ** 3) < 1e-11
+    ctx.close()
+
+
+def test_oracle_force_vanishes_at_reference_and_balances(oracle):
+    ctx, cells = _ctx(oracle)
+    xref, _ = _reference()
+    ctx.set_ref_cells(xref, *MODULI)
+    # the reference shape, also moved rigidly, carries no force (frame invariance)
+    assert np.abs(ctx.shell_res_force(xref, [0])).max() < 1e-11
+    rng = np.random.default_rng(2)
+    th, phi, w = G.gauss_grid(25, 50)
+    x1, _, _ = G.biconcave_surface(th, phi, G.random_rotation(rng), np.array([0.3, -0.2, 0.5]))
+    assert np.abs(ctx.shell_res_force(G._to_points(x1[None]), [0])).max() < 1e-9
+    # deformed cells: membrane forces are in equilibrium (zero net force and torque) up to
+    # the truncation of the degree < nlat expansion (about 1e-5 of the force scale here)
+    X = _deformed(3)
+    f = ctx.shell_res_force(X, [0, 0, 0])
+    _, dj, _, _ = ctx.cell_geometry(X, 3)
+    ds = dj * np.tile(w, 50 * 3)
+    nv = 25 * 50
+    for c in range(3):
+        sl = slice(c * nv, (c + 1) * nv)
+        scale = np.sum(np.linalg.norm(f[:, sl], axis=0) * ds[sl])
+        F = (f[:, sl] * ds[sl]).sum(1)
+        xc = X[:, sl] - X[:, sl].mean(1, keepdims=True)
+        T = (np.cross(xc.T, f[:, sl].T).T * ds[sl]).sum(1)
+        assert scale > 100.0
+        assert np.linalg.norm(F) < 1e-4 * scale and np.linalg.norm(T) < 1e-4 * scale
+    ctx.close()
+
+
+@pytest.mark.gpu
+def test_gpu_geometry_and_force_match_oracle(gpu, oracle):
+    xref, _ = _reference()
+    X = _deformed(5, seed=7)
+    ct = [0, 0, 0, 0, 0]
+    out = {}
+    for name, lib in (("o", oracle), ("g", gpu)):
+        ctx, _ = _ctx(lib)
+        ctx.set_ref_cells(xref, *MODULI)
+        out[name] = ctx.cell_geometry(X, 5) + (ctx.shell_res_force(X, ct),)
+        ctx.close()
+    o, g = out["o"], out["g"]
+    for a, b in zip(g[:4], o[:4]):
+        assert np.abs(a - b).max() <= 1e-12 * max(1.0, np.abs(b).max())
+    assert np.linalg.norm(g[4] - o[4]) <= 1e-11 * np.linalg.norm(o[4])
+
+
+def test_host_sph_transforms():
+    from rbc3d_gb300.dynamics import SphTransform, to_grid
+    rng = np.random.default_rng(3)
+    prm, cells, _ = G.config("C1", ncell=2)
+    T = SphTransform(cells.th, cells.phi, cells.w, 12)
+    # a degree < 12 field is reproduced by the filter
+    f = 0.7 + G.sh_eval(G.random_sh_coeffs(rng, lmax=11), cells.th, cells.phi)
+    assert np.abs(T.project(f) - f).max() < 1e-12
+    # positions of the biconcave cells (degree 5): the filtered equiangular spline
+    # equals the table built from the exact surface
+    X = to_grid(cells.x, cells.ncell, cells.nlat, cells.nlon)
+    assert np.abs(T.spline(X) - cells.spl_x).max() < 1e-11
+
+
+def _dyn_case(lib, ncell=1):
+    prm, _, _ = G.config("C1", ncell=ncell)
+    X = _deformed(ncell, seed=11, amp=0.06)
+    X[:, :] += 6.0  # inside the box
+    prm0, cells, _ = G.config("C1", ncell=ncell)
+    cells.x = X
+    ctx = Context(lib, prm)
+    return ctx, cells
+
+
+@pytest.mark.gpu
+def test_gpu_rk2_step_matches_oracle(gpu, oracle):
+    from rbc3d_gb300.dynamics import CellDynamics
+    xref, _ = _reference()
+    xs, fr = {}, {}
+    for name, lib in (("o", oracle), ("g", gpu)):
+        ctx, cells = _dyn_case(lib, 2)
+        ctx.set_cells(cells)
+        dyn = CellDynamics(ctx, cells, xref, MODULI, rtol=1e-11)
+        forces = []
+        for _ in range(2):
+            dyn.rk2(5e-3)
+            forces.append(dyn.last["force_rms"])
+        xs[name], fr[name] = dyn.x, forces
+        ctx.close()
+    assert np.abs(xs["g"] - xs["o"]).max() < 1e-10
+    assert np.allclose(fr["g"], fr["o"], rtol=1e-9)
+    assert fr["g"][1] < fr["g"][0]  # the deformed cells relax towards the reference shape
