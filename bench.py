@@ -399,18 +399,21 @@ def main():
     if not args.quick and not args.no_wall:
         from rbc3d_gb300.learned_run import run as wall_run
         t1 = time.perf_counter()
-        w = wall_run(ncell=64, warm_steps=50, test_steps=6, rtol=1e-8, restart=300, max_it=900, train_iters=30,
-                     history=48, seed=args.seed + rank)
+        w = wall_run(ncell=64, warm_steps=25, test_steps=3, rtol=1e-8, restart=300, max_it=900, train_iters=30,
+                     history=48, seed=args.seed + rank, dynamics="skalak", dt=1e-3)
         log(f"wall GMRES comparison in {time.perf_counter() - t1:.1f}s")
-        wall = {"workload": "C3 tube (R=8, L=48, 64 cells), FP64 matvec + FP64 Arnoldi, ||r|| < 1e-8 ||b||",
+        wall = {"workload": "C3 tube (R=8, L=48, 64 cells) under RK2 membrane dynamics (Skalak ES 1, ED 50, "
+                            "bending 5.4e-3, dt 1e-3), NoSlipWall after each RK2 stage; FP64 matvec + FP64 "
+                            "Arnoldi, ||r|| < 1e-8 ||b||",
                 **{k: w[k] for k in ("wall_dof", "restart", "history", "plain", "history_only", "learned",
                                      "speedup_learned", "speedup_history_only", "train_ms_per_step",
                                      "speedup_learned_incl_training", "mlp")},
-                "steps": "50 warm-up steps (plain solves, history + online training), 6 compared steps"}
+                "steps": "25 warm-up RK2 steps (50 plain solves: history + online training), then 3 steps "
+                         "(6 solves) each solved plain, from the history guess and from the learned guess"}
         # the same run with mixed-precision solves (FP32M operator inside FP64 refinement, FP64 residual)
         t1 = time.perf_counter()
-        wm = wall_run(ncell=64, warm_steps=50, test_steps=6, rtol=1e-8, restart=300, max_it=900, train_iters=30,
-                      history=48, seed=args.seed + rank, prec=FP32M)
+        wm = wall_run(ncell=64, warm_steps=25, test_steps=3, rtol=1e-8, restart=300, max_it=900, train_iters=30,
+                      history=48, seed=args.seed + rank, prec=FP32M, dynamics="skalak", dt=1e-3)
         log(f"mixed-precision wall GMRES comparison in {time.perf_counter() - t1:.1f}s")
         wall["mixed_fp32m"] = {k: wm[k] for k in ("plain", "history_only", "learned", "speedup_learned",
                                                   "speedup_history_only", "speedup_learned_incl_training")}

@@ -1,17 +1,19 @@
 """Learned vs plain wall GMRES along a run of the tube workload.
 
-Cells (biconcave, SH tractions) are advected through the straight periodic
-tube by a Poiseuille profile and rotated by its shear (a kinematic stand-in
-for the membrane dynamics); at every step the wall no-slip density is solved
-to ||r|| < rtol ||b|| with GMRES (FP64 matvec and Arnoldi).  The first
+Two ways to move the cells: "skalak" integrates the membrane dynamics with
+TimeInt_RK2 (ModTimeInt.F90:183-271): Compute_Rbc_Vel with the Skalak and
+bending residual force (rbc3d_shell_res_force), the cell velocity solve, and
+NoSlipWall after each stage; "kinematic" advects the cells rigidly with a
+Poiseuille profile and rotates them with its shear (one wall solve per step).
+Every wall no-slip solve runs to ||r|| < rtol ||b|| with GMRES.  The first
 `warm_steps` steps are plain solves (zero increment, i.e. warm start from the
 previous density as NoSlipWall) that fill the history and train the network
-online; afterwards every step is solved three times from the same state --
+online; afterwards every solve is done three times from the same state --
 plain, history guess only, history + network guess -- and iterations, times
 and final residuals are compared.  The plain solution continues the run and
 is recorded for the guess, so all arms see the same states.
 
-    python -m rbc3d_gb300.learned_run --cells 64 --warm 50 --test 10
+    python -m rbc3d_gb300.learned_run --cells 64 --warm 50 --test 10 --dynamics skalak
 """
 from __future__ import annotations
 
@@ -24,7 +26,13 @@ import numpy as np
 from . import geometry as G
 from . import library
 from .abi import FP32C, FP32M, FP64, Context
+from .dynamics import CellDynamics
 from .learned import WallGuess
+
+# Shell_ElasStrs / Shell_Bend moduli of the tube run: shear 1, area dilation
+# 50 (ED / ES), bending 5.4e-3 (the EB / ES ratio of the reference's example
+# cells, examples/cutout/ctube.F90:112-114)
+SKALAK_MODULI = (1.0, 50.0, 5.4e-3)
 
 
 def _unique_increment(wall, f1, f0):
@@ -34,7 +42,8 @@ def _unique_increment(wall, f1, f0):
 
 
 def run(ncell=64, warm_steps=30, test_steps=10, rtol=1e-8, restart=100, max_it=800, dt=5e-3, umax=8.0,
-        train_iters=10, width=512, depth=4, history=48, seed=20261203, prec=FP64, log=None):
+        train_iters=10, width=512, depth=4, history=48, seed=20261203, prec=FP64, log=None, dynamics="kinematic",
+        moduli=SKALAK_MODULI):
     prm, cells, wall = G.config("C3", seed=seed, ncell=ncell)
     lib = library()
     ctx = Context(lib, prm)
@@ -45,13 +54,23 @@ def run(ncell=64, warm_steps=30, test_steps=10, rtol=1e-8, restart=100, max_it=8
     guess = WallGuess(lib, wall, width=width, depth=depth, seed=seed, history=history)
     axis = (prm["Lb"][0] / 2, prm["Lb"][1] / 2)
     rng = np.random.default_rng(seed)
+    dyn = None
+    if dynamics == "skalak":
+        # membrane mechanics: reference cell = the undeformed biconcave shape
+        xr, _, _ = G.biconcave_surface(cells.th, cells.phi, np.eye(3), np.zeros(3))
+        dyn = CellDynamics(ctx, cells, G._to_points(xr[None]), moduli)
+        dyn.compute_rbc_vel(dyn.x)  # tractions and g of the initial state
+    elif dynamics != "kinematic":
+        raise ValueError(dynamics)
     ctx.no_slip_wall(rtol, max_it, restart, prec, check=False)  # initial density
     arms = {"plain": [], "history": [], "learned": []}
     losses, train_ms = [], []
-    for step in range(warm_steps + test_steps):
-        cells = G.poiseuille_step(cells, axis, 8.0, umax, dt)
-        ctx.set_cells(cells)
-        ctx.set_cell_density(f=cells.f, spl_F=cells.spl_F)
+    state = {"step": 0}
+
+    def wall_step(stage=0):
+        """NoSlipWall at the current cell state: the guess arms (test steps) from
+        the same state, then the plain solve that continues the run."""
+        step = state["step"]
         f0 = ctx.get_wall_density(wall.nvert)
         testing = step >= warm_steps
         if testing:
@@ -72,24 +91,38 @@ def run(ncell=64, warm_steps=30, test_steps=10, rtol=1e-8, restart=100, max_it=8
         if loss is not None:
             losses.append(loss)
         if log:
-            msg = f"step {step} plain its {st.iterations} ms {ms:.0f}"
+            msg = f"step {step}.{stage} plain its {st.iterations} ms {ms:.0f}"
             if testing:
                 for mode in ("history", "learned"):
                     a = arms[mode][-1]
                     msg += f" | {mode} its {a['its']} ms {a['ms']:.0f} r0 {a['r0']:.2e}"
             elif loss is not None:
                 msg += f" loss {loss:.3e}"
+            if dyn is not None:
+                msg += f" | force rms {dyn.last['force_rms']:.3e}"
             log(msg)
 
+    for step in range(warm_steps + test_steps):
+        state["step"] = step
+        if dyn is not None:
+            dyn.rk2(dt, after_stage=wall_step)  # TimeInt_RK2: NoSlipWall after each Compute_Rbc_Vel
+        else:
+            cells = G.poiseuille_step(cells, axis, 8.0, umax, dt)
+            ctx.set_cells(cells)
+            ctx.set_cell_density(f=cells.f, spl_F=cells.spl_F)
+            wall_step()
+    per_step = 2 if dyn is not None else 1
+
     def summary(mode):
-        a = arms[mode][-test_steps:]
+        a = arms[mode][-test_steps * per_step:]
         return {"its": float(np.mean([x["its"] for x in a])), "ms": float(np.mean([x["ms"] for x in a])),
                 "initial_rel_residual": float(np.mean([x["r0"] for x in a])),
                 "accepted": int(sum(x["accepted"] for x in a)),
                 "max_final_rel_residual": float(max(x["rel"] for x in a))}
 
     res = {"cells": ncell, "wall_dof": int(wall.ndof), "warm_steps": warm_steps, "test_steps": test_steps,
-           "rtol": rtol, "restart": restart, "history": history,
+           "rtol": rtol, "restart": restart, "history": history, "dynamics": dynamics, "dt": dt,
+           "solves_per_step": per_step,
            "plain": summary("plain"), "history_only": summary("history"), "learned": summary("learned")}
     res["speedup_learned"] = res["plain"]["ms"] / res["learned"]["ms"]
     res["speedup_history_only"] = res["plain"]["ms"] / res["history_only"]["ms"]
@@ -111,9 +144,13 @@ if __name__ == "__main__":
     ap.add_argument("--restart", type=int, default=300)
     ap.add_argument("--train-iters", type=int, default=30)
     ap.add_argument("--history", type=int, default=48)
+    ap.add_argument("--dynamics", choices=("kinematic", "skalak"), default="skalak",
+                    help="cell motion: RK2 membrane dynamics (Compute_Rbc_Vel) or rigid Poiseuille advection")
+    ap.add_argument("--dt", type=float, default=None)
     ap.add_argument("--prec", choices=("fp64", "fp32c", "fp32m"), default="fp64",
                     help="operator arithmetic of every arm (FP32 modes: mixed-precision solves)")
     a = ap.parse_args()
     prec = {"fp64": FP64, "fp32c": FP32C, "fp32m": FP32M}[a.prec]
+    dt = a.dt if a.dt is not None else (1e-3 if a.dynamics == "skalak" else 5e-3)
     print(json.dumps(run(a.cells, a.warm, a.test, restart=a.restart, train_iters=a.train_iters, history=a.history,
-                         prec=prec, log=print)))
+                         prec=prec, dynamics=a.dynamics, dt=dt, log=print)))

@@ -88,10 +88,11 @@ def test_mlp_training_fits_smooth_map(gpu):
 
 
 @pytest.mark.gpu
-def test_learned_guess_reaches_plain_tolerance(gpu):
+@pytest.mark.parametrize("dynamics,dt", [("kinematic", 5e-3), ("skalak", 1e-3)])
+def test_learned_guess_reaches_plain_tolerance(gpu, dynamics, dt):
     from rbc3d_gb300.learned_run import run
     res = run(ncell=8, warm_steps=8, test_steps=2, rtol=1e-8, restart=100, max_it=600, width=128, depth=2,
-              train_iters=20)
+              train_iters=20, dynamics=dynamics, dt=dt)
     for arm in ("plain", "history_only", "learned"):
         # every accepted solve meets the plain solve's ||r|| < rtol ||b||
         assert res[arm]["max_final_rel_residual"] <= 1e-8
