@@ -1,0 +1,62 @@
+"""Restart files (WriteRestart / ReadRestart, ModIO.F90:742-921) and Exodus
+Tri3 wall meshes (ReadWallMesh, ModIO.F90:547-605; Wall_Build_V2V,
+ModWall.F90:65-114)."""
+import os
+import struct
+
+import numpy as np
+import pytest
+
+from rbc3d_gb300 import geometry as G
+from rbc3d_gb300 import state_io as S
+
+
+def test_restart_round_trip_and_record_layout(tmp_path):
+    prm, cells, wall = G.config("C3", ncell=3)
+    r = S.Restart(Lb=np.array(prm["Lb"]), lt=120, time=0.12, vBkg=np.array(prm["vBkg"]),
+                  cells=S.cells_to_restart(cells, 12),
+                  walls=[S.RestartWall(wall.x.T.copy(), np.sin(wall.x.T), wall.e2v.T.copy())])
+    p = tmp_path / "restart.dat"
+    S.write_restart(p, r)
+    raw = p.read_bytes()
+    # first record: Lb(3) as 24 bytes framed by 4-byte length markers
+    assert struct.unpack("<i", raw[:4])[0] == 24 and struct.unpack("<i", raw[28:32])[0] == 24
+    assert np.array_equal(np.frombuffer(raw[4:28], "<f8"), r.Lb)
+    # the first cell's positions: Fortran order x(nlat, nlon, 3)
+    q = S.read_restart(p)
+    assert q.lt == 120 and q.time == 0.12 and np.array_equal(q.Lb, r.Lb) and np.array_equal(q.vBkg, r.vBkg)
+    assert len(q.cells) == 3 and len(q.walls) == 1
+    for a, b in zip(q.cells, r.cells):
+        assert (a.nlat0, a.nlon0, a.nlat, a.nlon, a.celltype) == (12, 24, 25, 50, 1)
+        assert np.array_equal(a.x, b.x) and a.starting_area == b.starting_area
+    X, ct = S.restart_positions(q)
+    assert np.array_equal(X, cells.x) and np.array_equal(ct, cells.celltype)
+    w = q.walls[0]
+    assert np.array_equal(w.x, wall.x.T) and np.array_equal(w.e2v, wall.e2v.T) and np.array_equal(w.f, np.sin(wall.x.T))
+    # a truncated file is an error, not a short read
+    (tmp_path / "cut.dat").write_bytes(raw[:-10])
+    with pytest.raises(EOFError):
+        S.read_restart(tmp_path / "cut.dat")
+
+
+def test_wall_mesh_round_trip_and_periodic_vertices(tmp_path):
+    wall = G.make_tube(8.0, 48.0, 48, 192, (8.25, 8.25))
+    p = tmp_path / "tube.e"
+    S.write_wall_mesh(p, wall.x.T, wall.e2v.T)
+    x, e2v = S.read_wall_mesh(p)
+    assert np.array_equal(x, wall.x.T) and np.array_equal(e2v, wall.e2v.T)
+    w2 = S.wall_from_mesh(p, [16.5, 16.5, 48.0])
+    # Wall_Build_V2V + GlobData_Init reproduce the tube's own unique-vertex ids
+    assert np.array_equal(w2.glb, wall.glb) and w2.ndof == wall.ndof
+
+
+@pytest.mark.skipif(not os.path.exists("/root/reference/examples/case/Input/new_cyl_D6_L13_33.e"),
+                    reason="reference example meshes not present")
+def test_reads_reference_example_mesh():
+    x, e2v = S.read_wall_mesh("/root/reference/examples/case/Input/new_cyl_D6_L13_33.e")
+    assert x.shape == (1328, 3) and e2v.shape == (2404, 3)
+    assert e2v.min() == 1 and e2v.max() == 1328
+    # every vertex is used and every triangle has positive area
+    assert len(np.unique(e2v)) == 1328
+    a = np.cross(x[e2v[:, 1] - 1] - x[e2v[:, 0] - 1], x[e2v[:, 2] - 1] - x[e2v[:, 0] - 1])
+    assert np.linalg.norm(a, axis=1).min() > 0
