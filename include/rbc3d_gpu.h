@@ -265,6 +265,16 @@ rbc3d_status rbc3d_cell_geometry(rbc3d_ctx* ctx, int ncell, const double* x, dou
  * whose negative Compute_Rbc_Vel (ModTimeInt.F90:747-752) takes as traction. */
 rbc3d_status rbc3d_shell_res_force(rbc3d_ctx* ctx, int ncell, const int* celltype,
                                    const double* x, double* f);
+
+/* AddIntraCellRepulsionForce (ModRepulsion.F90:126-266): for every point of a
+ * cell, the nearest point of the same cell that is farther than the polar
+ * patch radius on the reference sphere, closer than epsDist = 2 sqrt(area) /
+ * nlat, and seen against its outward normal (cosine >= 0.707); if one exists
+ * at distance d, f += force_coef exp(1 - d / epsDist) a3 at that point.
+ * x, a3, f: 3 x N; area per cell; count (may be NULL): points pushed. */
+rbc3d_status rbc3d_intra_cell_repulsion(rbc3d_ctx* ctx, int ncell, const double* x,
+                                        const double* a3, const double* area,
+                                        double force_coef, double* f, int* count);
 /* MyMatMult of ModNoSlip.F90:255 on a dof-length vector: y = A u. */
 rbc3d_status rbc3d_wall_matmult(rbc3d_ctx* ctx, int prec, const double* u,
                                 double* y);

@@ -1596,6 +1596,45 @@ rbc3d_status API(cell_geometry)(Ctx* c, int ncell, const double* x, double* a3, 
   return RBC3D_OK;
 }
 
+// AddIntraCellRepulsionForce (ModRepulsion.F90:126-266): every point of a
+// cell against the points of the same cell (those in the 27 hash cells
+// around it include every point within epsDist, the only ones that count)
+rbc3d_status API(intra_cell_repulsion)(Ctx* c, int ncell, const double* x, const double* a3, const double* area,
+                                       double force_coef, double* f, int* count) {
+  if (!c || ncell < 0 || (ncell > 0 && (!x || !a3 || !area || !f))) return fail(c, RBC3D_ERR_ARG, "intra_cell_repulsion");
+  if (c->th.empty() || c->radius <= 0) return fail(c, RBC3D_ERR_STATE, "cell grid not set");
+  const int nlat = c->nlat, nlon = c->nlon, nv = nlat * nlon;
+  const size_t n = (size_t)ncell * nv;
+  int cnt = 0;
+  for (int cell = 0; cell < ncell; ++cell) {
+    const double epsDist = 2 * std::sqrt(area[cell]) / nlat, epsRef = c->radius;
+    for (int ri = 0; ri < nv; ++ri) {
+      const size_t pi = (size_t)cell * nv + ri;
+      const int ilat = ri % nlat, ilon = ri / nlat;
+      double dist = HUGE_VAL;
+      for (int rj = 0; rj < nv; ++rj) {
+        const size_t pj = (size_t)cell * nv + rj;
+        const int jlat = rj % nlat, jlon = rj / nlat;
+        if (dist_on_sphere(c->th[ilat], c->phi[ilon], c->th[jlat], c->phi[jlon]) < epsRef) continue;
+        double xx[3], rr = 0;
+        for (int k = 0; k < 3; ++k) { xx[k] = x[pi + k * n] - x[pj + k * n]; rr += xx[k] * xx[k]; }
+        rr = std::sqrt(rr);
+        if (rr > epsDist) continue;
+        const double xxn = -(xx[0] * a3[pj] + xx[1] * a3[pj + n] + xx[2] * a3[pj + 2 * n]);
+        if (xxn / rr < 0.707) continue;
+        dist = std::min(dist, rr);
+      }
+      if (dist < epsDist) {
+        const double FF = force_coef * std::exp(1 - dist / epsDist);
+        for (int k = 0; k < 3; ++k) f[pi + k * n] += FF * a3[pi + k * n];
+        ++cnt;
+      }
+    }
+  }
+  if (count) *count = cnt;
+  return RBC3D_OK;
+}
+
 rbc3d_status API(shell_res_force)(Ctx* c, int ncell, const int* celltype, const double* x, double* f) {
   if (!c || ncell < 0 || (ncell > 0 && (!celltype || !x || !f))) return fail(c, RBC3D_ERR_ARG, "shell_res_force");
   if (c->nref == 0) return fail(c, RBC3D_ERR_STATE, "reference cells not set");

@@ -102,6 +102,7 @@ SIGNATURES = [
     ("set_ref_cells", C.c_int, [_vp, C.c_int, _dp, _dp, _dp, _dp]),
     ("cell_geometry", C.c_int, [_vp, C.c_int, _dp, _dp, _dp, _dp, _dp]),
     ("shell_res_force", C.c_int, [_vp, C.c_int, _ip, _dp, _dp]),
+    ("intra_cell_repulsion", C.c_int, [_vp, C.c_int, _dp, _dp, _dp, C.c_double, _dp, _ip]),
 ]
 # Device-timing entry points of the GPU library only.
 GPU_SIGNATURES = [
@@ -360,6 +361,16 @@ class Context:
         f = np.zeros_like(x)
         self._check(self.L.fn["shell_res_force"](self.h, int(ct.size), _ptr(ct, np.int32), _ptr(x), _ptr(f)))
         return f
+
+    def intra_cell_repulsion(self, x, a3, area, force_coef, f):
+        """AddIntraCellRepulsionForce: adds to f (3, N) in place; returns the
+        number of points pushed."""
+        x, a3, area = f64(x), f64(a3), f64(area)
+        assert f.dtype == np.float64 and f.flags.c_contiguous
+        n = C.c_int(0)
+        self._check(self.L.fn["intra_cell_repulsion"](self.h, int(area.size), _ptr(x), _ptr(a3), _ptr(area),
+                                                      float(force_coef), _ptr(f), C.byref(n)))
+        return n.value
 
     def counts(self):
         c = Counts()

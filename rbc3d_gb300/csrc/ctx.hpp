@@ -188,6 +188,8 @@ struct rbc3d_ctx {
     int nref = 0;
     DBuf<double> ref_ar, ref_b;
     std::vector<double> ES, ED, EB;
+    int excl_nv = 0;
+    DBuf<unsigned char> excl;  // repulsion: grid pairs within the patch radius on the reference sphere
   } mb;
 
   DBuf<double> scratch;           // GMRES basis / temporaries

@@ -1,7 +1,8 @@
 // membrane.cu -- membrane mechanics of the red cells on the device, FP64:
 // RBC_ComputeGeometry (ModRbc.F90:404-509), RBC_CovarGrad_Vec /
 // RBC_CovarGrad_Tensor (:527-658), Shell_ResForce (:815-899), Shell_ElasStrs
-// (:906-942, Skalak law) and Shell_Bend (:949-963).
+// (:906-942, Skalak law) and Shell_Bend (:949-963); the intra-cell
+// repulsion of AddIntraCellRepulsionForce (ModRepulsion.F90:126-266).
 //
 // Surface derivatives are ShAnalGau + ShGradGau (ModSphpk.F90:74-105,
 // 377-417): Spherepack's Gauss-grid analysis to degree < nlat and gradgs with
@@ -15,6 +16,7 @@
 // F[(cell * K + k) * nv + r], r = ilat + nlat * ilon; 2x2 tensors as K = 4
 // fields ij = 2 (i-1) + (j-1); derivatives of tensors as K = 8 fields
 // ((2 (i-1) + (j-1)) * 2 + (k-1)).
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -338,6 +340,39 @@ __global__ void k_mb_scatter(int ncell, int nv, const double* __restrict__ X, do
   for (int k = 0; k < 3; ++k) x[t + k * n] = X[((size_t)cell * 3 + k) * nv + r];
 }
 
+// AddIntraCellRepulsionForce per point: the nearest admissible point of the
+// same cell (excl: grid pairs closer than the patch radius on the reference
+// sphere, DistOnSphere tabulated per (ri, rj))
+__global__ void k_mb_repulsion(int ncell, int nv, int nlat, long long n, const double* __restrict__ x,
+                               const double* __restrict__ a3, const double* __restrict__ area,
+                               const unsigned char* __restrict__ excl, double force_coef, double* __restrict__ f,
+                               unsigned long long* __restrict__ cnt) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const int cell = (int)(p / nv), ri = (int)(p % nv);
+  const double epsDist = 2.0 * sqrt(area[cell]) / nlat, eps2 = epsDist * epsDist;
+  const double xi0 = x[p], xi1 = x[p + n], xi2 = x[p + 2 * n];
+  const size_t b = (size_t)cell * nv;
+  const unsigned char* row = excl + (size_t)ri * nv;
+  double dist = 1e300;
+  for (int rj = 0; rj < nv; ++rj) {
+    if (row[rj]) continue;
+    const size_t q = b + rj;
+    const double d0 = xi0 - x[q], d1 = xi1 - x[q + n], d2 = xi2 - x[q + 2 * n];
+    const double rr2 = d0 * d0 + d1 * d1 + d2 * d2;
+    if (rr2 > eps2) continue;  // rr > epsDist
+    const double rr = sqrt(rr2);
+    const double xxn = -(d0 * a3[q] + d1 * a3[q + n] + d2 * a3[q + 2 * n]);
+    if (xxn / rr < 0.707) continue;
+    dist = fmin(dist, rr);
+  }
+  if (dist < epsDist) {
+    const double FF = force_coef * exp(1.0 - dist / epsDist);
+    for (int k = 0; k < 3; ++k) f[p + k * n] += FF * a3[p + k * n];
+    atomicAdd(cnt, 1ull);
+  }
+}
+
 // d pbar(m, n, theta) / d theta from P (sin(theta) > 0 on the Gauss rows)
 void dpbar_table(int L, double theta, const double* P, double* dP) {
   const double x = std::cos(theta), s = std::sin(theta);
@@ -462,6 +497,46 @@ rbc3d_status rbc3d_cell_geometry(rbc3d_ctx* ctx, int ncell, const double* x, dou
   if (area) CUDA_TRY(cudaMemcpyAsync(area, G.area.p, sizeof(double) * ncell, cudaMemcpyDeviceToHost, ctx->st));
   if (vol) CUDA_TRY(cudaMemcpyAsync(vol, G.vol.p, sizeof(double) * ncell, cudaMemcpyDeviceToHost, ctx->st));
   CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  return RBC3D_OK;
+}
+
+rbc3d_status rbc3d_intra_cell_repulsion(rbc3d_ctx* ctx, int ncell, const double* x, const double* a3,
+                                        const double* area, double force_coef, double* f, int* count) {
+  if (!ctx || ncell < 0 || (ncell > 0 && (!x || !a3 || !area || !f)))
+    return ctx_fail(ctx, RBC3D_ERR_ARG, "intra_cell_repulsion: bad arguments");
+  if (ctx->h_th.empty() || ctx->radius <= 0) return ctx_fail(ctx, RBC3D_ERR_STATE, "cell grid not set");
+  if (count) *count = 0;
+  if (ncell == 0) return RBC3D_OK;
+  const int nlat = ctx->nlat, nlon = ctx->nlon, nv = nlat * nlon;
+  const size_t n = (size_t)ncell * nv;
+  auto& M = ctx->mb;
+  if (M.excl_nv != nv) {
+    // DistOnSphere (ModPolarPatch.F90:249-257) of every grid pair < patch radius
+    std::vector<unsigned char> ex((size_t)nv * nv);
+    for (int ri = 0; ri < nv; ++ri)
+      for (int rj = 0; rj < nv; ++rj) {
+        const double t0 = ctx->h_th[ri % nlat], p0 = ctx->h_phi[ri / nlat];
+        const double t1 = ctx->h_th[rj % nlat], p1 = ctx->h_phi[rj / nlat];
+        double d = std::cos(t0 - t1) - std::sin(t0) * std::sin(t1) * (1. - std::cos(p0 - p1));
+        d = std::acos(std::min(1.0, std::max(-1.0, d)));
+        ex[(size_t)ri * nv + rj] = d < ctx->radius ? 1 : 0;
+      }
+    CUDA_TRY(M.excl.upload(ex.data(), ex.size(), ctx->st));
+    M.excl_nv = nv;
+  }
+  DBuf<double> dx, da, dar, df;
+  DBuf<unsigned long long> dc;
+  CUDA_TRY(dx.upload(x, 3 * n, ctx->st)); CUDA_TRY(da.upload(a3, 3 * n, ctx->st));
+  CUDA_TRY(dar.upload(area, ncell, ctx->st)); CUDA_TRY(df.upload(f, 3 * n, ctx->st));
+  CUDA_TRY(dc.alloc(1)); CUDA_TRY(cudaMemsetAsync(dc.p, 0, sizeof(unsigned long long), ctx->st));
+  { k_mb_repulsion<<<mb_nblk((long long)n, 128), 128, 0, ctx->st>>>(ncell, nv, nlat, (long long)n, dx.p, da.p, dar.p,
+                                                                       M.excl.p, force_coef, df.p, dc.p); ++ctx->launches; }
+  CUDA_TRY(cudaGetLastError());
+  unsigned long long c = 0;
+  CUDA_TRY(cudaMemcpyAsync(f, df.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->st));
+  CUDA_TRY(cudaMemcpyAsync(&c, dc.p, sizeof(c), cudaMemcpyDeviceToHost, ctx->st));
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  if (count) *count = (int)c;
   return RBC3D_OK;
 }
 

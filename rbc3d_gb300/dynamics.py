@@ -6,11 +6,11 @@ One Compute_Rbc_Vel at positions x:
       GPU, the x / a3 / detJ spline tables from the filtered expansion, then
       rbc3d_set_cells (SourceList_UpdateCoord, TargetList_Update);
   Shell_ResForce, f = -f                           -> rbc3d_shell_res_force on the GPU;
+  AddIntraCellRepulsionForce                       -> rbc3d_intra_cell_repulsion on the GPU;
   Rbc_SphProject(f) + Rbc_BuildSurfaceSource(f)    -> ShFilter to degree < nlat0 on the
       Gauss grid, the f detJ spline, rbc3d_set_cell_density;
   Solve_RBC_Vel                                    -> rbc3d_solve_rbc_vel (g := v on the cells).
-The intra-cell repulsion of Compute_Rbc_Vel (AddIntraCellRepulsionForce) is
-not modelled.  The spherical-harmonic filter and the equiangular synthesis
+The spherical-harmonic filter and the equiangular synthesis
 that feed the spline tables are small host transforms in the conventions of
 Spherepack's shags / shsgs / shses:
   g = 1/2 sum_n a(0,n) pbar(0,n) + sum_{m>=1} sum_n pbar(m,n) (a(m,n) cos m phi - b(m,n) sin m phi).
@@ -102,8 +102,9 @@ class CellDynamics:
     grid, walls and wall density are set.  ``cells`` supplies the grid and the
     cell types; its positions are the initial state."""
 
-    def __init__(self, ctx, cells, xref, moduli, nlat0=12, rtol=1e-11, prec=FP64, max_it=200):
+    def __init__(self, ctx, cells, xref, moduli, nlat0=12, rtol=1e-11, prec=FP64, max_it=200, force_coef=10.0):
         self.ctx, self.nlat0, self.rtol, self.prec, self.max_it = ctx, nlat0, rtol, prec, max_it
+        self.force_coef = force_coef  # ForceCoef of AddIntraCellRepulsionForce (0: no repulsion)
         self.cells = cells
         self.nlat, self.nlon, self.ncell = cells.nlat, cells.nlon, cells.ncell
         self.T = SphTransform(cells.th, cells.phi, cells.w, nlat0)
@@ -122,13 +123,15 @@ class CellDynamics:
                       spl_x=T.spline(Xg), spl_a3=T.spline(Ag), spl_detJ=T.spline(Dg))
         ctx.set_cells(cur)
         f = -ctx.shell_res_force(x, c.celltype)
+        pushed = ctx.intra_cell_repulsion(x, a3, area, self.force_coef, f) if self.force_coef else 0
         Fg = T.project(to_grid(f, nc, nlat, nlon))
         f = to_points(Fg)
         ctx.set_cell_density(f=f, spl_F=T.spline(Fg * Dg))
         sol, v, st, _ = ctx.solve_rbc_vel(self.nlat0, rtol=self.rtol, max_it=self.max_it, restart=30, sol=self.sol,
                                           prec=self.prec)
         self.sol = sol
-        self.last = dict(force_rms=float(np.sqrt(np.mean(f * f))), solve_its=st.iterations, area=area)
+        self.last = dict(force_rms=float(np.sqrt(np.mean(f * f))), solve_its=st.iterations, area=area,
+                         repulsion_points=pushed)
         return v
 
     def rk2(self, dt, alpha=0.5, after_stage=None):

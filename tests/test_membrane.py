@@ -138,3 +138,54 @@ def test_gpu_rk2_step_matches_oracle(gpu, oracle):
     assert np.abs(xs["g"] - xs["o"]).max() < 1e-10
     assert np.allclose(fr["g"], fr["o"], rtol=1e-9)
     assert fr["g"][1] < fr["g"][0]  # the deformed cells relax towards the reference shape
+
+
+def _pinched(ncell=2, seed=5):
+    """Cells whose two dimples are pushed towards each other (the biconcave
+    faces approach within the repulsion range) plus a generic deformation."""
+    rng = np.random.default_rng(seed)
+    th, phi, _ = G.gauss_grid(25, 50)
+    X = []
+    for c in range(ncell):
+        x, _, _ = G.biconcave_surface(th, phi, np.eye(3), np.zeros(3))
+        x = x.copy()
+        x[..., 2] *= 0.35  # flatten: the dimples' faces 0.07 apart
+        d = np.stack([G.sh_eval(G.random_sh_coeffs(rng, lmax=3), th, phi) for _ in range(3)], axis=-1)
+        X.append(x + 0.01 * d + 4.0 * c + 3.0)
+    return G._to_points(np.array(X))
+
+
+def test_oracle_intra_cell_repulsion(oracle):
+    ctx, _ = _ctx(oracle)
+    X = _pinched()
+    a3, dj, area, _ = ctx.cell_geometry(X, 2)
+    f = np.zeros_like(X)
+    n = ctx.intra_cell_repulsion(X, a3, area, 10.0, f)
+    assert n > 0
+    pushed = np.linalg.norm(f, axis=0) > 0
+    assert pushed.sum() == n
+    # the push is along the outward normal with magnitude ForceCoef exp(1 - d/eps) in (10, 10e]
+    mag = np.linalg.norm(f[:, pushed], axis=0)
+    assert mag.min() > 10.0 and mag.max() <= 10.0 * math.e + 1e-9
+    assert np.allclose(f[:, pushed] / mag, a3[:, pushed], atol=1e-12)
+    # a sphere has no opposite faces within epsDist: no point is pushed
+    sph = G.make_sphere_cells([np.array([3.0, 3.0, 3.0])], radius=1.0)
+    a3s, _, ars, _ = ctx.cell_geometry(sph.x, 1)
+    fs = np.zeros_like(sph.x)
+    assert ctx.intra_cell_repulsion(sph.x, a3s, ars, 10.0, fs) == 0 and not fs.any()
+    ctx.close()
+
+
+@pytest.mark.gpu
+def test_gpu_intra_cell_repulsion_matches_oracle(gpu, oracle):
+    X = _pinched(3, seed=9)
+    out = {}
+    for name, lib in (("o", oracle), ("g", gpu)):
+        ctx, _ = _ctx(lib)
+        a3, dj, area, _ = ctx.cell_geometry(X, 3)
+        f = np.full_like(X, 0.25)
+        n = ctx.intra_cell_repulsion(X, a3, area, 10.0, f)
+        out[name] = (n, f)
+        ctx.close()
+    assert out["g"][0] == out["o"][0] > 0
+    assert np.abs(out["g"][1] - out["o"][1]).max() <= 1e-12 * np.abs(out["o"][1]).max()
