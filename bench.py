@@ -403,8 +403,8 @@ def main():
                      history=48, seed=args.seed + rank, dynamics="skalak", dt=1e-3)
         log(f"wall GMRES comparison in {time.perf_counter() - t1:.1f}s")
         wall = {"workload": "C3 tube (R=8, L=48, 64 cells) under RK2 membrane dynamics (Skalak ES 1, ED 50, "
-                            "bending 5.4e-3, dt 1e-3), NoSlipWall after each RK2 stage; FP64 matvec + FP64 "
-                            "Arnoldi, ||r|| < 1e-8 ||b||",
+                            "bending 5.4e-3, intra-cell repulsion 0.81, dt 1e-3), NoSlipWall after each RK2 "
+                            "stage; FP64 matvec + FP64 Arnoldi, ||r|| < 1e-8 ||b||",
                 **{k: w[k] for k in ("wall_dof", "restart", "history", "plain", "history_only", "learned",
                                      "speedup_learned", "speedup_history_only", "train_ms_per_step",
                                      "speedup_learned_incl_training", "mlp")},

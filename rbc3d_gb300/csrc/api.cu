@@ -127,12 +127,14 @@ rbc3d_status upload_splines(rbc3d_ctx* ctx, const double* h, int nvar, int set) 
   if (!h) return RBC3D_OK;
   size_t per = (size_t)ctx->m * ctx->nlon;
   size_t cnt = (size_t)ctx->ncell * 4 * per * nvar;
-  DBuf<double> tmp;
-  CUDA_TRY(tmp.upload(h, cnt, ctx->st));
+  // persistent staging buffer, stream-ordered reuse; the caller's buffer is
+  // released by the synchronisation at the end of the entry point
+  DBuf<double>& tmp = ctx->stage;
+  CUDA_TRY(tmp.alloc(cnt));
+  CUDA_TRY(cudaMemcpyAsync(tmp.p, h, sizeof(double) * cnt, cudaMemcpyHostToDevice, ctx->st));
   long long total = (long long)ctx->ncell * per;
   { k_repack<<<nblk(total, 256), 256, 0, ctx->st>>>(ctx->ncell, ctx->m, ctx->nlon, nvar, set, tmp.p, ctx->spl.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
-  CUDA_TRY(cudaStreamSynchronize(ctx->st));
   return RBC3D_OK;
 }
 
@@ -155,7 +157,36 @@ rbc3d_status finish_add(rbc3d_ctx* ctx, TargetSet& t, double* v) {
 }
 
 // Real space + corrections + linear term of AddIntOnRbcs on device (no download).
-rbc3d_status rbcs_dev(rbc3d_ctx* ctx, int which, double c1, double c2, int prec, unsigned terms) {
+rbc3d_status self_stage(rbc3d_ctx* ctx, int which, double c1, double c2, int prec) {
+  StageScope sc(ctx, 1);
+  if (prec == RBC3D_FP32M) {
+    if (!ctx->phi_uniform) return ctx_fail(ctx, RBC3D_ERR_ARG, "FP32M needs phi(j) = j*2*pi/nlon");
+    return run_self_mixed(ctx, which, c1, c2);
+  }
+  return run_self_corr(ctx, which, c1, c2);
+}
+
+rbc3d_status pme_stages(rbc3d_ctx* ctx, int which, double c1, double c2, unsigned terms, int prec) {
+  rbc3d_status s;
+  {
+    StageScope sc(ctx, 5);
+    if ((s = pme_spread(ctx, c1, c2, 1, (terms & RBC3D_TERM_WALLS) ? 1 : 0, prec))) return s;
+  }
+  {
+    StageScope sc(ctx, 6);
+    if ((s = pme_transform(ctx))) return s;
+  }
+  StageScope sc(ctx, 7);
+  return pme_gather(ctx, which);
+}
+
+__global__ void k_vadd(long long n, const double* __restrict__ a, double* __restrict__ v) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[i] += a[i];
+}
+
+rbc3d_status rbcs_dev(rbc3d_ctx* ctx, int which, double c1, double c2, int prec, unsigned terms,
+                      bool self_elsewhere = false) {
   if (ctx->npt == 0) return RBC3D_OK;
   // a density that was never set is zero (the reference's cells start with f = g = 0)
   if (!ctx->has_f) c1 = 0.0;
@@ -186,13 +217,7 @@ rbc3d_status rbcs_dev(rbc3d_ctx* ctx, int which, double c1, double c2, int prec,
     CUDA_TRY(cudaMemsetAsync(ctx->dcnt.p + 3, 0, sizeof(unsigned long long), ctx->st));
     CUDA_TRY(cudaMemsetAsync(ctx->dcnt.p + 6, 0, sizeof(unsigned long long), ctx->st));
     CUDA_TRY(cudaMemsetAsync(ctx->dcnt.p + 8, 0, sizeof(unsigned long long) * 3, ctx->st));
-    {
-      StageScope sc(ctx, 1);
-      if (prec == RBC3D_FP32M) {
-        if (!ctx->phi_uniform) return ctx_fail(ctx, RBC3D_ERR_ARG, "FP32M needs phi(j) = j*2*pi/nlon");
-        if ((s = run_self_mixed(ctx, which, c1, c2))) return s;
-      } else if ((s = run_self_corr(ctx, which, c1, c2))) return s;
-    }
+    if (!self_elsewhere && (s = self_stage(ctx, which, c1, c2, prec))) return s;
     {
       StageScope sc(ctx, 2);
       if ((s = run_near_corr(ctx, which, c1, c2, prec))) return s;
@@ -226,26 +251,43 @@ rbc3d_status matvec_dev(rbc3d_ctx* ctx, int which, double c1, double c2, unsigne
   TargetSet& t = ctx->tl[which];
   rbc3d_status s;
   if ((s = begin(ctx, t))) return s;
+  // A full cell matvec runs the own-cell patch correction and PME on the side
+  // stream, into their own accumulator, while the main stream does the pair
+  // sums, the near-singular pass, the linear term and the walls; the pipes
+  // they load differ (FP32 / L1 / FP64 / shared memory), so the kernels share
+  // the SMs.  The side accumulator is added at the join.
+  const bool side = ctx->st2 && which == RBC3D_TLIST_RBC && ctx->npt > 0 && (terms & RBC3D_TERM_CORR) &&
+                    (terms & RBC3D_TERM_PME);
+  if (side) {
+    const double sc1 = ctx->has_f ? c1 : 0.0, sc2 = ctx->has_g ? c2 : 0.0;
+    CUDA_TRY(t.v2.alloc(3 * (size_t)std::max(t.n, 1)));
+    CUDA_TRY(cudaEventRecord(ctx->ev_fork, ctx->st));
+    CUDA_TRY(cudaStreamWaitEvent(ctx->st2, ctx->ev_fork, 0));
+    std::swap(ctx->st, ctx->st2);
+    dbuf_swap(t.v, t.v2);
+    s = RBC3D_OK;
+    if (cudaMemsetAsync(t.v.p, 0, sizeof(double) * 3 * t.n, ctx->st) != cudaSuccess) s = RBC3D_ERR_CUDA;
+    if (!s) s = self_stage(ctx, which, sc1, sc2, prec);
+    if (!s) s = pme_stages(ctx, which, c1, c2, terms, prec);
+    dbuf_swap(t.v, t.v2);
+    std::swap(ctx->st, ctx->st2);
+    CUDA_TRY(cudaEventRecord(ctx->ev_join, ctx->st2));
+    if (s) return s;
+  }
   if (terms & (RBC3D_TERM_REAL | RBC3D_TERM_CORR | RBC3D_TERM_LINEAR))
-    if ((s = rbcs_dev(ctx, which, c1, c2, prec, terms))) return s;
+    if ((s = rbcs_dev(ctx, which, c1, c2, prec, terms, side))) return s;
   if (terms & RBC3D_TERM_WALLS) {
     StageScope sc(ctx, 4);
     if (which == RBC3D_TLIST_WALL) { if ((s = run_wall_self(ctx, c1))) return s; }
     else if ((s = run_wall_quad(ctx, which, c1, prec))) return s;
   }
-  if (terms & RBC3D_TERM_PME) {
-    {
-      StageScope sc(ctx, 5);
-      if ((s = pme_spread(ctx, c1, c2, 1, (terms & RBC3D_TERM_WALLS) ? 1 : 0, prec))) return s;
-    }
-    {
-      StageScope sc(ctx, 6);
-      if ((s = pme_transform(ctx))) return s;
-    }
-    {
-      StageScope sc(ctx, 7);
-      if ((s = pme_gather(ctx, which))) return s;
-    }
+  if (side) {
+    CUDA_TRY(cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0));
+    const long long n3 = 3ll * t.n;
+    { k_vadd<<<nblk(n3, 256), 256, 0, ctx->st>>>(n3, t.v2.p, t.v.p); ++ctx->launches; }
+    CUDA_TRY(cudaGetLastError());
+  } else if (terms & RBC3D_TERM_PME) {
+    if ((s = pme_stages(ctx, which, c1, c2, terms, prec))) return s;
   }
   return RBC3D_OK;
 }
@@ -294,7 +336,15 @@ rbc3d_status rbc3d_create(const rbc3d_params* prm, rbc3d_ctx** out) {
   }
   rbc3d_status s = RBC3D_OK;
   auto bail = [&](rbc3d_status code) { rbc3d_destroy(ctx); return code; };
-  if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) return bail(RBC3D_ERR_CUDA);
+  {
+    int lowest = 0, highest = 0;
+    cudaDeviceGetStreamPriorityRange(&lowest, &highest);
+    if (cudaStreamCreateWithPriority(&ctx->st, cudaStreamNonBlocking, highest) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&ctx->st2, cudaStreamNonBlocking, lowest) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess)
+      return bail(RBC3D_ERR_CUDA);
+  }
   // Ewald tables, ModEwaldFunc.F90:96-104, 151-162
   const int N = EWALD_NTAB;
   const double alpha = prm->alpha, rc = prm->rc;
@@ -346,8 +396,12 @@ rbc3d_status rbc3d_create(const rbc3d_params* prm, rbc3d_ctx** out) {
 rbc3d_status rbc3d_destroy(rbc3d_ctx* ctx) {
   if (!ctx) return RBC3D_OK;
   pme_release(ctx);
+  if (ctx->st2) cudaStreamSynchronize(ctx->st2);
   if (ctx->st) cudaStreamSynchronize(ctx->st);
   for (cudaEvent_t e : ctx->evpool) cudaEventDestroy(e);
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+  if (ctx->st2) cudaStreamDestroy(ctx->st2);
   if (ctx->t0) { cudaEventDestroy(ctx->t0); cudaEventDestroy(ctx->t1); }
   cudaStream_t st = ctx->st;
   delete ctx;
@@ -497,12 +551,12 @@ rbc3d_status rbc3d_set_cells(rbc3d_ctx* ctx, int ncell, const int* celltype, con
   if ((s = upload_splines(ctx, spl_a3, 3, SPL_A3))) return s;
   if ((s = upload_splines(ctx, spl_detJ, 1, SPL_DJ))) return s;
   if ((s = build_source_list(ctx))) return s;
-  if ((s = self_mixed_geom(ctx, x))) return s;
+  if ((s = self_mixed_geom(ctx))) return s;
   // tlist_rbc (TargetList_Update, ModTargetList.F90:95-131)
   TargetSet& t = ctx->tl[RBC3D_TLIST_RBC];
   t.n = ctx->npt;
   t.sorted = false;
-  DBuf<double> Ac;
+  DBuf<double>& Ac = ctx->acoef_dev;
   CUDA_TRY(Ac.upload(ctx->Acoef, RBC3D_MAX_CELLTYPES, ctx->st));
   CUDA_TRY(t.x.alloc(3 * N)); CUDA_TRY(t.Acoef.alloc(N)); CUDA_TRY(t.meta.alloc(N));
   CUDA_TRY(cudaMemcpyAsync(t.x.p, ctx->x.p, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, ctx->st));
@@ -533,7 +587,9 @@ rbc3d_status rbc3d_set_cell_density(rbc3d_ctx* ctx, const double* f, const doubl
     ctx->has_g = true;
   }
   if ((s = self_mixed_density(ctx, f != nullptr, g != nullptr))) return s;
-  return build_source_density(ctx);
+  if ((s = build_source_density(ctx))) return s;
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));  // the caller's host buffers are free again
+  return RBC3D_OK;
 }
 
 rbc3d_status rbc3d_set_walls(rbc3d_ctx* ctx, int nvert, int nele, const double* x, const int* e2v, const int* glb) {

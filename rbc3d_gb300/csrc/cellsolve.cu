@@ -220,9 +220,10 @@ struct CellSolveTabs {
 rbc3d_status cell_tabs(rbc3d_ctx* ctx, int L, CellSolveTabs& T) {
   const int nlat = ctx->nlat, nlon = ctx->nlon;
   std::vector<double> th(nlat), phi(nlon), w(nlat);
-  CUDA_TRY(cudaMemcpy(th.data(), ctx->th.p, sizeof(double) * nlat, cudaMemcpyDeviceToHost));
-  CUDA_TRY(cudaMemcpy(phi.data(), ctx->phi.p, sizeof(double) * nlon, cudaMemcpyDeviceToHost));
-  CUDA_TRY(cudaMemcpy(w.data(), ctx->w.p, sizeof(double) * nlat, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpyAsync(th.data(), ctx->th.p, sizeof(double) * nlat, cudaMemcpyDeviceToHost, ctx->st));
+  CUDA_TRY(cudaMemcpyAsync(phi.data(), ctx->phi.p, sizeof(double) * nlon, cudaMemcpyDeviceToHost, ctx->st));
+  CUDA_TRY(cudaMemcpyAsync(w.data(), ctx->w.p, sizeof(double) * nlat, cudaMemcpyDeviceToHost, ctx->st));
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));
   std::vector<double> PG((size_t)nlat * L * L), PE((size_t)(nlat + 1) * L * L), wf(nlat), cs((size_t)L * nlon),
       sn((size_t)L * nlon);
   for (int i = 0; i < nlat; ++i) pbar_table(L, th[i], &PG[(size_t)i * L * L]);

@@ -241,8 +241,10 @@ __device__ __forceinline__ void bspline_w(R xc, int P, int& imin, R* w) {
   }
 }
 
-#define CUDA_TRY(x)                                                   \
-  do {                                                                \
-    cudaError_t e__ = (x);                                            \
-    if (e__ != cudaSuccess) return ctx_fail_cuda(ctx, e__, #x);        \
+#define RBC3D_STR2(x) #x
+#define RBC3D_STR(x) RBC3D_STR2(x)
+#define CUDA_TRY(x)                                                                                  \
+  do {                                                                                               \
+    cudaError_t e__ = (x);                                                                           \
+    if (e__ != cudaSuccess) return ctx_fail_cuda(ctx, e__, #x " (" __FILE__ ":" RBC3D_STR(__LINE__) ")"); \
   } while (0)

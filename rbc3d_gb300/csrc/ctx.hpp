@@ -54,7 +54,16 @@ struct TargetSet {
   int nunits = 0;
   bool sorted = false;
   DBuf<double> v;       // 3n accumulator of the current matvec
+  DBuf<double> v2;      // 3n accumulator of the stages on the side stream
 };
+
+// exchange the buffers of two DBufs (no copy, no free)
+template <class T>
+inline void dbuf_swap(DBuf<T>& a, DBuf<T>& b) {
+  T* p = a.p; size_t n = a.n;
+  a.p = b.p; a.n = b.n;
+  b.p = p; b.n = n;
+}
 
 // Sources binned by the PME grid tile that holds their B-spline stencil's
 // origin: perm lists source indices tile by tile, chunk = (tile, begin, end)
@@ -110,7 +119,9 @@ struct rbc3d_ctx {
   double iLb[3]{};
   double Acoef[RBC3D_MAX_CELLTYPES]{}, Bcoef[RBC3D_MAX_CELLTYPES]{};
   std::string err;
-  cudaStream_t st = nullptr;
+  cudaStream_t st = nullptr;   // main stream (highest priority)
+  cudaStream_t st2 = nullptr;  // matvec side stream: self patch and PME next to the pair sums
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int device = 0;
 
   // Ewald / mask tables
@@ -193,6 +204,8 @@ struct rbc3d_ctx {
   } mb;
 
   DBuf<double> scratch;           // GMRES basis / temporaries
+  DBuf<double> stage;             // staging of uploaded spline tables (grow-only)
+  DBuf<double> acoef_dev, mix_xc; // Acoef per cell type; FP32M cell centres
   rbc3d_counts counts{};
 
   // stage timers: event pairs recorded around each stage, read on demand
@@ -251,7 +264,7 @@ rbc3d_status wall_residual_dev(rbc3d_ctx* ctx, int prec);
 // selfmix.cu
 rbc3d_status self_mixed_grid(rbc3d_ctx* ctx, const std::vector<double>& thG, const std::vector<double>& phiA,
                              const std::vector<double>& pw);
-rbc3d_status self_mixed_geom(rbc3d_ctx* ctx, const double* x_host);
+rbc3d_status self_mixed_geom(rbc3d_ctx* ctx);
 rbc3d_status self_mixed_density(rbc3d_ctx* ctx, bool f, bool g);
 rbc3d_status run_self_mixed(rbc3d_ctx* ctx, int tlist, double c1, double c2);
 inline bool valid_prec(int p) { return p == RBC3D_FP64 || p == RBC3D_FP32C || p == RBC3D_FP32M; }

@@ -581,7 +581,9 @@ rbc3d_status rbc3d_mlp_gradients(rbc3d_mlp* m, int n, const float* x, const floa
   if (s) return s;
   if ((s = mlp_bwd(m, n, loss))) return s;
   if ((s = gemm_status(m))) return s;
-  if (grads && cudaMemcpy(grads, m->G.p, m->nparam * sizeof(float), cudaMemcpyDeviceToHost)) return RBC3D_ERR_CUDA;
+  if (grads && (cudaMemcpyAsync(grads, m->G.p, m->nparam * sizeof(float), cudaMemcpyDeviceToHost, m->st) ||
+                cudaStreamSynchronize(m->st)))
+    return RBC3D_ERR_CUDA;
   return RBC3D_OK;
 }
 

@@ -749,15 +749,19 @@ rbc3d_status sort_points(rbc3d_ctx* ctx, int n, const double* x_dev, DBuf<int>& 
 rbc3d_status make_units(rbc3d_ctx* ctx, TargetSet& t, const DBuf<int>& cs, const DBuf<int>& ce) {
   int nc = ctx->hg.ncells;
   std::vector<int> hs(nc), he(nc);
-  CUDA_TRY(cudaMemcpy(hs.data(), cs.p, sizeof(int) * nc, cudaMemcpyDeviceToHost));
-  CUDA_TRY(cudaMemcpy(he.data(), ce.p, sizeof(int) * nc, cudaMemcpyDeviceToHost));
+  // stream-ordered reads: cudaMemcpy on the legacy stream does not wait for
+  // the context's non-blocking stream that wrote these arrays
+  CUDA_TRY(cudaMemcpyAsync(hs.data(), cs.p, sizeof(int) * nc, cudaMemcpyDeviceToHost, ctx->st));
+  CUDA_TRY(cudaMemcpyAsync(he.data(), ce.p, sizeof(int) * nc, cudaMemcpyDeviceToHost, ctx->st));
   // sources per cell (the pair work of a unit is its targets x the sources
   // of the 27 neighbour cells)
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));
   std::vector<long long> src(nc, 0);
   if (ctx->npt > 0 && ctx->s_cstart.p) {
     std::vector<int> ss(nc), se(nc);
-    CUDA_TRY(cudaMemcpy(ss.data(), ctx->s_cstart.p, sizeof(int) * nc, cudaMemcpyDeviceToHost));
-    CUDA_TRY(cudaMemcpy(se.data(), ctx->s_cend.p, sizeof(int) * nc, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpyAsync(ss.data(), ctx->s_cstart.p, sizeof(int) * nc, cudaMemcpyDeviceToHost, ctx->st));
+    CUDA_TRY(cudaMemcpyAsync(se.data(), ctx->s_cend.p, sizeof(int) * nc, cudaMemcpyDeviceToHost, ctx->st));
+    CUDA_TRY(cudaStreamSynchronize(ctx->st));
     for (int c = 0; c < nc; ++c) src[c] = se[c] - ss[c];
   }
   const int* N = ctx->hg.Nc;
@@ -855,8 +859,9 @@ rbc3d_status build_source_list(rbc3d_ctx* ctx) {
     CUDA_TRY(cudaGetLastError());
     const int nc = hg.ncells;
     std::vector<int> hs(nc), he(nc), toff(nc + 1, 0);
-    CUDA_TRY(cudaMemcpy(hs.data(), ctx->s_cstart.p, sizeof(int) * nc, cudaMemcpyDeviceToHost));
-    CUDA_TRY(cudaMemcpy(he.data(), ctx->s_cend.p, sizeof(int) * nc, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpyAsync(hs.data(), ctx->s_cstart.p, sizeof(int) * nc, cudaMemcpyDeviceToHost, ctx->st));
+    CUDA_TRY(cudaMemcpyAsync(he.data(), ctx->s_cend.p, sizeof(int) * nc, cudaMemcpyDeviceToHost, ctx->st));
+    CUDA_TRY(cudaStreamSynchronize(ctx->st));
     std::vector<int2> tiles, chunks;
     std::vector<int> coff(nc + 1, 0);
     for (int c = 0; c < nc; ++c) {

@@ -588,6 +588,12 @@ rbc3d_status pme_transform(rbc3d_ctx* ctx) {
   a.alpha = ctx->prm.alpha; a.vol = ctx->prm.Lb[0] * ctx->prm.Lb[1] * ctx->prm.Lb[2];
   a.sl = P.sl; a.dl = P.dl;
   a.bbx = P.bbx.p; a.bby = P.bby.p; a.bbz = P.bbz.p;
+  // the transforms run on the context's current stream (the matvec may put PME on its side stream)
+  if (P.prec == RBC3D_FP32C) {
+    cufftSetStream(P.r2c32_3, ctx->st); cufftSetStream(P.r2c32_12, ctx->st); cufftSetStream(P.c2r32_3, ctx->st);
+  } else {
+    cufftSetStream(P.r2c64_3, ctx->st); cufftSetStream(P.r2c64_12, ctx->st); cufftSetStream(P.c2r64_3, ctx->st);
+  }
   if (P.prec == RBC3D_FP32C) {
     CUDA_TRY(P.spec32.alloc(12 * P.GC)); CUDA_TRY(P.vspec32.alloc(3 * P.GC)); CUDA_TRY(P.vel32.alloc(3 * P.G));
     if (P.dl) { if (cufftExecR2C(P.r2c32_12, P.grid32.p, (cufftComplex*)P.spec32.p)) return ctx_fail(ctx, RBC3D_ERR_CUDA, "cufftExecR2C"); }

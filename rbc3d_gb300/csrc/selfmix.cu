@@ -37,6 +37,25 @@ struct SelfW {
   float cx[4], cy[4];
 };
 
+// mean of each cell's grid points (x SoA, 3 x npt)
+__global__ void k_cell_mean(int nv, long long npt, const double* __restrict__ x, double* __restrict__ xc) {
+  __shared__ double red[3][32];
+  const int cell = blockIdx.x;
+  double s[3] = {0, 0, 0};
+  for (int r = threadIdx.x; r < nv; r += blockDim.x)
+    for (int k = 0; k < 3; ++k) s[k] += x[(size_t)cell * nv + r + k * npt];
+  for (int k = 0; k < 3; ++k) {
+    double v = warp_sum(s[k]);
+    if ((threadIdx.x & 31) == 0) red[k][threadIdx.x >> 5] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[threadIdx.x][w];
+    xc[3 * cell + threadIdx.x] = t / nv;
+  }
+}
+
 __global__ void k_mix_geom(int ncell, int m, int n, const double* __restrict__ spl, const double* __restrict__ xc,
                            float* __restrict__ out) {
   long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -250,28 +269,21 @@ rbc3d_status self_mixed_grid(rbc3d_ctx* ctx, const std::vector<double>& thG, con
 }
 
 // FP32 node records and target positions for the current geometry.
-rbc3d_status self_mixed_geom(rbc3d_ctx* ctx, const double* x_host) {
+rbc3d_status self_mixed_geom(rbc3d_ctx* ctx) {
   const int nv = ctx->nlat * ctx->nlon;
-  std::vector<double> xc(3 * (size_t)ctx->ncell, 0.);
-  for (int c = 0; c < ctx->ncell; ++c)
-    for (int k = 0; k < 3; ++k) {
-      double s = 0;
-      for (int r = 0; r < nv; ++r) s += x_host[(size_t)c * nv + r + (size_t)k * ctx->npt];
-      xc[3 * c + k] = s / nv;
-    }
-  DBuf<double> dxc;
-  CUDA_TRY(dxc.upload(xc.data(), xc.size(), ctx->st));
+  // cell centres (mean of the grid points) from the uploaded positions
+  CUDA_TRY(ctx->mix_xc.alloc(3 * (size_t)ctx->ncell));
+  { k_cell_mean<<<ctx->ncell, 256, 0, ctx->st>>>(nv, ctx->npt, ctx->x.p, ctx->mix_xc.p); ++ctx->launches; }
   long long per = (long long)ctx->m * ctx->nlon;
   CUDA_TRY(ctx->mix_rec.alloc((size_t)ctx->ncell * per * REC));
   CUDA_TRY(ctx->mix_thi.alloc(ctx->npt));
   CUDA_TRY(ctx->mix_tlo.alloc(ctx->npt));
-  { k_mix_geom<<<nblk(ctx->ncell * per, 256), 256, 0, ctx->st>>>(ctx->ncell, ctx->m, ctx->nlon, ctx->spl.p, dxc.p,
+  { k_mix_geom<<<nblk(ctx->ncell * per, 256), 256, 0, ctx->st>>>(ctx->ncell, ctx->m, ctx->nlon, ctx->spl.p, ctx->mix_xc.p,
                                                                   ctx->mix_rec.p); ++ctx->launches; }
   { k_mix_targets<<<nblk(ctx->npt, 128), 128, 0, ctx->st>>>(ctx->npt, ctx->nlat, ctx->nlon, ctx->m, ctx->th.p,
-                                                             ctx->phi.p, ctx->spl.p, dxc.p, ctx->mix_thi.p,
+                                                             ctx->phi.p, ctx->spl.p, ctx->mix_xc.p, ctx->mix_thi.p,
                                                              ctx->mix_tlo.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
-  CUDA_TRY(cudaStreamSynchronize(ctx->st));
   return RBC3D_OK;
 }
 

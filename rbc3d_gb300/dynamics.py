@@ -102,7 +102,7 @@ class CellDynamics:
     grid, walls and wall density are set.  ``cells`` supplies the grid and the
     cell types; its positions are the initial state."""
 
-    def __init__(self, ctx, cells, xref, moduli, nlat0=12, rtol=1e-11, prec=FP64, max_it=200, force_coef=10.0):
+    def __init__(self, ctx, cells, xref, moduli, nlat0=12, rtol=1e-11, prec=FP64, max_it=200, force_coef=0.0):
         self.ctx, self.nlat0, self.rtol, self.prec, self.max_it = ctx, nlat0, rtol, prec, max_it
         self.force_coef = force_coef  # ForceCoef of AddIntraCellRepulsionForce (0: no repulsion)
         self.cells = cells

@@ -33,6 +33,10 @@ from .learned import WallGuess
 # 50 (ED / ES), bending 5.4e-3 (the EB / ES ratio of the reference's example
 # cells, examples/cutout/ctube.F90:112-114)
 SKALAK_MODULI = (1.0, 50.0, 5.4e-3)
+# ForceCoef of AddIntraCellRepulsionForce at the reference example's ratio to
+# the shear modulus (ForceCoef 10 in examples/case/Input/tube.in for cells
+# with ES 12.4)
+FORCE_COEF = 10.0 * SKALAK_MODULI[0] / 12.4
 
 
 def _unique_increment(wall, f1, f0):
@@ -43,7 +47,7 @@ def _unique_increment(wall, f1, f0):
 
 def run(ncell=64, warm_steps=30, test_steps=10, rtol=1e-8, restart=100, max_it=800, dt=5e-3, umax=8.0,
         train_iters=10, width=512, depth=4, history=48, seed=20261203, prec=FP64, log=None, dynamics="kinematic",
-        moduli=SKALAK_MODULI):
+        moduli=SKALAK_MODULI, force_coef=FORCE_COEF):
     prm, cells, wall = G.config("C3", seed=seed, ncell=ncell)
     lib = library()
     ctx = Context(lib, prm)
@@ -58,7 +62,7 @@ def run(ncell=64, warm_steps=30, test_steps=10, rtol=1e-8, restart=100, max_it=8
     if dynamics == "skalak":
         # membrane mechanics: reference cell = the undeformed biconcave shape
         xr, _, _ = G.biconcave_surface(cells.th, cells.phi, np.eye(3), np.zeros(3))
-        dyn = CellDynamics(ctx, cells, G._to_points(xr[None]), moduli)
+        dyn = CellDynamics(ctx, cells, G._to_points(xr[None]), moduli, force_coef=force_coef)
         dyn.compute_rbc_vel(dyn.x)  # tractions and g of the initial state
     elif dynamics != "kinematic":
         raise ValueError(dynamics)
