@@ -306,17 +306,29 @@ def main():
         setattr(pc, k, getattr(cells, k))
     for k, p in pin.items():
         setattr(pc, k, p)
-    h2d = sum(p.nbytes for p in pin.values())
+    # the caller's accumulator goes up and down (v += result on the device)
+    h2d = sum(p.nbytes for p in pin.values()) + vout.nbytes
     d2h = vout.nbytes
 
+    e2e_parts = {"set_cells": 0.0, "set_cell_density": 0.0, "matvec_with_download": 0.0}
+
     def e2e_step():
+        t0 = time.perf_counter()
         ctx.set_cells(pc)
+        t1 = time.perf_counter()
         ctx.set_cell_density(f=pc.f, g=pc.g, spl_F=pc.spl_F, spl_G=pc.spl_G)
+        t2 = time.perf_counter()
         vout[...] = 0.0
         ctx.matvec(TLIST_RBC, c, c, TERM_ALL, FP32C, v=vout)
+        t3 = time.perf_counter()
+        e2e_parts["set_cells"] += t1 - t0
+        e2e_parts["set_cell_density"] += t2 - t1
+        e2e_parts["matvec_with_download"] += t3 - t2
 
     for _ in range(2):
         e2e_step()
+    for k in e2e_parts:
+        e2e_parts[k] = 0.0
     barrier(dist)
     te = time.perf_counter()
     ke = max(3, args.steps // 2)
@@ -324,6 +336,7 @@ def main():
         e2e_step()
     te = dist_max(dist, (time.perf_counter() - te) / ke)
     e2e_value = ws * N / te
+    e2e_parts = {k: v / ke * 1e3 for k, v in e2e_parts.items()}
 
     # ---- roofline of the dominant stage (device time measured above)
     nq = 200  # RBC_SingInt points per target on the 25x50 grid (nrad 10 x nazm 20)
@@ -467,7 +480,7 @@ def main():
                       "stages_ms_per_step": stm,
                       "note": "own-cell polar patch in FP32 with FP64-accurate (hi/lo) geometry"},
             "e2e": {"value": e2e_value, "unit": "targets/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "ms_per_step": te * 1e3},
+                    "ms_per_step": te * 1e3, "host_ms_per_step": e2e_parts},
             "stages_ms_per_step": st_ms,
             "counts": {k: counts[k] for k in ("pairs_within_rc", "nbr_items", "nearsing_items", "self_items",
                                               "screen_misses", "near_replays", "near_projections")},

@@ -148,11 +148,23 @@ rbc3d_status begin(rbc3d_ctx* ctx, TargetSet& t) {
   CUDA_TRY(cudaMemsetAsync(t.v.p, 0, sizeof(double) * 3 * t.n, ctx->st));
   return RBC3D_OK;
 }
+__global__ void k_vadd2(long long n, const double* __restrict__ a, double* __restrict__ v) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[i] += a[i];
+}
+
+// v (caller's host array) += the matvec result: the caller's values go up,
+// are added on the device and come back (two copies of 3n doubles, no host loop)
 rbc3d_status finish_add(rbc3d_ctx* ctx, TargetSet& t, double* v) {
-  std::vector<double> tmp(3 * (size_t)t.n);
-  CUDA_TRY(cudaMemcpyAsync(tmp.data(), t.v.p, sizeof(double) * tmp.size(), cudaMemcpyDeviceToHost, ctx->st));
+  const size_t n3 = 3 * (size_t)t.n;
+  if (n3 == 0) return RBC3D_OK;
+  DBuf<double>& d = ctx->vadd;
+  CUDA_TRY(d.alloc(n3));
+  CUDA_TRY(cudaMemcpyAsync(d.p, v, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->st));
+  { k_vadd2<<<(int)((n3 + 255) / 256), 256, 0, ctx->st>>>((long long)n3, t.v.p, d.p); ++ctx->launches; }
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(v, d.p, sizeof(double) * n3, cudaMemcpyDeviceToHost, ctx->st));
   CUDA_TRY(cudaStreamSynchronize(ctx->st));
-  for (size_t i = 0; i < tmp.size(); ++i) v[i] += tmp[i];
   return RBC3D_OK;
 }
 

@@ -205,6 +205,13 @@ struct rbc3d_ctx {
 
   DBuf<double> scratch;           // GMRES basis / temporaries
   DBuf<double> stage;             // staging of uploaded spline tables (grow-only)
+  // grow-only temporaries of the set-up passes (cudaFree would synchronise the device)
+  DBuf<int> sort_key, sort_key2, sort_idx;  // sort_points
+  DBuf<char> sort_tmp;
+  DBuf<int2> list_tmp;                      // build_source_list: tile / chunk lists
+  DBuf<int> plan_key, plan_key2, plan_idx;  // build_spread_plan (may run on the side stream)
+  DBuf<char> plan_tmp;
+  DBuf<double> vadd;                        // finish_add: the caller's accumulator on the device
   DBuf<double> acoef_dev, mix_xc; // Acoef per cell type; FP32M cell centres
   rbc3d_counts counts{};
 

@@ -728,14 +728,14 @@ inline int nblk(long long n, int b) { return (int)((n + b - 1) / b); }
 
 rbc3d_status sort_points(rbc3d_ctx* ctx, int n, const double* x_dev, DBuf<int>& order, DBuf<int>& cs, DBuf<int>& ce) {
   const HashGrid& hg = ctx->hg;
-  DBuf<int> key, key2, idx;
+  DBuf<int>&key = ctx->sort_key, &key2 = ctx->sort_key2, &idx = ctx->sort_idx;
   CUDA_TRY(key.alloc(n)); CUDA_TRY(key2.alloc(n)); CUDA_TRY(idx.alloc(n)); CUDA_TRY(order.alloc(n));
   CUDA_TRY(cs.alloc(hg.ncells)); CUDA_TRY(ce.alloc(hg.ncells));
   { k_hash_keys<<<nblk(n, 256), 256, 0, ctx->st>>>(n, x_dev, hg.Nc[0], hg.Nc[1], hg.Nc[2], hg.Nc[0] / hg.L[0],
                                                   hg.Nc[1] / hg.L[1], hg.Nc[2] / hg.L[2], key.p, idx.p); ++ctx->launches; }
   size_t tmp = 0;
   cub::DeviceRadixSort::SortPairs(nullptr, tmp, key.p, key2.p, idx.p, order.p, n, 0, 32, ctx->st);
-  DBuf<char> tbuf;
+  DBuf<char>& tbuf = ctx->sort_tmp;
   CUDA_TRY(tbuf.alloc(tmp + 1));
   CUDA_TRY(cub::DeviceRadixSort::SortPairs(tbuf.p, tmp, key.p, key2.p, idx.p, order.p, n, 0, 32, ctx->st));
   CUDA_TRY(cudaMemsetAsync(cs.p, 0, sizeof(int) * hg.ncells, ctx->st));
@@ -874,23 +874,23 @@ rbc3d_status build_source_list(rbc3d_ctx* ctx) {
     coff[nc] = (int)chunks.size();
     CUDA_TRY(ctx->s_coff.upload(coff.data(), coff.size(), ctx->st));
     CUDA_TRY(ctx->s_cbox.alloc(2 * chunks.size() + 2));
+    // one upload of both lists (chunks, then tiles) into a persistent buffer
+    DBuf<int2>& lt = ctx->list_tmp;
+    std::vector<int2> both(chunks);
+    both.insert(both.end(), tiles.begin(), tiles.end());
+    if (!both.empty()) CUDA_TRY(lt.upload(both.data(), both.size(), ctx->st));
     if (!chunks.empty()) {
-      DBuf<int2> dc;
-      CUDA_TRY(dc.upload(chunks.data(), chunks.size(), ctx->st));
-      { k_tile_boxes<<<(int)chunks.size(), 32, 0, ctx->st>>>(dc.p, ctx->s_p0.p, ctx->s_cbox.p); ++ctx->launches; }
+      { k_tile_boxes<<<(int)chunks.size(), 32, 0, ctx->st>>>(lt.p, ctx->s_p0.p, ctx->s_cbox.p); ++ctx->launches; }
       CUDA_TRY(cudaGetLastError());
-      CUDA_TRY(cudaStreamSynchronize(ctx->st));
     }
     ctx->s_ntiles = (int)tiles.size();
     CUDA_TRY(ctx->s_toff.upload(toff.data(), toff.size(), ctx->st));
     CUDA_TRY(ctx->s_tbox.alloc(2 * tiles.size() + 2));
     if (!tiles.empty()) {
-      DBuf<int2> dt;
-      CUDA_TRY(dt.upload(tiles.data(), tiles.size(), ctx->st));
-      { k_tile_boxes<<<(int)tiles.size(), TILE, 0, ctx->st>>>(dt.p, ctx->s_p0.p, ctx->s_tbox.p); ++ctx->launches; }
+      { k_tile_boxes<<<(int)tiles.size(), TILE, 0, ctx->st>>>(lt.p + chunks.size(), ctx->s_p0.p, ctx->s_tbox.p); ++ctx->launches; }
       CUDA_TRY(cudaGetLastError());
-      CUDA_TRY(cudaStreamSynchronize(ctx->st));
     }
+    CUDA_TRY(cudaStreamSynchronize(ctx->st));  // the host lists are freed on return
   }
   ctx->src_sorted = true;
   ctx->pme.cplan.valid = false;  // the PME tiles follow the source positions

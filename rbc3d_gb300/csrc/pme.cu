@@ -452,7 +452,7 @@ rbc3d_status build_spread_plan(rbc3d_ctx* ctx, int n, const double* x, SpreadArg
   pl.valid = true;
   if (n == 0) return RBC3D_OK;
   TileArgs t = tile_args(ctx, 4);
-  DBuf<int> key, key2, idx;
+  DBuf<int>&key = ctx->plan_key, &key2 = ctx->plan_key2, &idx = ctx->plan_idx;
   CUDA_TRY(key.alloc(n)); CUDA_TRY(key2.alloc(n)); CUDA_TRY(idx.alloc(n)); CUDA_TRY(pl.perm.alloc(n));
   { k_tile_keys<<<nblk(n, 256), 256, 0, ctx->st>>>(n, x, a, t, key.p, idx.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
@@ -461,7 +461,7 @@ rbc3d_status build_spread_plan(rbc3d_ctx* ctx, int n, const double* x, SpreadArg
   while ((1 << bits) < ntiles) ++bits;
   size_t tmp = 0;
   cub::DeviceRadixSort::SortPairs(nullptr, tmp, key.p, key2.p, idx.p, pl.perm.p, n, 0, bits, ctx->st);
-  DBuf<char> tb;
+  DBuf<char>& tb = ctx->plan_tmp;
   CUDA_TRY(tb.alloc(tmp + 1));
   CUDA_TRY(cub::DeviceRadixSort::SortPairs(tb.p, tmp, key.p, key2.p, idx.p, pl.perm.p, n, 0, bits, ctx->st));
   std::vector<int> hk(n);
