@@ -214,7 +214,8 @@ def main():
     from rbc3d_gb300 import build as B
     B.build()
     from rbc3d_gb300 import library
-    from rbc3d_gb300.abi import FP32C, FP32M, FP64, TERM_ALL, TLIST_RBC, Context, STAGES
+    from rbc3d_gb300.abi import (FP32C, FP32M, FP64, STAGES, TERM_ALL, TERM_CORR, TERM_LINEAR, TERM_PME, TERM_REAL,
+                                 TLIST_RBC, Context)
 
     t0 = time.perf_counter()
     prm, cells = make_inputs(args.seed + rank, args.cells)
@@ -361,6 +362,50 @@ def main():
     else:
         roof = {"kernel": dom, "bound": "fp64", "achieved": None, "peak": peak64, "unit": "TFLOP/s",
                 "frac": None, "traffic": None}
+    # ---- per-kernel rooflines with the stages timed alone on one stream
+    # (REAL|CORR|LINEAR without PME keeps the matvec on the main stream)
+    def alone(prec, terms, reps=3):
+        ctx.matvec(TLIST_RBC, c, c, terms, prec, device_only=True)
+        ctx.set_profiling(1)
+        for _ in range(reps):
+            ctx.matvec(TLIST_RBC, c, c, terms, prec, device_only=True)
+        st = ctx.stage_times()
+        ctx.set_profiling(0)
+        return {k: v[0] / reps for k, v in st.items()}
+
+    hbm_peak, hbm_src = 6800.0, "fallback"
+    try:
+        mp = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
+        hbm_peak, hbm_src = float(mp["hbm_gbs"]), "measured (MEASURED_PEAKS.json)"
+    except Exception:
+        pass
+    s_c = alone(FP32C, TERM_REAL | TERM_CORR | TERM_LINEAR)
+    s_m = alone(FP32M, TERM_REAL | TERM_CORR | TERM_LINEAR)
+    s_p = alone(FP32C, TERM_PME)
+    G3 = 1
+    for d in prm["Nb"]:
+        G3 *= d
+    pme_ms = s_p["pme_spread"] + s_p["pme_fft_infl"] + s_p["pme_gather"]
+    pme_bytes = 4.0 * G3 * (12 + 12 + 12 + 12 + 3 + 3 + 3 + 3) + 4.0 * N * (3 + 3 + 3 + 1) + 4.0 * N * (3 + 3)
+    pair_fl = pairs * (FLOP_PAIR_SL + FLOP_PAIR_DL)
+    self_fl = counts["self_items"] * nq * FLOP_SELFQ_SLDL
+    rooflines = {
+        "k_pair32": {"bound": "fp32", "ms": s_c["pair"], "achieved": pair_fl / (s_c["pair"] * 1e-3) / 1e12,
+                     "peak": peak32, "unit": "TFLOP/s", "frac": pair_fl / (s_c["pair"] * 1e-3) / 1e12 / peak32,
+                     "work": f"{pairs} pairs within rc x {FLOP_PAIR_SL + FLOP_PAIR_DL} flops"},
+        "k_self": {"bound": "fp64", "ms": s_c["self"], "achieved": self_fl / (s_c["self"] * 1e-3) / 1e12,
+                   "peak": peak64, "unit": "TFLOP/s", "frac": self_fl / (s_c["self"] * 1e-3) / 1e12 / peak64,
+                   "work": f"{counts['self_items']} targets x {nq} patch points x {FLOP_SELFQ_SLDL} flops"},
+        "k_self_mix": {"bound": "l1 (ncu: L1 91% of peak)", "ms": s_m["self"],
+                       "achieved": self_fl / (s_m["self"] * 1e-3) / 1e12, "peak": peak32, "unit": "TFLOP/s",
+                       "frac": self_fl / (s_m["self"] * 1e-3) / 1e12 / peak32,
+                       "work": "the k_self patch work in FP32 with hi/lo geometry"},
+        "pme": {"bound": "hbm", "ms": pme_ms, "achieved": pme_bytes / (pme_ms * 1e-3) / 1e9, "peak": hbm_peak,
+                "unit": "GB/s", "frac": pme_bytes / (pme_ms * 1e-3) / 1e9 / hbm_peak, "peak_source": hbm_src,
+                "work": "algorithmic bytes 4 G (12+12+12+12+3+3+3+3) + 4 N (3+3+3+1) + 4 N (3+3), FP32 grids "
+                        "(a 128^3 grid set stays largely in the 129 MB L2)"},
+        "note": "stages timed alone on one stream (the matvec itself runs them on two streams)",
+    }
     tpath = os.path.join(HERE, "profiles", "traffic.json")
     if os.path.exists(tpath) and roof is not None:
         try:
@@ -485,6 +530,7 @@ def main():
             "counts": {k: counts[k] for k in ("pairs_within_rc", "nbr_items", "nearsing_items", "self_items",
                                               "screen_misses", "near_replays", "near_projections")},
             "roofline": roof,
+            "rooflines": rooflines,
             "fp32_over_fp64_plain": {"fp32c": value / fp64_value, "fp32m": fp32m_value / fp64_value,
                                      "target": 20.0,
                                      "note": "fp32c keeps the self patch in FP64 (GB300 FP64 is 1/74 of FP32); "
