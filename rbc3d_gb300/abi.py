@@ -205,6 +205,11 @@ class Context:
             pass
 
     # ---- surfaces
+    def set_cell_grid(self, th, phi, w):
+        """The cell grid alone (RBC_Create's colatitudes, longitudes, weights)."""
+        th, phi, w = f64(th), f64(phi), f64(w)
+        self._check(self.L.fn["set_cell_grid"](self.h, _ptr(th), _ptr(phi), _ptr(w)))
+
     def set_cells(self, cells):
         th, phi, w = f64(cells.th), f64(cells.phi), f64(cells.w)
         self._check(self.L.fn["set_cell_grid"](self.h, _ptr(th), _ptr(phi), _ptr(w)))

@@ -1,5 +1,5 @@
-"""State formats on either side of the path: RBC3D restart files and Exodus
-Tri3 wall meshes.
+"""State formats on either side of the path: RBC3D restart files, exported
+cell shapes and Exodus Tri3 wall meshes.
 
 * Restart files (WriteRestart / ReadRestart, ModIO.F90:742-921): Fortran
   sequential unformatted records as gfortran writes them (each record framed
@@ -155,6 +155,49 @@ def restart_positions(r: Restart):
 
 
 # ---------------------------------------------------------------------------
+# Cell shapes (ExportWriteRBC / ImportReadRBC, ModIO.F90:613-683): list-directed
+# text, "nlat0 nlon0", "nlat nlon", "celltype", then x(nlat, nlon, 3) in
+# Fortran order.  ImportReadRBC recentres the shape by (-5.25, -5.25, -5/7)
+# (the exported cell was offset to fit its box) and optionally adds xc.
+IMPORT_SHIFT = (-5.25, -5.25, -5.0 / 7.0)
+
+
+@dataclass
+class CellShape:
+    nlat0: int
+    nlon0: int
+    nlat: int
+    nlon: int
+    celltype: int          # 1-based
+    x: np.ndarray          # (nlat, nlon, 3)
+
+
+def export_write_rbc(path, c: CellShape):
+    """ExportWriteRBC: the header lines and the positions, four values per line."""
+    flat = np.asarray(c.x, dtype=np.float64).reshape(-1, order="F")
+    with open(path, "w") as fh:
+        fh.write(f" {c.nlat0:11d} {c.nlon0:11d}\n {c.nlat:11d} {c.nlon:11d}\n {c.celltype:11d}\n")
+        for i in range(0, flat.size, 4):
+            fh.write("".join(f" {v:25.17E}" for v in flat[i:i + 4]) + "\n")
+
+
+def import_read_rbc(path, xc=None, recentre=True) -> CellShape:
+    """ImportReadRBC: read a cell shape, recentre it as the reference does,
+    shift it by xc."""
+    with open(path) as fh:
+        tok = fh.read().split()
+    nlat0, nlon0, nlat, nlon, celltype = (int(t) for t in tok[:5])
+    vals = np.array([float(t.replace("D", "E").replace("d", "e")) for t in tok[5:5 + 3 * nlat * nlon]])
+    if vals.size != 3 * nlat * nlon:
+        raise ValueError(f"{path}: {vals.size} position values, expected {3 * nlat * nlon}")
+    x = vals.reshape((nlat, nlon, 3), order="F").copy()
+    if recentre:
+        x += np.asarray(IMPORT_SHIFT)
+    if xc is not None:
+        x += np.asarray(xc, dtype=np.float64)
+    return CellShape(nlat0, nlon0, nlat, nlon, celltype, x)
+
+
 def read_wall_mesh(path):
     """ReadWallMesh: (x (nvert, 3), e2v (nele, 3) 1-based) of a Tri3 Exodus file."""
     from scipy.io import netcdf_file

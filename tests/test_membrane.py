@@ -189,3 +189,60 @@ def test_gpu_intra_cell_repulsion_matches_oracle(gpu, oracle):
         ctx.close()
     assert out["g"][0] == out["o"][0] > 0
     assert np.abs(out["g"][1] - out["o"][1]).max() <= 1e-12 * np.abs(out["o"][1]).max()
+
+
+# ---------------------------------------------------------------------------
+# The reference's sample sickle cell (tests/golden/sickle_cell.npz, made by
+# tests/golden/make_sickle.py from sample_files/sample_cells/SickleCell.dat):
+# a strongly deformed shape on a 36 x 72 grid
+def _sickle_ctx(lib):
+    import os
+    from conftest import ROOT
+    z = np.load(os.path.join(ROOT, "tests", "golden", "sickle_cell.npz"))
+    nlat, nlon = int(z["nlat"]), int(z["nlon"])
+    prm, _, _ = G.config("C1", ncell=1)
+    prm = dict(prm, nlat=nlat, nlon=nlon)
+    ctx = Context(lib, prm)
+    th, phi, w = G.gauss_grid(nlat, nlon)
+    ctx.set_cell_grid(th, phi, w)
+    X = G._to_points(np.asarray(z["x"])[None] + 6.0)  # inside the box
+    return ctx, X, w, nlat, nlon
+
+
+def test_oracle_sickle_cell_mechanics(oracle):
+    ctx, X, w, nlat, nlon = _sickle_ctx(oracle)
+    a3, dj, area, vol = ctx.cell_geometry(X, 1)
+    # reduced volume of the sickle shape: between a biconcave disc (0.64) and a sphere (1)
+    rv = vol[0] / (4 / 3 * math.pi * (area[0] / (4 * math.pi)) ** 1.5)
+    assert area[0] > 0 and 0.5 < rv < 1.0
+    # the shape as its own reference carries no force; shrunk by 2% it does, in equilibrium
+    ctx.set_ref_cells(X, *MODULI)
+    assert np.abs(ctx.shell_res_force(X, [0])).max() < 1e-8
+    c = X.mean(axis=1, keepdims=True)
+    Xs = c + 0.98 * (X - c)
+    f = ctx.shell_res_force(Xs, [0])
+    _, djs, _, _ = ctx.cell_geometry(Xs, 1)
+    ds = djs * np.tile(w, nlon)
+    scale = np.sum(np.linalg.norm(f, axis=0) * ds)
+    assert scale > 1.0 and np.linalg.norm((f * ds).sum(1)) < 1e-3 * scale
+    ctx.close()
+
+
+@pytest.mark.gpu
+def test_gpu_sickle_cell_matches_oracle(gpu, oracle):
+    out = {}
+    for name, lib in (("o", oracle), ("g", gpu)):
+        ctx, X, w, nlat, nlon = _sickle_ctx(lib)
+        c = X.mean(axis=1, keepdims=True)
+        ctx.set_ref_cells(c + 1.03 * (X - c), *MODULI)
+        a3, dj, area, vol = ctx.cell_geometry(X, 1)
+        f = ctx.shell_res_force(X, [0])
+        fr = np.zeros_like(X)
+        n = ctx.intra_cell_repulsion(X, a3, area, 0.8, fr)
+        out[name] = (a3, dj, area, vol, f, fr, n)
+        ctx.close()
+    o, g = out["o"], out["g"]
+    for a, b in zip(g[:4], o[:4]):
+        assert np.abs(a - b).max() <= 1e-12 * max(1.0, np.abs(b).max())
+    assert np.linalg.norm(g[4] - o[4]) <= 1e-10 * np.linalg.norm(o[4])
+    assert g[6] == o[6] and np.abs(g[5] - o[5]).max() <= 1e-12 * max(1.0, np.abs(o[5]).max())

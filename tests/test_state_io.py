@@ -60,3 +60,26 @@ def test_reads_reference_example_mesh():
     assert len(np.unique(e2v)) == 1328
     a = np.cross(x[e2v[:, 1] - 1] - x[e2v[:, 0] - 1], x[e2v[:, 2] - 1] - x[e2v[:, 0] - 1])
     assert np.linalg.norm(a, axis=1).min() > 0
+
+
+def test_cell_shape_export_import_round_trip(tmp_path):
+    from conftest import ROOT
+    z = np.load(os.path.join(ROOT, "tests", "golden", "sickle_cell.npz"))
+    c = S.CellShape(int(z["nlat0"]), int(z["nlon0"]), int(z["nlat"]), int(z["nlon"]), int(z["celltype"]),
+                    np.asarray(z["x"]))
+    p = tmp_path / "cell.dat"
+    S.export_write_rbc(p, c)
+    d = S.import_read_rbc(p, recentre=False)
+    assert (d.nlat0, d.nlon0, d.nlat, d.nlon, d.celltype) == (12, 24, 36, 72, 1)
+    assert np.array_equal(d.x, c.x)
+    e = S.import_read_rbc(p, xc=[1.0, 2.0, 3.0])
+    assert np.allclose(e.x, c.x + np.array(S.IMPORT_SHIFT) + [1.0, 2.0, 3.0], rtol=0, atol=1e-14)
+
+
+@pytest.mark.skipif(not os.path.exists("/root/reference/sample_files/sample_cells/SickleCell.dat"),
+                    reason="reference sample cells not present")
+def test_sickle_fixture_matches_reference_file():
+    from conftest import ROOT
+    z = np.load(os.path.join(ROOT, "tests", "golden", "sickle_cell.npz"))
+    c = S.import_read_rbc("/root/reference/sample_files/sample_cells/SickleCell.dat")
+    assert np.array_equal(c.x, z["x"]) and c.nlat == 36 and c.nlon == 72
