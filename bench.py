@@ -200,6 +200,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline")
     ap.add_argument("--cells", type=int, default=None, help="smaller workload (profiling)")
     ap.add_argument("--quick", action="store_true", help="FP32C timing only (profiling)")
+    ap.add_argument("--quick-prec", choices=("fp32c", "fp32m"), default="fp32c",
+                    help="the mode --quick times (profiling)")
     ap.add_argument("--no-wall", action="store_true", help="skip the learned-guess wall GMRES comparison")
     ap.add_argument("--no-scaleup", action="store_true", help="skip the 2048-cell (PME 256^3) scale-up line")
     ap.add_argument("--no-cellsolve", action="store_true", help="skip the cell velocity GMRES line")
@@ -231,8 +233,9 @@ def main():
         ctx.matvec(TLIST_RBC, c, c, TERM_ALL, prec, device_only=True)
 
     # ---- FP32-compensated matvec, inputs resident in HBM
+    head = FP32M if (args.quick and args.quick_prec == "fp32m") else FP32C
     for _ in range(args.warmup):
-        step(FP32C)
+        step(head)
     counts = ctx.counts()
     l0 = counts["kernel_launches"]
     clk = Clocks()
@@ -241,7 +244,7 @@ def main():
     ctx.set_profiling(1)
     ctx.timer_start()
     for _ in range(args.steps):
-        step(FP32C)
+        step(head)
     ms = ctx.timer_stop()
     clocks = clk.stop()
     stages = ctx.stage_times()
@@ -254,7 +257,7 @@ def main():
 
     if args.quick:
         if rank == 0:
-            print(json.dumps({"quick": True, "ms_per_step": ms_step, "targets": N, "value": value,
+            print(json.dumps({"quick": True, "mode": args.quick_prec, "ms_per_step": ms_step, "targets": N, "value": value,
                               "stages_ms_per_step": {k: v[0] / args.steps for k, v in stages.items()},
                               "gpu_launches": launches}), flush=True)
         ctx.close()

@@ -232,14 +232,7 @@ struct NbrList {
   }
 };
 
-// Shared-memory source tile
-struct TileF {
-  float hx[TILE], hy[TILE], hz[TILE], lx[TILE], ly[TILE], lz[TILE];
-  float fx[TILE], fy[TILE], fz[TILE], gx[TILE], gy[TILE], gz[TILE];
-  float ax[TILE], ay[TILE], az[TILE];
-  float ux[TILE], uy[TILE], uz[TILE];
-  int surf[TILE], id[TILE];
-};
+// Shared-memory source tile of the FP64 pair kernel
 struct TileD {
   double x[TILE], y[TILE], z[TILE];
   double fx[TILE], fy[TILE], fz[TILE], gx[TILE], gy[TILE], gz[TILE];
