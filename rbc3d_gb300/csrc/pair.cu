@@ -371,11 +371,10 @@ __global__ void __launch_bounds__(TILE) k_pair32(PairArgs a) {
 
   // per-source bookkeeping in source order: neighbour-surface runs, the pair
   // count, the weight (0 when the pair does not contribute here)
+  // (the closest point per other surface: runs of accepted pairs of one
+  // surface, each run's minimum merged into L by surface, so sources that
+  // are out of reach need no bookkeeping)
   auto weight = [&](int sj, int idj, float r2, bool ok, int qglob) -> float {
-    if (a.collect && sj != run_surf) {
-      if (run_id >= 0) L.insert(run_surf, run_id, run_d2);
-      run_surf = sj; run_id = -1; run_d2 = 3.4e38f;
-    }
     if (!ok) return 0.f;
     ++npairs;
     float wgt = 1.f;
@@ -396,9 +395,13 @@ __global__ void __launch_bounds__(TILE) k_pair32(PairArgs a) {
           wgt = 1.f - (e.x + (sx - (float)i) * e.y);
         }
       }
-    } else {
-      if (a.collect && r2 < run_d2) { run_d2 = r2; run_id = idj; }
-      if (a.collect && r2 < a.rthr2_f) return 0.f;
+    } else if (a.collect) {
+      if (sj != run_surf) {
+        if (run_id >= 0) L.insert(run_surf, run_id, run_d2);
+        run_surf = sj; run_id = -1; run_d2 = 3.4e38f;
+      }
+      if (r2 < run_d2) { run_d2 = r2; run_id = idj; }
+      if (r2 < a.rthr2_f) return 0.f;
     }
     if (r2 < a.reps2_f) return 0.f;
     return wgt;
@@ -460,10 +463,7 @@ __global__ void __launch_bounds__(TILE) k_pair32(PairArgs a) {
           const float2 h2 = __ffma2_rn(hx, hx, __ffma2_rn(hy, hy, __fmul2_rn(hz, hz)));
           bool oka = h2.x <= a.rc2_loose, okb = h2.y <= a.rc2_loose;
           const int sa = C.surf[j], sb = C.surf[j + 1];
-          if (!(oka || okb)) {
-            if (a.collect) { weight(sa, 0, 0.f, false, 0); weight(sb, 0, 0.f, false, 0); }
-            continue;
-          }
+          if (!(oka || okb)) continue;
           const float2 xx = __fadd2_rn(hx, __fadd2_rn(ld2(C.lx, j), ntl0));
           const float2 yy = __fadd2_rn(hy, __fadd2_rn(ld2(C.ly, j), ntl1));
           const float2 zz = __fadd2_rn(hz, __fadd2_rn(ld2(C.lz, j), ntl2));
