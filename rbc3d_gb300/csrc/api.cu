@@ -564,11 +564,21 @@ rbc3d_status rbc3d_set_cells(rbc3d_ctx* ctx, int ncell, const int* celltype, con
   CUDA_TRY(cudaMemsetAsync(ctx->sg.p, 0, sizeof(double) * 3 * N, ctx->st));
   CUDA_TRY(cudaMemsetAsync(ctx->g.p, 0, sizeof(double) * 3 * N, ctx->st));
   CUDA_TRY(ctx->spl.alloc((size_t)ncell * SPL_NSET * ctx->m * ctx->nlon * SPL_NODE));
+  CUDA_TRY(ctx->stage.alloc((size_t)ncell * 4 * ctx->m * ctx->nlon * 3));  // before any side-stream work
   rbc3d_status s;
-  if ((s = upload_splines(ctx, spl_x, 3, SPL_X))) return s;
-  if ((s = upload_splines(ctx, spl_a3, 3, SPL_A3))) return s;
-  if ((s = upload_splines(ctx, spl_detJ, 1, SPL_DJ))) return s;
+  // the spline tables (the bulk of the upload) go up on the side stream
+  // while the main stream builds the source list from the positions
+  CUDA_TRY(cudaEventRecord(ctx->ev_fork, ctx->st));
+  CUDA_TRY(cudaStreamWaitEvent(ctx->st2, ctx->ev_fork, 0));
+  std::swap(ctx->st, ctx->st2);
+  s = upload_splines(ctx, spl_x, 3, SPL_X);
+  if (!s) s = upload_splines(ctx, spl_a3, 3, SPL_A3);
+  if (!s) s = upload_splines(ctx, spl_detJ, 1, SPL_DJ);
+  std::swap(ctx->st, ctx->st2);
+  CUDA_TRY(cudaEventRecord(ctx->ev_join, ctx->st2));
+  if (s) return s;
   if ((s = build_source_list(ctx))) return s;
+  CUDA_TRY(cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0));
   if ((s = self_mixed_geom(ctx))) return s;
   // tlist_rbc (TargetList_Update, ModTargetList.F90:95-131)
   TargetSet& t = ctx->tl[RBC3D_TLIST_RBC];
