@@ -516,10 +516,19 @@ rbc3d_status rbc3d_set_cell_grid(rbc3d_ctx* ctx, const double* th, const double*
       SelfW64 e;
       e.i1 = ((i1 % m) + m) % m;
       e.j1b = j1;
-      e.cx[0] = 1 + s * s * (-3. + 2. * s); e.cx[1] = s * s * (3. - 2. * s);
-      e.cx[2] = hx * s * (1. + s * (-2. + s)); e.cx[3] = hx * s * s * (-1. + s);
-      e.cy[0] = 1 + t * t * (-3. + 2. * t); e.cy[1] = t * t * (3. - 2. * t);
-      e.cy[2] = hy * t * (1. + t * (-2. + t)); e.cy[3] = hy * t * t * (-1. + t);
+      double cx[4], cy[4];
+      cx[0] = 1 + s * s * (-3. + 2. * s); cx[1] = s * s * (3. - 2. * s);
+      cx[2] = hx * s * (1. + s * (-2. + s)); cx[3] = hx * s * s * (-1. + s);
+      cy[0] = 1 + t * t * (-3. + 2. * t); cy[1] = t * t * (3. - 2. * t);
+      cy[2] = hy * t * (1. + t * (-2. + t)); cy[3] = hy * t * t * (-1. + t);
+      // node (i1,j1): u u1 u2 u12, then (i1,j2), (i2,j1), (i2,j2), as spline_w16
+      const int ax[4] = {0, 0, 1, 1}, ay[4] = {0, 1, 0, 1};
+      for (int k = 0; k < 4; ++k) {
+        e.w[4 * k + 0] = cx[ax[k]] * cy[ay[k]];
+        e.w[4 * k + 1] = cx[ax[k] + 2] * cy[ay[k]];
+        e.w[4 * k + 2] = cx[ax[k]] * cy[ay[k] + 2];
+        e.w[4 * k + 3] = cx[ax[k] + 2] * cy[ay[k] + 2];
+      }
       W[i] = e;
     }
     CUDA_TRY(ctx->self_w64.upload(reinterpret_cast<const char*>(W.data()), W.size() * sizeof(SelfW64), ctx->st));

@@ -97,7 +97,7 @@ __device__ __forceinline__ double dist_on_sphere(double th0, double phi0, double
 // column offset j1b (before adding the target's longitude index), cx, cy.
 struct SelfW64 {
   int i1, j1b;
-  double cx[4], cy[4];
+  double w[16];  // the 16 Spline_Interp weight products in spline_w16's order
 };
 struct SplW {
   int n11, n12, n21, n22;  // node ids (i1,j1) (i1,j2) (i2,j1) (i2,j2)

@@ -88,47 +88,61 @@ __global__ void __launch_bounds__(256) k_self(CorrArgs a) {
   const int NQ = a.nrad * a.nazm;
   const double phi0 = a.phi[ilon0];
   double dv[3] = {0, 0, 0};
+  const Tables& T = a.T;
   for (int q = lane; q < NQ; q += 32) {
-    int irad = q % a.nrad;
-    double th_j = a.thG[(size_t)ilat0 * NQ + q];
-    double p = a.phiA[(size_t)ilat0 * NQ + q] + phi0;  // PolarPatch_Build: atan2(...) + phi0
-    double phi_j = p - floor(p * RBC3D_I_2PI) * RBC3D_TWO_PI;
+    const int irad = q % a.nrad;
+    double w16[16];
     if (a.W64) {
-      // weights tabulated per (latitude, patch point); longitudes shift the stencil
-      const SelfW64 e = a.W64[(size_t)ilat0 * NQ + q];
+      // weight products tabulated per (latitude, patch point); longitudes shift the stencil
+      const SelfW64& e = a.W64[(size_t)ilat0 * NQ + q];
       const int j1 = imod(e.j1b + ilon0, a.nlon), j2 = (j1 + 1 == a.nlon) ? 0 : j1 + 1;
       const int i2 = (e.i1 + 1 == a.m) ? 0 : e.i1 + 1;
       W.n11 = e.i1 + a.m * j1; W.n12 = e.i1 + a.m * j2; W.n21 = i2 + a.m * j1; W.n22 = i2 + a.m * j2;
-      for (int k = 0; k < 4; ++k) { W.cx[k] = e.cx[k]; W.cy[k] = e.cy[k]; }
+#pragma unroll
+      for (int k = 0; k < 16; ++k) w16[k] = e.w[k];
     } else {
+      const double th_j = a.thG[(size_t)ilat0 * NQ + q];
+      const double p = a.phiA[(size_t)ilat0 * NQ + q] + phi0;  // PolarPatch_Build: atan2(...) + phi0
+      const double phi_j = p - floor(p * RBC3D_I_2PI) * RBC3D_TWO_PI;
       spline_weights_g(th_j, phi_j, a.G, W);
+      spline_w16(W, w16);
     }
-    double w16[16];
-    spline_w16(W, w16);
     double xj[3], xx[3];
     spline_eval16(sx, W, w16, 3, xj);
     for (int k = 0; k < 3; ++k) xx[k] = xj[k] - xi[k];
     const double r2 = xx[0] * xx[0] + xx[1] * xx[1] + xx[2] * xx[2];
     if (r2 >= a.rc2) continue;  // rr >= rc (ModRbcSingInt.F90:65)
     const double ir = rsqrt(r2), rr = r2 > 0. ? r2 * ir : 0.;
-    double wq = a.pw[irad];
+    // EwaldCoeff_SL / EwaldCoeff_DL share the table position (ModEwaldFunc.F90:86-180);
+    // below r_eps or beyond the table both are zero
+    if (!(rr >= T.r_eps)) continue;
+    const double sp = rr * T.ntab_over_rc;
+    const int it = (int)floor(sp);
+    if (it < 0 || it >= EWALD_NTAB) continue;
+    const double f1 = sp - it, f0 = (it + 1) - sp;
+    const double ir2 = ir * ir;
+    const double wq = a.pw[irad];
     if (c1 != 0.) {
-      double fj[3], EA, EB;
+      const double cs1 = __ldg(T.sl_c1 + it) * f0 + __ldg(T.sl_c1 + it + 1) * f1;
+      const double cs2 = __ldg(T.sl_c2 + it) * f0 + __ldg(T.sl_c2 + it + 1) * f1;
+      const double EA = (cs1 * ir + cs2) * ir2, EB = cs1 * ir - cs2;
+      double fj[3];
       spline_eval16(sF, W, w16, 3, fj);
-      for (int k = 0; k < 3; ++k) fj[k] = wq * fj[k];
-      ewald_sl64r(a.T, rr, ir, EA, EB);
-      double d = xx[0] * fj[0] + xx[1] * fj[1] + xx[2] * fj[2];
-      for (int k = 0; k < 3; ++k) dv[k] += c1 * (EA * xx[k] * d + EB * fj[k]);
+      // c1 wq (EA xx (xx . f) + EB f)
+      const double sw = c1 * wq, t = EA * (xx[0] * fj[0] + xx[1] * fj[1] + xx[2] * fj[2]);
+      for (int k = 0; k < 3; ++k) dv[k] = fma(sw, fma(t, xx[k], EB * fj[k]), dv[k]);
     }
     if (c2m != 0.) {
+      const double cd = __ldg(T.dl_c1 + it) * f0 + __ldg(T.dl_c1 + it + 1) * f1;
+      const double EA = cd * (ir2 * ir2 * ir);
       double gj[3], aj[3];
       spline_eval16(sG, W, w16, 3, gj);
-      for (int k = 0; k < 3; ++k) gj[k] = wq * gj[k];
       spline_eval16(sA, W, w16, 3, aj);
-      double EA = ewald_dl64r(a.T, rr, ir);
-      double dg = xx[0] * gj[0] + xx[1] * gj[1] + xx[2] * gj[2];
-      double da = xx[0] * aj[0] + xx[1] * aj[1] + xx[2] * aj[2];
-      for (int k = 0; k < 3; ++k) dv[k] += c2m * (EA * xx[k] * dg * da);
+      // c2 Bcoef wq EA xx (xx . g)(xx . a3)
+      const double dg = xx[0] * gj[0] + xx[1] * gj[1] + xx[2] * gj[2];
+      const double da = xx[0] * aj[0] + xx[1] * aj[1] + xx[2] * aj[2];
+      const double t = c2m * wq * EA * dg * da;
+      for (int k = 0; k < 3; ++k) dv[k] = fma(t, xx[k], dv[k]);
     }
   }
   for (int k = 0; k < 3; ++k) dv[k] = warp_sum(dv[k]);
