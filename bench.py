@@ -199,8 +199,8 @@ def main():
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline")
     ap.add_argument("--cells", type=int, default=None, help="smaller workload (profiling)")
-    ap.add_argument("--quick", action="store_true", help="FP32C timing only (profiling)")
-    ap.add_argument("--quick-prec", choices=("fp32c", "fp32m"), default="fp32c",
+    ap.add_argument("--quick", action="store_true", help="one mode's matvec timing only (profiling)")
+    ap.add_argument("--quick-prec", choices=("fp32c", "fp32m", "fp32d"), default="fp32d",
                     help="the mode --quick times (profiling)")
     ap.add_argument("--no-wall", action="store_true", help="skip the learned-guess wall GMRES comparison")
     ap.add_argument("--no-scaleup", action="store_true", help="skip the 2048-cell (PME 256^3) scale-up line")
@@ -216,7 +216,7 @@ def main():
     from rbc3d_gb300 import build as B
     B.build()
     from rbc3d_gb300 import library
-    from rbc3d_gb300.abi import (FP32C, FP32M, FP64, STAGES, TERM_ALL, TERM_CORR, TERM_LINEAR, TERM_PME, TERM_REAL,
+    from rbc3d_gb300.abi import (FP32C, FP32D, FP32M, FP64, STAGES, TERM_ALL, TERM_CORR, TERM_LINEAR, TERM_PME, TERM_REAL,
                                  TLIST_RBC, Context)
 
     t0 = time.perf_counter()
@@ -233,7 +233,7 @@ def main():
         ctx.matvec(TLIST_RBC, c, c, TERM_ALL, prec, device_only=True)
 
     # ---- FP32-compensated matvec, inputs resident in HBM
-    head = FP32M if (args.quick and args.quick_prec == "fp32m") else FP32C
+    head = {"fp32m": FP32M, "fp32c": FP32C}.get(args.quick_prec, FP32D) if args.quick else FP32D
     for _ in range(args.warmup):
         step(head)
     counts = ctx.counts()
@@ -287,10 +287,28 @@ def main():
     ctx.set_profiling(0)
     fp32m_value = ws * N / (msm * 1e-3)
 
+    # ---- FP32C: the own-cell polar patch on the FP64 pipe
+    for _ in range(2):
+        step(FP32C)
+    ctx.set_profiling(1)
+    ctx.timer_start()
+    for _ in range(args.steps):
+        step(FP32C)
+    msc = dist_max(dist, ctx.timer_stop()) / args.steps
+    stc = {k: v[0] / args.steps for k, v in ctx.stage_times().items()}
+    ctx.set_profiling(0)
+    fp32c_value = ws * N / (msc * 1e-3)
+    # the patch corrections alone (self + near-singular; the near pass is the
+    # same FP64 code in both modes): float-float patch against the FP64 patch
+    corr_c = ctx.matvec(TLIST_RBC, c, c, TERM_CORR, FP32C)
+    corr_d = ctx.matvec(TLIST_RBC, c, c, TERM_CORR, FP32D)
+    self_ff_vs_fp64 = float(np.linalg.norm(corr_d - corr_c) / np.linalg.norm(corr_c))
+
     # ---- relative L2 error of the FP32 modes against the FP64 plain form
     v64 = ctx.matvec(TLIST_RBC, c, c, TERM_ALL, FP64)
     err32c = float(np.linalg.norm(ctx.matvec(TLIST_RBC, c, c, TERM_ALL, FP32C) - v64) / np.linalg.norm(v64))
     err32m = float(np.linalg.norm(ctx.matvec(TLIST_RBC, c, c, TERM_ALL, FP32M) - v64) / np.linalg.norm(v64))
+    err32d = float(np.linalg.norm(ctx.matvec(TLIST_RBC, c, c, TERM_ALL, FP32D) - v64) / np.linalg.norm(v64))
     fp64_value = ws * N / (ms64 * 1e-3)
 
     # ---- end to end through the C ABI with pinned host buffers
@@ -323,7 +341,7 @@ def main():
         ctx.set_cell_density(f=pc.f, g=pc.g, spl_F=pc.spl_F, spl_G=pc.spl_G)
         t2 = time.perf_counter()
         vout[...] = 0.0
-        ctx.matvec(TLIST_RBC, c, c, TERM_ALL, FP32C, v=vout)
+        ctx.matvec(TLIST_RBC, c, c, TERM_ALL, FP32D, v=vout)
         t3 = time.perf_counter()
         e2e_parts["set_cells"] += t1 - t0
         e2e_parts["set_cell_density"] += t2 - t1
@@ -347,24 +365,12 @@ def main():
     peak32 = lib.fma_peak(FP32C)
     peak64 = lib.fma_peak(FP64)
     st_ms = {k: v[0] / args.steps for k, v in stages.items()}
-    dom = max(st_ms, key=lambda k: st_ms[k])
     pairs = counts["pairs_within_rc"]
-    roof = None
-    if dom == "self":
-        flops = counts["self_items"] * nq * FLOP_SELFQ_SLDL
-        ach = flops / (st_ms["self"] * 1e-3) / 1e12
-        roof = {"kernel": "k_self (RBC_SingInt, FP64)", "bound": "fp64", "achieved": ach, "peak": peak64,
-                "unit": "TFLOP/s", "frac": ach / peak64, "traffic": None,
-                "peak_source": "measured FP64 FMA chain (rbc3d_fma_peak), same GPU, same run"}
-    elif dom == "pair":
-        flops = pairs * (FLOP_PAIR_SL + FLOP_PAIR_DL)
-        ach = flops / (st_ms["pair"] * 1e-3) / 1e12
-        roof = {"kernel": "k_pair32 (AddIntOnRbcs pair sums, FP32)", "bound": "fp32", "achieved": ach,
-                "peak": peak32, "unit": "TFLOP/s", "frac": ach / peak32, "traffic": None,
-                "peak_source": "measured FP32 FMA chain (rbc3d_fma_peak), same GPU, same run"}
-    else:
-        roof = {"kernel": dom, "bound": "fp64", "achieved": None, "peak": peak64, "unit": "TFLOP/s",
-                "frac": None, "traffic": None}
+    # k_self_ff loads per patch point 4 stencil nodes x 4 slots x 6 float4
+    # quads of hi/lo values and 9 weight words (136 B); the L1 load peak is
+    # 128 B/clk/SM (nominal; no measured L1 figure exists)
+    l1_bytes = counts["self_items"] * nq * (4 * 4 * 6 * 16 + 136)
+    l1_peak = 128.0 * 152 * ((clocks or {}).get("sm_mhz") or 2070.0) * 1e6 / 1e9
     # ---- per-kernel rooflines with the stages timed alone on one stream
     # (REAL|CORR|LINEAR without PME keeps the matvec on the main stream)
     def alone(prec, terms, reps=3):
@@ -384,6 +390,7 @@ def main():
         pass
     s_c = alone(FP32C, TERM_REAL | TERM_CORR | TERM_LINEAR)
     s_m = alone(FP32M, TERM_REAL | TERM_CORR | TERM_LINEAR)
+    s_d = alone(FP32D, TERM_REAL | TERM_CORR | TERM_LINEAR)
     s_p = alone(FP32C, TERM_PME)
     G3 = 1
     for d in prm["Nb"]:
@@ -403,14 +410,28 @@ def main():
                        "achieved": self_fl / (s_m["self"] * 1e-3) / 1e12, "peak": peak32, "unit": "TFLOP/s",
                        "frac": self_fl / (s_m["self"] * 1e-3) / 1e12 / peak32,
                        "work": "the k_self patch work in FP32 with hi/lo geometry"},
+        "k_self_ff": {"bound": "l1", "ms": s_d["self"], "achieved": l1_bytes / (s_d["self"] * 1e-3) / 1e9,
+                      "peak": l1_peak, "unit": "GB/s", "frac": l1_bytes / (s_d["self"] * 1e-3) / 1e9 / l1_peak,
+                      "flops_achieved_tflops": self_fl / (s_d["self"] * 1e-3) / 1e12,
+                      "work": "L1 bytes requested by the lanes (the k_self patch work in float-float arithmetic)"},
         "pme": {"bound": "hbm", "ms": pme_ms, "achieved": pme_bytes / (pme_ms * 1e-3) / 1e9, "peak": hbm_peak,
                 "unit": "GB/s", "frac": pme_bytes / (pme_ms * 1e-3) / 1e9 / hbm_peak, "peak_source": hbm_src,
                 "work": "algorithmic bytes 4 G (12+12+12+12+3+3+3+3) + 4 N (3+3+3+1) + 4 N (3+3), FP32 grids "
                         "(a 128^3 grid set stays largely in the 129 MB L2)"},
         "note": "stages timed alone on one stream (the matvec itself runs them on two streams)",
     }
+    # ---- the dominant kernel of the headline mode, from the stages timed alone
+    # (the matvec's stage spans overlap across the two streams)
+    if s_d["self"] >= s_d["pair"]:
+        roof = {"kernel": "k_self_ff (RBC_SingInt, float-float)", **rooflines["k_self_ff"],
+                "peak_source": "nominal L1 load bandwidth 128 B/clk/SM x 152 SMs x the sampled SM clock "
+                               "(ncu: L1 data pipe ~80% busy, FMA pipe ~55%)"}
+    else:
+        roof = {"kernel": "k_pair32 (AddIntOnRbcs pair sums, FP32)", **rooflines["k_pair32"],
+                "peak_source": "measured FP32 FMA chain (rbc3d_fma_peak), same GPU, same run"}
+    roof["traffic"] = None
     tpath = os.path.join(HERE, "profiles", "traffic.json")
-    if os.path.exists(tpath) and roof is not None:
+    if os.path.exists(tpath):
         try:
             tr = json.load(open(tpath))
             roof["traffic"] = tr.get(roof["kernel"].split()[0])
@@ -438,10 +459,12 @@ def main():
 
         m32c = timed(FP32C, 2, 3)
         m32m = timed(FP32M, 2, 3)
+        m32d = timed(FP32D, 2, 3)
         m64 = timed(FP64, 1, 1)
         v64 = ctx5.matvec(TLIST_RBC, c, c, TERM_ALL, FP64)
         e32c = float(np.linalg.norm(ctx5.matvec(TLIST_RBC, c, c, TERM_ALL, FP32C) - v64) / np.linalg.norm(v64))
         e32m = float(np.linalg.norm(ctx5.matvec(TLIST_RBC, c, c, TERM_ALL, FP32M) - v64) / np.linalg.norm(v64))
+        e32d = float(np.linalg.norm(ctx5.matvec(TLIST_RBC, c, c, TERM_ALL, FP32D) - v64) / np.linalg.norm(v64))
         cnt5 = ctx5.counts()
         ctx5.close()
         log(f"scale-up in {time.perf_counter() - t1:.1f}s")
@@ -450,10 +473,11 @@ def main():
                  "targets": N5,
                  "fp32c": {"ms_per_step": m32c, "value": ws * N5 / (m32c * 1e-3), "rel_l2_vs_fp64_plain": e32c},
                  "fp32m": {"ms_per_step": m32m, "value": ws * N5 / (m32m * 1e-3), "rel_l2_vs_fp64_plain": e32m},
+                 "fp32d": {"ms_per_step": m32d, "value": ws * N5 / (m32d * 1e-3), "rel_l2_vs_fp64_plain": e32d},
                  "fp64_plain": {"ms_per_step": m64, "value": ws * N5 / (m64 * 1e-3)},
-                 "fp32c_over_fp64": m64 / m32c, "fp32m_over_fp64": m64 / m32m,
+                 "fp32c_over_fp64": m64 / m32c, "fp32m_over_fp64": m64 / m32m, "fp32d_over_fp64": m64 / m32d,
                  "pairs_within_rc": cnt5["pairs_within_rc"], "nearsing_items": cnt5["nearsing_items"],
-                 "steps": "fp32c, fp32m: 2 warm-up + 3 timed; fp64: 1 + 1"}
+                 "steps": "fp32c, fp32m, fp32d: 2 warm-up + 3 timed; fp64: 1 + 1"}
 
     # ---- wall no-slip GMRES on the tube workload: plain vs history vs learned guess
     wall = None
@@ -486,7 +510,7 @@ def main():
     if not args.quick and not args.no_cellsolve:
         t1 = time.perf_counter()
         arms = {}
-        for name, p in (("fp64", FP64), ("fp32m", FP32M), ("fp32c", FP32C)):
+        for name, p in (("fp64", FP64), ("fp32d", FP32D), ("fp32m", FP32M), ("fp32c", FP32C)):
             sol, v, st, code = ctx.solve_rbc_vel(12, rtol=1e-11, max_it=300, restart=30, prec=p, check=False)
             arms[name] = (sol, v, st, code)
         s64, v64 = arms["fp64"][0], arms["fp64"][1]
@@ -498,7 +522,7 @@ def main():
                                "final_rel_residual": st.rnorm / st.bnorm if st.bnorm > 0 else 0.0,
                                "rel_l2_vs_fp64_solution": float(np.linalg.norm(sol - s64) / np.linalg.norm(s64)),
                                "rel_l2_vs_fp64_velocity": float(np.linalg.norm(v - v64) / np.linalg.norm(v64))}
-        for name in ("fp32m", "fp32c"):
+        for name in ("fp32d", "fp32m", "fp32c"):
             cellsolve[name]["speedup_vs_fp64"] = arms["fp64"][2].ms / arms[name][2].ms
         log(f"cell solve comparison in {time.perf_counter() - t1:.1f}s")
 
@@ -517,12 +541,20 @@ def main():
         line = {
             "metric": "Ewald matvec targets/s", "value": value, "unit": "targets/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32c+f64corr",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+ff48-patch+f64-near",
             "data": "synthetic (seeded biconcave cells, SH densities)",
             "config": dict(WORKLOAD, targets=N, l2="working set (spline tables 307 MB, PME grids) > 129 MB L2"),
-            "rel_l2_vs_fp64_plain": err32c,
+            "mode": "FP32D: pair sums, PME in FP32 with compensated accumulation; own-cell polar patch in "
+                    "float-float arithmetic (48-bit significands, 2e-12 from the FP64 patch); near-singular "
+                    "correction in FP64",
+            "rel_l2_vs_fp64_plain": err32d,
+            "patch_corrections_rel_l2_vs_fp64_patch": self_ff_vs_fp64,
             "fp64_plain": {"value": fp64_value, "unit": "targets/s", "ms_per_step": ms64,
-                           "fp32c_over_fp64": value / fp64_value, "stages_ms_per_step": st64},
+                           "fp32d_over_fp64": value / fp64_value, "stages_ms_per_step": st64},
+            "fp32c": {"value": fp32c_value, "unit": "targets/s", "ms_per_step": msc,
+                      "over_fp64": fp32c_value / fp64_value, "rel_l2_vs_fp64_plain": err32c,
+                      "stages_ms_per_step": stc,
+                      "note": "own-cell polar patch on the FP64 pipe"},
             "fp32m": {"value": fp32m_value, "unit": "targets/s", "ms_per_step": msm,
                       "over_fp64": fp32m_value / fp64_value, "rel_l2_vs_fp64_plain": err32m,
                       "stages_ms_per_step": stm,
@@ -534,10 +566,11 @@ def main():
                                               "screen_misses", "near_replays", "near_projections")},
             "roofline": roof,
             "rooflines": rooflines,
-            "fp32_over_fp64_plain": {"fp32c": value / fp64_value, "fp32m": fp32m_value / fp64_value,
-                                     "target": 20.0,
-                                     "note": "fp32c keeps the self patch in FP64 (GB300 FP64 is 1/74 of FP32); "
-                                             "fp32m does it in FP32 with hi/lo geometry"},
+            "fp32_over_fp64_plain": {"fp32d": value / fp64_value, "fp32c": fp32c_value / fp64_value,
+                                     "fp32m": fp32m_value / fp64_value, "target": 20.0,
+                                     "note": "fp32d: self patch in float-float on the FP32 pipe (GB300 FP64 is "
+                                             "1/74 of FP32); fp32c: on the FP64 pipe; fp32m: in FP32 with hi/lo "
+                                             "geometry"},
             "scaleup_c5": scale,
             "wall_gmres": wall,
             "cell_gmres": cellsolve,

@@ -52,9 +52,13 @@ enum {
   RBC3D_FP32C = 1, /* pair sums, spread, FFT, gather in FP32 with per-target
                       compensated accumulation; self / near-singular
                       corrections FP64 */
-  RBC3D_FP32M = 2  /* as FP32C, but the own-cell polar patch (RBC_SingInt) in
+  RBC3D_FP32M = 2, /* as FP32C, but the own-cell polar patch (RBC_SingInt) in
                       FP32 with FP64-accurate (hi/lo) positions; needs the
                       uniform longitude grid phi(j) = j*2*pi/nlon */
+  RBC3D_FP32D = 3  /* as FP32C, but the own-cell polar patch in float-float
+                      arithmetic (hi + lo FP32 pairs, 48 significant bits) on
+                      the FP32 pipe: agrees with the FP64 patch to ~1e-13;
+                      needs the uniform longitude grid */
 };
 
 /* Target lists (t_TargetList instances of ModData.F90:19-20). */

@@ -9,7 +9,7 @@ from __future__ import annotations
 
 import os
 
-from .abi import (FP32C, FP32M, FP64, TERM_ALL, TERM_CORR, TERM_LINEAR, TERM_PME, TERM_REAL,
+from .abi import (FP32C, FP32D, FP32M, FP64, TERM_ALL, TERM_CORR, TERM_LINEAR, TERM_PME, TERM_REAL,
                   TERM_WALLS, TLIST_RAW, TLIST_RBC, TLIST_WALL, Context, Library, RBC3DError)
 
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "librbc3d_gb300.so")
@@ -34,6 +34,6 @@ def context(params: dict) -> Context:
     return Context(library(), params)
 
 
-__all__ = ["library", "context", "Context", "Library", "RBC3DError", "FP64", "FP32C", "FP32M", "TLIST_RBC",
+__all__ = ["library", "context", "Context", "Library", "RBC3DError", "FP64", "FP32C", "FP32M", "FP32D", "TLIST_RBC",
            "TLIST_WALL", "TLIST_RAW", "TERM_ALL", "TERM_REAL", "TERM_CORR", "TERM_LINEAR", "TERM_PME",
            "TERM_WALLS"]

@@ -12,7 +12,7 @@ import ctypes as C
 import numpy as np
 
 MAX_CELLTYPES = 8
-FP64, FP32C, FP32M = 0, 1, 2
+FP64, FP32C, FP32M, FP32D = 0, 1, 2, 3
 TLIST_RBC, TLIST_WALL, TLIST_RAW = 0, 1, 2
 TERM_REAL, TERM_CORR, TERM_LINEAR, TERM_PME, TERM_WALLS = 1, 2, 4, 8, 16
 TERM_ALL = 31

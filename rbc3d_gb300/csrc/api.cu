@@ -175,6 +175,7 @@ rbc3d_status self_stage(rbc3d_ctx* ctx, int which, double c1, double c2, int pre
     if (!ctx->phi_uniform) return ctx_fail(ctx, RBC3D_ERR_ARG, "FP32M needs phi(j) = j*2*pi/nlon");
     return run_self_mixed(ctx, which, c1, c2);
   }
+  if (prec == RBC3D_FP32D) return run_self_ff(ctx, which, c1, c2);
   return run_self_corr(ctx, which, c1, c2);
 }
 
@@ -197,8 +198,33 @@ __global__ void k_vadd(long long n, const double* __restrict__ a, double* __rest
   if (i < n) v[i] += a[i];
 }
 
+// The own-cell patch correction (with_self) and PME (with_pme) on the side
+// stream, into the side accumulator t.v2; the main stream joins at ev_join.
+rbc3d_status fork_side(rbc3d_ctx* ctx, int which, double c1, double c2, unsigned terms, int prec, bool with_self,
+                       bool with_pme) {
+  TargetSet& t = ctx->tl[which];
+  const double sc1 = ctx->has_f ? c1 : 0.0, sc2 = ctx->has_g ? c2 : 0.0;
+  CUDA_TRY(t.v2.alloc(3 * (size_t)std::max(t.n, 1)));
+  CUDA_TRY(cudaEventRecord(ctx->ev_fork, ctx->st));
+  CUDA_TRY(cudaStreamWaitEvent(ctx->st2, ctx->ev_fork, 0));
+  std::swap(ctx->st, ctx->st2);
+  dbuf_swap(t.v, t.v2);
+  rbc3d_status s = RBC3D_OK;
+  if (cudaMemsetAsync(t.v.p, 0, sizeof(double) * 3 * t.n, ctx->st) != cudaSuccess) s = RBC3D_ERR_CUDA;
+  if (!s && with_self) s = self_stage(ctx, which, sc1, sc2, prec);
+  if (!s && with_pme) s = pme_stages(ctx, which, c1, c2, terms, prec);
+  dbuf_swap(t.v, t.v2);
+  std::swap(ctx->st, ctx->st2);
+  CUDA_TRY(cudaEventRecord(ctx->ev_join, ctx->st2));
+  return s;
+}
+
+// near_side: the near-singular pass runs on the side stream after the pair
+// sums (which list its work items), into the side accumulator, next to the
+// patch correction on the main stream; the main stream waits for it before
+// reading the counters.
 rbc3d_status rbcs_dev(rbc3d_ctx* ctx, int which, double c1, double c2, int prec, unsigned terms,
-                      bool self_elsewhere = false) {
+                      bool self_elsewhere = false, bool near_side = false) {
   if (ctx->npt == 0) return RBC3D_OK;
   // a density that was never set is zero (the reference's cells start with f = g = 0)
   if (!ctx->has_f) c1 = 0.0;
@@ -229,8 +255,24 @@ rbc3d_status rbcs_dev(rbc3d_ctx* ctx, int which, double c1, double c2, int prec,
     CUDA_TRY(cudaMemsetAsync(ctx->dcnt.p + 3, 0, sizeof(unsigned long long), ctx->st));
     CUDA_TRY(cudaMemsetAsync(ctx->dcnt.p + 6, 0, sizeof(unsigned long long), ctx->st));
     CUDA_TRY(cudaMemsetAsync(ctx->dcnt.p + 8, 0, sizeof(unsigned long long) * 3, ctx->st));
+    if (near_side) {
+      CUDA_TRY(cudaEventRecord(ctx->ev_fork, ctx->st));
+      CUDA_TRY(cudaStreamWaitEvent(ctx->st2, ctx->ev_fork, 0));
+      std::swap(ctx->st, ctx->st2);
+      dbuf_swap(t.v, t.v2);
+      {
+        StageScope sc(ctx, 2);
+        s = run_near_corr(ctx, which, c1, c2, prec);
+      }
+      dbuf_swap(t.v, t.v2);
+      std::swap(ctx->st, ctx->st2);
+      CUDA_TRY(cudaEventRecord(ctx->ev_join, ctx->st2));
+      if (s) return s;
+    }
     if (!self_elsewhere && (s = self_stage(ctx, which, c1, c2, prec))) return s;
-    {
+    if (near_side) {
+      CUDA_TRY(cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0));
+    } else {
       StageScope sc(ctx, 2);
       if ((s = run_near_corr(ctx, which, c1, c2, prec))) return s;
     }
@@ -274,25 +316,16 @@ rbc3d_status matvec_dev(rbc3d_ctx* ctx, int which, double c1, double c2, unsigne
   // the short FP32 one (FP32M: 8.5 ms against 9.0 with PME on the main
   // stream), else the main one after the pair and near passes (FP32C: 52.7
   // against 53.1 ms)
-  const bool pme_side = prec == RBC3D_FP32M;
-  if (side) {
-    const double sc1 = ctx->has_f ? c1 : 0.0, sc2 = ctx->has_g ? c2 : 0.0;
-    CUDA_TRY(t.v2.alloc(3 * (size_t)std::max(t.n, 1)));
-    CUDA_TRY(cudaEventRecord(ctx->ev_fork, ctx->st));
-    CUDA_TRY(cudaStreamWaitEvent(ctx->st2, ctx->ev_fork, 0));
-    std::swap(ctx->st, ctx->st2);
-    dbuf_swap(t.v, t.v2);
-    s = RBC3D_OK;
-    if (cudaMemsetAsync(t.v.p, 0, sizeof(double) * 3 * t.n, ctx->st) != cudaSuccess) s = RBC3D_ERR_CUDA;
-    if (!s) s = self_stage(ctx, which, sc1, sc2, prec);
-    if (!s && pme_side) s = pme_stages(ctx, which, c1, c2, terms, prec);
-    dbuf_swap(t.v, t.v2);
-    std::swap(ctx->st, ctx->st2);
-    CUDA_TRY(cudaEventRecord(ctx->ev_join, ctx->st2));
-    if (s) return s;
-  }
+  // The float-float patch (FP32D) loads the FP32 pipe and L1 like the pair
+  // sums: next to them it took 15.6 ms against 7.3 alone, so it stays on the
+  // main stream after them, and the side stream takes PME and then the FP64
+  // near-singular pass, which loads the FP64 pipe.
+  const bool self_side = prec != RBC3D_FP32D;
+  const bool pme_side = prec == RBC3D_FP32M || prec == RBC3D_FP32D;
+  const bool near_side = side && prec == RBC3D_FP32D;
+  if (side && (s = fork_side(ctx, which, c1, c2, terms, prec, self_side, pme_side))) return s;
   if (terms & (RBC3D_TERM_REAL | RBC3D_TERM_CORR | RBC3D_TERM_LINEAR))
-    if ((s = rbcs_dev(ctx, which, c1, c2, prec, terms, side))) return s;
+    if ((s = rbcs_dev(ctx, which, c1, c2, prec, terms, side && self_side, near_side))) return s;
   if (terms & RBC3D_TERM_WALLS) {
     StageScope sc(ctx, 4);
     if (which == RBC3D_TLIST_WALL) { if ((s = run_wall_self(ctx, c1))) return s; }
@@ -388,6 +421,7 @@ rbc3d_status rbc3d_create(const rbc3d_params* prm, rbc3d_ctx** out) {
       ctx->t_mask32.upload(mk32.data(), mk32.size(), ctx->st) || ctx->dcnt.alloc(16) || ctx->xvint.alloc(3) ||
       ctx->dBcoef.upload(ctx->Bcoef, RBC3D_MAX_CELLTYPES, ctx->st))
     return bail(RBC3D_ERR_CUDA);
+  if (self_ff_tables(ctx, c1, c2, dl)) return bail(RBC3D_ERR_CUDA);
   Tables& T = ctx->T;
   T.sl_c1 = ctx->t_sl1.p; T.sl_c2 = ctx->t_sl2.p; T.dl_c1 = ctx->t_dl.p; T.mask = ctx->t_mask.p;
   T.sl32 = ctx->t_sl32.p; T.dl32 = ctx->t_dl32.p; T.mask32 = ctx->t_mask32.p;
@@ -532,6 +566,8 @@ rbc3d_status rbc3d_set_cell_grid(rbc3d_ctx* ctx, const double* th, const double*
       W[i] = e;
     }
     CUDA_TRY(ctx->self_w64.upload(reinterpret_cast<const char*>(W.data()), W.size() * sizeof(SelfW64), ctx->st));
+    rbc3d_status s = self_ff_grid(ctx, W, pw);
+    if (s) return s;
   }
   CUDA_TRY(ctx->thG.upload(thG.data(), thG.size(), ctx->st));
   CUDA_TRY(ctx->phiA.upload(phiA.data(), phiA.size(), ctx->st));

@@ -191,6 +191,15 @@ struct rbc3d_ctx {
   DBuf<float4> mix_thi, mix_tlo;
   bool phi_uniform = false;
 
+  // FP32D self patch: float-float node records [cell][slot x quad][node],
+  // the patch weights of k_self as hi/lo planes, pw and the Ewald tables as
+  // hi/lo; ff_sets: which record sets (bit 0 x, 1 f, 2 g, 3 a3) are current
+  DBuf<int2> ff_widx;
+  DBuf<float4> ff_rec, ff_w, ff_tab;
+  DBuf<float2> ff_pw;
+  DBuf<unsigned> ff_bnd;  // [set][cell][slot]: max |value| (float bits) for the sums' offsets
+  int ff_sets = 0;
+
   // membrane mechanics (membrane.cu): transform tables of the degree < nlat
   // expansion and the reference cells' a_rcp and b, [type][4][nv]
   struct MbState {
@@ -274,7 +283,14 @@ rbc3d_status self_mixed_grid(rbc3d_ctx* ctx, const std::vector<double>& thG, con
 rbc3d_status self_mixed_geom(rbc3d_ctx* ctx);
 rbc3d_status self_mixed_density(rbc3d_ctx* ctx, bool f, bool g);
 rbc3d_status run_self_mixed(rbc3d_ctx* ctx, int tlist, double c1, double c2);
-inline bool valid_prec(int p) { return p == RBC3D_FP64 || p == RBC3D_FP32C || p == RBC3D_FP32M; }
+rbc3d_status self_ff_tables(rbc3d_ctx* ctx, const std::vector<double>& c1, const std::vector<double>& c2,
+                            const std::vector<double>& dl);
+rbc3d_status self_ff_grid(rbc3d_ctx* ctx, const std::vector<SelfW64>& W, const std::vector<double>& pw);
+void self_ff_invalidate(rbc3d_ctx* ctx, bool geom, bool f, bool g);
+rbc3d_status run_self_ff(rbc3d_ctx* ctx, int tlist, double c1, double c2);
+inline bool valid_prec(int p) {
+  return p == RBC3D_FP64 || p == RBC3D_FP32C || p == RBC3D_FP32M || p == RBC3D_FP32D;
+}
 // mixed-precision solves: relative residual reduction asked of each inner
 // FP32 GMRES solve (well above the FP32 operators' ~3e-7 relative error)
 constexpr double RBC3D_IR_ETA = 1e-5;

@@ -270,6 +270,7 @@ rbc3d_status self_mixed_grid(rbc3d_ctx* ctx, const std::vector<double>& thG, con
 
 // FP32 node records and target positions for the current geometry.
 rbc3d_status self_mixed_geom(rbc3d_ctx* ctx) {
+  self_ff_invalidate(ctx, true, false, false);
   const int nv = ctx->nlat * ctx->nlon;
   // cell centres (mean of the grid points) from the uploaded positions
   CUDA_TRY(ctx->mix_xc.alloc(3 * (size_t)ctx->ncell));
@@ -288,6 +289,7 @@ rbc3d_status self_mixed_geom(rbc3d_ctx* ctx) {
 }
 
 rbc3d_status self_mixed_density(rbc3d_ctx* ctx, bool f, bool g) {
+  self_ff_invalidate(ctx, false, f, g);
   long long per = (long long)ctx->m * ctx->nlon;
   if (!ctx->mix_rec.p || (!f && !g)) return RBC3D_OK;
   { k_mix_dens<<<nblk(ctx->ncell * per, 256), 256, 0, ctx->st>>>(ctx->ncell, ctx->m, ctx->nlon, ctx->spl.p,

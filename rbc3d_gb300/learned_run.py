@@ -25,7 +25,7 @@ import numpy as np
 
 from . import geometry as G
 from . import library
-from .abi import FP32C, FP32M, FP64, Context
+from .abi import FP32C, FP32D, FP32M, FP64, Context
 from .dynamics import CellDynamics
 from .learned import WallGuess
 
@@ -154,7 +154,7 @@ if __name__ == "__main__":
     ap.add_argument("--prec", choices=("fp64", "fp32c", "fp32m"), default="fp64",
                     help="operator arithmetic of every arm (FP32 modes: mixed-precision solves)")
     a = ap.parse_args()
-    prec = {"fp64": FP64, "fp32c": FP32C, "fp32m": FP32M}[a.prec]
+    prec = {"fp64": FP64, "fp32c": FP32C, "fp32m": FP32M, "fp32d": FP32D}[a.prec]
     dt = a.dt if a.dt is not None else (1e-3 if a.dynamics == "skalak" else 5e-3)
     print(json.dumps(run(a.cells, a.warm, a.test, restart=a.restart, train_iters=a.train_iters, history=a.history,
                          prec=prec, dynamics=a.dynamics, dt=dt, log=print)))

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from rbc3d_gb300 import geometry as G
-from rbc3d_gb300.abi import FP32C, FP32M, FP64, Context
+from rbc3d_gb300.abi import FP32C, FP32D, FP32M, FP64, Context
 
 _dp = ctypes.POINTER(ctypes.c_double)
 NLAT0 = 12  # spherical-harmonic degree < 12 on the 25 x 50 grid
@@ -133,7 +133,7 @@ def test_gpu_cell_solve_matches_oracle(gpu, oracle, visc):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("prec", [FP32C, FP32M])
+@pytest.mark.parametrize("prec", [FP32C, FP32M, FP32D])
 def test_gpu_cell_solve_mixed_precision(gpu, prec):
     # FP32 double-layer operator inside FP64 refinement, to the reference's 1e-11
     prm, cells = _small(ncell=3, visc=5.0)

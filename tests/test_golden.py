@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from conftest import ROOT
-from rbc3d_gb300.abi import Context, FP32C, FP32M, FP64, TERM_ALL, TLIST_RAW, TLIST_RBC
+from rbc3d_gb300.abi import Context, FP32C, FP32D, FP32M, FP64, TERM_ALL, TLIST_RAW, TLIST_RBC
 
 import importlib.util
 
@@ -60,7 +60,7 @@ def test_oracle_reproduces_golden(oracle):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("prec,tol", [(FP64, 1e-10), (FP32C, 1e-6), (FP32M, 1e-6)])
+@pytest.mark.parametrize("prec,tol", [(FP64, 1e-10), (FP32C, 1e-6), (FP32M, 1e-6), (FP32D, 1e-6)])
 def test_gpu_matches_golden(gpu, prec, tol):
     g = np.load(os.path.join(ROOT, "tests", "golden", "golden_3cells_sldl.npz"))
     v, _, cnt = _run(gpu, prec)

@@ -12,7 +12,7 @@ import pytest
 
 from rbc3d_gb300 import RBC3DError
 from rbc3d_gb300 import geometry as G
-from rbc3d_gb300.abi import (Context, FP32C, FP32M, FP64, TERM_ALL, TERM_CORR, TERM_LINEAR, TERM_PME, TERM_REAL,
+from rbc3d_gb300.abi import (Context, FP32C, FP32D, FP32M, FP64, TERM_ALL, TERM_CORR, TERM_LINEAR, TERM_PME, TERM_REAL,
                              TLIST_RAW, TLIST_RBC, TLIST_WALL)
 
 pytestmark = pytest.mark.gpu
@@ -43,7 +43,7 @@ def sldl_case():
     return prm, cells
 
 
-@pytest.mark.parametrize("prec,tol", [(FP64, 1e-12), (FP32C, 1e-6), (FP32M, 1e-6)])
+@pytest.mark.parametrize("prec,tol", [(FP64, 1e-12), (FP32C, 1e-6), (FP32M, 1e-6), (FP32D, 1e-6)])
 def test_c1_single_layer(gpu, oracle, c1_case, prec, tol):
     prm, cells = c1_case
     o = setup(oracle, prm, cells, False)
@@ -60,7 +60,7 @@ def test_c1_single_layer(gpu, oracle, c1_case, prec, tol):
     assert rel(vg + pg, vo + po) < tol
 
 
-@pytest.mark.parametrize("prec,tol", [(FP64, 1e-10), (FP32C, 1e-6), (FP32M, 1e-6)])
+@pytest.mark.parametrize("prec,tol", [(FP64, 1e-10), (FP32C, 1e-6), (FP32M, 1e-6), (FP32D, 1e-6)])
 def test_sldl_with_near_singular(gpu, oracle, sldl_case, prec, tol):
     prm, cells = sldl_case
     o = setup(oracle, prm, cells, True)
@@ -119,6 +119,30 @@ def test_fp32c_vs_fp64_full_size_c2(gpu):
     assert rel(v32, v64) < 1e-6
     v32m = g.matvec(TLIST_RBC, C, C, TERM_ALL, FP32M)
     assert rel(v32m, v64) < 1e-6
+    v32d = g.matvec(TLIST_RBC, C, C, TERM_ALL, FP32D)
+    assert rel(v32d, v64) < 1e-6
+    # the float-float patch agrees with the FP64 patch far below the FP32 error
+    cc = g.matvec(TLIST_RBC, C, C, TERM_CORR, FP32C)
+    cd = g.matvec(TLIST_RBC, C, C, TERM_CORR, FP32D)
+    assert rel(cd, cc) < 1e-11
+
+
+@pytest.mark.parametrize("c1,c2", [(C, C), (C, 0.0), (0.0, C)])
+def test_fp32d_patch_matches_fp64_patch(gpu, sldl_case, c1, c2):
+    """RBC_SingInt in float-float arithmetic (FP32D) against the FP64 kernel
+    (FP32C): the patch corrections alone (self + near-singular, the latter the
+    same FP64 pass in both modes) agree to 1e-11 relative for SL+DL, SL and DL."""
+    prm, cells = sldl_case
+    g = setup(gpu, prm, cells, True)
+    cc = g.matvec(TLIST_RBC, c1, c2, TERM_CORR, FP32C)
+    cd = g.matvec(TLIST_RBC, c1, c2, TERM_CORR, FP32D)
+    assert np.linalg.norm(cc) > 0
+    assert rel(cd, cc) < 1e-11
+    # records are rebuilt after the density changes
+    g.set_cell_density(f=2 * cells.f, g=-cells.g, spl_F=2 * cells.spl_F, spl_G=-cells.spl_G)
+    cc2 = g.matvec(TLIST_RBC, c1, c2, TERM_CORR, FP32C)
+    cd2 = g.matvec(TLIST_RBC, c1, c2, TERM_CORR, FP32D)
+    assert rel(cd2, cc2) < 1e-11
 
 
 def test_linearity_in_density(gpu, sldl_case):
