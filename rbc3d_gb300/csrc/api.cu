@@ -219,12 +219,12 @@ rbc3d_status fork_side(rbc3d_ctx* ctx, int which, double c1, double c2, unsigned
   return s;
 }
 
-// near_side: the near-singular pass runs on the side stream after the pair
-// sums (which list its work items), into the side accumulator, next to the
-// patch correction on the main stream; the main stream waits for it before
-// reading the counters.
+// self_late: the patch correction forks to the (low-priority) side stream
+// after the pair sums, into the side accumulator, while the near-singular
+// pass runs on the main stream, one block per SM so that patch blocks fit
+// beside it.
 rbc3d_status rbcs_dev(rbc3d_ctx* ctx, int which, double c1, double c2, int prec, unsigned terms,
-                      bool self_elsewhere = false, bool near_side = false) {
+                      bool self_elsewhere = false, bool self_late = false) {
   if (ctx->npt == 0) return RBC3D_OK;
   // a density that was never set is zero (the reference's cells start with f = g = 0)
   if (!ctx->has_f) c1 = 0.0;
@@ -255,26 +255,25 @@ rbc3d_status rbcs_dev(rbc3d_ctx* ctx, int which, double c1, double c2, int prec,
     CUDA_TRY(cudaMemsetAsync(ctx->dcnt.p + 3, 0, sizeof(unsigned long long), ctx->st));
     CUDA_TRY(cudaMemsetAsync(ctx->dcnt.p + 6, 0, sizeof(unsigned long long), ctx->st));
     CUDA_TRY(cudaMemsetAsync(ctx->dcnt.p + 8, 0, sizeof(unsigned long long) * 3, ctx->st));
-    if (near_side) {
+    if (self_late) {  // after fork_side: t.v2 is zeroed and PME queued on the side stream
       CUDA_TRY(cudaEventRecord(ctx->ev_fork, ctx->st));
       CUDA_TRY(cudaStreamWaitEvent(ctx->st2, ctx->ev_fork, 0));
       std::swap(ctx->st, ctx->st2);
       dbuf_swap(t.v, t.v2);
-      {
-        StageScope sc(ctx, 2);
-        s = run_near_corr(ctx, which, c1, c2, prec);
-      }
+      s = self_stage(ctx, which, c1, c2, prec);
       dbuf_swap(t.v, t.v2);
       std::swap(ctx->st, ctx->st2);
       CUDA_TRY(cudaEventRecord(ctx->ev_join, ctx->st2));
       if (s) return s;
+    } else if (!self_elsewhere && (s = self_stage(ctx, which, c1, c2, prec))) {
+      return s;
     }
-    if (!self_elsewhere && (s = self_stage(ctx, which, c1, c2, prec))) return s;
-    if (near_side) {
-      CUDA_TRY(cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0));
-    } else {
+    {
       StageScope sc(ctx, 2);
-      if ((s = run_near_corr(ctx, which, c1, c2, prec))) return s;
+      ctx->near_cap_per_sm = self_late ? 1 : 0;
+      s = run_near_corr(ctx, which, c1, c2, prec);
+      ctx->near_cap_per_sm = 0;
+      if (s) return s;
     }
   }
   if (terms & RBC3D_TERM_LINEAR) {
@@ -317,15 +316,17 @@ rbc3d_status matvec_dev(rbc3d_ctx* ctx, int which, double c1, double c2, unsigne
   // stream), else the main one after the pair and near passes (FP32C: 52.7
   // against 53.1 ms)
   // The float-float patch (FP32D) loads the FP32 pipe and L1 like the pair
-  // sums: next to them it took 15.6 ms against 7.3 alone, so it stays on the
-  // main stream after them, and the side stream takes PME and then the FP64
-  // near-singular pass, which loads the FP64 pipe.
-  const bool self_side = prec != RBC3D_FP32D;
-  const bool pme_side = prec == RBC3D_FP32M || prec == RBC3D_FP32D;
-  const bool near_side = side && prec == RBC3D_FP32D;
-  if (side && (s = fork_side(ctx, which, c1, c2, terms, prec, self_side, pme_side))) return s;
+  // sums: next to them it took 15.6 ms against 6.9 alone.  So the side
+  // stream runs PME next to the pair sums and then the patch, forked after
+  // them, while the main stream runs the FP64 near-singular pass next to the
+  // patch: 12.2 ms, against 13.7 with PME on the main stream and 13.4 with
+  // PME on a third (also low-priority) stream, where the FFTs interleave
+  // with the patch.
+  const bool late = side && prec == RBC3D_FP32D;
+  const bool pme_side = prec == RBC3D_FP32M || late;
+  if (side && (s = fork_side(ctx, which, c1, c2, terms, prec, !late, pme_side))) return s;
   if (terms & (RBC3D_TERM_REAL | RBC3D_TERM_CORR | RBC3D_TERM_LINEAR))
-    if ((s = rbcs_dev(ctx, which, c1, c2, prec, terms, side && self_side, near_side))) return s;
+    if ((s = rbcs_dev(ctx, which, c1, c2, prec, terms, side && !late, late))) return s;
   if (terms & RBC3D_TERM_WALLS) {
     StageScope sc(ctx, 4);
     if (which == RBC3D_TLIST_WALL) { if ((s = run_wall_self(ctx, c1))) return s; }
