@@ -319,9 +319,10 @@ rbc3d_status matvec_dev(rbc3d_ctx* ctx, int which, double c1, double c2, unsigne
   // sums: next to them it took 15.6 ms against 6.9 alone.  So the side
   // stream runs PME next to the pair sums and then the patch, forked after
   // them, while the main stream runs the FP64 near-singular pass next to the
-  // patch: 12.2 ms, against 13.7 with PME on the main stream and 13.4 with
-  // PME on a third (also low-priority) stream, where the FFTs interleave
-  // with the patch.
+  // patch: 12.2 ms, against 13.7 with PME on the main stream, 13.4 with PME
+  // on a third low-priority stream (the FFTs interleave with the patch) and
+  // 13.5 with PME on a third stream of medium priority (it starves the
+  // patch).
   const bool late = side && prec == RBC3D_FP32D;
   const bool pme_side = prec == RBC3D_FP32M || late;
   if (side && (s = fork_side(ctx, which, c1, c2, terms, prec, !late, pme_side))) return s;
