@@ -221,8 +221,7 @@ rbc3d_status fork_side(rbc3d_ctx* ctx, int which, double c1, double c2, unsigned
 
 // self_late: the patch correction forks to the (low-priority) side stream
 // after the pair sums, into the side accumulator, while the near-singular
-// pass runs on the main stream, one block per SM so that patch blocks fit
-// beside it.
+// pass runs on the main stream.
 rbc3d_status rbcs_dev(rbc3d_ctx* ctx, int which, double c1, double c2, int prec, unsigned terms,
                       bool self_elsewhere = false, bool self_late = false) {
   if (ctx->npt == 0) return RBC3D_OK;
@@ -270,10 +269,7 @@ rbc3d_status rbcs_dev(rbc3d_ctx* ctx, int which, double c1, double c2, int prec,
     }
     {
       StageScope sc(ctx, 2);
-      ctx->near_cap_per_sm = self_late ? 1 : 0;
-      s = run_near_corr(ctx, which, c1, c2, prec);
-      ctx->near_cap_per_sm = 0;
-      if (s) return s;
+      if ((s = run_near_corr(ctx, which, c1, c2, prec))) return s;
     }
   }
   if (terms & RBC3D_TERM_LINEAR) {
@@ -318,8 +314,8 @@ rbc3d_status matvec_dev(rbc3d_ctx* ctx, int which, double c1, double c2, unsigne
   // The float-float patch (FP32D) loads the FP32 pipe and L1 like the pair
   // sums: next to them it took 15.6 ms against 6.9 alone.  So the side
   // stream runs PME next to the pair sums and then the patch, forked after
-  // them, while the main stream runs the FP64 near-singular pass next to the
-  // patch: 12.2 ms, against 13.7 with PME on the main stream, 13.4 with PME
+  // them, while the main stream runs the FP64 near-singular pass beside the
+  // end of PME: 12.2 ms, against 13.7 with PME on the main stream, 13.4 with PME
   // on a third low-priority stream (the FFTs interleave with the patch) and
   // 13.5 with PME on a third stream of medium priority (it starves the
   // patch).

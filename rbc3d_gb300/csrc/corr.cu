@@ -762,9 +762,6 @@ rbc3d_status run_near_corr(rbc3d_ctx* ctx, int tlist, double c1, double c2, int 
     a.nlist = ctx->dcnt.p + 10;
   }
   CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_near, 128, 0));
-  // next to the float-float patch (FP32D) one block per SM, so that a patch
-  // block fits beside it in the register file
-  if (ctx->near_cap_per_sm > 0) per_sm = std::min(per_sm, ctx->near_cap_per_sm);
   CUDA_TRY(ctx->near_queue.alloc(1));
   CUDA_TRY(cudaMemsetAsync(ctx->near_queue.p, 0, sizeof(unsigned long long), ctx->st));
   a.queue = ctx->near_queue.p;

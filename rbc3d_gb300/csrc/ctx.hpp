@@ -199,7 +199,6 @@ struct rbc3d_ctx {
   DBuf<float2> ff_pw;
   DBuf<unsigned> ff_bnd;  // [set][cell][slot]: max |value| (float bits) for the sums' offsets
   int ff_sets = 0;
-  int near_cap_per_sm = 0;  // k_near blocks per SM (0: as many as fit)
 
   // membrane mechanics (membrane.cu): transform tables of the degree < nlat
   // expansion and the reference cells' a_rcp and b, [type][4][nv]
