@@ -359,6 +359,7 @@ def main():
     te = dist_max(dist, (time.perf_counter() - te) / ke)
     e2e_value = ws * N / te
     e2e_parts = {k: v / ke * 1e3 for k, v in e2e_parts.items()}
+    h2d_gbs = lib.h2d_bandwidth(h2d)  # one pinned copy of the step's upload volume
 
     # ---- roofline of the dominant stage (device time measured above)
     nq = 200  # RBC_SingInt points per target on the 25x50 grid (nrad 10 x nazm 20)
@@ -560,7 +561,10 @@ def main():
                       "stages_ms_per_step": stm,
                       "note": "own-cell polar patch in FP32 with FP64-accurate (hi/lo) geometry"},
             "e2e": {"value": e2e_value, "unit": "targets/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "ms_per_step": te * 1e3, "host_ms_per_step": e2e_parts},
+                    "ms_per_step": te * 1e3, "host_ms_per_step": e2e_parts,
+                    "h2d_gbs_measured": h2d_gbs,
+                    "floor_ms": ms_step + h2d / (h2d_gbs * 1e9) * 1e3,
+                    "floor": "device matvec + the step's uploads at the measured pinned copy bandwidth"},
             "stages_ms_per_step": st_ms,
             "counts": {k: counts[k] for k in ("pairs_within_rc", "nbr_items", "nearsing_items", "self_items",
                                               "screen_misses", "near_replays", "near_projections")},

@@ -348,6 +348,10 @@ rbc3d_status rbc3d_host_free(void* p);
  * (prec = RBC3D_FP32C) or FP64 (RBC3D_FP64): a register-resident FMA chain
  * over all SMs, used as the roofline of the CUDA-core-bound kernels. */
 rbc3d_status rbc3d_fma_peak(int prec, double* tflops);
+/* Measured host-to-device copy bandwidth (GB/s) of this GPU from page-locked
+ * memory: one copy of `bytes` timed with CUDA events (best of 3 after a
+ * warm-up); the floor of the uploads an end-to-end step makes. */
+rbc3d_status rbc3d_h2d_bandwidth(unsigned long long bytes, double* gbs);
 
 #ifdef __cplusplus
 }

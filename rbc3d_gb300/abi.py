@@ -113,6 +113,7 @@ GPU_SIGNATURES = [
     ("host_alloc", C.c_int, [C.c_ulonglong, C.POINTER(C.c_void_p)]),
     ("host_free", C.c_int, [_vp]),
     ("fma_peak", C.c_int, [C.c_int, _dp]),
+    ("h2d_bandwidth", C.c_int, [C.c_ulonglong, _dp]),
 ]
 STAGES = ["pair", "self", "near", "linear", "walls", "pme_spread", "pme_fft_infl", "pme_gather"]
 
@@ -150,6 +151,14 @@ class Library:
                 f.restype = res
                 f.argtypes = args
                 self.fn[name] = f
+
+    def h2d_bandwidth(self, nbytes):
+        """Measured pinned host-to-device copy bandwidth, GB/s."""
+        t = C.c_double()
+        st = self.fn["h2d_bandwidth"](int(nbytes), C.byref(t))
+        if st:
+            raise RBC3DError(st, "h2d_bandwidth")
+        return t.value
 
     def fma_peak(self, prec):
         t = C.c_double()
@@ -209,10 +218,15 @@ class Context:
         """The cell grid alone (RBC_Create's colatitudes, longitudes, weights)."""
         th, phi, w = f64(th), f64(phi), f64(w)
         self._check(self.L.fn["set_cell_grid"](self.h, _ptr(th), _ptr(phi), _ptr(w)))
+        self._grid = (th.copy(), phi.copy(), w.copy())
 
     def set_cells(self, cells):
         th, phi, w = f64(cells.th), f64(cells.phi), f64(cells.w)
-        self._check(self.L.fn["set_cell_grid"](self.h, _ptr(th), _ptr(phi), _ptr(w)))
+        # RbcPolarPatch_Create and the grid tables: once per grid, not per position update
+        grid = getattr(self, "_grid", None)
+        if grid is None or not all(a.shape == b.shape and np.array_equal(a, b) for a, b in zip(grid, (th, phi, w))):
+            self._check(self.L.fn["set_cell_grid"](self.h, _ptr(th), _ptr(phi), _ptr(w)))
+            self._grid = (th.copy(), phi.copy(), w.copy())
         ct = i32(cells.celltype)
         arrs = [f64(cells.x), f64(cells.a3), f64(cells.detJ), f64(cells.area), f64(cells.meshSize),
                 f64(cells.spl_x), f64(cells.spl_a3), f64(cells.spl_detJ)]

@@ -621,12 +621,16 @@ rbc3d_status rbc3d_set_cells(rbc3d_ctx* ctx, int ncell, const int* celltype, con
   CUDA_TRY(cudaEventRecord(ctx->ev_join, ctx->st2));
   if (s) return s;
   if ((s = build_source_list(ctx))) return s;
-  CUDA_TRY(cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0));
-  if ((s = self_mixed_geom(ctx))) return s;
-  // tlist_rbc (TargetList_Update, ModTargetList.F90:95-131)
+  // tlist_rbc (TargetList_Update, ModTargetList.F90:95-131): its work units
+  // and the PME spread plan depend on the positions only, and are built while
+  // the spline tables are still going up on the side stream
   TargetSet& t = ctx->tl[RBC3D_TLIST_RBC];
   t.n = ctx->npt;
   t.sorted = false;
+  if ((s = sort_targets(ctx, RBC3D_TLIST_RBC))) return s;
+  if ((s = pme_prepare_cells(ctx))) return s;
+  CUDA_TRY(cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0));
+  if ((s = self_mixed_geom(ctx))) return s;
   DBuf<double>& Ac = ctx->acoef_dev;
   CUDA_TRY(Ac.upload(ctx->Acoef, RBC3D_MAX_CELLTYPES, ctx->st));
   CUDA_TRY(t.x.alloc(3 * N)); CUDA_TRY(t.Acoef.alloc(N)); CUDA_TRY(t.meta.alloc(N));
@@ -888,6 +892,40 @@ rbc3d_status rbc3d_host_free(void* p) { return cudaFreeHost(p) == cudaSuccess ? 
 rbc3d_status rbc3d_fma_peak(int prec, double* tflops) {
   if (!tflops) return RBC3D_ERR_ARG;
   return fma_peak(prec, tflops);
+}
+
+rbc3d_status rbc3d_h2d_bandwidth(unsigned long long bytes, double* gbs) {
+  if (!gbs || bytes == 0) return RBC3D_ERR_ARG;
+  void* h = nullptr;
+  void* d = nullptr;
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  rbc3d_status s = RBC3D_OK;
+  float best = 0.f;
+  if (cudaMallocHost(&h, bytes) != cudaSuccess || cudaMalloc(&d, bytes) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+      cudaEventCreate(&e1) != cudaSuccess || cudaMemsetAsync(d, 0, bytes, st) != cudaSuccess) {
+    s = RBC3D_ERR_NOMEM;
+  } else {
+    std::memset(h, 0, bytes);
+    for (int it = 0; it < 4 && !s; ++it) {
+      float ms = 0.f;
+      if (cudaEventRecord(e0, st) != cudaSuccess ||
+          cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+          cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+          cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+        s = RBC3D_ERR_CUDA;
+      else if (it > 0 && (best == 0.f || ms < best))
+        best = ms;
+    }
+  }
+  if (!s) *gbs = best > 0.f ? (double)bytes / (best * 1e-3) / 1e9 : 0.0;
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (st) cudaStreamDestroy(st);
+  if (d) cudaFree(d);
+  if (h) cudaFreeHost(h);
+  return s;
 }
 
 }  // extern "C"

@@ -189,6 +189,7 @@ struct rbc3d_ctx {
   DBuf<float> mix_rec, mix_pw;
   DBuf<char> mix_w;
   DBuf<float4> mix_thi, mix_tlo;
+  int mix_sets = 0;  // current FP32M node-record parts: bit 0 geometry, 1 f, 2 g
   bool phi_uniform = false;
 
   // FP32D self patch: float-float node records [cell][slot x quad][node],
@@ -252,6 +253,7 @@ rbc3d_status sort_points_by_cell(rbc3d_ctx* ctx, int n, const double* x_dev, DBu
 rbc3d_status matvec_dev(rbc3d_ctx* ctx, int which, double c1, double c2, unsigned terms, int prec);
 rbc3d_status build_source_density(rbc3d_ctx* ctx);
 rbc3d_status sort_targets(rbc3d_ctx* ctx, int tlist);
+rbc3d_status pme_prepare_cells(rbc3d_ctx* ctx);
 rbc3d_status run_pair_sum(rbc3d_ctx* ctx, int tlist, double c1, double c2, int prec, bool collect_nbr);
 rbc3d_status run_linear(rbc3d_ctx* ctx, int tlist, double c2);
 // corr.cu

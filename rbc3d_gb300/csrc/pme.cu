@@ -533,6 +533,18 @@ rbc3d_status launch_spread(rbc3d_ctx* ctx, const SpreadArgs& a, const SpreadPlan
   }
 }
 
+// The cell sources' spread plan (tile binning of the sorted positions), built
+// when the positions change rather than in the first spread after them.
+rbc3d_status pme_prepare_cells(rbc3d_ctx* ctx) {
+  PmeState& P = ctx->pme;
+  if (P.cplan.valid || ctx->npt == 0 || !ctx->s_x.p) return RBC3D_OK;
+  SpreadArgs a{};
+  for (int d = 0; d < 3; ++d) { a.N[d] = ctx->prm.Nb[d]; a.ih[d] = ctx->prm.Nb[d] / ctx->prm.Lb[d]; }
+  a.P = ctx->prm.P; a.G = P.G;
+  a.n = ctx->npt; a.x = ctx->s_x.p;
+  return build_spread_plan(ctx, a.n, a.x, a, P.cplan);
+}
+
 rbc3d_status pme_spread(rbc3d_ctx* ctx, double c1, double c2, int cells, int walls, int prec) {
   PmeState& P = ctx->pme;
   if (prec != RBC3D_FP64) prec = RBC3D_FP32C;  // FP32C and FP32M share the FP32 PME

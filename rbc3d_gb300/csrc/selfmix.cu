@@ -275,12 +275,11 @@ rbc3d_status self_mixed_geom(rbc3d_ctx* ctx) {
   // cell centres (mean of the grid points) from the uploaded positions
   CUDA_TRY(ctx->mix_xc.alloc(3 * (size_t)ctx->ncell));
   { k_cell_mean<<<ctx->ncell, 256, 0, ctx->st>>>(nv, ctx->npt, ctx->x.p, ctx->mix_xc.p); ++ctx->launches; }
-  long long per = (long long)ctx->m * ctx->nlon;
-  CUDA_TRY(ctx->mix_rec.alloc((size_t)ctx->ncell * per * REC));
+  // the node records are built on first use (run_self_mixed); the target
+  // positions serve the float-float patch too
+  ctx->mix_sets = 0;
   CUDA_TRY(ctx->mix_thi.alloc(ctx->npt));
   CUDA_TRY(ctx->mix_tlo.alloc(ctx->npt));
-  { k_mix_geom<<<nblk(ctx->ncell * per, 256), 256, 0, ctx->st>>>(ctx->ncell, ctx->m, ctx->nlon, ctx->spl.p, ctx->mix_xc.p,
-                                                                  ctx->mix_rec.p); ++ctx->launches; }
   { k_mix_targets<<<nblk(ctx->npt, 128), 128, 0, ctx->st>>>(ctx->npt, ctx->nlat, ctx->nlon, ctx->m, ctx->th.p,
                                                              ctx->phi.p, ctx->spl.p, ctx->mix_xc.p, ctx->mix_thi.p,
                                                              ctx->mix_tlo.p); ++ctx->launches; }
@@ -290,18 +289,32 @@ rbc3d_status self_mixed_geom(rbc3d_ctx* ctx) {
 
 rbc3d_status self_mixed_density(rbc3d_ctx* ctx, bool f, bool g) {
   self_ff_invalidate(ctx, false, f, g);
-  long long per = (long long)ctx->m * ctx->nlon;
-  if (!ctx->mix_rec.p || (!f && !g)) return RBC3D_OK;
-  { k_mix_dens<<<nblk(ctx->ncell * per, 256), 256, 0, ctx->st>>>(ctx->ncell, ctx->m, ctx->nlon, ctx->spl.p,
-                                                                  ctx->mix_rec.p, f, g); ++ctx->launches; }
-  CUDA_TRY(cudaGetLastError());
-  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  if (f) ctx->mix_sets &= ~2;
+  if (g) ctx->mix_sets &= ~4;
   return RBC3D_OK;
 }
 
 rbc3d_status run_self_mixed(rbc3d_ctx* ctx, int tlist, double c1, double c2) {
   TargetSet& t = ctx->tl[tlist];
   if (tlist != RBC3D_TLIST_RBC || t.n == 0 || ctx->ncell == 0) return RBC3D_OK;
+  // FP32 node records of the current geometry and densities (bit 0 geometry, 1 f, 2 g)
+  const long long per = (long long)ctx->m * ctx->nlon;
+  if (!ctx->mix_rec.p || ctx->mix_rec.n < (size_t)ctx->ncell * per * REC) {
+    CUDA_TRY(ctx->mix_rec.alloc((size_t)ctx->ncell * per * REC));
+    ctx->mix_sets = 0;
+  }
+  if (!(ctx->mix_sets & 1)) {
+    { k_mix_geom<<<nblk(ctx->ncell * per, 256), 256, 0, ctx->st>>>(ctx->ncell, ctx->m, ctx->nlon, ctx->spl.p,
+                                                                    ctx->mix_xc.p, ctx->mix_rec.p); ++ctx->launches; }
+    ctx->mix_sets |= 1;
+  }
+  const bool df = ctx->has_f && !(ctx->mix_sets & 2), dg = ctx->has_g && !(ctx->mix_sets & 4);
+  if (df || dg) {
+    { k_mix_dens<<<nblk(ctx->ncell * per, 256), 256, 0, ctx->st>>>(ctx->ncell, ctx->m, ctx->nlon, ctx->spl.p,
+                                                                    ctx->mix_rec.p, df, dg); ++ctx->launches; }
+    ctx->mix_sets |= (df ? 2 : 0) | (dg ? 4 : 0);
+  }
+  CUDA_TRY(cudaGetLastError());
   MixArgs a;
   a.nt = t.n; a.ncell = ctx->ncell; a.nlat = ctx->nlat; a.nlon = ctx->nlon; a.m = ctx->m;
   a.NQ = ctx->nrad * ctx->nazm; a.nrad = ctx->nrad;
