@@ -56,3 +56,46 @@ def test_create_rejects_bad_params():
     p = Params()  # all zeros: invalid
     h = ctypes.c_void_p()
     assert lib.fn["create"](ctypes.byref(p), ctypes.byref(h)) == 1
+
+
+def test_cell_grid_uploaded_once_per_grid(oracle):
+    """Context.set_cells calls rbc3d_set_cell_grid (RbcPolarPatch_Create and
+    the grid tables) when the grid changes, not on every position update."""
+    import numpy as np
+
+    from rbc3d_gb300 import geometry as G
+    from rbc3d_gb300.abi import Context
+    prm, cells, _ = G.config("C1", ncell=2)
+    calls = []
+    real = oracle.fn["set_cell_grid"]
+
+    def counting(*args):
+        calls.append(1)
+        return real(*args)
+
+    oracle.fn["set_cell_grid"] = counting
+    try:
+        ctx = Context(oracle, prm)
+        ctx.set_cells(cells)
+        ctx.set_cells(cells)
+        assert len(calls) == 1
+        # another grid (latitudes moved) goes up again, and the first one after it
+        other = type("Cells", (), {k: getattr(cells, k) for k in dir(cells) if not k.startswith("_")})()
+        other.th = np.array(cells.th) * (1 - 1e-9)
+        ctx.set_cells(other)
+        ctx.set_cells(cells)
+        assert len(calls) == 3
+        # an explicit grid call is remembered
+        ctx.set_cell_grid(other.th, cells.phi, cells.w)
+        ctx.set_cells(cells)
+        assert len(calls) == 5
+        ctx.close()
+    finally:
+        oracle.fn["set_cell_grid"] = real
+
+
+def test_precision_modes_match_the_header():
+    from rbc3d_gb300 import abi
+    h = open(os.path.join(ROOT, "include", "rbc3d_gpu.h")).read()
+    vals = {k: int(v) for k, v in re.findall(r"\bRBC3D_(FP64|FP32C|FP32M|FP32D)\s*=\s*(\d+)", h)}
+    assert vals == {"FP64": abi.FP64, "FP32C": abi.FP32C, "FP32M": abi.FP32M, "FP32D": abi.FP32D}
