@@ -19,7 +19,7 @@ mode 3 of rbc3d_no_slip_wall, one extra matvec), so the network can only
 lower the initial residual, and runs to the same absolute tolerance
 rtol * ||b|| as the plain solve.  A solve that does not reach it within the
 iteration budget is redone from the previous density (the plain guess, a
-zero increment), which stays the fallback and the judge.
+zero increment), which stays the fallback and the yardstick.
 """
 from __future__ import annotations
 

@@ -1,7 +1,7 @@
 """Parity of the CUDA path (through the C ABI) with the FP64 oracle.
 
-Bar (the benchmark spec): relative L2 velocity error <= 1e-6 for the FP32C matvec;
-the FP64 plain form agrees with the oracle to rounding (1e-10).  Counts of
+Bar: relative L2 velocity error <= 1e-6 for the FP32 matvec modes (FP32C,
+FP32D, FP32M); the FP64 plain form agrees with the oracle to rounding (1e-10).  Counts of
 pairs within rc, neighbour-cell items and near-singular corrections must be
 identical."""
 import math
