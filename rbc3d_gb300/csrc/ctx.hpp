@@ -192,7 +192,7 @@ struct rbc3d_ctx {
   int mix_sets = 0;  // current FP32M node-record parts: bit 0 geometry, 1 f, 2 g
   bool phi_uniform = false;
 
-  // FP32D self patch: float-float node records [cell][slot x quad][node],
+  // FP32D self patch: float-float node records [cell][slot x quad][node tile][hi, lo],
   // the patch weights of k_self as hi/lo planes, pw and the Ewald tables as
   // hi/lo; ff_sets: which record sets (bit 0 x, 1 f, 2 g, 3 a3) are current
   DBuf<int2> ff_widx;

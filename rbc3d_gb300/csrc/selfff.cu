@@ -24,13 +24,15 @@
 //
 // Data layout.  Per node and slot d (u, u_th, u_ph, u_thph) the 12 values x
 // (relative to the cell centre), f and g density sets and a3 (three
-// components each) are stored as three float4 quads of hi parts and three
-// of lo parts, each quad in its own plane [cell][d*6 + quad][node tile]:
-// the lanes of a warp interpolate at neighbouring patch points, and with
-// 2 x 4 node tiles per 128-byte line their stencil nodes share lines (a
-// record per node put each lane's load in its own line and kept the L1 data
-// pipe 95% busy).  Consecutive values share one bicubic weight, so they run in
-// pairs as packed FP32x2 operations.  Patch weights per (target latitude,
+// components each) are stored as three quads; a quad's hi and lo parts form
+// one 32-byte entry, read with one 256-bit load, in its own plane
+// [cell][d*3 + quad][node tile]: the lanes of a warp interpolate at
+// neighbouring patch points, and with 2 x 2 node tiles per 128-byte line
+// their stencil nodes share lines (a record per node put each lane's load
+// in its own line and kept the L1 data pipe 95% busy; separate hi and lo
+// planes of 16-byte entries took two loads and two lines per quad).
+// Consecutive values share one bicubic weight, so they run in pairs as
+// packed FP32x2 operations.  Patch weights per (target latitude,
 // patch point) are the 16 Spline_Interp products as hi/lo planes (coalesced
 // across the lanes, which walk consecutive patch points); target positions
 // are the FP32M hi/lo records relative to the same cell centre.
@@ -43,25 +45,26 @@ namespace {
 
 inline int nblk(long long n, int b) { return (int)((n + b - 1) / b); }
 
-constexpr int FF_PLANES = 24;  // float4 planes per cell: 4 slots x (3 hi + 3 lo quads)
+constexpr int FF_PLANES = 24;  // float4 per node: 4 slots x 3 quads x (hi, lo)
 
 // Position of spline node (i, j) in a plane: tiles of 2^ti (latitude rows) x
-// 2^tj (longitude columns) = 8 nodes, one 128-byte line per plane.  2 x 4
-// tiles measured best for the 25 x 50 grid (k_self_ff at 256 cells: 6.81 ms;
-// 4 x 2 7.02, 8 x 1 7.07, 1 x 8 7.65).
+// 2^tj (longitude columns), one 128-byte line of 32-byte entries per plane.
+// With 16-byte entries (8 per line) 2 x 4 tiles measured best for the
+// 25 x 50 grid (k_self_ff at 256 cells: 6.81 ms; 4 x 2 7.02, 8 x 1 7.07,
+// 1 x 8 7.65); 32-byte entries in 2 x 2 tiles: 6.68 ms in the matvec.
 struct NodeMap {
   int ti, tj, nti;  // log2 tile sizes, tiles along i
   long long per;    // padded nodes per plane
   __device__ __forceinline__ int pos(int i, int j) const {
-    return (((j >> tj) * nti + (i >> ti)) << 3) + (i & ((1 << ti) - 1)) + ((j & ((1 << tj) - 1)) << ti);
+    return (((j >> tj) * nti + (i >> ti)) << (ti + tj)) + (i & ((1 << ti) - 1)) + ((j & ((1 << tj) - 1)) << ti);
   }
 };
 inline NodeMap node_map(int m, int n) {
   NodeMap M;
-  M.ti = 1; M.tj = 2;
+  M.ti = 1; M.tj = 1;
   M.nti = (m + (1 << M.ti) - 1) >> M.ti;
   const int ntj = (n + (1 << M.tj) - 1) >> M.tj;
-  M.per = 8ll * M.nti * ntj;
+  M.per = (long long)M.nti * ntj << (M.ti + M.tj);
   return M;
 }
 
@@ -108,6 +111,13 @@ struct ffacc {
   }
 };
 
+// one 32-byte read-only load (hi quad, lo quad of one node)
+__device__ __forceinline__ void ld8(const float4* p, float4& h, float4& l) {
+  asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=f"(h.x), "=f"(h.y), "=f"(h.z), "=f"(h.w), "=f"(l.x), "=f"(l.y), "=f"(l.z), "=f"(l.w)
+      : "l"(p));
+}
+
 // packed FP32x2 helpers (round to nearest, as the scalar forms)
 __device__ __forceinline__ float2 sub2(float2 a, float2 b) {
   unsigned long long d;
@@ -147,7 +157,7 @@ struct FFArgs {
   int nt, ncell, nlat, nlon, m, NQ, nrad;
   const double* tA;
   double* v;
-  const float4* rec;    // [cell][FF_PLANES][m*nlon]
+  const float4* rec;    // [cell][slot x quad][node tile][hi, lo]
   const int2* widx;     // (i1, j1b) per (latitude, patch point)
   const float4* w;      // 8 planes of nlat*NQ: hi of slot d of nodes 0..3 (d = 0..3), then lo
   const float2* pw;     // patch weights, hi/lo
@@ -242,11 +252,12 @@ __device__ __forceinline__ void patch_point(const FFArgs& a, const Tgt& T, int q
     for (int k = 0; k < 4; ++k) {
       const float2 wh = make_float2(whs[k], whs[k]), nwh = make_float2(-whs[k], -whs[k]);
       const float2 wl = make_float2(wls[k], wls[k]);
-      const float4* r = T.base + nodes[k] + (size_t)(6 * d) * per;
+      const float4* r = T.base + 2 * ((size_t)(3 * d) * per + nodes[k]);
       float2 vh[DL ? 6 : 4], vl[DL ? 6 : 4];
 #pragma unroll
       for (int i = 0; i < (DL ? 3 : 2); ++i) {  // SL: quads (x.x x.y x.z f.x) (f.y f.z . .)
-        const float4 h = __ldg(r + (size_t)i * per), l = __ldg(r + (size_t)(3 + i) * per);
+        float4 h, l;
+        ld8(r + 2 * (size_t)i * per, h, l);
         vh[2 * i] = make_float2(h.x, h.y); vh[2 * i + 1] = make_float2(h.z, h.w);
         vl[2 * i] = make_float2(l.x, l.y); vl[2 * i + 1] = make_float2(l.z, l.w);
       }
@@ -357,8 +368,8 @@ __global__ void k_ff_rec(int ncell, int m, long long per, NodeMap map, const dou
   const int prev = __shfl_up_sync(0xffffffffu, cell, 1);
   const bool lead = lane == 0 || prev != cell;
   const int ni = valid ? (int)(node % m) : 0, nj = valid ? (int)(node / m) : 0;
-  float* o = reinterpret_cast<float*>(out + (size_t)cell * FF_PLANES * map.per + map.pos(ni, nj));
-  const size_t pstride = 4 * (size_t)map.per;  // floats between planes
+  float* o = reinterpret_cast<float*>(out + (size_t)cell * FF_PLANES * map.per) + 8 * (size_t)map.pos(ni, nj);
+  const size_t pstride = 8 * (size_t)map.per;  // floats between planes of 32-byte entries
   const int src[4] = {SPL_X, SPL_F, SPL_G, SPL_A3};
   for (int s = 0; s < 4; ++s) {
     if (!(sets & (1 << s))) continue;
@@ -370,7 +381,7 @@ __global__ void k_ff_rec(int ncell, int m, long long per, NodeMap map, const dou
           double v = sp[3 * d + c];
           if (s == 0 && d == 0) v -= xc[3 * cell + c];
           const int q = (3 * s + c) >> 2, e = (3 * s + c) & 3;
-          split(v, o + (6 * d + q) * pstride + e, o + (6 * d + 3 + q) * pstride + e);
+          split(v, o + (3 * d + q) * pstride + e, o + (3 * d + q) * pstride + 4 + e);
           mx = max(mx, __float_as_uint(__double2float_ru(fabs(v))));
         }
       mx = __reduce_max_sync(0xffffffffu, mx);
