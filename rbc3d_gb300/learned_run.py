@@ -151,7 +151,7 @@ if __name__ == "__main__":
     ap.add_argument("--dynamics", choices=("kinematic", "skalak"), default="skalak",
                     help="cell motion: RK2 membrane dynamics (Compute_Rbc_Vel) or rigid Poiseuille advection")
     ap.add_argument("--dt", type=float, default=None)
-    ap.add_argument("--prec", choices=("fp64", "fp32c", "fp32m"), default="fp64",
+    ap.add_argument("--prec", choices=("fp64", "fp32c", "fp32m", "fp32d"), default="fp64",
                     help="operator arithmetic of every arm (FP32 modes: mixed-precision solves)")
     a = ap.parse_args()
     prec = {"fp64": FP64, "fp32c": FP32C, "fp32m": FP32M, "fp32d": FP32D}[a.prec]
