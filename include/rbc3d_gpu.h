@@ -57,7 +57,7 @@ enum {
                       uniform longitude grid phi(j) = j*2*pi/nlon */
   RBC3D_FP32D = 3  /* as FP32C, but the own-cell polar patch in float-float
                       arithmetic (hi + lo FP32 pairs, 48 significant bits) on
-                      the FP32 pipe: agrees with the FP64 patch to ~1e-13;
+                      the FP32 pipe: agrees with the FP64 patch to 2e-12;
                       needs the uniform longitude grid */
 };
 

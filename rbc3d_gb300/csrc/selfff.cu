@@ -20,7 +20,10 @@
 //     same tables as hi/lo) is evaluated with Dekker's float-float product
 //     and sum, and 1/r by rsqrtf, an FP32 Newton step and a float-float
 //     Newton step.
-// The patch correction agrees with the FP64 kernel to ~1e-13 relative.
+// The patch corrections agree with the FP64 kernel to 2.3e-12 relative
+// (rel-L2, 256-cell workload); the interpolation sums carry errors of a few
+// 1e-12 of sum |w v| (the FP32 correction term is rounded on the scale of
+// the FastTwoSum offset).
 //
 // Data layout.  Per node and slot d (u, u_th, u_ph, u_thph) the 12 values x
 // (relative to the cell centre), f and g density sets and a3 (three
