@@ -426,7 +426,7 @@ def main():
     if s_d["self"] >= s_d["pair"]:
         roof = {"kernel": "k_self_ff (RBC_SingInt, float-float)", **rooflines["k_self_ff"],
                 "peak_source": "nominal L1 load bandwidth 128 B/clk/SM x 152 SMs x the sampled SM clock "
-                               "(ncu: L1 data pipe ~80% busy, FMA pipe ~55%)"}
+                               "(ncu: L1 data pipe 78% of its wavefront peak, FMA pipe 65%)"}
     else:
         roof = {"kernel": "k_pair32 (AddIntOnRbcs pair sums, FP32)", **rooflines["k_pair32"],
                 "peak_source": "measured FP32 FMA chain (rbc3d_fma_peak), same GPU, same run"}
