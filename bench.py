@@ -48,11 +48,18 @@ FLOP_PAIR_DL = 27   # EwaldCoeff_DL lerp + stresslet term, ModIntOnRbcs.F90:99-1
 FLOP_SELFQ_SL = 294  # one RBC_SingInt patch point, SL: 2 bicubic 3-var interps + kernel
 FLOP_SELFQ_SLDL = 550  # one patch point, SL+DL: 4 bicubic 3-var interps + both kernels
 
-WORKLOAD = {
-    "workload": "Ewald-split SL+DL matvec, 256 biconcave cells, 25x50 grid (320000 targets), "
-                "periodic L=40, rc=3 (alpha=1.5757), PME 128^3 P=6, viscRat=5",
-    "config": "C2",
+WORKLOADS = {
+    "C2": {"workload": "Ewald-split SL+DL matvec, 256 biconcave cells, 25x50 grid (320000 targets), "
+                       "periodic L=40, rc=3 (alpha=1.5757), PME 128^3 P=6, viscRat=5",
+           "config": "C2", "targets": 320000,
+           "l2": "inputs larger than L2: spline tables 307 MB + PME grids, > 129 MB L2"},
+    "C5": {"workload": "Ewald-split SL+DL matvec, 2048 biconcave cells, 25x50 grid (2560000 targets), "
+                       "periodic L=80, rc=3 (alpha=1.5757), PME 256^3 P=6, viscRat=5",
+           "config": "C5", "targets": 2560000,
+           "l2": "inputs larger than L2: spline tables 2.5 GB + PME grids, > 129 MB L2"},
 }
+WORKLOAD = WORKLOADS["C2"]
+NQ = 200  # RBC_SingInt points per target on the 25x50 grid (nrad 10 x nazm 20)
 
 
 def log(*a):
@@ -130,12 +137,12 @@ def barrier(dist):
         dist.barrier()
 
 
-def make_inputs(seed, ncell=None):
+def make_inputs(seed, ncell=None, name="C2"):
     from rbc3d_gb300 import geometry as G
-    prm, cells, _ = G.config("C2", seed=seed, ncell=ncell)
+    prm, cells, _ = G.config(name, seed=seed, ncell=ncell)
     if ncell:  # same cell density as the 256-cell box (profiling runs)
         prm["Lb"] = [40.0 * (ncell / 256.0) ** (1 / 3)] * 3
-        prm, cells, _ = G.config("C2", seed=seed, ncell=ncell, L=prm["Lb"][0])
+        prm, cells, _ = G.config(name, seed=seed, ncell=ncell, L=prm["Lb"][0])
     return prm, cells
 
 
@@ -148,7 +155,8 @@ def oracle_lib():
 
 
 def time_oracle(prm, cells, steps, threads=None):
-    """Full FP64 CPU matvec (oracle) on the host cores; returns (s per step, cores)."""
+    """Full FP64 CPU matvec (oracle) on the host cores: (seconds per step,
+    cores used, the velocity vector of the last step)."""
     import ctypes
     from rbc3d_gb300.abi import Context, TLIST_RBC, TERM_ALL
     L = oracle_lib()
@@ -161,13 +169,13 @@ def time_oracle(prm, cells, steps, threads=None):
     ctx.set_cells(cells)
     ctx.set_cell_density(f=cells.f, g=cells.g, spl_F=cells.spl_F, spl_G=cells.spl_G)
     c = 1.0 / (4 * math.pi)
-    ts = []
+    ts, v = [], None
     for _ in range(steps):
         t0 = time.perf_counter()
-        ctx.matvec(TLIST_RBC, c, c, TERM_ALL)
+        v = ctx.matvec(TLIST_RBC, c, c, TERM_ALL)
         ts.append(time.perf_counter() - t0)
     ctx.close()
-    return ts, used
+    return ts, used, v
 
 
 def run_reference(args, dist):
@@ -176,18 +184,193 @@ def run_reference(args, dist):
         return 0
     prm, cells = make_inputs(args.seed)
     N = cells.x.shape[1]
-    ts, cores = time_oracle(prm, cells, args.warmup + args.steps)
+    ts, cores, _ = time_oracle(prm, cells, args.warmup + args.steps)
     t = sum(ts[args.warmup:]) / max(args.steps, 1)
     val = N / t
     line = {"impl": "reference", "metric": "Ewald matvec targets/s", "value": val, "unit": "targets/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded)", "config": WORKLOAD,
+            "data": "synthetic (seeded biconcave cells, SH densities)", "config": WORKLOAD,
             "cpu_baseline": {"value": val, "unit": "targets/s", "cores": cores, "kind": "port",
                              "sample": f"full matvec, {N} targets, {args.steps} timed steps"},
             "e2e": {"value": val, "unit": "targets/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+class Bench:
+    """Timings of one workload on one context (all modes share the context)."""
+
+    def __init__(self, lib, prm, cells, dist, ws):
+        from rbc3d_gb300.abi import Context
+        self.lib, self.prm, self.cells, self.dist, self.ws = lib, prm, cells, dist, ws
+        self.N = cells.x.shape[1]
+        self.ctx = Context(lib, prm)
+        self.ctx.set_cells(cells)
+        self.ctx.set_cell_density(f=cells.f, g=cells.g, spl_F=cells.spl_F, spl_G=cells.spl_G)
+        self.c = 1.0 / (4 * math.pi)
+
+    def step(self, prec, terms=None):
+        from rbc3d_gb300.abi import TERM_ALL, TLIST_RBC
+        self.ctx.matvec(TLIST_RBC, self.c, self.c, TERM_ALL if terms is None else terms, prec, device_only=True)
+
+    def timed(self, prec, warm, steps, clocks=None):
+        """(ms per step, max over ranks; stage ms per step; kernel launches; clocks)."""
+        for _ in range(warm):
+            self.step(prec)
+        l0 = self.ctx.counts()["kernel_launches"]
+        barrier(self.dist)
+        if clocks:
+            clocks.start()
+        self.ctx.set_profiling(1)
+        self.ctx.timer_start()
+        for _ in range(steps):
+            self.step(prec)
+        ms = self.ctx.timer_stop()
+        clk = clocks.stop() if clocks else None
+        st = {k: v[0] / steps for k, v in self.ctx.stage_times().items()}
+        self.ctx.set_profiling(0)
+        launches = self.ctx.counts()["kernel_launches"] - l0
+        return dist_max(self.dist, ms) / steps, st, launches, clk
+
+    def vector(self, prec, terms=None):
+        from rbc3d_gb300.abi import TERM_ALL, TLIST_RBC
+        return self.ctx.matvec(TLIST_RBC, self.c, self.c, TERM_ALL if terms is None else terms, prec)
+
+    def alone(self, prec, terms, reps=3):
+        """Stage times with the stages run alone on the main stream (no PME in
+        the call keeps the matvec on one stream)."""
+        self.step(prec, terms)
+        self.ctx.set_profiling(1)
+        for _ in range(reps):
+            self.step(prec, terms)
+        st = self.ctx.stage_times()
+        self.ctx.set_profiling(0)
+        return {k: v[0] / reps for k, v in st.items()}
+
+    def e2e(self, prec, steps):
+        """The matvec through the C ABI from pinned host buffers: positions,
+        densities and spline tables uploaded every step, the caller's velocity
+        accumulator up and the velocities down."""
+        from rbc3d_gb300.abi import TERM_ALL, TLIST_RBC
+        cells, lib, ctx, c = self.cells, self.lib, self.ctx, self.c
+        pin = {}
+        for k in ("x", "a3", "detJ", "area", "meshSize", "spl_x", "spl_a3", "spl_detJ", "f", "g", "spl_F", "spl_G"):
+            a = np.ascontiguousarray(getattr(cells, k), dtype=np.float64)
+            p = lib.pinned(a.shape)
+            p[...] = a
+            pin[k] = p
+        vout = lib.pinned((3, self.N))
+
+        class PinnedCells:
+            pass
+
+        pc = PinnedCells()
+        for k in ("nlat", "nlon", "th", "phi", "w", "ncell", "celltype"):
+            setattr(pc, k, getattr(cells, k))
+        for k, p in pin.items():
+            setattr(pc, k, p)
+        h2d = sum(p.nbytes for p in pin.values()) + vout.nbytes
+        d2h = vout.nbytes
+        parts = {"set_cells": 0.0, "set_cell_density": 0.0, "matvec_with_download": 0.0}
+
+        def one():
+            t0 = time.perf_counter()
+            ctx.set_cells(pc)
+            t1 = time.perf_counter()
+            ctx.set_cell_density(f=pc.f, g=pc.g, spl_F=pc.spl_F, spl_G=pc.spl_G)
+            t2 = time.perf_counter()
+            vout[...] = 0.0
+            ctx.matvec(TLIST_RBC, c, c, TERM_ALL, prec, v=vout)
+            t3 = time.perf_counter()
+            parts["set_cells"] += t1 - t0
+            parts["set_cell_density"] += t2 - t1
+            parts["matvec_with_download"] += t3 - t2
+
+        for _ in range(2):
+            one()
+        for k in parts:
+            parts[k] = 0.0
+        barrier(self.dist)
+        te = time.perf_counter()
+        for _ in range(steps):
+            one()
+        te = dist_max(self.dist, (time.perf_counter() - te) / steps)
+        return {"value": self.ws * self.N / te, "unit": "targets/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": te * 1e3,
+                "host_ms_per_step": {k: v / steps * 1e3 for k, v in parts.items()},
+                "h2d_gbs_measured": lib.h2d_bandwidth(h2d)}
+
+    def close(self):
+        self.ctx.close()
+
+
+def rooflines_of(b, counts, peak32, peak64, hbm_peak, hbm_src, sm_mhz):
+    """Per-kernel rooflines from algorithmic work, each stage timed alone."""
+    from rbc3d_gb300.abi import FP32C, FP32D, FP32M, TERM_CORR, TERM_LINEAR, TERM_PME, TERM_REAL
+    s_c = b.alone(FP32C, TERM_REAL | TERM_CORR | TERM_LINEAR)
+    s_m = b.alone(FP32M, TERM_REAL | TERM_CORR | TERM_LINEAR)
+    s_d = b.alone(FP32D, TERM_REAL | TERM_CORR | TERM_LINEAR)
+    s_p = b.alone(FP32C, TERM_PME)
+    G3 = 1
+    for d in b.prm["Nb"]:
+        G3 *= d
+    N = b.N
+    pme_ms = s_p["pme_spread"] + s_p["pme_fft_infl"] + s_p["pme_gather"]
+    pme_bytes = 4.0 * G3 * (12 + 12 + 12 + 12 + 3 + 3 + 3 + 3) + 4.0 * N * (3 + 3 + 3 + 1) + 4.0 * N * (3 + 3)
+    pairs = counts["pairs_within_rc"]
+    pair_fl = pairs * (FLOP_PAIR_SL + FLOP_PAIR_DL)
+    self_fl = counts["self_items"] * NQ * FLOP_SELFQ_SLDL
+    # requested L1 load bytes of k_self_ff per patch point: 4 stencil nodes x
+    # 4 slots x 3 quads x 32 B (hi and lo) + 136 B of weights
+    l1_bytes = counts["self_items"] * NQ * (4 * 4 * 3 * 32 + 136)
+    l1_peak = 128.0 * 152 * sm_mhz * 1e6 / 1e9
+
+    def fl(name, ms, flops, peak, bound, work):
+        a = flops / (ms * 1e-3) / 1e12
+        return {"kernel": name, "bound": bound, "ms": ms, "achieved": a, "peak": peak, "unit": "TFLOP/s",
+                "frac": a / peak, "work": work}
+
+    r = {
+        "k_pair32": fl("k_pair32", s_c["pair"], pair_fl, peak32, "fp32",
+                       f"{pairs} pairs within rc x {FLOP_PAIR_SL + FLOP_PAIR_DL} flops"),
+        "k_self_ff": fl("k_self_ff", s_d["self"], self_fl, peak32, "fp32",
+                        f"{counts['self_items']} targets x {NQ} patch points x {FLOP_SELFQ_SLDL} flops of the FP64 "
+                        "formula, evaluated in float-float on the FP32 pipe"),
+        "k_self": fl("k_self", s_c["self"], self_fl, peak64, "fp64",
+                     f"{counts['self_items']} targets x {NQ} x {FLOP_SELFQ_SLDL} flops"),
+        "k_self_mix": fl("k_self_mix", s_m["self"], self_fl, peak32, "fp32", "the k_self work in FP32"),
+        "pme": {"kernel": "k_spread_tile + cuFFT + k_influence + k_gather", "bound": "hbm", "ms": pme_ms,
+                "achieved": pme_bytes / (pme_ms * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                "frac": pme_bytes / (pme_ms * 1e-3) / 1e9 / hbm_peak, "peak_source": hbm_src,
+                "work": "algorithmic bytes 4 G (12+12+12+12+3+3+3+3) + 4 N (3+3+3+1) + 4 N (3+3), FP32 grids"},
+        "near_ms_fp32d": s_d["near"],
+        "note": "stages timed alone on one stream (the matvec runs them on two); FP32 peak = measured FMA chain "
+                "(rbc3d_fma_peak), FP64 likewise",
+    }
+    r["k_self_ff"]["l1_request_gbs"] = l1_bytes / (s_d["self"] * 1e-3) / 1e9
+    r["k_self_ff"]["l1_request_frac_of_nominal"] = r["k_self_ff"]["l1_request_gbs"] / l1_peak
+    return r, s_d
+
+
+def headline_roofline(r, s_d, targets):
+    """The dominant kernel of the FP32D matvec (longest stage timed alone);
+    traffic = the ncu bytes per target of that kernel x this launch's targets."""
+    key = "k_self_ff" if s_d["self"] >= s_d["pair"] else "k_pair32"
+    roof = dict(r[key])
+    roof["peak_source"] = "measured FP32 FMA chain over all SMs (rbc3d_fma_peak), same GPU, same run"
+    roof["traffic"] = None
+    tpath = os.path.join(HERE, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        try:
+            roof["traffic"] = json.load(open(tpath))[key]["bytes_per_target"] * targets
+        except Exception:
+            pass
+    return roof
 
 
 def main():
@@ -200,10 +383,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline")
     ap.add_argument("--cells", type=int, default=None, help="smaller workload (profiling)")
     ap.add_argument("--quick", action="store_true", help="one mode's matvec timing only (profiling)")
-    ap.add_argument("--quick-prec", choices=("fp32c", "fp32m", "fp32d"), default="fp32d",
+    ap.add_argument("--quick-prec", choices=("fp32c", "fp32m", "fp32d", "fp64"), default="fp32d",
                     help="the mode --quick times (profiling)")
     ap.add_argument("--no-wall", action="store_true", help="skip the learned-guess wall GMRES comparison")
-    ap.add_argument("--no-scaleup", action="store_true", help="skip the 2048-cell (PME 256^3) scale-up line")
+    ap.add_argument("--no-scaleup", action="store_true", help="skip the 2048-cell (PME 256^3) workload")
     ap.add_argument("--no-cellsolve", action="store_true", help="skip the cell velocity GMRES line")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -216,273 +399,114 @@ def main():
     from rbc3d_gb300 import build as B
     B.build()
     from rbc3d_gb300 import library
-    from rbc3d_gb300.abi import (FP32C, FP32D, FP32M, FP64, STAGES, TERM_ALL, TERM_CORR, TERM_LINEAR, TERM_PME, TERM_REAL,
-                                 TLIST_RBC, Context)
+    from rbc3d_gb300.abi import FP32C, FP32D, FP32M, FP64, TERM_CORR
 
     t0 = time.perf_counter()
     prm, cells = make_inputs(args.seed + rank, args.cells)
     log(f"inputs generated in {time.perf_counter() - t0:.1f}s")
-    N = cells.x.shape[1]
     lib = library()
-    ctx = Context(lib, prm)
-    ctx.set_cells(cells)
-    ctx.set_cell_density(f=cells.f, g=cells.g, spl_F=cells.spl_F, spl_G=cells.spl_G)
-    c = 1.0 / (4 * math.pi)
+    b = Bench(lib, prm, cells, dist, ws)
+    N = b.N
+    cpu_on = rank == 0 and ws == 1 and not args.no_cpu
 
-    def step(prec):
-        ctx.matvec(TLIST_RBC, c, c, TERM_ALL, prec, device_only=True)
-
-    # ---- FP32-compensated matvec, inputs resident in HBM
-    head = {"fp32m": FP32M, "fp32c": FP32C}.get(args.quick_prec, FP32D) if args.quick else FP32D
-    for _ in range(args.warmup):
-        step(head)
-    counts = ctx.counts()
-    l0 = counts["kernel_launches"]
+    # ---- headline: FP32D matvec with every input resident in HBM
+    head = {"fp32m": FP32M, "fp32c": FP32C, "fp64": FP64}.get(args.quick_prec, FP32D) if args.quick else FP32D
     clk = Clocks()
-    barrier(dist)
-    clk.start()
-    ctx.set_profiling(1)
-    ctx.timer_start()
-    for _ in range(args.steps):
-        step(head)
-    ms = ctx.timer_stop()
-    clocks = clk.stop()
-    stages = ctx.stage_times()
-    ctx.set_profiling(0)
-    counts = ctx.counts()
-    launches = counts["kernel_launches"] - l0
-    ms = dist_max(dist, ms)
-    ms_step = ms / args.steps
+    ms_step, stages, launches, clocks = b.timed(head, args.warmup, args.steps, clk)
     value = ws * N / (ms_step * 1e-3)
-
+    counts = b.ctx.counts()
     if args.quick:
         if rank == 0:
-            print(json.dumps({"quick": True, "mode": args.quick_prec, "ms_per_step": ms_step, "targets": N, "value": value,
-                              "stages_ms_per_step": {k: v[0] / args.steps for k, v in stages.items()},
-                              "gpu_launches": launches}), flush=True)
-        ctx.close()
+            print(json.dumps({"quick": True, "mode": args.quick_prec, "ms_per_step": ms_step, "targets": N,
+                              "value": value, "stages_ms_per_step": stages, "gpu_launches": launches}), flush=True)
+        b.close()
         return 0
 
-    # ---- FP64 plain form (same algorithm, everything FP64)
-    for _ in range(2):
-        step(FP64)
-    k64 = max(2, args.steps // 3)
-    ctx.set_profiling(1)
-    ctx.timer_start()
-    for _ in range(k64):
-        step(FP64)
-    ms64 = dist_max(dist, ctx.timer_stop()) / k64
-    st64 = {k: v[0] / k64 for k, v in ctx.stage_times().items()}
-    ctx.set_profiling(0)
+    # ---- the other modes on the same context
+    ms64, st64, _, _ = b.timed(FP64, 2, max(3, args.steps // 3))
+    msm, stm, _, _ = b.timed(FP32M, 2, args.steps)
+    msc, stc, _, _ = b.timed(FP32C, 2, args.steps)
+    fp64_value, fp32m_value, fp32c_value = (ws * N / (m * 1e-3) for m in (ms64, msm, msc))
+    # the patch corrections alone (self + near-singular; the near pass is the same
+    # FP64 code in both modes): float-float patch against the FP64 patch
+    self_ff_vs_fp64 = rel(b.vector(FP32D, TERM_CORR), b.vector(FP32C, TERM_CORR))
+    vec = {name: b.vector(p) for name, p in (("fp64", FP64), ("fp32c", FP32C), ("fp32m", FP32M), ("fp32d", FP32D))}
+    err_fp64 = {k: rel(v, vec["fp64"]) for k, v in vec.items() if k != "fp64"}
 
-    # ---- FP32M: FP32C with the own-cell polar patch in FP32 + hi/lo geometry
-    for _ in range(2):
-        step(FP32M)
-    ctx.set_profiling(1)
-    ctx.timer_start()
-    for _ in range(args.steps):
-        step(FP32M)
-    msm = dist_max(dist, ctx.timer_stop()) / args.steps
-    stm = {k: v[0] / args.steps for k, v in ctx.stage_times().items()}
-    ctx.set_profiling(0)
-    fp32m_value = ws * N / (msm * 1e-3)
+    e2e = b.e2e(FP32D, max(3, args.steps // 2))
+    e2e["floor_ms"] = ms_step + e2e["h2d_bytes_per_step"] / (e2e["h2d_gbs_measured"] * 1e9) * 1e3
+    e2e["floor"] = "device matvec + the step's uploads at the measured pinned copy bandwidth"
 
-    # ---- FP32C: the own-cell polar patch on the FP64 pipe
-    for _ in range(2):
-        step(FP32C)
-    ctx.set_profiling(1)
-    ctx.timer_start()
-    for _ in range(args.steps):
-        step(FP32C)
-    msc = dist_max(dist, ctx.timer_stop()) / args.steps
-    stc = {k: v[0] / args.steps for k, v in ctx.stage_times().items()}
-    ctx.set_profiling(0)
-    fp32c_value = ws * N / (msc * 1e-3)
-    # the patch corrections alone (self + near-singular; the near pass is the
-    # same FP64 code in both modes): float-float patch against the FP64 patch
-    corr_c = ctx.matvec(TLIST_RBC, c, c, TERM_CORR, FP32C)
-    corr_d = ctx.matvec(TLIST_RBC, c, c, TERM_CORR, FP32D)
-    self_ff_vs_fp64 = float(np.linalg.norm(corr_d - corr_c) / np.linalg.norm(corr_c))
-
-    # ---- relative L2 error of the FP32 modes against the FP64 plain form
-    v64 = ctx.matvec(TLIST_RBC, c, c, TERM_ALL, FP64)
-    err32c = float(np.linalg.norm(ctx.matvec(TLIST_RBC, c, c, TERM_ALL, FP32C) - v64) / np.linalg.norm(v64))
-    err32m = float(np.linalg.norm(ctx.matvec(TLIST_RBC, c, c, TERM_ALL, FP32M) - v64) / np.linalg.norm(v64))
-    err32d = float(np.linalg.norm(ctx.matvec(TLIST_RBC, c, c, TERM_ALL, FP32D) - v64) / np.linalg.norm(v64))
-    fp64_value = ws * N / (ms64 * 1e-3)
-
-    # ---- end to end through the C ABI with pinned host buffers
-    pin = {}
-    for k in ("x", "a3", "detJ", "area", "meshSize", "spl_x", "spl_a3", "spl_detJ", "f", "g", "spl_F", "spl_G"):
-        a = np.ascontiguousarray(getattr(cells, k), dtype=np.float64)
-        p = lib.pinned(a.shape)
-        p[...] = a
-        pin[k] = p
-    vout = lib.pinned((3, N))
-
-    class PinnedCells:
-        pass
-
-    pc = PinnedCells()
-    for k in ("nlat", "nlon", "th", "phi", "w", "ncell", "celltype"):
-        setattr(pc, k, getattr(cells, k))
-    for k, p in pin.items():
-        setattr(pc, k, p)
-    # the caller's accumulator goes up and down (v += result on the device)
-    h2d = sum(p.nbytes for p in pin.values()) + vout.nbytes
-    d2h = vout.nbytes
-
-    e2e_parts = {"set_cells": 0.0, "set_cell_density": 0.0, "matvec_with_download": 0.0}
-
-    def e2e_step():
-        t0 = time.perf_counter()
-        ctx.set_cells(pc)
-        t1 = time.perf_counter()
-        ctx.set_cell_density(f=pc.f, g=pc.g, spl_F=pc.spl_F, spl_G=pc.spl_G)
-        t2 = time.perf_counter()
-        vout[...] = 0.0
-        ctx.matvec(TLIST_RBC, c, c, TERM_ALL, FP32D, v=vout)
-        t3 = time.perf_counter()
-        e2e_parts["set_cells"] += t1 - t0
-        e2e_parts["set_cell_density"] += t2 - t1
-        e2e_parts["matvec_with_download"] += t3 - t2
-
-    for _ in range(2):
-        e2e_step()
-    for k in e2e_parts:
-        e2e_parts[k] = 0.0
-    barrier(dist)
-    te = time.perf_counter()
-    ke = max(3, args.steps // 2)
-    for _ in range(ke):
-        e2e_step()
-    te = dist_max(dist, (time.perf_counter() - te) / ke)
-    e2e_value = ws * N / te
-    e2e_parts = {k: v / ke * 1e3 for k, v in e2e_parts.items()}
-    h2d_gbs = lib.h2d_bandwidth(h2d)  # one pinned copy of the step's upload volume
-
-    # ---- roofline of the dominant stage (device time measured above)
-    nq = 200  # RBC_SingInt points per target on the 25x50 grid (nrad 10 x nazm 20)
     peak32 = lib.fma_peak(FP32C)
     peak64 = lib.fma_peak(FP64)
-    st_ms = {k: v[0] / args.steps for k, v in stages.items()}
-    pairs = counts["pairs_within_rc"]
-    # k_self_ff loads per patch point 4 stencil nodes x 4 slots x 6 float4
-    # quads of hi/lo values and 9 weight words (136 B); the L1 load peak is
-    # 128 B/clk/SM (nominal; no measured L1 figure exists)
-    l1_bytes = counts["self_items"] * nq * (4 * 4 * 6 * 16 + 136)
-    l1_peak = 128.0 * 152 * ((clocks or {}).get("sm_mhz") or 2070.0) * 1e6 / 1e9
-    # ---- per-kernel rooflines with the stages timed alone on one stream
-    # (REAL|CORR|LINEAR without PME keeps the matvec on the main stream)
-    def alone(prec, terms, reps=3):
-        ctx.matvec(TLIST_RBC, c, c, terms, prec, device_only=True)
-        ctx.set_profiling(1)
-        for _ in range(reps):
-            ctx.matvec(TLIST_RBC, c, c, terms, prec, device_only=True)
-        st = ctx.stage_times()
-        ctx.set_profiling(0)
-        return {k: v[0] / reps for k, v in st.items()}
-
     hbm_peak, hbm_src = 6800.0, "fallback"
     try:
         mp = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
         hbm_peak, hbm_src = float(mp["hbm_gbs"]), "measured (MEASURED_PEAKS.json)"
     except Exception:
         pass
-    s_c = alone(FP32C, TERM_REAL | TERM_CORR | TERM_LINEAR)
-    s_m = alone(FP32M, TERM_REAL | TERM_CORR | TERM_LINEAR)
-    s_d = alone(FP32D, TERM_REAL | TERM_CORR | TERM_LINEAR)
-    s_p = alone(FP32C, TERM_PME)
-    G3 = 1
-    for d in prm["Nb"]:
-        G3 *= d
-    pme_ms = s_p["pme_spread"] + s_p["pme_fft_infl"] + s_p["pme_gather"]
-    pme_bytes = 4.0 * G3 * (12 + 12 + 12 + 12 + 3 + 3 + 3 + 3) + 4.0 * N * (3 + 3 + 3 + 1) + 4.0 * N * (3 + 3)
-    pair_fl = pairs * (FLOP_PAIR_SL + FLOP_PAIR_DL)
-    self_fl = counts["self_items"] * nq * FLOP_SELFQ_SLDL
-    rooflines = {
-        "k_pair32": {"bound": "fp32", "ms": s_c["pair"], "achieved": pair_fl / (s_c["pair"] * 1e-3) / 1e12,
-                     "peak": peak32, "unit": "TFLOP/s", "frac": pair_fl / (s_c["pair"] * 1e-3) / 1e12 / peak32,
-                     "work": f"{pairs} pairs within rc x {FLOP_PAIR_SL + FLOP_PAIR_DL} flops"},
-        "k_self": {"bound": "fp64", "ms": s_c["self"], "achieved": self_fl / (s_c["self"] * 1e-3) / 1e12,
-                   "peak": peak64, "unit": "TFLOP/s", "frac": self_fl / (s_c["self"] * 1e-3) / 1e12 / peak64,
-                   "work": f"{counts['self_items']} targets x {nq} patch points x {FLOP_SELFQ_SLDL} flops"},
-        "k_self_mix": {"bound": "l1 (ncu: L1 91% of peak)", "ms": s_m["self"],
-                       "achieved": self_fl / (s_m["self"] * 1e-3) / 1e12, "peak": peak32, "unit": "TFLOP/s",
-                       "frac": self_fl / (s_m["self"] * 1e-3) / 1e12 / peak32,
-                       "work": "the k_self patch work in FP32 with hi/lo geometry"},
-        "k_self_ff": {"bound": "l1", "ms": s_d["self"], "achieved": l1_bytes / (s_d["self"] * 1e-3) / 1e9,
-                      "peak": l1_peak, "unit": "GB/s", "frac": l1_bytes / (s_d["self"] * 1e-3) / 1e9 / l1_peak,
-                      "flops_achieved_tflops": self_fl / (s_d["self"] * 1e-3) / 1e12,
-                      "work": "L1 bytes requested by the lanes (the k_self patch work in float-float arithmetic)"},
-        "pme": {"bound": "hbm", "ms": pme_ms, "achieved": pme_bytes / (pme_ms * 1e-3) / 1e9, "peak": hbm_peak,
-                "unit": "GB/s", "frac": pme_bytes / (pme_ms * 1e-3) / 1e9 / hbm_peak, "peak_source": hbm_src,
-                "work": "algorithmic bytes 4 G (12+12+12+12+3+3+3+3) + 4 N (3+3+3+1) + 4 N (3+3), FP32 grids "
-                        "(a 128^3 grid set stays largely in the 129 MB L2)"},
-        "note": "stages timed alone on one stream (the matvec itself runs them on two streams)",
-    }
-    # ---- the dominant kernel of the headline mode, from the stages timed alone
-    # (the matvec's stage spans overlap across the two streams)
-    if s_d["self"] >= s_d["pair"]:
-        roof = {"kernel": "k_self_ff (RBC_SingInt, float-float)", **rooflines["k_self_ff"],
-                "peak_source": "nominal L1 load bandwidth 128 B/clk/SM x 152 SMs x the sampled SM clock "
-                               "(ncu: L1 data pipe 78% of its wavefront peak, FMA pipe 65%)"}
-    else:
-        roof = {"kernel": "k_pair32 (AddIntOnRbcs pair sums, FP32)", **rooflines["k_pair32"],
-                "peak_source": "measured FP32 FMA chain (rbc3d_fma_peak), same GPU, same run"}
-    roof["traffic"] = None
-    tpath = os.path.join(HERE, "profiles", "traffic.json")
-    if os.path.exists(tpath):
+    sm_mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    rooflines, s_d = rooflines_of(b, counts, peak32, peak64, hbm_peak, hbm_src, sm_mhz)
+    roof = headline_roofline(rooflines, s_d, N)
+
+    # ---- CPU baseline on the same inputs (rank 0, N = 1): the oracle on all
+    # host threads; its vector gives the error of every mode against the oracle
+    cpu, err_oracle = None, None
+    if cpu_on:
         try:
-            tr = json.load(open(tpath))
-            roof["traffic"] = tr.get(roof["kernel"].split()[0])
-        except Exception:
-            pass
+            ts, cores, vo = time_oracle(prm, cells, 1)
+            cpu = {"value": N / ts[0], "unit": "targets/s", "cores": cores, "kind": "port",
+                   "sample": f"one full FP64 matvec of the same workload ({N} targets), {ts[0]:.1f}s"}
+            err_oracle = {k: rel(v, vo) for k, v in vec.items()}
+        except Exception as e:  # the baseline is reported, not required
+            cpu = {"value": None, "unit": "targets/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"unavailable: {e}"}
+    b.close()
+    del vec
 
-    # ---- scale-up: 2048 cells, L = 80, PME 256^3 (2.56 M targets), all three modes
-    scale = None
-    if not args.quick and not args.no_scaleup:
-        from rbc3d_gb300 import geometry as G
+    # ---- 2048 cells, L = 80, PME 256^3 (2.56 M targets): the same fields
+    c5 = None
+    if not args.no_scaleup and not args.cells:
         t1 = time.perf_counter()
-        prm5, cells5, _ = G.config("C5", seed=args.seed + rank)
-        N5 = cells5.x.shape[1]
-        ctx5 = Context(lib, prm5)
-        ctx5.set_cells(cells5)
-        ctx5.set_cell_density(f=cells5.f, g=cells5.g, spl_F=cells5.spl_F, spl_G=cells5.spl_G)
-
-        def timed(prec, warm, steps):
-            for _ in range(warm):
-                ctx5.matvec(TLIST_RBC, c, c, TERM_ALL, prec, device_only=True)
-            ctx5.timer_start()
-            for _ in range(steps):
-                ctx5.matvec(TLIST_RBC, c, c, TERM_ALL, prec, device_only=True)
-            return dist_max(dist, ctx5.timer_stop()) / steps
-
-        m32c = timed(FP32C, 2, 3)
-        m32m = timed(FP32M, 2, 3)
-        m32d = timed(FP32D, 2, 3)
-        m64 = timed(FP64, 1, 1)
-        v64 = ctx5.matvec(TLIST_RBC, c, c, TERM_ALL, FP64)
-        e32c = float(np.linalg.norm(ctx5.matvec(TLIST_RBC, c, c, TERM_ALL, FP32C) - v64) / np.linalg.norm(v64))
-        e32m = float(np.linalg.norm(ctx5.matvec(TLIST_RBC, c, c, TERM_ALL, FP32M) - v64) / np.linalg.norm(v64))
-        e32d = float(np.linalg.norm(ctx5.matvec(TLIST_RBC, c, c, TERM_ALL, FP32D) - v64) / np.linalg.norm(v64))
-        cnt5 = ctx5.counts()
-        ctx5.close()
-        log(f"scale-up in {time.perf_counter() - t1:.1f}s")
-        scale = {"workload": "2048 biconcave cells, 25x50 grid (2,560,000 targets), periodic L=80, rc=3, "
-                             "PME 256^3 P=6, SL+DL, viscRat=5 (C5)",
-                 "targets": N5,
-                 "fp32c": {"ms_per_step": m32c, "value": ws * N5 / (m32c * 1e-3), "rel_l2_vs_fp64_plain": e32c},
-                 "fp32m": {"ms_per_step": m32m, "value": ws * N5 / (m32m * 1e-3), "rel_l2_vs_fp64_plain": e32m},
-                 "fp32d": {"ms_per_step": m32d, "value": ws * N5 / (m32d * 1e-3), "rel_l2_vs_fp64_plain": e32d},
-                 "fp64_plain": {"ms_per_step": m64, "value": ws * N5 / (m64 * 1e-3)},
-                 "fp32c_over_fp64": m64 / m32c, "fp32m_over_fp64": m64 / m32m, "fp32d_over_fp64": m64 / m32d,
-                 "pairs_within_rc": cnt5["pairs_within_rc"], "nearsing_items": cnt5["nearsing_items"],
-                 "steps": "fp32c, fp32m, fp32d: 2 warm-up + 3 timed; fp64: 1 + 1"}
+        prm5, cells5 = make_inputs(args.seed + rank, name="C5")
+        b5 = Bench(lib, prm5, cells5, dist, ws)
+        N5 = b5.N
+        k5 = max(10, args.steps // 2)
+        m5d, st5d, l5, _ = b5.timed(FP32D, 3, k5)
+        m5m, _, _, _ = b5.timed(FP32M, 2, k5)
+        m5c, _, _, _ = b5.timed(FP32C, 1, 3)
+        m564, _, _, _ = b5.timed(FP64, 1, 3)
+        cnt5 = b5.ctx.counts()
+        vec5 = {n: b5.vector(p) for n, p in (("fp64", FP64), ("fp32c", FP32C), ("fp32m", FP32M), ("fp32d", FP32D))}
+        e5 = b5.e2e(FP32D, 5)
+        e5["floor_ms"] = m5d + e5["h2d_bytes_per_step"] / (e5["h2d_gbs_measured"] * 1e9) * 1e3
+        r5, s5d = rooflines_of(b5, cnt5, peak32, peak64, hbm_peak, hbm_src, sm_mhz)
+        b5.close()
+        c5 = {"config": WORKLOADS["C5"], "value": ws * N5 / (m5d * 1e-3), "unit": "targets/s",
+              "ms_per_step": m5d, "steps": k5, "warmup": 3, "stages_ms_per_step": st5d, "gpu_launches": l5,
+              "fp64_plain": {"value": ws * N5 / (m564 * 1e-3), "ms_per_step": m564, "steps": 3},
+              "fp32c": {"value": ws * N5 / (m5c * 1e-3), "ms_per_step": m5c, "steps": 3},
+              "fp32m": {"value": ws * N5 / (m5m * 1e-3), "ms_per_step": m5m, "steps": k5},
+              "fp32_over_fp64_plain": {"fp32d": m564 / m5d, "fp32c": m564 / m5c, "fp32m": m564 / m5m},
+              "rel_l2_vs_fp64_plain": {k: rel(v, vec5["fp64"]) for k, v in vec5.items() if k != "fp64"},
+              "e2e": e5, "roofline": headline_roofline(r5, s5d, N5), "rooflines": r5,
+              "counts": {k: cnt5[k] for k in ("pairs_within_rc", "nbr_items", "nearsing_items", "self_items")}}
+        if cpu_on:
+            try:
+                ts5, cores5, vo5 = time_oracle(prm5, cells5, 1)
+                c5["cpu_baseline"] = {"value": N5 / ts5[0], "unit": "targets/s", "cores": cores5, "kind": "port",
+                                      "sample": f"one full FP64 matvec of the same workload ({N5} targets), "
+                                                f"{ts5[0]:.1f}s"}
+                c5["rel_l2_vs_oracle"] = {k: rel(v, vo5) for k, v in vec5.items()}
+                del vo5
+            except Exception as e:
+                c5["cpu_baseline"] = {"value": None, "sample": f"unavailable: {e}"}
+        del vec5
+        log(f"2048-cell workload in {time.perf_counter() - t1:.1f}s")
 
     # ---- wall no-slip GMRES on the tube workload: plain vs history vs learned guess
     wall = None
-    if not args.quick and not args.no_wall:
+    if not args.no_wall and not args.cells:
         from rbc3d_gb300.learned_run import run as wall_run
         t1 = time.perf_counter()
         w = wall_run(ncell=64, warm_steps=25, test_steps=3, rtol=1e-8, restart=300, max_it=900, train_iters=30,
@@ -496,7 +520,6 @@ def main():
                                      "speedup_learned_incl_training", "mlp")},
                 "steps": "25 warm-up RK2 steps (50 plain solves: history + online training), then 3 steps "
                          "(6 solves) each solved plain, from the history guess and from the learned guess"}
-        # the same run with mixed-precision solves (FP32M operator inside FP64 refinement, FP64 residual)
         t1 = time.perf_counter()
         wm = wall_run(ncell=64, warm_steps=25, test_steps=3, rtol=1e-8, restart=300, max_it=900, train_iters=30,
                       history=48, seed=args.seed + rank, prec=FP32M, dynamics="skalak", dt=1e-3)
@@ -506,14 +529,19 @@ def main():
         wall["mixed_fp32m"]["learned_over_fp64_plain"] = w["plain"]["ms"] / wm["learned"]["ms"]
 
     # ---- cell velocity GMRES (Solve_RBC_Vel, degree 12, rtol 1e-11 as the reference
-    # sets it) on the same 256 cells: FP64 solve vs the mixed-precision solves
+    # sets it) on the 256 cells: FP64 solve vs the mixed-precision solves
     cellsolve = None
-    if not args.quick and not args.no_cellsolve:
+    if not args.no_cellsolve and not args.cells:
+        from rbc3d_gb300.abi import Context
         t1 = time.perf_counter()
+        ctx = Context(lib, prm)
+        ctx.set_cells(cells)
+        ctx.set_cell_density(f=cells.f, g=cells.g, spl_F=cells.spl_F, spl_G=cells.spl_G)
         arms = {}
         for name, p in (("fp64", FP64), ("fp32d", FP32D), ("fp32m", FP32M), ("fp32c", FP32C)):
             sol, v, st, code = ctx.solve_rbc_vel(12, rtol=1e-11, max_it=300, restart=30, prec=p, check=False)
             arms[name] = (sol, v, st, code)
+        ctx.close()
         s64, v64 = arms["fp64"][0], arms["fp64"][1]
         cellsolve = {"workload": "Solve_RBC_Vel on the 256-cell workload (viscRat 5, SH degree 12, "
                                  f"{3 * 144 * 256} unknowns), restart 30, ||r|| < 1e-11 ||b|| (FP64 residual)"}
@@ -521,51 +549,38 @@ def main():
             cellsolve[name] = {"ms": st.ms, "iterations": st.iterations, "matvecs": st.matvecs,
                                "refinements": st.refinements, "status": code,
                                "final_rel_residual": st.rnorm / st.bnorm if st.bnorm > 0 else 0.0,
-                               "rel_l2_vs_fp64_solution": float(np.linalg.norm(sol - s64) / np.linalg.norm(s64)),
-                               "rel_l2_vs_fp64_velocity": float(np.linalg.norm(v - v64) / np.linalg.norm(v64))}
+                               "rel_l2_vs_fp64_solution": rel(sol, s64) if name != "fp64" else 0.0,
+                               "rel_l2_vs_fp64_velocity": rel(v, v64) if name != "fp64" else 0.0}
         for name in ("fp32d", "fp32m", "fp32c"):
             cellsolve[name]["speedup_vs_fp64"] = arms["fp64"][2].ms / arms[name][2].ms
         log(f"cell solve comparison in {time.perf_counter() - t1:.1f}s")
 
-    # ---- CPU baseline (rank 0, N = 1 only): oracle, all host threads
-    cpu = None
-    if rank == 0 and ws == 1 and not args.no_cpu:
-        try:
-            ts, cores = time_oracle(prm, cells, 1)
-            cpu = {"value": N / ts[0], "unit": "targets/s", "cores": cores, "kind": "port",
-                   "sample": f"one full FP64 matvec of the same workload ({N} targets), {ts[0]:.1f}s"}
-        except Exception as e:  # the baseline is reported, not required
-            cpu = {"value": None, "unit": "targets/s", "cores": os.cpu_count(), "kind": "port",
-                   "sample": f"unavailable: {e}"}
-
     if rank == 0:
+        config = dict(WORKLOAD) if not args.cells else {"workload": f"{args.cells} cells (profiling)",
+                                                        "targets": N}
         line = {
             "metric": "Ewald matvec targets/s", "value": value, "unit": "targets/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+ff48-patch+f64-near",
             "data": "synthetic (seeded biconcave cells, SH densities)",
-            "config": dict(WORKLOAD, targets=N, l2="working set (spline tables 307 MB, PME grids) > 129 MB L2"),
+            "config": config,
             "mode": "FP32D: pair sums, PME in FP32 with compensated accumulation; own-cell polar patch in "
                     "float-float arithmetic (48-bit significands, 2e-12 from the FP64 patch); near-singular "
                     "correction in FP64",
-            "rel_l2_vs_fp64_plain": err32d,
+            "rel_l2_vs_oracle": err_oracle,
+            "rel_l2_vs_fp64_plain": err_fp64["fp32d"],
             "patch_corrections_rel_l2_vs_fp64_patch": self_ff_vs_fp64,
             "fp64_plain": {"value": fp64_value, "unit": "targets/s", "ms_per_step": ms64,
                            "fp32d_over_fp64": value / fp64_value, "stages_ms_per_step": st64},
             "fp32c": {"value": fp32c_value, "unit": "targets/s", "ms_per_step": msc,
-                      "over_fp64": fp32c_value / fp64_value, "rel_l2_vs_fp64_plain": err32c,
-                      "stages_ms_per_step": stc,
-                      "note": "own-cell polar patch on the FP64 pipe"},
+                      "over_fp64": fp32c_value / fp64_value, "rel_l2_vs_fp64_plain": err_fp64["fp32c"],
+                      "stages_ms_per_step": stc, "note": "own-cell polar patch on the FP64 pipe"},
             "fp32m": {"value": fp32m_value, "unit": "targets/s", "ms_per_step": msm,
-                      "over_fp64": fp32m_value / fp64_value, "rel_l2_vs_fp64_plain": err32m,
+                      "over_fp64": fp32m_value / fp64_value, "rel_l2_vs_fp64_plain": err_fp64["fp32m"],
                       "stages_ms_per_step": stm,
                       "note": "own-cell polar patch in FP32 with FP64-accurate (hi/lo) geometry"},
-            "e2e": {"value": e2e_value, "unit": "targets/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "ms_per_step": te * 1e3, "host_ms_per_step": e2e_parts,
-                    "h2d_gbs_measured": h2d_gbs,
-                    "floor_ms": ms_step + h2d / (h2d_gbs * 1e9) * 1e3,
-                    "floor": "device matvec + the step's uploads at the measured pinned copy bandwidth"},
-            "stages_ms_per_step": st_ms,
+            "e2e": e2e,
+            "stages_ms_per_step": stages,
             "counts": {k: counts[k] for k in ("pairs_within_rc", "nbr_items", "nearsing_items", "self_items",
                                               "screen_misses", "near_replays", "near_projections")},
             "roofline": roof,
@@ -575,7 +590,7 @@ def main():
                                      "note": "fp32d: self patch in float-float on the FP32 pipe (GB300 FP64 is "
                                              "1/74 of FP32); fp32c: on the FP64 pipe; fp32m: in FP32 with hi/lo "
                                              "geometry"},
-            "scaleup_c5": scale,
+            "c5": c5,
             "wall_gmres": wall,
             "cell_gmres": cellsolve,
             "fma_peaks_tflops": {"fp32": peak32, "fp64": peak64},
@@ -584,7 +599,6 @@ def main():
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
-    ctx.close()
     return 0
 
 

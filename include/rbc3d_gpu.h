@@ -307,6 +307,14 @@ rbc3d_status rbc3d_mlp_train_step(rbc3d_mlp* m, int n, const float* x, const flo
  * (ModNoSlip.F90:110-113) for the current wall density: ndof values. */
 rbc3d_status rbc3d_wall_rhs(rbc3d_ctx* ctx, int prec, double* b);
 
+/* MinDistToTri(xTar, x, s0, t0, x0), ModIntOnWalls.F90:480 (host code, no
+ * context): distance from xtar to the triangle x(3,3) (column-major, x(l,:)
+ * vertex l), the barycentric (s0, t0) of the closest point and the point x0.
+ * For host callers of the reference's repulsion routines
+ * (ModRepulsion.F90:600) once ModIntOnWalls is replaced; outputs may be NULL. */
+rbc3d_status rbc3d_min_dist_to_tri(const double xtar[3], const double x[9], double* s0, double* t0,
+                                   double x0[3], double* dist);
+
 /* Allocation-free linear double-layer term.  No counterpart in the reference:
  * it serves callers that cannot allocate device memory -- programs whose
  * device arrays belong to another owner (OpenACC / CUDA Fortran data regions,
@@ -317,10 +325,14 @@ rbc3d_status rbc3d_wall_rhs(rbc3d_ctx* ctx, int prec, double* b);
  * celltype: ncell; Acoef: nt; v: 3 nt), enqueued on `stream` (a
  * cudaStream_t, NULL for the default stream).  It allocates nothing: its
  * per-cell scratch is a fixed array inside the library, so ncell is limited
- * to 8192 (larger values return RBC3D_ERR_ARG).  The first call on a device
- * looks up that array's device address; make this first call before any
- * stream capture.  The array is shared by every call: calls that overlap on
- * the GPU race. */
+ * to 8192 (larger values, or nlat*nlon*ncell above INT_MAX, return
+ * RBC3D_ERR_ARG).  Every call looks up that array's device address on the
+ * current device (the first lookup on a device loads the library's device
+ * code); make the first call before any stream capture.  The array is shared
+ * by every call: calls that overlap on the GPU race.  Cell types are read on
+ * the device: a cell whose type lies outside [0, ncelltypes) contributes
+ * nothing.  ncell == 0, nt == 0 or c2 == 0 return RBC3D_OK without touching
+ * v. */
 rbc3d_status rbc3d_add_linear_int_noalloc(int ncell, int nlat, int nlon, const double* x, const double* g,
                                           const double* a3, const double* detJ, const double* w,
                                           const int* celltype, int ncelltypes, const double* viscRat,

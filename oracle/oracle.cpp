@@ -1417,6 +1417,7 @@ rbc3d_status API(set_cells)(Ctx* c, int ncell, const int* celltype, const double
 }
 
 rbc3d_status API(set_cell_density)(Ctx* c, const double* f, const double* g, const double* spl_F, const double* spl_G) {
+  if ((f && !spl_F) || (g && !spl_G)) return fail(c, RBC3D_ERR_ARG, "density without spline table");
   size_t N = c->npt, S = (size_t)c->ncell * 4 * 2 * c->nlat * c->nlon;
   int nv = c->nlat * c->nlon;
   auto mk = [&](const double* src, std::vector<double>& raw, std::vector<double>& scaled) {

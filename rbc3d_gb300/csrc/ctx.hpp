@@ -214,6 +214,7 @@ struct rbc3d_ctx {
   } mb;
 
   DBuf<double> scratch;           // GMRES basis / temporaries
+  DBuf<double> dotpart;           // GMRES: per-slice partial dot products
   DBuf<double> stage;             // staging of uploaded spline tables (grow-only)
   // grow-only temporaries of the set-up passes (cudaFree would synchronise the device)
   DBuf<int> sort_key, sort_key2, sort_idx;  // sort_points

@@ -34,6 +34,37 @@ __global__ void k_dots(int n, int nv, const double* __restrict__ V, size_t ld, c
     if (threadIdx.x == 0) out[j] = t;
   }
 }
+// Sliced dot products for the Arnoldi step: block (slice, j) sums V_j . w
+// over rows [slice*kDotRows, (slice+1)*kDotRows); k_dots_sum then adds the
+// slices of each j in slice order.  Fixed summation order (deterministic), and
+// (j, slice) blocks fill the GPU where one block per basis vector would not.
+constexpr int kDotRows = 2048;
+constexpr int kDotThreads = 256;
+__global__ void __launch_bounds__(kDotThreads) k_dots_part(int n, const double* __restrict__ V, size_t ld,
+                                                           const double* __restrict__ w, double* __restrict__ part,
+                                                           int nslice) {
+  const int sl = blockIdx.x, j = blockIdx.y;
+  const double* vj = V + (size_t)j * ld;
+  const int i1 = min(n, (sl + 1) * kDotRows);
+  double s = 0;
+  for (int i = sl * kDotRows + threadIdx.x; i < i1; i += kDotThreads) s += vj[i] * w[i];
+  __shared__ double red[kDotThreads / 32];
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int k = 0; k < kDotThreads / 32; ++k) t += red[k];
+    part[(size_t)j * nslice + sl] = t;
+  }
+}
+__global__ void k_dots_sum(int nv, int nslice, const double* __restrict__ part, double* __restrict__ out) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nv) return;
+  double s = 0;
+  for (int k = 0; k < nslice; ++k) s += part[(size_t)j * nslice + k];
+  out[j] = s;
+}
 __global__ void k_orth(int n, int nv, const double* __restrict__ V, size_t ld, const double* __restrict__ h,
                        double* __restrict__ w) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -89,8 +120,22 @@ __global__ void k_xupdate(int n, int k, const double* __restrict__ V, size_t ld,
 
 inline int gm_nblk(long long n, int b) { return (int)((n + b - 1) / b); }
 
+// out[j] = V_j . w for j < nv (device), on the context stream.  Partial sums
+// go to ctx->dotpart; without room for them one block per j does the sum.
+inline void dev_dots(rbc3d_ctx* ctx, int n, int nv, const double* V, size_t ld, const double* w, double* out) {
+  const int nslice = gm_nblk(n, kDotRows);
+  if (nslice <= 1 || ctx->dotpart.alloc((size_t)nv * nslice) != cudaSuccess) {
+    k_dots<<<nv, 512, 0, ctx->st>>>(n, nv, V, ld, w, out);
+    ++ctx->launches;
+    return;
+  }
+  k_dots_part<<<dim3(nslice, nv), kDotThreads, 0, ctx->st>>>(n, V, ld, w, ctx->dotpart.p, nslice);
+  k_dots_sum<<<gm_nblk(nv, 128), 128, 0, ctx->st>>>(nv, nslice, ctx->dotpart.p, out);
+  ctx->launches += 2;
+}
+
 inline double dev_norm(rbc3d_ctx* ctx, int n, const double* v, double* tmp) {
-  { k_dots<<<1, 512, 0, ctx->st>>>(n, 1, v, 0, v, tmp); ++ctx->launches; }
+  dev_dots(ctx, n, 1, v, 0, v, tmp);
   double h = 0;
   cudaMemcpyAsync(&h, tmp, sizeof(double), cudaMemcpyDeviceToHost, ctx->st);
   cudaStreamSynchronize(ctx->st);
@@ -126,7 +171,7 @@ rbc3d_status gmres_cycles(rbc3d_ctx* ctx, int n, MV&& matvec, const double* b, d
     int k;
     for (k = 0; k < R && its < max_it; ++k) {
       if ((s = matvec(V.p + k * ld, w.p))) return s;
-      { k_dots<<<k + 1, 512, 0, ctx->st>>>(n, k + 1, V.p, ld, w.p, hcol.p); ++ctx->launches; }
+      dev_dots(ctx, n, k + 1, V.p, ld, w.p, hcol.p);
       { k_orth<<<gm_nblk(n, 256), 256, 0, ctx->st>>>(n, k + 1, V.p, ld, hcol.p, w.p); ++ctx->launches; }
       double hn = dev_norm(ctx, n, w.p, tmp.p);
       if (hn > 0) { k_axpby<<<gm_nblk(n, 256), 256, 0, ctx->st>>>(n, 1.0 / hn, w.p, 0.0, V.p + (k + 1) * ld); ++ctx->launches; }

@@ -31,10 +31,10 @@ struct TriRules {
 };
 __constant__ TriRules c_rules;
 
-__device__ __forceinline__ double dot3(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+__host__ __device__ __forceinline__ double dot3(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
 
 // MinDistToTri, ModIntOnWalls.F90:480-577.  xv[l][c]: vertex l component c.
-__device__ double min_dist_to_tri(const double* xt, const double xv[3][3], double& s0, double& t0) {
+__host__ __device__ double min_dist_to_tri(const double* xt, const double xv[3][3], double& s0, double& t0) {
   double x12[3], x13[3], x1T[3];
   for (int c = 0; c < 3; ++c) { x12[c] = xv[1][c] - xv[0][c]; x13[c] = xv[2][c] - xv[0][c]; x1T[c] = xv[0][c] - xt[c]; }
   double a = dot3(x12, x12), b = dot3(x12, x13), c = dot3(x13, x13);
@@ -643,5 +643,24 @@ extern "C" rbc3d_status rbc3d_wall_rhs(rbc3d_ctx* ctx, int prec, double* b) {
   { k_assemble<<<nblk(W.nvert, 256), 256, 0, ctx->st>>>(W.nvert, W.glb.p, W.writer.p, ctx->tl[RBC3D_TLIST_WALL].v.p, -1.0, db.p); ++ctx->launches; }
   CUDA_TRY(cudaMemcpyAsync(b, db.p, sizeof(double) * W.ndof, cudaMemcpyDeviceToHost, ctx->st));
   CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  return RBC3D_OK;
+}
+
+// MinDistToTri on the host (ModIntOnWalls.F90:480-577), for host callers of
+// the reference's repulsion routines (ModRepulsion.F90:600).  x: x(3,3)
+// column-major as the reference (x(l,:) = vertex l); any output may be NULL.
+extern "C" rbc3d_status rbc3d_min_dist_to_tri(const double xtar[3], const double x[9], double* s0, double* t0,
+                                              double x0[3], double* dist) {
+  if (!xtar || !x) return RBC3D_ERR_ARG;
+  double xv[3][3];
+  for (int l = 0; l < 3; ++l)
+    for (int c = 0; c < 3; ++c) xv[l][c] = x[l + 3 * c];
+  double s = 0, t = 0;
+  const double d = min_dist_to_tri(xtar, xv, s, t);
+  if (s0) *s0 = s;
+  if (t0) *t0 = t;
+  if (x0)
+    for (int c = 0; c < 3; ++c) x0[c] = (1 - s - t) * xv[0][c] + s * xv[1][c] + t * xv[2][c];
+  if (dist) *dist = d;
   return RBC3D_OK;
 }

@@ -50,10 +50,17 @@ def test_wall_mesh_round_trip_and_periodic_vertices(tmp_path):
     assert np.array_equal(w2.glb, wall.glb) and w2.ndof == wall.ndof
 
 
-@pytest.mark.skipif(not os.path.exists("/root/reference/examples/case/Input/new_cyl_D6_L13_33.e"),
-                    reason="reference example meshes not present")
+def reference_file(rel):
+    """A file of the RBC3D source tree, found under the directory named by the
+    environment variable RBC3D_REFERENCE_DIR; the test is skipped without it."""
+    root = os.environ.get("RBC3D_REFERENCE_DIR")
+    if not root or not os.path.exists(os.path.join(root, rel)):
+        pytest.skip(f"RBC3D_REFERENCE_DIR does not hold {rel}")
+    return os.path.join(root, rel)
+
+
 def test_reads_reference_example_mesh():
-    x, e2v = S.read_wall_mesh("/root/reference/examples/case/Input/new_cyl_D6_L13_33.e")
+    x, e2v = S.read_wall_mesh(reference_file("examples/case/Input/new_cyl_D6_L13_33.e"))
     assert x.shape == (1328, 3) and e2v.shape == (2404, 3)
     assert e2v.min() == 1 and e2v.max() == 1328
     # every vertex is used and every triangle has positive area
@@ -76,10 +83,8 @@ def test_cell_shape_export_import_round_trip(tmp_path):
     assert np.allclose(e.x, c.x + np.array(S.IMPORT_SHIFT) + [1.0, 2.0, 3.0], rtol=0, atol=1e-14)
 
 
-@pytest.mark.skipif(not os.path.exists("/root/reference/sample_files/sample_cells/SickleCell.dat"),
-                    reason="reference sample cells not present")
 def test_sickle_fixture_matches_reference_file():
     from conftest import ROOT
     z = np.load(os.path.join(ROOT, "tests", "golden", "sickle_cell.npz"))
-    c = S.import_read_rbc("/root/reference/sample_files/sample_cells/SickleCell.dat")
+    c = S.import_read_rbc(reference_file("sample_files/sample_cells/SickleCell.dat"))
     assert np.array_equal(c.x, z["x"]) and c.nlat == 36 and c.nlon == 72
