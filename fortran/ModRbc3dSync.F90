@@ -6,8 +6,8 @@
 ! TargetList_Update, e.g. common/ModTimeInt.F90:744-745,770,790).  Those CPU
 ! lists stay as they are (the repulsion routines read them); the drop-in
 ! modules in this directory push the same state to the GPU at their entry:
-!   Rbc3dGpu_Init         once, after GlobData_Init (context, cell grid,
-!                         wall mesh, self-wall operator)
+!   Rbc3dGpu_Init         once, from TimeInt_Init's PrepareSingIntOnWall or
+!                         PME_Init (context, cell grid, wall mesh)
 !   Rbc3dGpu_SyncCells    positions, geometry and spline tables of rbcs(:)
 !                         (rbc3d_set_cells) and their densities
 !                         (rbc3d_set_cell_density)
@@ -76,7 +76,6 @@ contains
       e2v = reshape(wall%e2v, [3*wall%nele])
       call rbc3d_check(rbc3d_set_walls(gpu_ctx, wall%nvert, wall%nele, xw, e2v, wall%indxVertGlb), &
                        'rbc3d_set_walls')
-      call rbc3d_check(rbc3d_prepare_sing_int_on_wall(gpu_ctx), 'rbc3d_prepare_sing_int_on_wall')
       call Rbc3dGpu_SyncWall
       deallocate (xw, e2v)
     end if
