@@ -121,7 +121,9 @@ typedef struct rbc3d_solve_opts {
                     (never a larger initial residual than 0);
                     3: two guess vectors x1, x2 (2 x dof doubles), combined
                     as p x1 + q x2 with the least-squares p, q (one extra
-                    matvec) */
+                    matvec);
+                    4: wall solve only: the prediction of the learned
+                    spectral operator (rbc3d_wall_spectral_init) */
 } rbc3d_solve_opts;
 
 typedef struct rbc3d_solve_stats {
@@ -290,7 +292,8 @@ rbc3d_status rbc3d_get_counts(const rbc3d_ctx* ctx, rbc3d_counts* out);
 
 /* ---- learned wall-density initial guess (no counterpart in the reference) --
  * A per-vertex MLP: nin -> width (SiLU) x depth -> nout.  GEMMs run on the
- * tensor cores with BF16 operands and FP32 accumulation (mma.sync m16n8k16);
+ * tensor cores with BF16 operands and FP32 accumulation (tcgen05.mma with
+ * TMEM accumulators);
  * master weights, Adam moments and the loss are FP32.  Row-major FP32 host
  * arrays.  Parameters are packed [W_0 (dout x din), b_0, W_1, b_1, ...]. */
 typedef struct rbc3d_mlp rbc3d_mlp;
@@ -306,6 +309,32 @@ rbc3d_status rbc3d_mlp_train_step(rbc3d_mlp* m, int n, const float* x, const flo
 /* Right-hand side of the wall solve, b = -AssembleArray(Compute_Wall_Residual_Vel)
  * (ModNoSlip.F90:110-113) for the current wall density: ndof values. */
 rbc3d_status rbc3d_wall_rhs(rbc3d_ctx* ctx, int prec, double* b);
+
+/* Learned spectral operator of the wall solve (no counterpart in the
+ * reference, whose NoSlipWall starts from a zero increment).  For a wall that
+ * is a uniform stack of nring rings along the periodic z axis (unique vertex
+ * g = ring * nper + i, every element shifted by one ring again an element),
+ * the wall operator is block diagonal in the axial Fourier modes; the model
+ * learns each mode's block from the solved pairs of the run: per mode an
+ * orthonormal basis of the transformed right-hand sides and the matching
+ * solutions, grown by Gram-Schmidt while a pair's new direction exceeds tau
+ * times the mode's norm (tau 1e-7 works).  The prediction for b is the
+ * least-squares fit of its solution on the pairs seen, mode by mode.
+ * init: checks the mesh (RBC3D_ERR_ARG if it is not such a stack), resets
+ * the model; record != 0 makes every converged rbc3d_no_slip_wall teach the
+ * model the pair (b - r, x), r the true residual it stopped at (= A x).
+ * The wall's next rbc3d_set_walls discards the model.
+ * add: the pair (A x, x) for a solved increment x (ndof values, the layout of
+ * rbc3d_wall_rhs; A x is formed with the FP64 wall operator, so the pair is
+ * exact whatever the tolerance x was solved to); *added (may be NULL) = the
+ * number of modes whose basis grew.
+ * predict: x0 (ndof) for the right-hand side b, and rem (ndof, may be NULL)
+ * the part of b outside the learned span.
+ * size: modes, basis size per mode (nmodes ints, may be NULL), pairs seen. */
+rbc3d_status rbc3d_wall_spectral_init(rbc3d_ctx* ctx, int nring, double tau, int record);
+rbc3d_status rbc3d_wall_spectral_add(rbc3d_ctx* ctx, const double* x, int* added);
+rbc3d_status rbc3d_wall_spectral_predict(rbc3d_ctx* ctx, const double* b, double* x0, double* rem);
+rbc3d_status rbc3d_wall_spectral_size(rbc3d_ctx* ctx, int* nmodes, int* nbasis, long long* pairs);
 
 /* MinDistToTri(xTar, x, s0, t0, x0), ModIntOnWalls.F90:480 (host code, no
  * context): distance from xtar to the triangle x(3,3) (column-major, x(l,:)

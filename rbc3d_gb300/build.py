@@ -13,7 +13,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librbc3d_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["api.cu", "pair.cu", "corr.cu", "pme.cu", "walls.cu", "peak.cu", "noalloc.cu", "selfmix.cu", "mlp.cu", "cellsolve.cu", "membrane.cu", "selfff.cu"]
+SOURCES = ["api.cu", "pair.cu", "corr.cu", "pme.cu", "walls.cu", "peak.cu", "noalloc.cu", "selfmix.cu", "mlp.cu", "cellsolve.cu", "membrane.cu", "selfff.cu", "wallspec.cu"]
 
 
 def nvcc():

@@ -446,6 +446,7 @@ rbc3d_status rbc3d_create(const rbc3d_params* prm, rbc3d_ctx** out) {
 rbc3d_status rbc3d_destroy(rbc3d_ctx* ctx) {
   if (!ctx) return RBC3D_OK;
   pme_release(ctx);
+  wall_spec_release(ctx);
   if (ctx->st2) cudaStreamSynchronize(ctx->st2);
   if (ctx->st) cudaStreamSynchronize(ctx->st);
   for (cudaEvent_t e : ctx->evpool) cudaEventDestroy(e);
@@ -687,6 +688,7 @@ rbc3d_status rbc3d_set_walls(rbc3d_ctx* ctx, int nvert, int nele, const double* 
   }
   W.hf.assign(3 * (size_t)nvert, 0.);
   W.prepared = false;
+  wall_spec_release(ctx);  // a new mesh invalidates the learned spectral operator
   ctx->pme.wplan.valid = false;
   rbc3d_status s = wall_setup(ctx);
   if (s) return s;
@@ -870,9 +872,10 @@ rbc3d_status rbc3d_wall_matmult(rbc3d_ctx* ctx, int prec, const double* u, doubl
 
 rbc3d_status rbc3d_no_slip_wall(rbc3d_ctx* ctx, const rbc3d_solve_opts* opt, const double* guess,
                                 rbc3d_solve_stats* st) {
-  if (!ctx || !opt || opt->guess < 0 || opt->guess > 3 || (opt->guess > 0 && !guess) || opt->rtol < 0 ||
-      opt->max_it < 0 || !valid_prec(opt->prec))
+  if (!ctx || !opt || opt->guess < 0 || opt->guess > 4 || (opt->guess > 0 && opt->guess < 4 && !guess) ||
+      opt->rtol < 0 || opt->max_it < 0 || !valid_prec(opt->prec))
     return RBC3D_ERR_ARG;
+  if (opt->guess == 4 && !ctx->wspec.ready) return ctx_fail(ctx, RBC3D_ERR_STATE, "wall spectral model not initialised");
   return wall_solve(ctx, opt, guess, st);
 }
 

@@ -114,6 +114,32 @@ struct WallState {
   long long nnz = 0;
 };
 
+// Learned spectral operator of the wall solve (wallspec.cu): for a wall that
+// is a uniform stack of nring rings of nper vertices along z, per axial
+// Fourier mode an orthonormal basis Q of the transformed right-hand sides of
+// past solves and the matching transformed solutions Z (A_m Z = Q), so that
+// x_m = Z Q^H b_m predicts the solution of a new right-hand side.
+struct WallSpec {
+  bool ready = false, record = false;
+  int nring = 0, dim = 0, nm = 0, kmax = 0;  // dim = 3 nper, nm = nring / 2 + 1
+  double tau = 1e-7;                        // basis growth threshold (relative to the mode's norm)
+  cufftHandle d2z = 0, z2d = 0;
+  DBuf<double2> Q, Z;                       // [mode][kmax][dim]
+  DBuf<int> nb;                             // basis size per mode
+  DBuf<double2> bh, xh, rh;                 // transformed vectors [mode][dim]
+  DBuf<double> tmp, fin;                    // 2 ndof host-call staging; ndof transform input
+  DBuf<int> added;                          // per mode, last add
+  long long pairs = 0;
+};
+
+// Spherical-harmonic transform tables of the cell grid at degree < L
+// (cellsolve.cu): Gauss and equiangular pbar rows, weights, cos / sin(m phi),
+// FFT_Diff matrices; kept across calls until the grid or L changes.
+struct ShTabs {
+  int L = 0;
+  DBuf<double> PG, PE, wf, cs, sn, Dm, Dn;
+};
+
 struct rbc3d_ctx {
   rbc3d_params prm{};
   double iLb[3]{};
@@ -183,6 +209,7 @@ struct rbc3d_ctx {
 
   PmeState pme;
   WallState wall;
+  WallSpec wspec;
 
   // FP32M self patch: FP32 node records, per-(latitude, patch point) weights,
   // target positions relative to the cell centre (hi/lo)
@@ -200,6 +227,7 @@ struct rbc3d_ctx {
   DBuf<float2> ff_pw;
   DBuf<unsigned> ff_bnd;  // [set][cell][slot]: max |value| (float bits) for the sums' offsets
   int ff_sets = 0;
+  DBuf<short> ff_perm;    // [latitude][k]: lane order of the patch points
 
   // membrane mechanics (membrane.cu): transform tables of the degree < nlat
   // expansion and the reference cells' a_rcp and b, [type][4][nv]
@@ -213,6 +241,8 @@ struct rbc3d_ctx {
     DBuf<unsigned char> excl;  // repulsion: grid pairs within the patch radius on the reference sphere
   } mb;
 
+  ShTabs shtab;                   // transform tables of the cell solve and the device surface sources
+  DBuf<double> sh_c, sh_e;        // surface sources: coefficients, equiangular staging (grow-only)
   DBuf<double> scratch;           // GMRES basis / temporaries
   DBuf<double> dotpart;           // GMRES: per-slice partial dot products
   DBuf<double> stage;             // staging of uploaded spline tables (grow-only)
@@ -279,6 +309,10 @@ rbc3d_status run_wall_self(rbc3d_ctx* ctx, double c1);
 rbc3d_status wall_solve(rbc3d_ctx* ctx, const rbc3d_solve_opts* opt, const double* guess, rbc3d_solve_stats* st);
 rbc3d_status wall_matmult_dev(rbc3d_ctx* ctx, int prec, const double* u_dev, double* y_dev);
 rbc3d_status wall_residual_dev(rbc3d_ctx* ctx, int prec);
+// wallspec.cu
+rbc3d_status wall_spec_predict_dev(rbc3d_ctx* ctx, const double* b_dev, double* x0_dev, double* rem_dev);
+rbc3d_status wall_spec_add_dev(rbc3d_ctx* ctx, const double* b_dev, const double* x_dev);
+void wall_spec_release(rbc3d_ctx* ctx);
 
 // selfmix.cu
 rbc3d_status self_mixed_grid(rbc3d_ctx* ctx, const std::vector<double>& thG, const std::vector<double>& phiA,
@@ -300,6 +334,12 @@ constexpr double RBC3D_IR_ETA = 1e-5;
 
 // cellsolve.cu: Spherepack pbar(m, n, theta), P[m*L + n] for 0 <= m <= n < L
 void pbar_table(int L, double theta, double* P);
+// Rbc_BuildSurfaceSource on the device from the context's point fields:
+// geom -> the x, a3 and detJ tables, f / g -> the f detJ / g detJ tables
+rbc3d_status surface_sources_dev(rbc3d_ctx* ctx, int nlat0, bool geom, bool f, bool g);
+// membrane.cu: RBC_ComputeGeometry of the context's cells from ctx->x
+// (device): a3, detJ (point layout) and area into the context's arrays
+rbc3d_status cells_geometry_dev(rbc3d_ctx* ctx);
 
 // peak.cu
 rbc3d_status fma_peak(int prec, double* tflops);

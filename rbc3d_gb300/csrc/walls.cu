@@ -548,8 +548,13 @@ rbc3d_status wall_solve(rbc3d_ctx* ctx, const rbc3d_solve_opts* o, const double*
   { k_assemble<<<nblk(W.nvert, 256), 256, 0, ctx->st>>>(W.nvert, W.glb.p, W.writer.p, ctx->tl[RBC3D_TLIST_WALL].v.p, -1.0,
                                                        b.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
-  if (o->guess && guess) CUDA_TRY(cudaMemcpyAsync(x.p, guess, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->st));
-  else CUDA_TRY(cudaMemsetAsync(x.p, 0, sizeof(double) * n, ctx->st));
+  if (o->guess == 4) {  // the learned spectral operator's prediction (wallspec.cu)
+    if ((s = wall_spec_predict_dev(ctx, b.p, x.p, nullptr))) return s;
+  } else if (o->guess && guess) {
+    CUDA_TRY(cudaMemcpyAsync(x.p, guess, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->st));
+  } else {
+    CUDA_TRY(cudaMemsetAsync(x.p, 0, sizeof(double) * n, ctx->st));
+  }
   DBuf<double> x2, w2;  // guess mode 3: second guess vector and its image
   if (o->guess == 3 && guess) {
     CUDA_TRY(x2.alloc(n)); CUDA_TRY(w2.alloc(n));
@@ -619,6 +624,13 @@ rbc3d_status wall_solve(rbc3d_ctx* ctx, const rbc3d_solve_opts* o, const double*
     if ((s = gmres_ir(ctx, n, matvec64, matvec, b.p, x.p, r.p, beta, ttol, o->max_it, R, RBC3D_IR_ETA, S))) return s;
   } else if ((s = gmres_cycles(ctx, n, matvec, b.p, x.p, r.p, beta, ttol, o->max_it, R, S))) {
     return s;
+  }
+  // every converged solve teaches the spectral model the pair (A x, x) =
+  // (b - r, x), r the true residual the solve ended on: exact whatever the
+  // tolerance the solve stopped at
+  if (S.converged && ctx->wspec.ready && ctx->wspec.record) {
+    { k_axpby<<<nblk(n, 256), 256, 0, ctx->st>>>(n, -1.0, r.p, 1.0, b.p); ++ctx->launches; }
+    if ((s = wall_spec_add_dev(ctx, b.p, x.p))) return s;
   }
   // wall f = f0 + expand(x)
   { k_expand<<<nblk(W.nvert, 256), 256, 0, ctx->st>>>(W.nvert, W.glb.p, x.p, W.f.p); ++ctx->launches; }

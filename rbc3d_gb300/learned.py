@@ -3,23 +3,30 @@ reference).
 
 The wall solve of NoSlipWall (ModNoSlip.F90:45-150) finds the density
 increment x with A x = b, b the residual wall velocity with the previous
-density (ModNoSlip.F90:110-113).  Along a run consecutive right-hand sides
-are close, and every solved step gives a pair (b_i, x_i) with A x_i = b_i to
-the solve tolerance.  The guess has two parts:
+density (ModNoSlip.F90:110-113).  Every solved step of a run gives a pair
+(b_i, x_i) with A x_i = b_i to the solve tolerance; the learned guess is
+trained on those pairs as the run goes:
 
-* history: c = argmin ||b - B c|| over the last K pairs (B = [b_i]; no
-  matvec, since A X = B), x_h = X c, remainder r_h = b - B c;
-* network: a per-vertex MLP maps local-frame features of r_h (r_h and two
-  graph-Laplacian powers of it, a stencil standing in for the inverse of the
-  first-kind operator, plus x_h) to the remainder e = x - x_h, trained online
-  on the pairs (r_h, e) of the solved steps.
+* spectral operator (rbc3d_wall_spectral_*, device): the tube wall is a
+  uniform stack of rings along the periodic axis, so A is block diagonal in
+  the axial Fourier modes; per mode the model keeps an orthonormal basis of
+  the transformed right-hand sides seen and the matching solutions, and
+  predicts x_s for a new b mode by mode (a pair seen at one position of the
+  tube teaches every position).  It learns the exact pairs (A x_i, x_i) and
+  also returns the part r_s of b outside the learned span.
+* network: a per-vertex MLP (BF16 tensor-core GEMMs, FP32 accumulation,
+  rbc3d_mlp_*) maps local-frame features of r_s (r_s and two graph-Laplacian
+  powers of it, plus x_s) to the remainder e = x - x_s, trained online on
+  the pairs of the solved steps.
 
-GMRES then starts from p x_h + q e_hat with the least-squares p, q (guess
-mode 3 of rbc3d_no_slip_wall, one extra matvec), so the network can only
-lower the initial residual, and runs to the same absolute tolerance
-rtol * ||b|| as the plain solve.  A solve that does not reach it within the
-iteration budget is redone from the previous density (the plain guess, a
-zero increment), which stays the fallback and the yardstick.
+GMRES then starts from p x_s + q e_hat with the least-squares p, q (guess
+mode 3 of rbc3d_no_slip_wall, one extra matvec) and runs to the same
+absolute tolerance rtol * ||b|| as the plain solve.  A solve that does not
+reach it within the iteration budget is redone from the previous density
+(the plain guess, a zero increment), which stays the fallback and the
+yardstick.  The history projection of the previous design (least squares
+over the last K right-hand sides, no symmetry) is kept as the comparison
+arm "history".
 """
 from __future__ import annotations
 
@@ -45,6 +52,11 @@ def _bind(lib):
         "rbc3d_mlp_gradients": (C.c_int, [C.c_void_p, C.c_int, _fp, _fp, _fp, _fp]),
         "rbc3d_mlp_train_step": (C.c_int, [C.c_void_p, C.c_int, _fp, _fp, C.c_float, _fp]),
         "rbc3d_wall_rhs": (C.c_int, [C.c_void_p, C.c_int, _dp]),
+        "rbc3d_wall_spectral_init": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_int]),
+        "rbc3d_wall_spectral_add": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_int)]),
+        "rbc3d_wall_spectral_predict": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
+        "rbc3d_wall_spectral_size": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                               C.POINTER(C.c_longlong)]),
     }
     out = {}
     for name, (res, args) in sig.items():
@@ -152,14 +164,30 @@ def vertex_smoother(wall):
     return sp.diags(1.0 / deg) @ A - sp.identity(nv, format="csr")
 
 
-class WallGuess:
-    """Online-trained initial guess for rbc3d_no_slip_wall (history
-    projection + MLP correction of the remainder)."""
+def ring_count(wall):
+    """Number of rings when the unique wall vertices form a stack of rings
+    along z (unique id = ring * nper + i, as make_tube and periodic Exodus
+    tubes number them), else None.  The library checks the mesh itself."""
+    nu = wall.ndof // 3
+    x = np.zeros((nu, 3))
+    x[wall.glb - 1] = wall.x.T
+    z = x[:, 2]
+    nper = int(np.sum(np.abs(z - z[0]) < 1e-9 * (1 + abs(z[0]))))
+    if nper < 1 or nu % nper:
+        return None
+    return nu // nper
 
-    def __init__(self, lib, wall, width=512, depth=4, seed=0, history=48, buffer_steps=32, nlap=2):
+
+class WallGuess:
+    """Online-trained initial guess for rbc3d_no_slip_wall: the learned
+    spectral operator (device) and the MLP correction of its remainder; the
+    history projection is kept as a comparison arm."""
+
+    def __init__(self, lib, ctx, wall, width=512, depth=4, seed=0, history=48, buffer_steps=32, nlap=2, tau=1e-7):
         self.nlap = nlap
         self.mlp = MLP(lib, 3 * (nlap + 2), width, depth, 3, seed)
         self.fn = self.mlp.fn
+        self.ctx = ctx
         self.frames = vertex_frames(wall)
         self.lap = vertex_smoother(wall)
         self.nv = wall.ndof // 3
@@ -168,8 +196,17 @@ class WallGuess:
         self.hist_b, self.hist_x = [], []
         self.buf = []
         self.buffer_steps = buffer_steps
-        self.k = None  # rms(e) / rms(r_h), set from data
+        self.k = None  # rms(e) / rms(r_s), set from data
         self.lap_scale = None
+        self.pairs = 0
+        nring = ring_count(wall)
+        if nring is None:
+            raise RBC3DError(1, "the learned spectral operator needs a tube wall meshed as a stack of rings")
+        self._ok(self.fn["rbc3d_wall_spectral_init"](ctx.h, nring, tau, 0), "rbc3d_wall_spectral_init")
+
+    def _ok(self, st, what):
+        if st:
+            raise RBC3DError(st, f"{what}: {self.ctx.L.fn['last_error'](self.ctx.h).decode()}")
 
     def _to_local(self, v3):  # (nv,3) -> (nv,3) in the local frame
         return np.einsum("vac,vc->va", self.frames, v3)
@@ -182,7 +219,8 @@ class WallGuess:
         return np.sqrt(np.mean(a * a)) + 1e-300
 
     def project(self, b):
-        """History part: (x_h, r_h) for right-hand side b (zeros if no history)."""
+        """History arm: least squares over the last K right-hand sides,
+        (x_h, r_h) (zeros if no history)."""
         if not self.hist_b:
             return np.zeros_like(b), b.copy()
         Bm = np.stack(self.hist_b, 1)
@@ -190,7 +228,25 @@ class WallGuess:
         c, *_ = np.linalg.lstsq(Bm, b, rcond=None)
         return Xm @ c, b - Bm @ c
 
-    def features(self, r, xh):
+    def spectral(self, b):
+        """Spectral operator: (x_s, r_s), the prediction for b and the part of
+        b outside the learned span."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        xs, rs = np.empty_like(b), np.empty_like(b)
+        self._ok(self.fn["rbc3d_wall_spectral_predict"](self.ctx.h, _ptr(b), _ptr(xs), _ptr(rs)),
+                 "rbc3d_wall_spectral_predict")
+        return xs, rs
+
+    def basis_sizes(self):
+        nm = C.c_int()
+        self._ok(self.fn["rbc3d_wall_spectral_size"](self.ctx.h, C.byref(nm), None, None), "rbc3d_wall_spectral_size")
+        nb = np.zeros(nm.value, dtype=np.int32)
+        pairs = C.c_longlong()
+        self._ok(self.fn["rbc3d_wall_spectral_size"](self.ctx.h, C.byref(nm), nb.ctypes.data_as(C.POINTER(C.c_int)),
+                                                     C.byref(pairs)), "rbc3d_wall_spectral_size")
+        return nb, pairs.value
+
+    def features(self, r, xs):
         g = r.reshape(self.nv, 3)
         rl = self._to_local(g)
         sr = self._rms(rl)
@@ -202,23 +258,30 @@ class WallGuess:
         if self.lap_scale is None:  # fixed per-order scales: the stencil map stays linear in r
             self.lap_scale = [self._rms(l3) for l3 in lap]
         cols += [l3 / c for l3, c in zip(lap, self.lap_scale)]
-        xl = self._to_local(xh.reshape(self.nv, 3))
+        xl = self._to_local(xs.reshape(self.nv, 3))
         cols.append(xl / self._rms(xl))
         return np.concatenate(cols, axis=1), sr
 
     def record(self, b, x):
-        """A solved step (A x = b): training pair for the network, then history."""
-        if len(self.hist_b) >= 2:
-            xh, rh = self.project(b)
-            X, sr = self.features(rh, xh)
-            el = self._to_local((x - xh).reshape(self.nv, 3)) / sr
+        """A solved step (A x = b to the solve tolerance): a training pair for
+        the network (from the spectral prediction made before the pair is
+        learned), then the pair for the spectral operator and the history."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        if self.pairs >= 2:
+            xs, rs = self.spectral(b)
+            X, sr = self.features(rs, xs)
+            el = self._to_local((x - xs).reshape(self.nv, 3)) / sr
             k = self._rms(el)
             self.k = k if self.k is None else 0.8 * self.k + 0.2 * k
             self.buf.append((X.astype(np.float32), el))
             if len(self.buf) > self.buffer_steps:
                 self.buf.pop(0)
-        self.hist_b.append(np.array(b, dtype=np.float64))
-        self.hist_x.append(np.array(x, dtype=np.float64))
+        # the spectral operator learns the exact pair (A x, x), formed on the device
+        self._ok(self.fn["rbc3d_wall_spectral_add"](self.ctx.h, _ptr(x), None), "rbc3d_wall_spectral_add")
+        self.pairs += 1
+        self.hist_b.append(b.copy())
+        self.hist_x.append(x.copy())
         if len(self.hist_b) > self.K:
             self.hist_b.pop(0)
             self.hist_x.pop(0)
@@ -236,13 +299,13 @@ class WallGuess:
         return loss
 
     def predict(self, b):
-        """(x_h, e_hat): history guess and network correction."""
-        xh, rh = self.project(b)
+        """(x_s, e_hat): the spectral prediction and the network's correction."""
+        xs, rs = self.spectral(b)
         if self.k is None:
-            return xh, np.zeros_like(b)
-        X, sr = self.features(rh, xh)
+            return xs, np.zeros_like(b)
+        X, sr = self.features(rs, xs)
         y = self.mlp.forward(X)
-        return xh, np.ascontiguousarray(self._to_global(y.astype(np.float64) * (self.k * sr)).reshape(-1))
+        return xs, np.ascontiguousarray(self._to_global(y.astype(np.float64) * (self.k * sr)).reshape(-1))
 
     def rhs(self, ctx, prec):
         # the solves' right-hand side is FP64 in every mode (the mixed-precision
@@ -254,19 +317,27 @@ class WallGuess:
         return b
 
     def solve(self, ctx, wall, rtol, max_it, restart, prec, mode="learned"):
-        """One NoSlipWall step from the guess `mode` ("learned": history +
-        network, "history": history only).  Returns (stats, accepted, total_ms,
-        b); with accepted False the plain solve (zero increment) was run."""
+        """One NoSlipWall step from the guess `mode`: "learned" (spectral
+        operator + network, least-squares combination), "spectral" (the
+        spectral operator alone, predicted on the device: guess mode 4) or
+        "history" (the history projection, scaled).  Returns (stats, accepted,
+        total_ms, b); with accepted False the plain solve (zero increment) was
+        run."""
         t0 = time.perf_counter()
         f0 = ctx.get_wall_density(wall.nvert)
-        b = self.rhs(ctx, prec)
-        if self.hist_b:
-            xh, eh = self.predict(b)
-            if mode == "learned" and self.k is not None:
-                st, code = ctx.no_slip_wall(rtol, max_it, restart, prec, guess=np.concatenate([xh, eh]),
-                                            check=False, guess_mode=3)
+        b = None
+        if self.pairs:
+            if mode == "spectral":
+                st, code = ctx.no_slip_wall(rtol, max_it, restart, prec, check=False, guess_mode=4)
             else:
-                st, code = ctx.no_slip_wall(rtol, max_it, restart, prec, guess=xh, check=False, guess_mode=2)
+                b = self.rhs(ctx, prec)
+                if mode == "learned":
+                    xs, eh = self.predict(b)
+                    st, code = ctx.no_slip_wall(rtol, max_it, restart, prec, guess=np.concatenate([xs, eh]),
+                                                check=False, guess_mode=3)
+                else:
+                    xh, _ = self.project(b)
+                    st, code = ctx.no_slip_wall(rtol, max_it, restart, prec, guess=xh, check=False, guess_mode=2)
             if code == 0 and st.converged and st.rnorm <= rtol * st.bnorm:
                 return st, True, (time.perf_counter() - t0) * 1e3, b
             ctx.set_wall_density(f0)  # fallback: the plain guess

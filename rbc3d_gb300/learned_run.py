@@ -27,7 +27,7 @@ from . import geometry as G
 from . import library
 from .abi import FP32C, FP32D, FP32M, FP64, Context
 from .dynamics import CellDynamics
-from .learned import WallGuess
+from .learned import WallGuess, ring_count
 
 # Shell_ElasStrs / Shell_Bend moduli of the tube run: shear 1, area dilation
 # 50 (ED / ES), bending 5.4e-3 (the EB / ES ratio of the reference's example
@@ -55,7 +55,7 @@ def run(ncell=64, warm_steps=30, test_steps=10, rtol=1e-8, restart=100, max_it=8
     ctx.set_cell_density(f=cells.f, spl_F=cells.spl_F)
     ctx.set_walls(wall)
     ctx.prepare_sing_int_on_wall()
-    guess = WallGuess(lib, wall, width=width, depth=depth, seed=seed, history=history)
+    guess = WallGuess(lib, ctx, wall, width=width, depth=depth, seed=seed, history=history)
     axis = (prm["Lb"][0] / 2, prm["Lb"][1] / 2)
     rng = np.random.default_rng(seed)
     dyn = None
@@ -67,7 +67,7 @@ def run(ncell=64, warm_steps=30, test_steps=10, rtol=1e-8, restart=100, max_it=8
     elif dynamics != "kinematic":
         raise ValueError(dynamics)
     ctx.no_slip_wall(rtol, max_it, restart, prec, check=False)  # initial density
-    arms = {"plain": [], "history": [], "learned": []}
+    arms = {"plain": [], "history": [], "spectral": [], "learned": []}
     losses, train_ms = [], []
     state = {"step": 0}
 
@@ -78,7 +78,7 @@ def run(ncell=64, warm_steps=30, test_steps=10, rtol=1e-8, restart=100, max_it=8
         f0 = ctx.get_wall_density(wall.nvert)
         testing = step >= warm_steps
         if testing:
-            for mode in ("history", "learned"):
+            for mode in ("history", "spectral", "learned"):
                 st, ok, ms, _ = guess.solve(ctx, wall, rtol, max_it, restart, prec, mode=mode)
                 arms[mode].append(dict(its=st.iterations, ms=ms, rel=st.rnorm / st.bnorm, accepted=ok,
                                        r0=st.rnorm0 / st.bnorm))
@@ -97,7 +97,7 @@ def run(ncell=64, warm_steps=30, test_steps=10, rtol=1e-8, restart=100, max_it=8
         if log:
             msg = f"step {step}.{stage} plain its {st.iterations} ms {ms:.0f}"
             if testing:
-                for mode in ("history", "learned"):
+                for mode in ("history", "spectral", "learned"):
                     a = arms[mode][-1]
                     msg += f" | {mode} its {a['its']} ms {a['ms']:.0f} r0 {a['r0']:.2e}"
             elif loss is not None:
@@ -127,9 +127,16 @@ def run(ncell=64, warm_steps=30, test_steps=10, rtol=1e-8, restart=100, max_it=8
     res = {"cells": ncell, "wall_dof": int(wall.ndof), "warm_steps": warm_steps, "test_steps": test_steps,
            "rtol": rtol, "restart": restart, "history": history, "dynamics": dynamics, "dt": dt,
            "solves_per_step": per_step,
-           "plain": summary("plain"), "history_only": summary("history"), "learned": summary("learned")}
+           "plain": summary("plain"), "history_only": summary("history"), "spectral_only": summary("spectral"),
+           "learned": summary("learned")}
     res["speedup_learned"] = res["plain"]["ms"] / res["learned"]["ms"]
     res["speedup_history_only"] = res["plain"]["ms"] / res["history_only"]["ms"]
+    res["speedup_spectral_only"] = res["plain"]["ms"] / res["spectral_only"]["ms"]
+    res["learned_over_history_its"] = res["learned"]["its"] / res["history_only"]["its"]
+    nb, npairs = guess.basis_sizes()
+    res["spectral"] = {"modes": int(nb.size), "pairs": int(npairs), "basis_min": int(nb.min()),
+                       "basis_median": float(np.median(nb)), "basis_max": int(nb.max()),
+                       "block": wall.ndof // ring_count(wall)}
     res["train_ms_per_step"] = float(np.mean(train_ms))
     res["speedup_learned_incl_training"] = res["plain"]["ms"] / (res["learned"]["ms"] + res["train_ms_per_step"])
     res["final_loss"] = float(losses[-1]) if losses else None

@@ -1,6 +1,8 @@
 """Learned initial guess for the wall GMRES: the BF16 MLP against its FP64
-numpy restatement, online training, and the guarded solve (every accepted
-solve reaches the same rtol * ||b|| as the plain one)."""
+numpy restatement, online training, the spectral operator's translation
+equivariance, the guarded solve (every accepted solve reaches the same
+rtol * ||b|| as the plain one) and what the learned guess gains over the
+history projection."""
 import math
 
 import numpy as np
@@ -96,7 +98,86 @@ def test_learned_guess_reaches_plain_tolerance(gpu, dynamics, dt):
     for arm in ("plain", "history_only", "learned"):
         # every accepted solve meets the plain solve's ||r|| < rtol ||b||
         assert res[arm]["max_final_rel_residual"] <= 1e-8
-    # the least-squares combination (guess mode 3) starts no higher than the history guess
-    assert res["learned"]["initial_rel_residual"] <= res["history_only"]["initial_rel_residual"] * (1 + 1e-9)
+    assert res["spectral_only"]["max_final_rel_residual"] <= 1e-8
+    # the network's least-squares combination (guess mode 3) starts no higher
+    # than the spectral prediction alone
+    assert res["learned"]["initial_rel_residual"] <= res["spectral_only"]["initial_rel_residual"] * (1 + 1e-6)
     # what the guess gains over the plain solve (iterations from the same states)
     assert res["learned"]["its"] < res["plain"]["its"]
+
+
+@pytest.mark.gpu
+def test_learned_guess_beats_history_projection(gpu):
+    """What the learned guess gains over the method without it: on held-out
+    steps (each step's pair is learned only after every arm has solved it),
+    the learned guess (spectral operator + network) starts at least 10x
+    lower than the history projection over the same pairs and needs at
+    least 25% fewer GMRES iterations to the same ||r|| < 1e-8 ||b||."""
+    from rbc3d_gb300.learned_run import run
+    res = run(ncell=16, warm_steps=12, test_steps=3, rtol=1e-8, restart=300, max_it=900, width=128, depth=2,
+              train_iters=20, dynamics="kinematic", dt=5e-3, history=48)
+    print({k: (res[k]["its"], res[k]["initial_rel_residual"]) for k in ("plain", "history_only", "spectral_only",
+                                                                         "learned")})
+    assert res["learned"]["accepted"] == res["history_only"]["accepted"] == res["spectral_only"]["accepted"] == 3
+    assert res["learned"]["max_final_rel_residual"] <= 1e-8
+    assert res["learned"]["initial_rel_residual"] <= 0.1 * res["history_only"]["initial_rel_residual"]
+    assert res["learned"]["its"] <= 0.75 * res["history_only"]["its"]
+
+
+@pytest.mark.gpu
+def test_spectral_operator_learns_translations(gpu):
+    """One pair (A x, x) teaches the operator at every axial position: the
+    prediction for A x shifted by k rings is x shifted by k rings, and its
+    residual is the operator's own translation error (none for shifts of 3
+    rings = 4 PME mesh cells, about 3e-7 of ||b|| for other shifts on a
+    random density)."""
+    from rbc3d_gb300.abi import Context
+    from rbc3d_gb300.learned import WallGuess
+    prm, cells, wall = G.config("C3", ncell=2)
+    ctx = Context(gpu, prm)
+    ctx.set_cells(cells)
+    ctx.set_cell_density(f=cells.f, spl_F=cells.spl_F)
+    ctx.set_walls(wall)
+    ctx.prepare_sing_int_on_wall()
+    wg = WallGuess(gpu, ctx, wall, width=64, depth=1)
+    rng = np.random.default_rng(4)
+    nring, blk = 192, wall.ndof // 192
+    shift = lambda v, k: np.roll(v.reshape(nring, blk), k, axis=0).reshape(-1)
+    x = rng.standard_normal(wall.ndof)
+    b = ctx.wall_matmult(x)
+    wg.record(b, x)
+    nb, pairs = wg.basis_sizes()
+    assert pairs == 1 and nb.min() == nb.max() == 1
+    for k, tol in ((3, 1e-12), (1, 2e-6), (50, 2e-6)):
+        bk = shift(b, k)
+        xs, rs = wg.spectral(bk)
+        assert np.linalg.norm(xs - shift(x, k)) <= 1e-10 * np.linalg.norm(x), k
+        assert np.linalg.norm(rs) <= 1e-12 * np.linalg.norm(b)
+        assert np.linalg.norm(bk - ctx.wall_matmult(xs)) <= tol * np.linalg.norm(b), k
+    # a right-hand side outside the learned span is left in the remainder
+    y = rng.standard_normal(wall.ndof)
+    by = ctx.wall_matmult(y)
+    xs, rs = wg.spectral(by)
+    assert np.linalg.norm(rs) > 0.5 * np.linalg.norm(by)
+    # a second, independent pair grows every mode's basis
+    wg.record(by, y)
+    nb, pairs = wg.basis_sizes()
+    assert pairs == 2 and nb.min() == 2
+    xs, rs = wg.spectral(by)
+    assert np.linalg.norm(xs - y) <= 1e-10 * np.linalg.norm(y)
+    # the same pair again adds nothing
+    wg.record(by, y)
+    nb, _ = wg.basis_sizes()
+    assert nb.max() == 2
+    # guess mode 4: the solve starts from the device prediction
+    ctx.set_wall_density(np.zeros((3, wall.nvert)))
+    st, code = ctx.no_slip_wall(1e-8, 600, 300, check=False, guess_mode=4)
+    assert code == 0 and st.converged == 1 and st.rnorm <= 1e-8 * st.bnorm
+    wg.mlp.close()
+    ctx.close()
+
+
+def test_ring_count_of_the_tube():
+    from rbc3d_gb300.learned import ring_count
+    prm, cells, wall = G.config("C3", ncell=1)
+    assert ring_count(wall) == 192
