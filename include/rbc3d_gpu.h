@@ -178,6 +178,16 @@ rbc3d_status rbc3d_set_cell_density(rbc3d_ctx* ctx, const double* f,
  * TargetList_Update(walls) (ModWall.F90:118, ModTimeInt.F90:80-82).
  * x (nvert x 3), e2v (nele x 3, 1-based), indxVertGlb (nvert, 1-based unique
  * vertex id, GlobData_Init ModData.F90:47-58). */
+/* The same two steps from the raw surface fields alone, with the derived
+ * geometry and tables computed on the device as the reference derives them:
+ * set_cells_x = RBC_ComputeGeometry (a3, detJ, area, meshSize; ModRbc.F90:404)
+ * + Rbc_BuildSurfaceSource(xFlag) (the x, a3, detJ spline tables through
+ * ShAnalGau, ShFilter to degree < nlat0, ShSynthEqu, Spline_Build_On_Sphere;
+ * ModRbc.F90:716) + SourceList_UpdateCoord + TargetList_Update;
+ * set_cell_density_x = Rbc_BuildSurfaceSource(fFlag/gFlag) +
+ * SourceList_UpdateDensity.  x, f, g: N x 3; f or g may be NULL. */
+rbc3d_status rbc3d_set_cells_x(rbc3d_ctx* ctx, int ncell, const int* celltype, int nlat0, const double* x);
+rbc3d_status rbc3d_set_cell_density_x(rbc3d_ctx* ctx, int nlat0, const double* f, const double* g);
 rbc3d_status rbc3d_set_walls(rbc3d_ctx* ctx, int nvert, int nele,
                              const double* x, const int* e2v,
                              const int* indxVertGlb);

@@ -114,6 +114,8 @@ GPU_SIGNATURES = [
     ("host_free", C.c_int, [_vp]),
     ("fma_peak", C.c_int, [C.c_int, _dp]),
     ("h2d_bandwidth", C.c_int, [C.c_ulonglong, _dp]),
+    ("set_cells_x", C.c_int, [_vp, C.c_int, _ip, C.c_int, _dp]),
+    ("set_cell_density_x", C.c_int, [_vp, C.c_int, _dp, _dp]),
 ]
 STAGES = ["pair", "self", "near", "linear", "walls", "pme_spread", "pme_fft_infl", "pme_gather"]
 
@@ -232,6 +234,26 @@ class Context:
                 f64(cells.spl_x), f64(cells.spl_a3), f64(cells.spl_detJ)]
         self._check(self.L.fn["set_cells"](self.h, int(cells.ncell), _ptr(ct, np.int32),
                                            *[_ptr(a) for a in arrs]))
+
+    def set_cells_x(self, cells, nlat0, x=None):
+        """Cells from positions alone (GPU library): geometry and spline tables
+        derived on the device as RBC_ComputeGeometry + Rbc_BuildSurfaceSource
+        (degree < nlat0).  `cells` supplies the grid and cell types; x (3, N)
+        defaults to cells.x."""
+        th, phi, w = f64(cells.th), f64(cells.phi), f64(cells.w)
+        grid = getattr(self, "_grid", None)
+        if grid is None or not all(a.shape == b.shape and np.array_equal(a, b) for a, b in zip(grid, (th, phi, w))):
+            self._check(self.L.fn["set_cell_grid"](self.h, _ptr(th), _ptr(phi), _ptr(w)))
+            self._grid = (th.copy(), phi.copy(), w.copy())
+        ct = i32(cells.celltype)
+        x = f64(cells.x if x is None else x)
+        self._check(self.L.fn["set_cells_x"](self.h, int(cells.ncell), _ptr(ct, np.int32), int(nlat0), _ptr(x)))
+
+    def set_cell_density_x(self, nlat0, f=None, g=None):
+        """Raw densities alone (GPU library): the f detJ / g detJ tables derived
+        on the device as Rbc_BuildSurfaceSource (degree < nlat0)."""
+        f, g = f64(f), f64(g)
+        self._check(self.L.fn["set_cell_density_x"](self.h, int(nlat0), _ptr(f), _ptr(g)))
 
     def set_cell_density(self, f=None, g=None, spl_F=None, spl_G=None):
         f, g, sF, sG = f64(f), f64(g), f64(spl_F), f64(spl_G)

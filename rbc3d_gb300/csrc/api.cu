@@ -467,6 +467,7 @@ rbc3d_status rbc3d_set_cell_grid(rbc3d_ctx* ctx, const double* th, const double*
   if (!ctx || !th || !phi || !w) return RBC3D_ERR_ARG;
   const int nlat = ctx->nlat, nlon = ctx->nlon;
   ctx->h_th.assign(th, th + nlat); ctx->h_phi.assign(phi, phi + nlon); ctx->h_w.assign(w, w + nlat);
+  ctx->shtab.L = 0;  // transform tables of the previous grid
   CUDA_TRY(ctx->th.upload(th, nlat, ctx->st)); CUDA_TRY(ctx->phi.upload(phi, nlon, ctx->st));
   CUDA_TRY(ctx->w.upload(w, nlat, ctx->st));
   std::vector<float4> us(nlat * nlon);
@@ -578,6 +579,8 @@ rbc3d_status rbc3d_set_cell_grid(rbc3d_ctx* ctx, const double* th, const double*
   return RBC3D_OK;
 }
 
+rbc3d_status cells_tail(rbc3d_ctx* ctx);
+
 rbc3d_status rbc3d_set_cells(rbc3d_ctx* ctx, int ncell, const int* celltype, const double* x, const double* a3,
                              const double* detJ, const double* area, const double* meshSize, const double* spl_x,
                              const double* spl_a3, const double* spl_detJ) {
@@ -621,10 +624,20 @@ rbc3d_status rbc3d_set_cells(rbc3d_ctx* ctx, int ncell, const int* celltype, con
   std::swap(ctx->st, ctx->st2);
   CUDA_TRY(cudaEventRecord(ctx->ev_join, ctx->st2));
   if (s) return s;
+  return cells_tail(ctx);
+}
+
+// The position-dependent set-up after the cells' arrays are on the device
+// (the spline tables may still be in flight on the side stream, joined by
+// ev_join): source list, tlist_rbc, PME spread plan, FP32M records.
+rbc3d_status cells_tail(rbc3d_ctx* ctx) {
+  rbc3d_status s;
+  const int nv = ctx->nlat * ctx->nlon;
+  const size_t N = ctx->npt;
   if ((s = build_source_list(ctx))) return s;
   // tlist_rbc (TargetList_Update, ModTargetList.F90:95-131): its work units
   // and the PME spread plan depend on the positions only, and are built while
-  // the spline tables are still going up on the side stream
+  // the spline tables are still being written on the side stream
   TargetSet& t = ctx->tl[RBC3D_TLIST_RBC];
   t.n = ctx->npt;
   t.sorted = false;
@@ -662,6 +675,77 @@ rbc3d_status rbc3d_set_cell_density(rbc3d_ctx* ctx, const double* f, const doubl
     if ((s = upload_splines(ctx, spl_G, 3, SPL_G))) return s;
     ctx->has_g = true;
   }
+  if ((s = self_mixed_density(ctx, f != nullptr, g != nullptr))) return s;
+  if ((s = build_source_density(ctx))) return s;
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));  // the caller's host buffers are free again
+  return RBC3D_OK;
+}
+
+__global__ void k_mesh_size(int ncell, int nlat, const double* __restrict__ area, double* __restrict__ msz) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < ncell) msz[c] = sqrt(area[c] / ((double)nlat * nlat));  // ModRbc.F90:504
+}
+
+// Cells from their positions alone: RBC_ComputeGeometry (a3, detJ, area,
+// meshSize; ModRbc.F90:404-509) and Rbc_BuildSurfaceSource(xFlag) (the x, a3
+// and detJ tables, ShFilter to degree < nlat0; ModRbc.F90:716-807) on the
+// device, then SourceList_UpdateCoord / TargetList_Update as rbc3d_set_cells.
+rbc3d_status rbc3d_set_cells_x(rbc3d_ctx* ctx, int ncell, const int* celltype, int nlat0, const double* x) {
+  if (!ctx || ncell < 0 || (ncell > 0 && (!celltype || !x)))
+    return ctx_fail(ctx, RBC3D_ERR_ARG, "set_cells_x: bad arguments");
+  if (ctx->h_th.empty()) return ctx_fail(ctx, RBC3D_ERR_STATE, "cell grid not set");
+  if (nlat0 < 1 || nlat0 > ctx->nlat || 2 * (nlat0 - 1) >= ctx->nlon)
+    return ctx_fail(ctx, RBC3D_ERR_ARG, "set_cells_x: need 1 <= nlat0 <= nlat, 2 (nlat0 - 1) < nlon");
+  for (int c = 0; c < ncell; ++c)
+    if (celltype[c] < 0 || celltype[c] >= ctx->prm.ncelltypes) return ctx_fail(ctx, RBC3D_ERR_ARG, "bad celltype");
+  const int nv = ctx->nlat * ctx->nlon;
+  ctx->ncell = ncell;
+  ctx->npt = ncell * nv;
+  ctx->has_f = ctx->has_g = false;
+  ctx->src_density = false;
+  if (ncell == 0) return RBC3D_OK;
+  const size_t N = ctx->npt;
+  ctx->h_celltype.assign(celltype, celltype + ncell);
+  CUDA_TRY(ctx->celltype.upload(celltype, ncell, ctx->st));
+  CUDA_TRY(ctx->x.upload(x, 3 * N, ctx->st));
+  CUDA_TRY(ctx->a3.alloc(3 * N)); CUDA_TRY(ctx->detJ.alloc(N));
+  CUDA_TRY(ctx->area.alloc(ncell)); CUDA_TRY(ctx->meshSize.alloc(ncell));
+  CUDA_TRY(ctx->f.alloc(3 * N)); CUDA_TRY(ctx->g.alloc(3 * N)); CUDA_TRY(ctx->sf.alloc(3 * N)); CUDA_TRY(ctx->sg.alloc(3 * N));
+  CUDA_TRY(cudaMemsetAsync(ctx->sg.p, 0, sizeof(double) * 3 * N, ctx->st));
+  CUDA_TRY(cudaMemsetAsync(ctx->g.p, 0, sizeof(double) * 3 * N, ctx->st));
+  CUDA_TRY(ctx->spl.alloc((size_t)ncell * SPL_NSET * ctx->m * ctx->nlon * SPL_NODE));
+  rbc3d_status s;
+  if ((s = cells_geometry_dev(ctx))) return s;
+  { k_mesh_size<<<nblk(ncell, 128), 128, 0, ctx->st>>>(ncell, ctx->nlat, ctx->area.p, ctx->meshSize.p); ++ctx->launches; }
+  std::vector<double> msz(ncell);
+  CUDA_TRY(cudaMemcpyAsync(msz.data(), ctx->meshSize.p, sizeof(double) * ncell, cudaMemcpyDeviceToHost, ctx->st));
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  ctx->near_rthr = 0.5 * *std::min_element(msz.begin(), msz.end());
+  // the spline tables are built on the side stream while the main stream
+  // builds the source list from the positions
+  CUDA_TRY(cudaEventRecord(ctx->ev_fork, ctx->st));
+  CUDA_TRY(cudaStreamWaitEvent(ctx->st2, ctx->ev_fork, 0));
+  std::swap(ctx->st, ctx->st2);
+  s = surface_sources_dev(ctx, nlat0, true, false, false);
+  std::swap(ctx->st, ctx->st2);
+  CUDA_TRY(cudaEventRecord(ctx->ev_join, ctx->st2));
+  if (s) return s;
+  return cells_tail(ctx);
+}
+
+// Densities from the raw surface values alone: Rbc_BuildSurfaceSource(fFlag /
+// gFlag) (the f detJ and g detJ tables, ShFilter to degree < nlat0) on the
+// device, then SourceList_UpdateDensity as rbc3d_set_cell_density.
+rbc3d_status rbc3d_set_cell_density_x(rbc3d_ctx* ctx, int nlat0, const double* f, const double* g) {
+  if (!ctx) return RBC3D_ERR_ARG;
+  if (ctx->npt == 0) return RBC3D_OK;
+  const size_t N = ctx->npt;
+  rbc3d_status s;
+  if (f) CUDA_TRY(ctx->f.upload(f, 3 * N, ctx->st));
+  if (g) CUDA_TRY(ctx->g.upload(g, 3 * N, ctx->st));
+  if ((s = surface_sources_dev(ctx, nlat0, false, f != nullptr, g != nullptr))) return s;
+  if (f) ctx->has_f = true;
+  if (g) ctx->has_g = true;
   if ((s = self_mixed_density(ctx, f != nullptr, g != nullptr))) return s;
   if ((s = build_source_density(ctx))) return s;
   CUDA_TRY(cudaStreamSynchronize(ctx->st));  // the caller's host buffers are free again

@@ -69,6 +69,7 @@ std::vector<double> diff_matrix(int M) {
 
 struct ShArgs {
   int L, nlat, nlon, nrow, ncell, npt;
+  int nvar;           // components of the field (1 or 3); coefficient and staging layouts keep stride 3
   const double* P;    // [row][m][n]
   const double* wf;   // analysis weight per Gauss row: wG_i * 2 / nlon
   const double* cs;   // cos(m phi_j) [m][j]
@@ -91,7 +92,7 @@ __device__ __forceinline__ int pack_b(int L, int m, int n, int k) {
 __global__ void k_sh_anal(ShArgs a, const double* __restrict__ v, const double* __restrict__ fac,
                           double* __restrict__ cvec) {
   extern __shared__ double sm[];
-  const int cell = blockIdx.x / 3, comp = blockIdx.x % 3;
+  const int cell = blockIdx.x / a.nvar, comp = blockIdx.x % a.nvar;
   const int nlat = a.nlat, nlon = a.nlon, L = a.L, nv = nlat * nlon;
   double* g = sm;               // nv
   double* C = g + nv;           // [m][i]
@@ -132,7 +133,7 @@ __global__ void k_sh_anal(ShArgs a, const double* __restrict__ v, const double* 
 // staging layout f[((cell*3 + comp) * nlon + j) * nrow + i]
 __global__ void k_sh_synth(ShArgs a, const double* __restrict__ cvec, double* __restrict__ out, int equi) {
   extern __shared__ double sm[];
-  const int cell = blockIdx.x / 3, comp = blockIdx.x % 3;
+  const int cell = blockIdx.x / a.nvar, comp = blockIdx.x % a.nvar;
   const int L = a.L, nrow = a.nrow, nlon = a.nlon;
   double* A = sm;           // [m][n]
   double* Bc = A + L * L;
@@ -167,11 +168,13 @@ __global__ void k_sh_synth(ShArgs a, const double* __restrict__ cvec, double* __
 }
 
 // Spline_Build_On_Sphere (ModSpline.F90:121-143) of one (cell, comp) from the
-// equiangular staging layout into the GdetJ set of the node-major tables.
-__global__ void k_spline_build(int nlat, int nlon, const double* __restrict__ f, const double* __restrict__ Dm,
-                               const double* __restrict__ Dn, double* __restrict__ spl) {
+// equiangular staging layout into set `set` of the node-major tables (a
+// one-component set leaves components 1 and 2 of its nodes at zero).
+__global__ void k_spline_build(int nlat, int nlon, int nvar, int set, const double* __restrict__ f,
+                               const double* __restrict__ Dm, const double* __restrict__ Dn,
+                               double* __restrict__ spl) {
   extern __shared__ double sm[];
-  const int cell = blockIdx.x / 3, comp = blockIdx.x % 3;
+  const int cell = blockIdx.x / nvar, comp = blockIdx.x % nvar;
   const int M = 2 * nlat, N = nlon, per = M * N;
   double* u = sm;        // [j][i]
   double* u2 = u + per;  // [j][i]
@@ -181,7 +184,7 @@ __global__ void k_spline_build(int nlat, int nlon, const double* __restrict__ f,
     u[t] = i < nlat ? fc[(size_t)j * (nlat + 1) + i] : fc[(size_t)((j + N / 2) % N) * (nlat + 1) + (M - i)];
   }
   __syncthreads();
-  double* dst = spl + ((size_t)cell * SPL_NSET + SPL_G) * per * SPL_NODE;
+  double* dst = spl + ((size_t)cell * SPL_NSET + set) * per * SPL_NODE;
   for (int t = threadIdx.x; t < per; t += blockDim.x) {
     const int i = t % M, j = t / M;
     double d1 = 0, d2 = 0;
@@ -192,6 +195,8 @@ __global__ void k_spline_build(int nlat, int nlon, const double* __restrict__ f,
     o[0 * 3 + comp] = u[t];
     o[1 * 3 + comp] = d1;
     o[2 * 3 + comp] = d2;
+    if (nvar == 1)
+      for (int kind = 0; kind < 4; ++kind) o[kind * 3 + 1] = o[kind * 3 + 2] = 0.0;
   }
   __syncthreads();
   // u12 = FFT_Diff of u1 along the longitude = Dm applied to u2
@@ -212,12 +217,10 @@ __global__ void k_add_vbkg(int n, const double* __restrict__ A, double b0, doubl
   v[i + 2 * (size_t)n] += b2 * iA;
 }
 
-struct CellSolveTabs {
-  int L = 0;
-  DBuf<double> PG, PE, wf, cs, sn, Dm, Dn;
-};
+using CellSolveTabs = ShTabs;
 
 rbc3d_status cell_tabs(rbc3d_ctx* ctx, int L, CellSolveTabs& T) {
+  if (T.L == L && T.PG.p) return RBC3D_OK;  // tables of this grid and degree are current
   const int nlat = ctx->nlat, nlon = ctx->nlon;
   std::vector<double> th(nlat), phi(nlon), w(nlat);
   CUDA_TRY(cudaMemcpyAsync(th.data(), ctx->th.p, sizeof(double) * nlat, cudaMemcpyDeviceToHost, ctx->st));
@@ -242,9 +245,10 @@ rbc3d_status cell_tabs(rbc3d_ctx* ctx, int L, CellSolveTabs& T) {
   return RBC3D_OK;
 }
 
-ShArgs sh_args(const rbc3d_ctx* ctx, const CellSolveTabs& T, bool equi) {
+ShArgs sh_args(const rbc3d_ctx* ctx, const CellSolveTabs& T, bool equi, int nvar = 3) {
   ShArgs a;
   a.L = T.L; a.nlat = ctx->nlat; a.nlon = ctx->nlon; a.ncell = ctx->ncell; a.npt = ctx->npt;
+  a.nvar = nvar;
   a.nrow = equi ? ctx->nlat + 1 : ctx->nlat;
   a.P = equi ? T.PE.p : T.PG.p;
   a.wf = T.wf.p; a.cs = T.cs.p; a.sn = T.sn.p;
@@ -252,17 +256,37 @@ ShArgs sh_args(const rbc3d_ctx* ctx, const CellSolveTabs& T, bool equi) {
 }
 
 // Glob_Sph_Trans PHYS_TO_FOUR of a point-layout field (times fac when given)
-rbc3d_status sh_anal(rbc3d_ctx* ctx, const CellSolveTabs& T, const double* v, const double* fac, double* c) {
-  ShArgs a = sh_args(ctx, T, false);
+rbc3d_status sh_anal(rbc3d_ctx* ctx, const CellSolveTabs& T, const double* v, const double* fac, double* c,
+                     int nvar = 3) {
+  ShArgs a = sh_args(ctx, T, false, nvar);
   const size_t sm = sizeof(double) * ((size_t)a.nlat * a.nlon + 2 * (size_t)T.L * a.nlat);
-  { k_sh_anal<<<3 * ctx->ncell, 128, sm, ctx->st>>>(a, v, fac, c); ++ctx->launches; }
+  { k_sh_anal<<<nvar * ctx->ncell, 128, sm, ctx->st>>>(a, v, fac, c); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   return RBC3D_OK;
 }
-rbc3d_status sh_synth(rbc3d_ctx* ctx, const CellSolveTabs& T, const double* c, double* out, bool equi) {
-  ShArgs a = sh_args(ctx, T, equi);
+rbc3d_status sh_synth(rbc3d_ctx* ctx, const CellSolveTabs& T, const double* c, double* out, bool equi, int nvar = 3) {
+  ShArgs a = sh_args(ctx, T, equi, nvar);
   const size_t sm = sizeof(double) * (2 * (size_t)T.L * T.L + 2 * (size_t)T.L * a.nrow);
-  { k_sh_synth<<<3 * ctx->ncell, 128, sm, ctx->st>>>(a, c, out, equi ? 1 : 0); ++ctx->launches; }
+  { k_sh_synth<<<nvar * ctx->ncell, 128, sm, ctx->st>>>(a, c, out, equi ? 1 : 0); ++ctx->launches; }
+  CUDA_TRY(cudaGetLastError());
+  return RBC3D_OK;
+}
+
+// Rbc_BuildSurfaceSource for one field (ModRbc.F90:716-807): ShAnalGau of v
+// (times fac when given), ShFilter to degree < L, ShSynthEqu on the nlat + 1
+// equiangular rows, Spline_Build_On_Sphere into spline set `set`.
+rbc3d_status build_spline_set(rbc3d_ctx* ctx, const CellSolveTabs& T, const double* v, const double* fac, int nvar,
+                              int set, DBuf<double>& cg, DBuf<double>& fe) {
+  rbc3d_status s;
+  CUDA_TRY(cg.alloc((size_t)ctx->ncell * 3 * T.L * T.L));
+  CUDA_TRY(fe.alloc((size_t)ctx->ncell * 3 * ctx->nlon * (ctx->nlat + 1)));
+  if ((s = sh_anal(ctx, T, v, fac, cg.p, nvar))) return s;
+  if ((s = sh_synth(ctx, T, cg.p, fe.p, true, nvar))) return s;
+  const int per = 2 * ctx->nlat * ctx->nlon;
+  const size_t sm = sizeof(double) * 2 * (size_t)per;
+  if (sm > 48 * 1024) CUDA_TRY(cudaFuncSetAttribute(k_spline_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  { k_spline_build<<<nvar * ctx->ncell, 256, sm, ctx->st>>>(ctx->nlat, ctx->nlon, nvar, set, fe.p, T.Dm.p, T.Dn.p,
+                                                             ctx->spl.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   return RBC3D_OK;
 }
@@ -274,19 +298,29 @@ rbc3d_status set_g_device(rbc3d_ctx* ctx, const CellSolveTabs& T, const double* 
   rbc3d_status s;
   CUDA_TRY(ctx->g.alloc(3 * N));
   CUDA_TRY(cudaMemcpyAsync(ctx->g.p, g, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, ctx->st));
-  if ((s = sh_anal(ctx, T, g, ctx->detJ.p, cg.p))) return s;  // ShAnalGau(g detJ) + ShFilter
-  if ((s = sh_synth(ctx, T, cg.p, fe.p, true))) return s;     // ShSynthEqu
-  const int per = 2 * ctx->nlat * ctx->nlon;
-  const size_t sm = sizeof(double) * 2 * (size_t)per;
-  if (sm > 48 * 1024) CUDA_TRY(cudaFuncSetAttribute(k_spline_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  { k_spline_build<<<3 * ctx->ncell, 256, sm, ctx->st>>>(ctx->nlat, ctx->nlon, fe.p, T.Dm.p, T.Dn.p, ctx->spl.p); ++ctx->launches; }
-  CUDA_TRY(cudaGetLastError());
+  if ((s = build_spline_set(ctx, T, g, ctx->detJ.p, 3, SPL_G, cg, fe))) return s;  // Rbc_BuildSurfaceSource(gFlag)
   ctx->has_g = true;
   if ((s = self_mixed_density(ctx, false, true))) return s;
   return build_source_density(ctx);
 }
 
 }  // namespace
+
+rbc3d_status surface_sources_dev(rbc3d_ctx* ctx, int nlat0, bool geom, bool f, bool g) {
+  if (nlat0 < 1 || nlat0 > ctx->nlat || 2 * (nlat0 - 1) >= ctx->nlon)
+    return ctx_fail(ctx, RBC3D_ERR_ARG, "surface sources: need 1 <= nlat0 <= nlat, 2 (nlat0 - 1) < nlon");
+  CellSolveTabs& T = ctx->shtab;
+  rbc3d_status s;
+  if ((s = cell_tabs(ctx, nlat0, T))) return s;
+  if (geom) {
+    if ((s = build_spline_set(ctx, T, ctx->x.p, nullptr, 3, SPL_X, ctx->sh_c, ctx->sh_e))) return s;
+    if ((s = build_spline_set(ctx, T, ctx->a3.p, nullptr, 3, SPL_A3, ctx->sh_c, ctx->sh_e))) return s;
+    if ((s = build_spline_set(ctx, T, ctx->detJ.p, nullptr, 1, SPL_DJ, ctx->sh_c, ctx->sh_e))) return s;
+  }
+  if (f && (s = build_spline_set(ctx, T, ctx->f.p, ctx->detJ.p, 3, SPL_F, ctx->sh_c, ctx->sh_e))) return s;
+  if (g && (s = build_spline_set(ctx, T, ctx->g.p, ctx->detJ.p, 3, SPL_G, ctx->sh_c, ctx->sh_e))) return s;
+  return RBC3D_OK;
+}
 
 extern "C" int rbc3d_cell_dof(const rbc3d_ctx* ctx, int nlat0) { return ctx ? 3 * nlat0 * nlat0 * ctx->ncell : 0; }
 
@@ -302,7 +336,7 @@ extern "C" rbc3d_status rbc3d_solve_rbc_vel(rbc3d_ctx* ctx, const rbc3d_solve_op
   if (ctx->npt == 0) return RBC3D_OK;
   auto t0 = std::chrono::steady_clock::now();
   rbc3d_solve_stats S{};
-  CellSolveTabs T;
+  CellSolveTabs& T = ctx->shtab;
   rbc3d_status s;
   if ((s = cell_tabs(ctx, nlat0, T))) return s;
   const size_t N = ctx->npt;

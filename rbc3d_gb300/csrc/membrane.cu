@@ -428,18 +428,25 @@ struct Geom {
   DBuf<double> X, A1, A2, Ga, Gar, A1r, A2r, A3, detJ, Gb, area, vol;
 };
 
+rbc3d_status mb_geometry_dev(rbc3d_ctx* ctx, int ncell, const double* x_dev, Geom& G);
+
 rbc3d_status mb_geometry(rbc3d_ctx* ctx, int ncell, const double* x_host, Geom& G) {
+  DBuf<double> xs;
+  CUDA_TRY(xs.upload(x_host, 3 * (size_t)ncell * ctx->nlat * ctx->nlon, ctx->st));
+  return mb_geometry_dev(ctx, ncell, xs.p, G);  // synchronises before xs is freed
+}
+
+rbc3d_status mb_geometry_dev(rbc3d_ctx* ctx, int ncell, const double* x_dev, Geom& G) {
   const int nv = ctx->nlat * ctx->nlon;
   const size_t n = (size_t)ncell * nv;
-  DBuf<double> xs, A31, A32;
-  CUDA_TRY(xs.upload(x_host, 3 * n, ctx->st));
+  DBuf<double> A31, A32;
   CUDA_TRY(G.X.alloc(3 * n)); CUDA_TRY(G.A1.alloc(3 * n)); CUDA_TRY(G.A2.alloc(3 * n));
   CUDA_TRY(G.Ga.alloc(4 * n)); CUDA_TRY(G.Gar.alloc(4 * n)); CUDA_TRY(G.A1r.alloc(3 * n)); CUDA_TRY(G.A2r.alloc(3 * n));
   CUDA_TRY(G.A3.alloc(3 * n)); CUDA_TRY(G.detJ.alloc(n)); CUDA_TRY(G.Gb.alloc(4 * n));
   CUDA_TRY(G.area.alloc(ncell)); CUDA_TRY(G.vol.alloc(ncell));
   CUDA_TRY(A31.alloc(3 * n)); CUDA_TRY(A32.alloc(3 * n));
   const int nb = mb_nblk((long long)n, 256);
-  { k_mb_gather<<<nb, 256, 0, ctx->st>>>(ncell, nv, xs.p, G.X.p); ++ctx->launches; }
+  { k_mb_gather<<<nb, 256, 0, ctx->st>>>(ncell, nv, x_dev, G.X.p); ++ctx->launches; }
   grad(ctx, 3 * ncell, G.X.p, G.A1.p, G.A2.p);
   { k_mb_geom<<<nb, 256, 0, ctx->st>>>(ncell, nv, ctx->nlat, ctx->mb.sinth.p, G.A1.p, G.A2.p, G.Ga.p, G.Gar.p, G.A1r.p,
                                         G.A2r.p, G.A3.p, G.detJ.p); ++ctx->launches; }
@@ -447,11 +454,26 @@ rbc3d_status mb_geometry(rbc3d_ctx* ctx, int ncell, const double* x_host, Geom& 
   { k_mb_curv<<<nb, 256, 0, ctx->st>>>(ncell, nv, G.A1.p, G.A2.p, A31.p, A32.p, G.Gb.p); ++ctx->launches; }
   { k_mb_sums<<<ncell, 256, 0, ctx->st>>>(nv, ctx->nlat, ctx->w.p, G.X.p, G.A3.p, G.detJ.p, G.area.p, G.vol.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
-  CUDA_TRY(cudaStreamSynchronize(ctx->st));  // xs, A31, A32 are freed on return
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));  // A31, A32 (and the caller's staging) are freed on return
   return RBC3D_OK;
 }
 
 }  // namespace
+
+rbc3d_status cells_geometry_dev(rbc3d_ctx* ctx) {
+  rbc3d_status s;
+  if ((s = mb_tables(ctx))) return s;
+  const int nv = ctx->nlat * ctx->nlon;
+  const size_t n = (size_t)ctx->ncell * nv;
+  Geom G;
+  if ((s = mb_geometry_dev(ctx, ctx->ncell, ctx->x.p, G))) return s;
+  { k_mb_scatter<<<mb_nblk((long long)n, 256), 256, 0, ctx->st>>>(ctx->ncell, nv, G.A3.p, ctx->a3.p); ++ctx->launches; }
+  CUDA_TRY(cudaMemcpyAsync(ctx->detJ.p, G.detJ.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->st));
+  CUDA_TRY(cudaMemcpyAsync(ctx->area.p, G.area.p, sizeof(double) * ctx->ncell, cudaMemcpyDeviceToDevice, ctx->st));
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));  // G is freed on return
+  return RBC3D_OK;
+}
 
 extern "C" {
 

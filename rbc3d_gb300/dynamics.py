@@ -2,13 +2,15 @@
 and the RK2 step of TimeInt_RK2 (ModTimeInt.F90:183-271).
 
 One Compute_Rbc_Vel at positions x:
-  RBC_ComputeGeometry + Rbc_BuildSurfaceSource(x)  -> rbc3d_cell_geometry on the
-      GPU, the x / a3 / detJ spline tables from the filtered expansion, then
-      rbc3d_set_cells (SourceList_UpdateCoord, TargetList_Update);
+  RBC_ComputeGeometry + Rbc_BuildSurfaceSource(x)  -> rbc3d_set_cells_x on the GPU
+      (a3, detJ, area and the x / a3 / detJ spline tables of the filtered
+      expansion, SourceList_UpdateCoord, TargetList_Update); with the oracle
+      the same derivation runs on the host;
   Shell_ResForce, f = -f                           -> rbc3d_shell_res_force on the GPU;
   AddIntraCellRepulsionForce                       -> rbc3d_intra_cell_repulsion on the GPU;
   Rbc_SphProject(f) + Rbc_BuildSurfaceSource(f)    -> ShFilter to degree < nlat0 on the
-      Gauss grid, the f detJ spline, rbc3d_set_cell_density;
+      Gauss grid (host), the f detJ spline and SourceList_UpdateDensity on the
+      GPU (rbc3d_set_cell_density_x);
   Solve_RBC_Vel                                    -> rbc3d_solve_rbc_vel (g := v on the cells).
 The spherical-harmonic filter and the equiangular synthesis
 that feed the spline tables are small host transforms in the conventions of
@@ -116,17 +118,32 @@ class CellDynamics:
     def compute_rbc_vel(self, x):
         ctx, c, T = self.ctx, self.cells, self.T
         nc, nlat, nlon = self.ncell, self.nlat, self.nlon
-        a3, detJ, area, _ = ctx.cell_geometry(x, nc)
-        Xg, Ag, Dg = to_grid(x, nc, nlat, nlon), to_grid(a3, nc, nlat, nlon), to_grid(detJ[None], nc, nlat, nlon)
-        cur = G.Cells(nlat=nlat, nlon=nlon, th=c.th, phi=c.phi, w=c.w, ncell=nc, celltype=c.celltype,
-                      x=x, a3=a3, detJ=detJ, area=area, meshSize=np.sqrt(area / nlat ** 2),
-                      spl_x=T.spline(Xg), spl_a3=T.spline(Ag), spl_detJ=T.spline(Dg))
-        ctx.set_cells(cur)
+        device = "set_cells_x" in ctx.L.fn  # the GPU library derives the sources itself
+        if device:
+            # RBC_ComputeGeometry + Rbc_BuildSurfaceSource(xFlag) + the list
+            # updates on the device (rbc3d_set_cells_x)
+            ctx.set_cells_x(c, self.nlat0, x=x)
+        else:
+            # the same derivation on the host (the oracle's path)
+            a3, detJ, area, _ = ctx.cell_geometry(x, nc)
+            Xg, Ag, Dg = to_grid(x, nc, nlat, nlon), to_grid(a3, nc, nlat, nlon), to_grid(detJ[None], nc, nlat, nlon)
+            ctx.set_cells(G.Cells(nlat=nlat, nlon=nlon, th=c.th, phi=c.phi, w=c.w, ncell=nc, celltype=c.celltype,
+                                  x=x, a3=a3, detJ=detJ, area=area, meshSize=np.sqrt(area / nlat ** 2),
+                                  spl_x=T.spline(Xg), spl_a3=T.spline(Ag), spl_detJ=T.spline(Dg)))
         f = -ctx.shell_res_force(x, c.celltype)
-        pushed = ctx.intra_cell_repulsion(x, a3, area, self.force_coef, f) if self.force_coef else 0
+        if self.force_coef:
+            if device:
+                a3, _, area, _ = ctx.cell_geometry(x, nc)  # host arrays of the repulsion call
+            pushed = ctx.intra_cell_repulsion(x, a3, area, self.force_coef, f)
+        else:
+            pushed, area = 0, None
+        # Rbc_SphProject(f), then Rbc_BuildSurfaceSource(fFlag) + SourceList_UpdateDensity
         Fg = T.project(to_grid(f, nc, nlat, nlon))
         f = to_points(Fg)
-        ctx.set_cell_density(f=f, spl_F=T.spline(Fg * Dg))
+        if device:
+            ctx.set_cell_density_x(self.nlat0, f=f)
+        else:
+            ctx.set_cell_density(f=f, spl_F=T.spline(Fg * Dg))
         sol, v, st, _ = ctx.solve_rbc_vel(self.nlat0, rtol=self.rtol, max_it=self.max_it, restart=30, sol=self.sol,
                                           prec=self.prec)
         self.sol = sol
