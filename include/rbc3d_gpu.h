@@ -291,6 +291,19 @@ rbc3d_status rbc3d_shell_res_force(rbc3d_ctx* ctx, int ncell, const int* celltyp
 rbc3d_status rbc3d_intra_cell_repulsion(rbc3d_ctx* ctx, int ncell, const double* x,
                                         const double* a3, const double* area,
                                         double force_coef, double* f, int* count);
+/* InterCellRepulsion (ModRepulsion.F90:270-402) with Closest_Neighbor_Cell and
+ * Closest_Neighbor_Wall (:480-613), one rank: every point of the context's
+ * cells finds the nearest point of another cell (over the 27 hash cells
+ * around it; projected onto that cell's spline surface, Spline_FindProjection,
+ * when within 2 epsDist) and the nearest point of the wall's triangles
+ * (MinDistToTri); closer than epsDist it moves by 0.5 xx (epsDist - rr) / rr,
+ * xx its separation.  Cells whose type has |viscRat| < viscRatThresh move
+ * point by point; with rigidsep the others move rigidly by the mean move of
+ * their moved points.  x (3 x N, out): the moved positions (the context keeps
+ * the old ones until the next rbc3d_set_cells); distMin: the minimum surface
+ * separation found; nmoved: points moved (both may be NULL). */
+rbc3d_status rbc3d_inter_cell_repulsion(rbc3d_ctx* ctx, double epsDist, double viscRatThresh, int rigidsep,
+                                        double* x, double* distMin, int* nmoved);
 /* MyMatMult of ModNoSlip.F90:255 on a dof-length vector: y = A u. */
 rbc3d_status rbc3d_wall_matmult(rbc3d_ctx* ctx, int prec, const double* u,
                                 double* y);

@@ -1636,6 +1636,128 @@ rbc3d_status API(intra_cell_repulsion)(Ctx* c, int ncell, const double* x, const
   return RBC3D_OK;
 }
 
+// InterCellRepulsion (ModRepulsion.F90:270-402) with Closest_Neighbor_Cell
+// (:480-551) and Closest_Neighbor_Wall (:556-613), one rank (every target
+// active): each cell point finds the nearest point of another cell over the
+// 27 hash cells around it (projected onto that cell's spline surface when
+// within 2 epsDist) and the nearest point of the wall's triangles; closer
+// than epsDist it moves by 0.5 xx (epsDist - rr) / rr.  Cells of types with
+// |viscRat| < viscRatThresh move pointwise, others (rigidsep) by the mean
+// move of their moved points.  xout: the moved positions (3 x N).
+rbc3d_status API(inter_cell_repulsion)(Ctx* c, double epsDist, double viscRatThresh, int rigidsep, double* xout,
+                                       double* distMin, int* nmoved) {
+  if (!c || !xout) return fail(c, RBC3D_ERR_ARG, "inter_cell_repulsion");
+  const int nv = c->nlat * c->nlon, N = c->npt;
+  std::vector<double> dx(3 * (size_t)N, 0.);
+  double dmin = HUGE_VAL;
+  int cnt = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(min : dmin) reduction(+ : cnt)
+  for (int i = 0; i < N; ++i) {
+    const double xi[3] = {c->x[i], c->x[i + (size_t)N], c->x[i + 2 * (size_t)N]};
+    const int surf_i = i / nv;
+    // Closest_Neighbor_Cell
+    double dist1 = HUGE_VAL, x1[3] = {0, 0, 0};
+    int j0 = -1;
+    {
+      const HashList& h = c->hcell;
+      int i1, i2, i3;
+      hash_index(h, xi, i1, i2, i3);
+      for (int j1 = std::max(i1 - 1, 0); j1 <= std::min(i1 + 1, h.Nc[0] + 1); ++j1)
+        for (int j2 = std::max(i2 - 1, 0); j2 <= std::min(i2 + 1, h.Nc[1] + 1); ++j2)
+          for (int j3 = std::max(i3 - 1, 0); j3 <= std::min(i3 + 1, h.Nc[2] + 1); ++j3)
+            for (int j = h.hoc[h.id(j1, j2, j3)]; j >= 0; j = h.next[j]) {
+              if (j / nv == surf_i) continue;
+              double xx[3], rr = 0;
+              for (int k = 0; k < 3; ++k) {
+                xx[k] = xi[k] - c->x[j + (size_t)k * N];
+                xx[k] = xx[k] - nint(xx[k] * c->iLb[k]) * c->prm.Lb[k];
+                rr += xx[k] * xx[k];
+              }
+              rr = std::sqrt(rr);
+              if (rr < dist1) { dist1 = rr; j0 = j; }
+            }
+    }
+    if (j0 >= 0 && dist1 <= 2 * epsDist) {
+      const int cell0 = j0 / nv, r = j0 % nv, ilat0 = r % c->nlat, ilon0 = r / c->nlat;
+      double x0[3], xtar[3];
+      cellx(c, c->x, cell0, ilat0, ilon0, x0);
+      for (int k = 0; k < 3; ++k) {
+        double xx = xi[k] - x0[k];
+        xx = xx - nint(xx * c->iLb[k]) * c->prm.Lb[k];
+        xtar[k] = x0[k] + xx;
+      }
+      double th0 = c->th[ilat0], phi0 = c->phi[ilon0];
+      Spline sx;
+      cell_spline(c, c->spl_x, 3, cell0, sx);
+      spline_find_projection(sx, xtar, th0, phi0, x1);
+      double d2 = 0;
+      for (int k = 0; k < 3; ++k) d2 += (xtar[k] - x1[k]) * (xtar[k] - x1[k]);
+      dist1 = std::sqrt(d2);
+    }
+    // Closest_Neighbor_Wall
+    double dist2 = HUGE_VAL, x2[3] = {0, 0, 0};
+    if (c->nvert > 0) {
+      const HashList& h = c->hwall;
+      int i1, i2, i3;
+      hash_index(h, xi, i1, i2, i3);
+      for (int j1 = std::max(i1 - 1, 0); j1 <= std::min(i1 + 1, h.Nc[0] + 1); ++j1)
+        for (int j2 = std::max(i2 - 1, 0); j2 <= std::min(i2 + 1, h.Nc[1] + 1); ++j2)
+          for (int j3 = std::max(i3 - 1, 0); j3 <= std::min(i3 + 1, h.Nc[2] + 1); ++j3)
+            for (int e = h.hoc[h.id(j1, j2, j3)]; e >= 0; e = h.next[e]) {
+              double xe[9], fe[9], xtar[3];
+              tri_coords(c, e, xe, fe);
+              for (int k = 0; k < 3; ++k) {
+                double xx = xi[k] - xe[0 + 3 * k];
+                xx = xx - nint(xx * c->iLb[k]) * c->prm.Lb[k];
+                xtar[k] = xe[0 + 3 * k] + xx;
+              }
+              double s0, t0;
+              const double rr = min_dist_to_tri(xtar, xe, s0, t0);
+              if (rr < dist2) {
+                dist2 = rr;
+                for (int k = 0; k < 3; ++k) x2[k] = (1 - s0 - t0) * xe[0 + 3 * k] + s0 * xe[1 + 3 * k] + t0 * xe[2 + 3 * k];
+              }
+            }
+    }
+    const bool cellwin = dist1 < dist2;
+    const double dist = cellwin ? dist1 : dist2;
+    const double* xj = cellwin ? x1 : x2;
+    dmin = std::min(dmin, dist);
+    if (dist < epsDist) {
+      double xx[3], rr = 0;
+      for (int k = 0; k < 3; ++k) {
+        xx[k] = xi[k] - xj[k];
+        xx[k] = xx[k] - nint(xx[k] * c->iLb[k]) * c->prm.Lb[k];
+        rr += xx[k] * xx[k];
+      }
+      rr = std::sqrt(rr);
+      for (int k = 0; k < 3; ++k) dx[i + (size_t)k * N] = 0.5 * xx[k] * (epsDist - rr) / rr;
+      ++cnt;
+    }
+  }
+  for (size_t q = 0; q < 3 * (size_t)N; ++q) xout[q] = c->x[q];
+  for (int cell = 0; cell < c->ncell; ++cell) {
+    const size_t p0 = (size_t)cell * nv;
+    if (std::fabs(c->prm.viscRat[c->celltype[cell]]) < viscRatThresh) {
+      for (int k = 0; k < 3; ++k)
+        for (int r = 0; r < nv; ++r) xout[p0 + r + (size_t)k * N] += dx[p0 + r + (size_t)k * N];
+    } else if (rigidsep) {
+      double m[3] = {0, 0, 0};
+      int nd = 0;
+      for (int r = 0; r < nv; ++r) {
+        const double a = dx[p0 + r], b = dx[p0 + r + (size_t)N], d = dx[p0 + r + 2 * (size_t)N];
+        if (a * a + b * b + d * d > 0.) { m[0] += a; m[1] += b; m[2] += d; ++nd; }
+      }
+      if (nd > 0)
+        for (int k = 0; k < 3; ++k)
+          for (int r = 0; r < nv; ++r) xout[p0 + r + (size_t)k * N] += m[k] / nd;
+    }
+  }
+  if (distMin) *distMin = dmin;
+  if (nmoved) *nmoved = cnt;
+  return RBC3D_OK;
+}
+
 rbc3d_status API(shell_res_force)(Ctx* c, int ncell, const int* celltype, const double* x, double* f) {
   if (!c || ncell < 0 || (ncell > 0 && (!celltype || !x || !f))) return fail(c, RBC3D_ERR_ARG, "shell_res_force");
   if (c->nref == 0) return fail(c, RBC3D_ERR_STATE, "reference cells not set");

@@ -103,6 +103,7 @@ SIGNATURES = [
     ("cell_geometry", C.c_int, [_vp, C.c_int, _dp, _dp, _dp, _dp, _dp]),
     ("shell_res_force", C.c_int, [_vp, C.c_int, _ip, _dp, _dp]),
     ("intra_cell_repulsion", C.c_int, [_vp, C.c_int, _dp, _dp, _dp, C.c_double, _dp, _ip]),
+    ("inter_cell_repulsion", C.c_int, [_vp, C.c_double, C.c_double, C.c_int, _dp, _dp, _ip]),
 ]
 # Device-timing entry points of the GPU library only.
 GPU_SIGNATURES = [
@@ -412,6 +413,17 @@ class Context:
         self._check(self.L.fn["intra_cell_repulsion"](self.h, int(area.size), _ptr(x), _ptr(a3), _ptr(area),
                                                       float(force_coef), _ptr(f), C.byref(n)))
         return n.value
+
+    def inter_cell_repulsion(self, eps_dist, visc_thresh, rigidsep=False):
+        """InterCellRepulsion on the context's cells and wall: (moved positions
+        (3, N), minimum surface separation, points moved)."""
+        n = self.num_targets(0)
+        x = np.zeros((3, max(n, 0)))
+        dmin = C.c_double()
+        nm = C.c_int()
+        self._check(self.L.fn["inter_cell_repulsion"](self.h, float(eps_dist), float(visc_thresh), int(rigidsep),
+                                                      _ptr(x), C.byref(dmin), C.byref(nm)))
+        return x, dmin.value, nm.value
 
     def counts(self):
         c = Counts()

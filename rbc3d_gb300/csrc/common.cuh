@@ -241,6 +241,42 @@ __device__ __forceinline__ void bspline_w(R xc, int P, int& imin, R* w) {
   }
 }
 
+
+__host__ __device__ __forceinline__ double tri_dot3(const double* a, const double* b) {
+  return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+// MinDistToTri, ModIntOnWalls.F90:480-577.  xv[l][c]: vertex l component c.
+__host__ __device__ inline double min_dist_to_tri(const double* xt, const double xv[3][3], double& s0, double& t0) {
+  double x12[3], x13[3], x1T[3];
+  for (int c = 0; c < 3; ++c) { x12[c] = xv[1][c] - xv[0][c]; x13[c] = xv[2][c] - xv[0][c]; x1T[c] = xv[0][c] - xt[c]; }
+  double a = tri_dot3(x12, x12), b = tri_dot3(x12, x13), c = tri_dot3(x13, x13);
+  double det = a * c - b * b, invDet = 1. / det;
+  double d = tri_dot3(x12, x1T), e = tri_dot3(x13, x1T), f = tri_dot3(x1T, x1T);
+  double s = b * e - c * d, t = b * d - a * e;
+  int region;
+  if (s + t <= det) {
+    if (s < 0) region = (t < 0) ? 4 : 3;
+    else if (t < 0) region = 5;
+    else region = 0;
+  } else {
+    if (s < 0) region = 2;
+    else if (t < 0) region = 6;
+    else region = 1;
+  }
+  if (region == 2) region = (-(c + e) < 0) ? 3 : 1;
+  else if (region == 4) region = (d < 0) ? 5 : 3;
+  else if (region == 6) region = (b + e - a - d < 0) ? 1 : 5;
+  switch (region) {
+    case 0: s = invDet * s; t = invDet * t; break;
+    case 1: s = (c + e - b - d) / (a - 2 * b + c); s = fmin(1., fmax(0., s)); t = 1. - s; break;
+    case 3: s = 0.; t = -e / c; t = fmin(1., fmax(0., t)); break;
+    case 5: t = 0.; s = -d / a; s = fmin(1., fmax(0., s)); break;
+  }
+  s0 = s; t0 = t;
+  return sqrt(a * s * s + 2 * b * s * t + c * t * t + 2 * d * s + 2 * e * t + f);
+}
+
+
 #define RBC3D_STR2(x) #x
 #define RBC3D_STR(x) RBC3D_STR2(x)
 #define CUDA_TRY(x)                                                                                  \

@@ -10,6 +10,9 @@
 // lanes 0..16 and the 27 normal-equation sums are butterfly warp reductions,
 // which leave bit-identical values on every lane so the subsequent 6x6 solve
 // and every branch stay warp-uniform.  In ReAdd lane = azimuth (nazm = 32).
+#include <cmath>
+#include <cstring>
+
 #include "ctx.hpp"
 
 namespace {
@@ -699,6 +702,175 @@ __global__ void __launch_bounds__(128) k_near(CorrArgs a) {
   }
 }
 
+// InterCellRepulsion (ModRepulsion.F90:270-402): one warp per cell point.
+struct RepArgs {
+  int n, nv, nlat, nlon, m;
+  const double* x;      // cell points, point layout (3 x n)
+  const double* sx;     // sorted source positions (3 x n)
+  const int4* smeta;    // (surf 1-based, ilat, ilon, point index)
+  const int* cs;
+  const int* ce;
+  const double* spl;
+  const double* th;
+  const double* phi;
+  int Nc[3];
+  double L[3], iL[3];
+  double eps;
+  // wall (one), or nele == 0
+  int nvert, nele;
+  const double* wx;     // vertices (3 x nvert)
+  const int* e2v;       // (nele x 3), 0-based
+  const int* wcs;
+  const int* wce;
+  const int* worder;
+  double* dx;           // 3 x n, moves (zero where none)
+  unsigned long long* dmin;   // minimum surface separation (double bits)
+  unsigned long long* nmoved;
+};
+
+__device__ __forceinline__ double rep_minimg(double d, double L, double iL) { return d - round(d * iL) * L; }
+
+// lexicographic warp minimum of (d, key): all lanes receive the winner
+__device__ __forceinline__ void warp_argmin(double& d, int& key) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const double d2 = __shfl_xor_sync(0xffffffffu, d, o);
+    const int k2 = __shfl_xor_sync(0xffffffffu, key, o);
+    if (d2 < d || (d2 == d && k2 < key)) { d = d2; key = k2; }
+  }
+}
+
+__global__ void __launch_bounds__(128) k_inter_rep(RepArgs a) {
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= a.n) return;
+  const double xi[3] = {a.x[i], a.x[i + (size_t)a.n], a.x[i + 2 * (size_t)a.n]};
+  const int surf_i = i / a.nv + 1;
+  int ci[3];
+  for (int d = 0; d < 3; ++d) ci[d] = imod((int)floor(xi[d] * a.Nc[d] * a.iL[d]), a.Nc[d]);
+  // Closest_Neighbor_Cell: the nearest mesh point of another cell over the
+  // 27 hash cells around xi (lanes over the sources of each hash cell)
+  double dist1 = 1e300;
+  int q1 = 0x7fffffff;
+  for (int nb = 0; nb < 27; ++nb) {
+    const int hc = imod(ci[0] + nb % 3 - 1, a.Nc[0]) +
+                   a.Nc[0] * (imod(ci[1] + (nb / 3) % 3 - 1, a.Nc[1]) + a.Nc[1] * imod(ci[2] + nb / 9 - 1, a.Nc[2]));
+    for (int q = a.cs[hc] + lane; q < a.ce[hc]; q += 32) {
+      if (a.smeta[q].x == surf_i) continue;
+      double r2 = 0;
+      for (int d = 0; d < 3; ++d) {
+        const double xx = rep_minimg(xi[d] - a.sx[q + (size_t)d * a.n], a.L[d], a.iL[d]);
+        r2 += xx * xx;
+      }
+      const double rr = sqrt(r2);
+      if (rr < dist1 || (rr == dist1 && q < q1)) { dist1 = rr; q1 = q; }
+    }
+  }
+  warp_argmin(dist1, q1);
+  double x1[3] = {0, 0, 0};
+  if (q1 != 0x7fffffff && dist1 <= 2 * a.eps) {
+    // projection onto that cell's spline surface (Spline_FindProjection)
+    const int4 m = a.smeta[q1];
+    const int cell0 = m.x - 1, p0 = m.w;
+    double xtar[3];
+    for (int d = 0; d < 3; ++d) {
+      const double x0 = a.x[p0 + (size_t)d * a.n];
+      xtar[d] = x0 + rep_minimg(xi[d] - x0, a.L[d], a.iL[d]);
+    }
+    double th0 = a.th[m.y], phi0 = a.phi[m.z];
+    const double* sx = a.spl + ((size_t)cell0 * SPL_NSET + SPL_X) * (size_t)a.m * a.nlon * SPL_NODE;
+    find_projection(sx, a.m, a.nlon, xtar, th0, phi0, x1);
+    double d2 = 0;
+    for (int d = 0; d < 3; ++d) d2 += (xtar[d] - x1[d]) * (xtar[d] - x1[d]);
+    dist1 = sqrt(d2);
+  }
+  // Closest_Neighbor_Wall: the nearest point of the wall's triangles whose
+  // centroids lie in the 27 hash cells around xi
+  double dist2 = 1e300;
+  int e2 = 0x7fffffff;
+  double x2[3] = {0, 0, 0};
+  if (a.nele > 0) {
+    double best[3] = {0, 0, 0};
+    for (int nb = 0; nb < 27; ++nb) {
+      const int hc = imod(ci[0] + nb % 3 - 1, a.Nc[0]) +
+                     a.Nc[0] * (imod(ci[1] + (nb / 3) % 3 - 1, a.Nc[1]) + a.Nc[1] * imod(ci[2] + nb / 9 - 1, a.Nc[2]));
+      for (int q = a.wcs[hc] + lane; q < a.wce[hc]; q += 32) {
+        const int e = a.worder[q];
+        double xv[3][3], xtar[3];
+        for (int l = 0; l < 3; ++l) {
+          const int iv = a.e2v[e + (size_t)l * a.nele];
+          for (int d = 0; d < 3; ++d) xv[l][d] = a.wx[iv + (size_t)d * a.nvert];
+        }
+        for (int d = 0; d < 3; ++d) xtar[d] = xv[0][d] + rep_minimg(xi[d] - xv[0][d], a.L[d], a.iL[d]);
+        double s0, t0;
+        const double rr = min_dist_to_tri(xtar, xv, s0, t0);
+        if (rr < dist2 || (rr == dist2 && e < e2)) {
+          dist2 = rr;
+          e2 = e;
+          for (int d = 0; d < 3; ++d) best[d] = (1 - s0 - t0) * xv[0][d] + s0 * xv[1][d] + t0 * xv[2][d];
+        }
+      }
+    }
+    const int emine = e2;
+    warp_argmin(dist2, e2);
+    // the winning lane's closest point
+    const unsigned ball = __ballot_sync(0xffffffffu, emine == e2 && e2 != 0x7fffffff);
+    if (ball) {
+      const int src = __ffs(ball) - 1;
+      for (int d = 0; d < 3; ++d) x2[d] = __shfl_sync(0xffffffffu, best[d], src);
+    }
+  }
+  if (lane != 0) return;
+  const bool cellwin = dist1 < dist2;
+  const double dist = cellwin ? dist1 : dist2;
+  const double* xj = cellwin ? x1 : x2;
+  if (dist < 1e300) atomicMin(a.dmin, (unsigned long long)__double_as_longlong(dist));
+  if (dist < a.eps) {
+    double xx[3], r2 = 0;
+    for (int d = 0; d < 3; ++d) {
+      xx[d] = rep_minimg(xi[d] - xj[d], a.L[d], a.iL[d]);
+      r2 += xx[d] * xx[d];
+    }
+    const double rr = sqrt(r2);
+    for (int d = 0; d < 3; ++d) a.dx[i + (size_t)d * a.n] = 0.5 * xx[d] * (a.eps - rr) / rr;
+    atomicAdd(a.nmoved, 1ull);
+  }
+}
+
+// The moves applied per cell: pointwise for |viscRat| < thresh, else (rigidsep)
+// the mean move of the cell's moved points for every point; xo = x + move.
+__global__ void __launch_bounds__(256) k_inter_rep_apply(int nv, int n, const double* __restrict__ x,
+                                                         const double* __restrict__ dx, const int* __restrict__ celltype,
+                                                         const double* __restrict__ visc, double thresh, int rigidsep,
+                                                         double* __restrict__ xo) {
+  const int cell = blockIdx.x;
+  const size_t p0 = (size_t)cell * nv;
+  const bool soft = fabs(visc[celltype[cell]]) < thresh;
+  __shared__ double red[4][256];
+  double m[4] = {0, 0, 0, 0};
+  if (!soft && rigidsep) {
+    for (int r = threadIdx.x; r < nv; r += blockDim.x) {
+      const double a = dx[p0 + r], b = dx[p0 + r + (size_t)n], c = dx[p0 + r + 2 * (size_t)n];
+      if (a * a + b * b + c * c > 0.) { m[0] += a; m[1] += b; m[2] += c; m[3] += 1.0; }
+    }
+    for (int k = 0; k < 4; ++k) red[k][threadIdx.x] = m[k];
+    __syncthreads();
+    for (int hh = blockDim.x / 2; hh > 0; hh >>= 1) {
+      if ((int)threadIdx.x < hh)
+        for (int k = 0; k < 4; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + hh];
+      __syncthreads();
+    }
+    for (int k = 0; k < 4; ++k) m[k] = red[k][0];
+  }
+  for (int r = threadIdx.x; r < nv; r += blockDim.x)
+    for (int d = 0; d < 3; ++d) {
+      const size_t q = p0 + r + (size_t)d * n;
+      double v = x[q];
+      if (soft) v += dx[q];
+      else if (rigidsep && m[3] > 0) v += m[d] / m[3];
+      xo[q] = v;
+    }
+}
+
 void fill_args(rbc3d_ctx* ctx, int tlist, double c1, double c2, CorrArgs& a, const double* Bc) {
   TargetSet& t = ctx->tl[tlist];
   a.nt = t.n; a.tx = t.x.p; a.tA = t.Acoef.p; a.tmeta = t.meta.p; a.v = t.v.p;
@@ -767,5 +939,50 @@ rbc3d_status run_near_corr(rbc3d_ctx* ctx, int tlist, double c1, double c2, int 
   a.queue = ctx->near_queue.p;
   { k_near<<<nsm * std::max(per_sm, 1), 128, 0, ctx->st>>>(a); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
+  return RBC3D_OK;
+}
+
+// InterCellRepulsion (ModRepulsion.F90:270-402) with Closest_Neighbor_Cell and
+// Closest_Neighbor_Wall (:480-613) on the context's cells and wall.
+extern "C" rbc3d_status rbc3d_inter_cell_repulsion(rbc3d_ctx* ctx, double epsDist, double viscRatThresh,
+                                                   int rigidsep, double* x, double* distMin, int* nmoved) {
+  if (!ctx || !x || !(epsDist > 0)) return RBC3D_ERR_ARG;
+  const int n = ctx->npt;
+  if (distMin) *distMin = HUGE_VAL;
+  if (nmoved) *nmoved = 0;
+  if (n == 0) return RBC3D_OK;
+  if (!ctx->src_sorted) return ctx_fail(ctx, RBC3D_ERR_STATE, "inter_cell_repulsion: cells not set");
+  WallState& W = ctx->wall;
+  if (W.nele > 0 && !W.cstart.p) return ctx_fail(ctx, RBC3D_ERR_STATE, "inter_cell_repulsion: wall lists not built");
+  RepArgs a;
+  a.n = n; a.nv = ctx->nlat * ctx->nlon; a.nlat = ctx->nlat; a.nlon = ctx->nlon; a.m = ctx->m;
+  a.x = ctx->x.p; a.sx = ctx->s_x.p; a.smeta = ctx->s_meta.p; a.cs = ctx->s_cstart.p; a.ce = ctx->s_cend.p;
+  a.spl = ctx->spl.p; a.th = ctx->th.p; a.phi = ctx->phi.p;
+  for (int d = 0; d < 3; ++d) { a.Nc[d] = ctx->hg.Nc[d]; a.L[d] = ctx->prm.Lb[d]; a.iL[d] = ctx->iLb[d]; }
+  a.eps = epsDist;
+  a.nvert = W.nvert; a.nele = W.nele; a.wx = W.x.p; a.e2v = W.e2v.p;
+  a.wcs = W.cstart.p; a.wce = W.cend.p; a.worder = W.order.p;
+  DBuf<double> dx, xo, visc;
+  DBuf<unsigned long long> cnt;
+  CUDA_TRY(dx.alloc(3 * (size_t)n)); CUDA_TRY(xo.alloc(3 * (size_t)n)); CUDA_TRY(cnt.alloc(2));
+  CUDA_TRY(visc.upload(ctx->prm.viscRat, RBC3D_MAX_CELLTYPES, ctx->st));
+  CUDA_TRY(cudaMemsetAsync(dx.p, 0, sizeof(double) * 3 * (size_t)n, ctx->st));
+  unsigned long long init[2] = {0ull, 0ull};
+  const double big = HUGE_VAL;
+  std::memcpy(&init[0], &big, sizeof(big));  // positive doubles order as their bit patterns
+  CUDA_TRY(cudaMemcpyAsync(cnt.p, init, sizeof(init), cudaMemcpyHostToDevice, ctx->st));
+  a.dx = dx.p; a.dmin = cnt.p; a.nmoved = cnt.p + 1;
+  { k_inter_rep<<<(int)(((long long)n * 32 + 127) / 128), 128, 0, ctx->st>>>(a); ++ctx->launches; }
+  { k_inter_rep_apply<<<ctx->ncell, 256, 0, ctx->st>>>(a.nv, n, ctx->x.p, dx.p, ctx->celltype.p, visc.p, viscRatThresh,
+                                                        rigidsep, xo.p); ++ctx->launches; }
+  CUDA_TRY(cudaGetLastError());
+  unsigned long long out[2] = {0, 0};
+  CUDA_TRY(cudaMemcpyAsync(out, cnt.p, sizeof(out), cudaMemcpyDeviceToHost, ctx->st));
+  CUDA_TRY(cudaMemcpyAsync(x, xo.p, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToHost, ctx->st));
+  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  double dm;
+  std::memcpy(&dm, &out[0], sizeof(dm));
+  if (distMin) *distMin = dm;
+  if (nmoved) *nmoved = (int)out[1];
   return RBC3D_OK;
 }

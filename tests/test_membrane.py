@@ -247,3 +247,68 @@ def test_gpu_sickle_cell_matches_oracle(gpu, oracle):
         assert np.abs(a - b).max() <= 1e-10 * max(1.0, np.abs(b).max())
     assert np.linalg.norm(g[4] - o[4]) <= 1e-9 * np.linalg.norm(o[4])
     assert g[6] == o[6] and np.abs(g[5] - o[5]).max() <= 1e-10 * max(1.0, np.abs(o[5]).max())
+
+
+def _packed(lib, wall=False):
+    """Cells packed closer than their size (10 cells, centres at least 2.0
+    apart in a 12^3 box), or 6 cells inside a radius-4 tube whose wall they
+    come within a few tenths of: many points within the repulsion distance of
+    another cell or of the wall.  Two cell types (viscRat 5 and 50)."""
+    if wall:
+        rng = np.random.default_rng(8)
+        L = [9.0, 9.0, 12.0]
+        prm = dict(Lb=L, alpha=G.alpha_for_cutoff(2.9, 1e-6), rc=2.9, eps=1e-6, Nb=[48, 48, 64], P=6, nlat=25,
+                   nlon=50, ncelltypes=2, viscRat=[5.0, 50.0], vBkg=[0, 0, 0])
+        w = G.make_tube(4.0, 12.0, 24, 48, (4.5, 4.5))
+        cells = G.make_cells(rng, 6, L, 2.2, inside=lambda c: (c[0] - 4.5) ** 2 + (c[1] - 4.5) ** 2 < 2.5 ** 2)
+    else:
+        rng = np.random.default_rng(6)
+        L = [12.0] * 3
+        prm = dict(Lb=L, alpha=G.alpha_for_cutoff(3.0, 1e-6), rc=3.0, eps=1e-6, Nb=[32] * 3, P=6, nlat=25, nlon=50,
+                   ncelltypes=2, viscRat=[5.0, 50.0], vBkg=[0, 0, 0])
+        w = None
+        cells = G.make_cells(rng, 10, L, 2.0)
+    cells.celltype = (np.arange(cells.ncell) % 2).astype(np.int32)
+    ctx = Context(lib, prm)
+    ctx.set_cells(cells)
+    if w is not None:
+        ctx.set_walls(w)
+    return ctx, cells
+
+
+def test_oracle_inter_cell_repulsion_moves_close_points(oracle):
+    ctx, cells = _packed(oracle)
+    eps = 0.3
+    x, dmin, n = ctx.inter_cell_repulsion(eps, 10.0, rigidsep=False)
+    assert n > 0 and dmin < eps
+    moved = np.linalg.norm(x - cells.x, axis=0)
+    nv = cells.nlat * cells.nlon
+    soft = np.repeat(cells.celltype == 0, nv)
+    # type 1 (viscRat 50 >= 10, no rigidsep) stays; type 0 moves by at most eps / 2
+    assert np.all(moved[~soft] == 0) and 0 < moved[soft].max() <= 0.5 * eps + 1e-12
+    # with rigidsep the stiff cells move rigidly
+    x2, _, n2 = ctx.inter_cell_repulsion(eps, 10.0, rigidsep=True)
+    d = (x2 - cells.x).reshape(3, cells.ncell, nv)
+    for c in np.flatnonzero(cells.celltype == 1):
+        assert np.allclose(d[:, c, :], d[:, c, :1], atol=1e-14)
+    assert n2 == n
+    # the tube case: points near the wall move too
+    ctx, cells = _packed(oracle, wall=True)
+    x, dmin, n = ctx.inter_cell_repulsion(0.5, 10.0)
+    assert n > 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("wall,eps", [(False, 0.3), (True, 0.5)])
+def test_gpu_inter_cell_repulsion_matches_oracle(gpu, oracle, wall, eps):
+    out = {}
+    for name, lib in (("o", oracle), ("g", gpu)):
+        ctx, cells = _packed(lib, wall)
+        out[name] = [ctx.inter_cell_repulsion(eps, 10.0, rigidsep=r) for r in (False, True)]
+        ctx.close()
+    for r in range(2):
+        xo, do, no = out["o"][r]
+        xg, dg, ng = out["g"][r]
+        assert ng == no > 0
+        assert abs(dg - do) <= 1e-12 * max(do, 1e-300)
+        assert np.abs(xg - xo).max() <= 1e-12
