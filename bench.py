@@ -252,14 +252,20 @@ class Bench:
         self.ctx.set_profiling(0)
         return {k: v[0] / reps for k, v in st.items()}
 
-    def e2e(self, prec, steps):
-        """The matvec through the C ABI from pinned host buffers: positions,
-        densities and spline tables uploaded every step, the caller's velocity
-        accumulator up and the velocities down."""
+    def e2e(self, prec, steps, raw=True, nlat0=12):
+        """The matvec through the C ABI from pinned host buffers, the caller's
+        velocity accumulator up and the velocities down every step.  raw: the
+        caller holds positions and raw densities only, as RBC3D's time
+        integrator does (rbc3d_set_cells_x / rbc3d_set_cell_density_x derive
+        the geometry and the spline tables on the device, degree < nlat0);
+        else positions, geometry, densities and all spline tables go up."""
         from rbc3d_gb300.abi import TERM_ALL, TLIST_RBC
         cells, lib, ctx, c = self.cells, self.lib, self.ctx, self.c
+        resident = self.vector(prec) if raw else None
         pin = {}
-        for k in ("x", "a3", "detJ", "area", "meshSize", "spl_x", "spl_a3", "spl_detJ", "f", "g", "spl_F", "spl_G"):
+        keys = ("x", "f", "g") if raw else ("x", "a3", "detJ", "area", "meshSize", "spl_x", "spl_a3", "spl_detJ",
+                                            "f", "g", "spl_F", "spl_G")
+        for k in keys:
             a = np.ascontiguousarray(getattr(cells, k), dtype=np.float64)
             p = lib.pinned(a.shape)
             p[...] = a
@@ -280,9 +286,15 @@ class Bench:
 
         def one():
             t0 = time.perf_counter()
-            ctx.set_cells(pc)
+            if raw:
+                ctx.set_cells_x(pc, nlat0)
+            else:
+                ctx.set_cells(pc)
             t1 = time.perf_counter()
-            ctx.set_cell_density(f=pc.f, g=pc.g, spl_F=pc.spl_F, spl_G=pc.spl_G)
+            if raw:
+                ctx.set_cell_density_x(nlat0, f=pc.f, g=pc.g)
+            else:
+                ctx.set_cell_density(f=pc.f, g=pc.g, spl_F=pc.spl_F, spl_G=pc.spl_G)
             t2 = time.perf_counter()
             vout[...] = 0.0
             ctx.matvec(TLIST_RBC, c, c, TERM_ALL, prec, v=vout)
@@ -300,10 +312,19 @@ class Bench:
         for _ in range(steps):
             one()
         te = dist_max(self.dist, (time.perf_counter() - te) / steps)
-        return {"value": self.ws * self.N / te, "unit": "targets/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": te * 1e3,
-                "host_ms_per_step": {k: v / steps * 1e3 for k, v in parts.items()},
-                "h2d_gbs_measured": lib.h2d_bandwidth(h2d)}
+        out = {"value": self.ws * self.N / te, "unit": "targets/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "ms_per_step": te * 1e3,
+               "host_ms_per_step": {k: v / steps * 1e3 for k, v in parts.items()},
+               "h2d_gbs_measured": lib.h2d_bandwidth(h2d),
+               "inputs": ("positions and raw densities (geometry and spline tables derived on the device, degree "
+                          f"< {nlat0})") if raw else "positions, geometry, densities and spline tables"}
+        if raw:
+            # the synthetic workload's resident tables are analytic samples; the
+            # derived ones filter a3 and detJ as the reference does
+            out["rel_l2_vs_resident_tables"] = rel(np.array(vout), resident)
+            ctx.set_cells(cells)  # back to the resident inputs
+            ctx.set_cell_density(f=cells.f, g=cells.g, spl_F=cells.spl_F, spl_G=cells.spl_G)
+        return out
 
     def close(self):
         self.ctx.close()
@@ -388,6 +409,8 @@ def main():
     ap.add_argument("--no-wall", action="store_true", help="skip the learned-guess wall GMRES comparison")
     ap.add_argument("--no-scaleup", action="store_true", help="skip the 2048-cell (PME 256^3) workload")
     ap.add_argument("--no-cellsolve", action="store_true", help="skip the cell velocity GMRES line")
+    ap.add_argument("--wall-steps", type=int, nargs=2, default=(100, 10), metavar=("TRAIN", "TEST"),
+                    help="RK2 steps of the learned-guess comparison: training steps, compared steps")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     dist = dist_init()
@@ -433,9 +456,10 @@ def main():
     vec = {name: b.vector(p) for name, p in (("fp64", FP64), ("fp32c", FP32C), ("fp32m", FP32M), ("fp32d", FP32D))}
     err_fp64 = {k: rel(v, vec["fp64"]) for k, v in vec.items() if k != "fp64"}
 
-    e2e = b.e2e(FP32D, max(3, args.steps // 2))
+    e2e = b.e2e(FP32D, max(3, args.steps // 2), raw=True)
     e2e["floor_ms"] = ms_step + e2e["h2d_bytes_per_step"] / (e2e["h2d_gbs_measured"] * 1e9) * 1e3
     e2e["floor"] = "device matvec + the step's uploads at the measured pinned copy bandwidth"
+    e2e_tables = b.e2e(FP32D, max(3, args.steps // 2), raw=False)
 
     peak32 = lib.fma_peak(FP32C)
     peak64 = lib.fma_peak(FP64)
@@ -478,7 +502,7 @@ def main():
         m564, _, _, _ = b5.timed(FP64, 1, 3)
         cnt5 = b5.ctx.counts()
         vec5 = {n: b5.vector(p) for n, p in (("fp64", FP64), ("fp32c", FP32C), ("fp32m", FP32M), ("fp32d", FP32D))}
-        e5 = b5.e2e(FP32D, 5)
+        e5 = b5.e2e(FP32D, 5, raw=True)
         e5["floor_ms"] = m5d + e5["h2d_bytes_per_step"] / (e5["h2d_gbs_measured"] * 1e9) * 1e3
         r5, s5d = rooflines_of(b5, cnt5, peak32, peak64, hbm_peak, hbm_src, sm_mhz)
         b5.close()
@@ -508,25 +532,33 @@ def main():
     wall = None
     if not args.no_wall and not args.cells:
         from rbc3d_gb300.learned_run import run as wall_run
+        keys = ("wall_dof", "restart", "history", "plain", "history_only", "spectral_only", "learned",
+                "speedup_learned", "speedup_history_only", "speedup_spectral_only", "learned_over_history_its",
+                "train_ms_per_step", "speedup_learned_incl_training", "spectral", "mlp")
         t1 = time.perf_counter()
-        w = wall_run(ncell=64, warm_steps=25, test_steps=3, rtol=1e-8, restart=300, max_it=900, train_iters=30,
+        warm, test = args.wall_steps
+        w = wall_run(ncell=64, warm_steps=warm, test_steps=test, rtol=1e-8, restart=300, max_it=900, train_iters=30,
                      history=48, seed=args.seed + rank, dynamics="skalak", dt=1e-3)
         log(f"wall GMRES comparison in {time.perf_counter() - t1:.1f}s")
         wall = {"workload": "C3 tube (R=8, L=48, 64 cells) under RK2 membrane dynamics (Skalak ES 1, ED 50, "
                             "bending 5.4e-3, intra-cell repulsion 0.81, dt 1e-3), NoSlipWall after each RK2 "
                             "stage; FP64 matvec + FP64 Arnoldi, ||r|| < 1e-8 ||b||",
-                **{k: w[k] for k in ("wall_dof", "restart", "history", "plain", "history_only", "learned",
-                                     "speedup_learned", "speedup_history_only", "train_ms_per_step",
-                                     "speedup_learned_incl_training", "mlp")},
-                "steps": "25 warm-up RK2 steps (50 plain solves: history + online training), then 3 steps "
-                         "(6 solves) each solved plain, from the history guess and from the learned guess"}
+                **{k: w[k] for k in keys},
+                "steps": f"{warm} RK2 steps ({2 * warm} plain solves: the pairs that train the spectral operator "
+                         f"and the MLP online), then {test} steps ({2 * test} solves) each solved plain, from the "
+                         "history projection, from the spectral operator alone and from the learned guess "
+                         "(spectral operator + MLP); each compared step's pair is learned only after every arm "
+                         "has solved it (held out)"}
         t1 = time.perf_counter()
-        wm = wall_run(ncell=64, warm_steps=25, test_steps=3, rtol=1e-8, restart=300, max_it=900, train_iters=30,
-                      history=48, seed=args.seed + rank, prec=FP32M, dynamics="skalak", dt=1e-3)
+        wm_warm, wm_test = max(10, warm // 2), max(3, test // 2)
+        wm = wall_run(ncell=64, warm_steps=wm_warm, test_steps=wm_test, rtol=1e-8, restart=300, max_it=900,
+                      train_iters=30, history=48, seed=args.seed + rank, prec=FP32M, dynamics="skalak", dt=1e-3)
         log(f"mixed-precision wall GMRES comparison in {time.perf_counter() - t1:.1f}s")
-        wall["mixed_fp32m"] = {k: wm[k] for k in ("plain", "history_only", "learned", "speedup_learned",
-                                                  "speedup_history_only", "speedup_learned_incl_training")}
+        wall["mixed_fp32m"] = {k: wm[k] for k in ("plain", "history_only", "spectral_only", "learned",
+                                                  "speedup_learned", "speedup_history_only", "speedup_spectral_only",
+                                                  "speedup_learned_incl_training")}
         wall["mixed_fp32m"]["learned_over_fp64_plain"] = w["plain"]["ms"] / wm["learned"]["ms"]
+        wall["mixed_fp32m"]["steps"] = f"{wm_warm} training + {wm_test} compared RK2 steps"
 
     # ---- cell velocity GMRES (Solve_RBC_Vel, degree 12, rtol 1e-11 as the reference
     # sets it) on the 256 cells: FP64 solve vs the mixed-precision solves
@@ -580,6 +612,7 @@ def main():
                       "stages_ms_per_step": stm,
                       "note": "own-cell polar patch in FP32 with FP64-accurate (hi/lo) geometry"},
             "e2e": e2e,
+            "e2e_host_tables": e2e_tables,
             "stages_ms_per_step": stages,
             "counts": {k: counts[k] for k in ("pairs_within_rc", "nbr_items", "nearsing_items", "self_items",
                                               "screen_misses", "near_replays", "near_projections")},

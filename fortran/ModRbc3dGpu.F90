@@ -275,6 +275,60 @@ module ModRbc3dGpu
       real(c_double), intent(inout) :: f(*)
       integer(c_int), intent(out) :: count
     end function
+    integer(c_int) function rbc3d_set_cells_x(ctx, ncell, celltype, nlat0, x) bind(C, name="rbc3d_set_cells_x")
+      import
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: ncell, nlat0
+      integer(c_int), intent(in) :: celltype(*)
+      real(c_double), intent(in) :: x(*)
+    end function
+    integer(c_int) function rbc3d_set_cell_density_x(ctx, nlat0, f, g) bind(C, name="rbc3d_set_cell_density_x")
+      import
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: nlat0
+      type(c_ptr), value :: f, g                          ! c_loc(...) or c_null_ptr
+    end function
+    integer(c_int) function rbc3d_inter_cell_repulsion(ctx, epsDist, viscRatThresh, rigidsep, x, distMin, nmoved) &
+        bind(C, name="rbc3d_inter_cell_repulsion")
+      import
+      type(c_ptr), value :: ctx
+      real(c_double), value :: epsDist, viscRatThresh
+      integer(c_int), value :: rigidsep
+      real(c_double), intent(out) :: x(*)
+      real(c_double), intent(out) :: distMin
+      integer(c_int), intent(out) :: nmoved
+    end function
+    integer(c_int) function rbc3d_wall_rhs(ctx, prec, b) bind(C, name="rbc3d_wall_rhs")
+      import
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: prec
+      real(c_double), intent(out) :: b(*)
+    end function
+    integer(c_int) function rbc3d_wall_spectral_init(ctx, nring, tau, record) bind(C, name="rbc3d_wall_spectral_init")
+      import
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: nring, record
+      real(c_double), value :: tau
+    end function
+    integer(c_int) function rbc3d_wall_spectral_add(ctx, x, added) bind(C, name="rbc3d_wall_spectral_add")
+      import
+      type(c_ptr), value :: ctx
+      real(c_double), intent(in) :: x(*)
+      integer(c_int), intent(out) :: added
+    end function
+    integer(c_int) function rbc3d_wall_spectral_predict(ctx, b, x0, rem) bind(C, name="rbc3d_wall_spectral_predict")
+      import
+      type(c_ptr), value :: ctx
+      real(c_double), intent(in) :: b(*)
+      real(c_double), intent(out) :: x0(*), rem(*)
+    end function
+    integer(c_int) function rbc3d_wall_spectral_size(ctx, nmodes, nbasis, pairs) bind(C, name="rbc3d_wall_spectral_size")
+      import
+      type(c_ptr), value :: ctx
+      integer(c_int), intent(out) :: nmodes
+      integer(c_int), intent(out) :: nbasis(*)
+      integer(c_long_long), intent(out) :: pairs
+    end function
     integer(c_int) function rbc3d_min_dist_to_tri(xtar, x, s0, t0, x0, dist) bind(C, name="rbc3d_min_dist_to_tri")
       import
       real(c_double), intent(in) :: xtar(3), x(9)
