@@ -260,6 +260,8 @@ rbc3d_status sh_anal(rbc3d_ctx* ctx, const CellSolveTabs& T, const double* v, co
                      int nvar = 3) {
   ShArgs a = sh_args(ctx, T, false, nvar);
   const size_t sm = sizeof(double) * ((size_t)a.nlat * a.nlon + 2 * (size_t)T.L * a.nlat);
+  if (sm > 227 * 1024) return ctx_fail(ctx, RBC3D_ERR_ARG, "sh_anal: cell grid too large for one block");
+  if (sm > 48 * 1024) CUDA_TRY(cudaFuncSetAttribute(k_sh_anal, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   { k_sh_anal<<<nvar * ctx->ncell, 128, sm, ctx->st>>>(a, v, fac, c); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   return RBC3D_OK;
@@ -267,6 +269,8 @@ rbc3d_status sh_anal(rbc3d_ctx* ctx, const CellSolveTabs& T, const double* v, co
 rbc3d_status sh_synth(rbc3d_ctx* ctx, const CellSolveTabs& T, const double* c, double* out, bool equi, int nvar = 3) {
   ShArgs a = sh_args(ctx, T, equi, nvar);
   const size_t sm = sizeof(double) * (2 * (size_t)T.L * T.L + 2 * (size_t)T.L * a.nrow);
+  if (sm > 227 * 1024) return ctx_fail(ctx, RBC3D_ERR_ARG, "sh_synth: degree too large for one block");
+  if (sm > 48 * 1024) CUDA_TRY(cudaFuncSetAttribute(k_sh_synth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   { k_sh_synth<<<nvar * ctx->ncell, 128, sm, ctx->st>>>(a, c, out, equi ? 1 : 0); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   return RBC3D_OK;
@@ -284,6 +288,7 @@ rbc3d_status build_spline_set(rbc3d_ctx* ctx, const CellSolveTabs& T, const doub
   if ((s = sh_synth(ctx, T, cg.p, fe.p, true, nvar))) return s;
   const int per = 2 * ctx->nlat * ctx->nlon;
   const size_t sm = sizeof(double) * 2 * (size_t)per;
+  if (sm > 227 * 1024) return ctx_fail(ctx, RBC3D_ERR_ARG, "spline build: cell grid too large for one block");
   if (sm > 48 * 1024) CUDA_TRY(cudaFuncSetAttribute(k_spline_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   { k_spline_build<<<nvar * ctx->ncell, 256, sm, ctx->st>>>(ctx->nlat, ctx->nlon, nvar, set, fe.p, T.Dm.p, T.Dn.p,
                                                              ctx->spl.p); ++ctx->launches; }

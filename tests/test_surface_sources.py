@@ -43,7 +43,8 @@ def test_device_surface_sources_match_host_derivation(gpu, nlat0):
     dev = Context(gpu, prm)
     dev.set_cells_x(cells, nlat0)
     dev.set_cell_density_x(nlat0, f=cells.f, g=cells.g)
-    for prec, tol in ((FP64, 1e-12), (FP32D, 1e-6)):
+    # the two transforms sum in different orders: 1.7e-12 measured in FP64
+    for prec, tol in ((FP64, 1e-11), (FP32D, 1e-6)):
         a = ref_ctx.matvec(TLIST_RBC, C, C, TERM_ALL, prec)
         ca = ref_ctx.counts()
         b = dev.matvec(TLIST_RBC, C, C, TERM_ALL, prec)
@@ -63,20 +64,25 @@ def test_device_surface_sources_match_host_derivation(gpu, nlat0):
 
 def test_device_surface_sources_of_the_synthetic_cells(gpu):
     """The synthetic workloads carry analytic tables; the device derivation
-    filters a3 and detJ to degree < nlat0 as the reference does, which moves
-    the matvec by the truncation of that filter only."""
+    filters every field to degree < nlat0 as the reference does (ShFilter),
+    which moves the matvec by the truncation of that filter only: the
+    difference shrinks as the kept degree grows (the oracle's 4-cell case:
+    4.2e-3 at nlat0 12, 1.6e-4 at 20, 1.0e-4 at 24)."""
     prm, cells, _ = G.config("C2", ncell=24)
     prm["Lb"] = [20.0] * 3
     a_ctx = Context(gpu, prm)
     a_ctx.set_cells(cells)
     a_ctx.set_cell_density(f=cells.f, g=cells.g, spl_F=cells.spl_F, spl_G=cells.spl_G)
-    d_ctx = Context(gpu, prm)
-    d_ctx.set_cells_x(cells, 12)
-    d_ctx.set_cell_density_x(12, f=cells.f, g=cells.g)
     a = a_ctx.matvec(TLIST_RBC, C, C, TERM_ALL, FP64)
-    b = d_ctx.matvec(TLIST_RBC, C, C, TERM_ALL, FP64)
-    err = np.linalg.norm(a - b) / np.linalg.norm(a)
-    print(f"analytic vs device-derived tables: {err:.2e}")
-    assert err < 1e-4
+    err = {}
+    for nlat0 in (12, 24):
+        d_ctx = Context(gpu, prm)
+        d_ctx.set_cells_x(cells, nlat0)
+        d_ctx.set_cell_density_x(nlat0, f=cells.f, g=cells.g)
+        b = d_ctx.matvec(TLIST_RBC, C, C, TERM_ALL, FP64)
+        err[nlat0] = np.linalg.norm(a - b) / np.linalg.norm(a)
+        d_ctx.close()
+    print(f"analytic vs device-derived tables: {err}")
+    assert err[12] < 1e-2
+    assert err[24] < 3e-4 and err[24] < 0.1 * err[12]
     a_ctx.close()
-    d_ctx.close()
