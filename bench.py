@@ -533,7 +533,8 @@ def main():
     if not args.no_wall and not args.cells:
         from rbc3d_gb300.learned_run import run as wall_run
         keys = ("wall_dof", "restart", "history", "plain", "history_only", "spectral_only", "learned",
-                "speedup_learned", "speedup_history_only", "speedup_spectral_only", "learned_over_history_its",
+                "spectral_preconditioned", "speedup_learned", "speedup_history_only", "speedup_spectral_only",
+                "speedup_spectral_preconditioned", "learned_over_history_its",
                 "train_ms_per_step", "speedup_learned_incl_training", "spectral", "mlp")
         t1 = time.perf_counter()
         warm, test = args.wall_steps
@@ -546,15 +547,17 @@ def main():
                 **{k: w[k] for k in keys},
                 "steps": f"{warm} RK2 steps ({2 * warm} plain solves: the pairs that train the spectral operator "
                          f"and the MLP online), then {test} steps ({2 * test} solves) each solved plain, from the "
-                         "history projection, from the spectral operator alone and from the learned guess "
-                         "(spectral operator + MLP); each compared step's pair is learned only after every arm "
-                         "has solved it (held out)"}
+                         "history projection, from the spectral operator alone, from the learned guess "
+                         "(spectral operator + MLP) and with the spectral operator as the right preconditioner "
+                         "(guess mode 5); each compared step's pair is learned only after every arm has solved it "
+                         "(held out)"}
         t1 = time.perf_counter()
         wm_warm, wm_test = max(10, warm // 2), max(3, test // 2)
         wm = wall_run(ncell=64, warm_steps=wm_warm, test_steps=wm_test, rtol=1e-8, restart=300, max_it=900,
                       train_iters=30, history=48, seed=args.seed + rank, prec=FP32M, dynamics="skalak", dt=1e-3)
         log(f"mixed-precision wall GMRES comparison in {time.perf_counter() - t1:.1f}s")
         wall["mixed_fp32m"] = {k: wm[k] for k in ("plain", "history_only", "spectral_only", "learned",
+                                                  "spectral_preconditioned", "speedup_spectral_preconditioned",
                                                   "speedup_learned", "speedup_history_only", "speedup_spectral_only",
                                                   "speedup_learned_incl_training")}
         wall["mixed_fp32m"]["learned_over_fp64_plain"] = w["plain"]["ms"] / wm["learned"]["ms"]

@@ -123,7 +123,12 @@ typedef struct rbc3d_solve_opts {
                     as p x1 + q x2 with the least-squares p, q (one extra
                     matvec);
                     4: wall solve only: the prediction of the learned
-                    spectral operator (rbc3d_wall_spectral_init) */
+                    spectral operator (rbc3d_wall_spectral_init);
+                    5: wall solve only: that prediction as x0, and the
+                    operator as a right preconditioner (GMRES on A M; the
+                    residual and the convergence test stay those of
+                    b - A x): the inverse of each axial mode whose learned
+                    basis is complete, the identity on the others */
 } rbc3d_solve_opts;
 
 typedef struct rbc3d_solve_stats {

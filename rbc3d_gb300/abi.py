@@ -356,7 +356,7 @@ class Context:
 
     def no_slip_wall(self, rtol, max_it, restart=30, prec=FP64, guess=None, check=True, guess_mode=1):
         o = SolveOpts(rtol=rtol, max_it=max_it, restart=restart, prec=prec,
-                      guess=0 if (guess is None and guess_mode != 4) else guess_mode)
+                      guess=0 if (guess is None and guess_mode not in (4, 5)) else guess_mode)
         st = SolveStats()
         g = f64(guess)
         code = self.L.fn["no_slip_wall"](self.h, C.byref(o), _ptr(g), C.byref(st))

@@ -956,10 +956,10 @@ rbc3d_status rbc3d_wall_matmult(rbc3d_ctx* ctx, int prec, const double* u, doubl
 
 rbc3d_status rbc3d_no_slip_wall(rbc3d_ctx* ctx, const rbc3d_solve_opts* opt, const double* guess,
                                 rbc3d_solve_stats* st) {
-  if (!ctx || !opt || opt->guess < 0 || opt->guess > 4 || (opt->guess > 0 && opt->guess < 4 && !guess) ||
+  if (!ctx || !opt || opt->guess < 0 || opt->guess > 5 || (opt->guess > 0 && opt->guess < 4 && !guess) ||
       opt->rtol < 0 || opt->max_it < 0 || !valid_prec(opt->prec))
     return RBC3D_ERR_ARG;
-  if (opt->guess == 4 && !ctx->wspec.ready) return ctx_fail(ctx, RBC3D_ERR_STATE, "wall spectral model not initialised");
+  if (opt->guess >= 4 && !ctx->wspec.ready) return ctx_fail(ctx, RBC3D_ERR_STATE, "wall spectral model not initialised");
   return wall_solve(ctx, opt, guess, st);
 }
 

@@ -167,44 +167,124 @@ __global__ void k_sh_synth(ShArgs a, const double* __restrict__ cvec, double* __
   }
 }
 
-// Spline_Build_On_Sphere (ModSpline.F90:121-143) of one (cell, comp) from the
-// equiangular staging layout into set `set` of the node-major tables (a
-// one-component set leaves components 1 and 2 of its nodes at zero).
-__global__ void k_spline_build(int nlat, int nlon, int nvar, int set, const double* __restrict__ f,
-                               const double* __restrict__ Dm, const double* __restrict__ Dn,
-                               double* __restrict__ spl) {
+// Rbc_BuildSurfaceSource for one (cell, comp) in one pass (ModRbc.F90:716-807):
+// ShAnalGau of v (times fac) on the Gauss rows, ShFilter to degree < L, then
+// the node values of Spline_Build_On_Sphere (ModSpline.F90:121-143) on the
+// doubled meridian grid (M = 2 nlat rows, N = nlon columns): u, its FFT_Diff
+// along the meridian great circle (u_th), along the longitude (u_ph) and both
+// (u_thph).  The filtered field restricted to a meridian great circle or to a
+// latitude circle is a trigonometric polynomial of degree < L <= M/2, on
+// which FFT_Diff is exact, so the derivatives are taken from the expansion
+// itself: u_ph from m times the sine and cosine parts, u_th from dPE, the
+// FFT_Diff of the pbar samples continued around the great circle (built on
+// the host).  The two halves of the grid hold the same points: node (i >= nlat,
+// j) is the point (M - i, j + N/2) with u_th and u_thph negated, and the
+// columns j and j + N/2 of a row differ only in the sign of the odd-m terms,
+// so the block evaluates the (nlat + 1) x N/2 column pairs once.  Needs an
+// equispaced, even longitude grid (the FFT_Diff axis).
+struct SplArgs {
+  int L, nlat, nlon, npt, nvar, set;
+  const double* PG;   // pbar at the Gauss rows [i][m][n]
+  const double* PE;   // pbar at the equiangular rows i pi / nlat, i <= nlat
+  const double* dPE;  // FFT_Diff of pbar along the meridian great circle, same rows
+  const double* wf;   // analysis weight per Gauss row
+  const double* cs;   // cos(m phi_j) [m][j]
+  const double* sn;
+};
+
+__global__ void __launch_bounds__(256) k_sh_spline(SplArgs a, const double* __restrict__ v,
+                                                   const double* __restrict__ fac, double* __restrict__ spl) {
   extern __shared__ double sm[];
-  const int cell = blockIdx.x / nvar, comp = blockIdx.x % nvar;
-  const int M = 2 * nlat, N = nlon, per = M * N;
-  double* u = sm;        // [j][i]
-  double* u2 = u + per;  // [j][i]
-  const double* fc = f + (size_t)(cell * 3 + comp) * nlon * (nlat + 1);
-  for (int t = threadIdx.x; t < per; t += blockDim.x) {
-    const int i = t % M, j = t / M;
-    u[t] = i < nlat ? fc[(size_t)j * (nlat + 1) + i] : fc[(size_t)((j + N / 2) % N) * (nlat + 1) + (M - i)];
+  const int cell = blockIdx.x / a.nvar, comp = blockIdx.x % a.nvar;
+  const int L = a.L, nlat = a.nlat, nlon = a.nlon, nv = nlat * nlon, R = nlat + 1, N2 = nlon / 2;
+  double* A = sm;               // [m][n]
+  double* B = A + L * L;
+  double* Gt = B + L * L;       // [m][r], r <= nlat: G, H, G', H'
+  double* Ht = Gt + L * R;
+  double* Gd = Ht + L * R;
+  double* Hd = Gd + L * R;
+  double* g = Hd + L * R;       // [i + nlat j]
+  double* C = g + nv;           // [m][i]
+  double* S = C + L * nlat;
+  const size_t base = (size_t)cell * nv;
+  for (int r = threadIdx.x; r < nv; r += blockDim.x)
+    g[r] = v[base + r + (size_t)comp * a.npt] * (fac ? fac[base + r] : 1.0);
+  __syncthreads();
+  // ShAnalGau, longitude part: columns j and j + N/2 paired (cos and sin of
+  // m (phi + pi) are (-1)^m those of m phi)
+  for (int t = threadIdx.x; t < L * nlat; t += blockDim.x) {
+    const int m = t / nlat, i = t % nlat;
+    const double sgn = (m & 1) ? -1.0 : 1.0;
+    double c = 0, s = 0;
+    for (int j = 0; j < N2; ++j) {
+      const double x = g[i + nlat * j] + sgn * g[i + nlat * (j + N2)];
+      c += x * a.cs[m * nlon + j];
+      s += x * a.sn[m * nlon + j];
+    }
+    C[t] = c;
+    S[t] = s;
   }
   __syncthreads();
-  double* dst = spl + ((size_t)cell * SPL_NSET + set) * per * SPL_NODE;
-  for (int t = threadIdx.x; t < per; t += blockDim.x) {
-    const int i = t % M, j = t / M;
-    double d1 = 0, d2 = 0;
-    for (int l = 0; l < M; ++l) d1 += Dm[(size_t)i * M + l] * u[j * M + l];
-    for (int l = 0; l < N; ++l) d2 += Dn[(size_t)j * N + l] * u[l * M + i];
-    u2[t] = d2;
-    double* o = dst + (size_t)t * SPL_NODE;
-    o[0 * 3 + comp] = u[t];
-    o[1 * 3 + comp] = d1;
-    o[2 * 3 + comp] = d2;
-    if (nvar == 1)
-      for (int kind = 0; kind < 4; ++kind) o[kind * 3 + 1] = o[kind * 3 + 2] = 0.0;
+  // Legendre part and ShFilter (n < L)
+  for (int t = threadIdx.x; t < L * L; t += blockDim.x) {
+    const int m = t / L, n = t % L;
+    double sa = 0, sb = 0;
+    if (n >= m)
+      for (int i = 0; i < nlat; ++i) {
+        const double p = a.PG[((size_t)i * L + m) * L + n] * a.wf[i];
+        sa += p * C[m * nlat + i];
+        sb -= p * S[m * nlat + i];
+      }
+    A[t] = sa;
+    B[t] = m > 0 ? sb : 0.0;
   }
   __syncthreads();
-  // u12 = FFT_Diff of u1 along the longitude = Dm applied to u2
-  for (int t = threadIdx.x; t < per; t += blockDim.x) {
-    const int i = t % M, j = t / M;
-    double s = 0;
-    for (int l = 0; l < M; ++l) s += Dm[(size_t)i * M + l] * u2[j * M + l];
-    dst[(size_t)t * SPL_NODE + 3 * 3 + comp] = s;
+  // G_m, H_m and their theta derivatives on the equiangular rows (the m = 0
+  // term of the synthesis carries a factor 1/2)
+  for (int t = threadIdx.x; t < L * R; t += blockDim.x) {
+    const int m = t / R, r = t % R;
+    double gs = 0, hs = 0, gd = 0, hd = 0;
+    for (int n = m; n < L; ++n) {
+      const size_t q = ((size_t)r * L + m) * L + n;
+      const double p = a.PE[q], dp = a.dPE[q];
+      gs += p * A[m * L + n]; hs += p * B[m * L + n];
+      gd += dp * A[m * L + n]; hd += dp * B[m * L + n];
+    }
+    const double h = m == 0 ? 0.5 : 1.0;
+    Gt[t] = h * gs; Ht[t] = h * hs; Gd[t] = h * gd; Hd[t] = h * hd;
+  }
+  __syncthreads();
+  const int M = 2 * nlat;
+  double* dst = spl + ((size_t)cell * SPL_NSET + a.set) * (size_t)M * nlon * SPL_NODE;
+  for (int t = threadIdx.x; t < R * N2; t += blockDim.x) {
+    const int r = t % R, j = t / R;
+    double e[4] = {0, 0, 0, 0}, o[4] = {0, 0, 0, 0};  // u, u_th, u_ph, u_thph: even and odd m
+    for (int m = 0; m < L; ++m) {
+      const double c = a.cs[m * nlon + j], s = a.sn[m * nlon + j];
+      const double gm = Gt[m * R + r], hm = Ht[m * R + r], gdm = Gd[m * R + r], hdm = Hd[m * R + r];
+      const double w[4] = {gm * c - hm * s, gdm * c - hdm * s, -m * (gm * s + hm * c), -m * (gdm * s + hdm * c)};
+      double* acc = (m & 1) ? o : e;
+      for (int k = 0; k < 4; ++k) acc[k] += w[k];
+    }
+    double p1[4], p2[4];  // the points (r, j) and (r, j + N/2)
+    for (int k = 0; k < 4; ++k) { p1[k] = e[k] + o[k]; p2[k] = e[k] - o[k]; }
+    auto put = [&](int i, int jj, const double* val, double sg) {
+      double* d = dst + ((size_t)jj * M + i) * SPL_NODE;
+      d[0 * 3 + comp] = val[0];
+      d[1 * 3 + comp] = sg * val[1];
+      d[2 * 3 + comp] = val[2];
+      d[3 * 3 + comp] = sg * val[3];
+      if (a.nvar == 1)
+        for (int kind = 0; kind < 4; ++kind) d[kind * 3 + 1] = d[kind * 3 + 2] = 0.0;
+    };
+    if (r < nlat) {
+      put(r, j, p1, 1.0);
+      put(r, j + N2, p2, 1.0);
+    }
+    if (r >= 1) {
+      put(M - r, j + N2, p1, -1.0);
+      put(M - r, j, p2, -1.0);
+    }
   }
 }
 
@@ -235,11 +315,25 @@ rbc3d_status cell_tabs(rbc3d_ctx* ctx, int L, CellSolveTabs& T) {
   for (int i = 0; i < nlat; ++i) wf[i] = w[i] / RBC3D_PI;
   for (int m = 0; m < L; ++m)
     for (int j = 0; j < nlon; ++j) { cs[(size_t)m * nlon + j] = std::cos(m * phi[j]); sn[(size_t)m * nlon + j] = std::sin(m * phi[j]); }
-  std::vector<double> Dm = diff_matrix(2 * nlat), Dn = diff_matrix(nlon);
+  // dPE: FFT_Diff along the meridian great circle (M = 2 nlat points
+  // theta_l = l pi / nlat, pbar continued past the pole by its own formula,
+  // sin^m theta times a polynomial in cos theta) of pbar, at the rows l <= nlat
+  const int M = 2 * nlat;
+  std::vector<double> Dm = diff_matrix(M), Pext((size_t)M * L * L), dPE((size_t)(nlat + 1) * L * L, 0.0);
+  for (int l = 0; l < M; ++l) pbar_table(L, l * RBC3D_PI / nlat, &Pext[(size_t)l * L * L]);
+  for (int r = 0; r <= nlat; ++r)
+    for (int l = 0; l < M; ++l) {
+      const double d = Dm[(size_t)r * M + l];
+      for (int q = 0; q < L * L; ++q) dPE[(size_t)r * L * L + q] += d * Pext[(size_t)l * L * L + q];
+    }
+  // the spline tables' derivatives assume FFT_Diff's axis: phi_j = phi_0 + 2 pi j / nlon, nlon even
+  T.equi_lon = nlon % 2 == 0;
+  for (int j = 0; j < nlon && T.equi_lon; ++j)
+    T.equi_lon = std::fabs(phi[j] - phi[0] - 2.0 * RBC3D_PI * j / nlon) <= 1e-12;
   CUDA_TRY(T.PG.upload(PG.data(), PG.size(), ctx->st)); CUDA_TRY(T.PE.upload(PE.data(), PE.size(), ctx->st));
   CUDA_TRY(T.wf.upload(wf.data(), wf.size(), ctx->st));
   CUDA_TRY(T.cs.upload(cs.data(), cs.size(), ctx->st)); CUDA_TRY(T.sn.upload(sn.data(), sn.size(), ctx->st));
-  CUDA_TRY(T.Dm.upload(Dm.data(), Dm.size(), ctx->st)); CUDA_TRY(T.Dn.upload(Dn.data(), Dn.size(), ctx->st));
+  CUDA_TRY(T.dPE.upload(dPE.data(), dPE.size(), ctx->st));
   CUDA_TRY(cudaStreamSynchronize(ctx->st));
   T.L = L;
   return RBC3D_OK;
@@ -276,34 +370,31 @@ rbc3d_status sh_synth(rbc3d_ctx* ctx, const CellSolveTabs& T, const double* c, d
   return RBC3D_OK;
 }
 
-// Rbc_BuildSurfaceSource for one field (ModRbc.F90:716-807): ShAnalGau of v
-// (times fac when given), ShFilter to degree < L, ShSynthEqu on the nlat + 1
-// equiangular rows, Spline_Build_On_Sphere into spline set `set`.
+// Rbc_BuildSurfaceSource for one field (ModRbc.F90:716-807) into spline set
+// `set`: one k_sh_spline block per (cell, component).
 rbc3d_status build_spline_set(rbc3d_ctx* ctx, const CellSolveTabs& T, const double* v, const double* fac, int nvar,
-                              int set, DBuf<double>& cg, DBuf<double>& fe) {
-  rbc3d_status s;
-  CUDA_TRY(cg.alloc((size_t)ctx->ncell * 3 * T.L * T.L));
-  CUDA_TRY(fe.alloc((size_t)ctx->ncell * 3 * ctx->nlon * (ctx->nlat + 1)));
-  if ((s = sh_anal(ctx, T, v, fac, cg.p, nvar))) return s;
-  if ((s = sh_synth(ctx, T, cg.p, fe.p, true, nvar))) return s;
-  const int per = 2 * ctx->nlat * ctx->nlon;
-  const size_t sm = sizeof(double) * 2 * (size_t)per;
+                              int set) {
+  if (!T.equi_lon) return ctx_fail(ctx, RBC3D_ERR_ARG, "spline tables need an equispaced longitude grid of even size");
+  SplArgs a;
+  a.L = T.L; a.nlat = ctx->nlat; a.nlon = ctx->nlon; a.npt = (int)ctx->npt; a.nvar = nvar; a.set = set;
+  a.PG = T.PG.p; a.PE = T.PE.p; a.dPE = T.dPE.p; a.wf = T.wf.p; a.cs = T.cs.p; a.sn = T.sn.p;
+  const size_t L = T.L, R = ctx->nlat + 1;
+  const size_t sm = sizeof(double) * (2 * L * L + 4 * L * R + (size_t)ctx->nlat * ctx->nlon + 2 * L * ctx->nlat);
   if (sm > 227 * 1024) return ctx_fail(ctx, RBC3D_ERR_ARG, "spline build: cell grid too large for one block");
-  if (sm > 48 * 1024) CUDA_TRY(cudaFuncSetAttribute(k_spline_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  { k_spline_build<<<nvar * ctx->ncell, 256, sm, ctx->st>>>(ctx->nlat, ctx->nlon, nvar, set, fe.p, T.Dm.p, T.Dn.p,
-                                                             ctx->spl.p); ++ctx->launches; }
+  if (sm > 48 * 1024) CUDA_TRY(cudaFuncSetAttribute(k_sh_spline, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  { k_sh_spline<<<nvar * ctx->ncell, 256, sm, ctx->st>>>(a, v, fac, ctx->spl.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   return RBC3D_OK;
 }
 
 // rbc%g <- g (device, point layout), Rbc_BuildSurfaceSource(gFlag) and
 // SourceList_UpdateDensity(updateG)
-rbc3d_status set_g_device(rbc3d_ctx* ctx, const CellSolveTabs& T, const double* g, DBuf<double>& cg, DBuf<double>& fe) {
+rbc3d_status set_g_device(rbc3d_ctx* ctx, const CellSolveTabs& T, const double* g) {
   const size_t N = ctx->npt;
   rbc3d_status s;
   CUDA_TRY(ctx->g.alloc(3 * N));
   CUDA_TRY(cudaMemcpyAsync(ctx->g.p, g, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, ctx->st));
-  if ((s = build_spline_set(ctx, T, g, ctx->detJ.p, 3, SPL_G, cg, fe))) return s;  // Rbc_BuildSurfaceSource(gFlag)
+  if ((s = build_spline_set(ctx, T, g, ctx->detJ.p, 3, SPL_G))) return s;  // Rbc_BuildSurfaceSource(gFlag)
   ctx->has_g = true;
   if ((s = self_mixed_density(ctx, false, true))) return s;
   return build_source_density(ctx);
@@ -318,12 +409,12 @@ rbc3d_status surface_sources_dev(rbc3d_ctx* ctx, int nlat0, bool geom, bool f, b
   rbc3d_status s;
   if ((s = cell_tabs(ctx, nlat0, T))) return s;
   if (geom) {
-    if ((s = build_spline_set(ctx, T, ctx->x.p, nullptr, 3, SPL_X, ctx->sh_c, ctx->sh_e))) return s;
-    if ((s = build_spline_set(ctx, T, ctx->a3.p, nullptr, 3, SPL_A3, ctx->sh_c, ctx->sh_e))) return s;
-    if ((s = build_spline_set(ctx, T, ctx->detJ.p, nullptr, 1, SPL_DJ, ctx->sh_c, ctx->sh_e))) return s;
+    if ((s = build_spline_set(ctx, T, ctx->x.p, nullptr, 3, SPL_X))) return s;
+    if ((s = build_spline_set(ctx, T, ctx->a3.p, nullptr, 3, SPL_A3))) return s;
+    if ((s = build_spline_set(ctx, T, ctx->detJ.p, nullptr, 1, SPL_DJ))) return s;
   }
-  if (f && (s = build_spline_set(ctx, T, ctx->f.p, ctx->detJ.p, 3, SPL_F, ctx->sh_c, ctx->sh_e))) return s;
-  if (g && (s = build_spline_set(ctx, T, ctx->g.p, ctx->detJ.p, 3, SPL_G, ctx->sh_c, ctx->sh_e))) return s;
+  if (f && (s = build_spline_set(ctx, T, ctx->f.p, ctx->detJ.p, 3, SPL_F))) return s;
+  if (g && (s = build_spline_set(ctx, T, ctx->g.p, ctx->detJ.p, 3, SPL_G))) return s;
   return RBC3D_OK;
 }
 
@@ -348,9 +439,9 @@ extern "C" rbc3d_status rbc3d_solve_rbc_vel(rbc3d_ctx* ctx, const rbc3d_solve_op
   const int n = 3 * nlat0 * nlat0 * ctx->ncell, R = o->restart > 0 ? o->restart : 30;
   const double ip4 = 1.0 / (4.0 * RBC3D_PI);
   TargetSet& t = ctx->tl[RBC3D_TLIST_RBC];
-  DBuf<double> b, x, r, g, cg, fe, tmp;
+  DBuf<double> b, x, r, g, tmp;
   CUDA_TRY(b.alloc(n)); CUDA_TRY(x.alloc(n)); CUDA_TRY(r.alloc(n)); CUDA_TRY(g.alloc(3 * N));
-  CUDA_TRY(cg.alloc(n)); CUDA_TRY(fe.alloc((size_t)ctx->ncell * 3 * (ctx->nlat + 1) * ctx->nlon)); CUDA_TRY(tmp.alloc(8));
+  CUDA_TRY(tmp.alloc(8));
   // Compute_Rhs (:455-515): single layer of the cells and walls, PME, background flow
   const unsigned all = RBC3D_TERM_REAL | RBC3D_TERM_CORR | RBC3D_TERM_LINEAR | RBC3D_TERM_WALLS | RBC3D_TERM_PME;
   if ((s = matvec_dev(ctx, RBC3D_TLIST_RBC, ip4, 0.0, all, RBC3D_FP64))) return s;
@@ -371,7 +462,7 @@ extern "C" rbc3d_status rbc3d_solve_rbc_vel(rbc3d_ctx* ctx, const rbc3d_solve_op
       S.matvecs++;
       rbc3d_status e;
       if ((e = sh_synth(ctx, T, u, g.p, false))) return e;
-      if ((e = set_g_device(ctx, T, g.p, cg, fe))) return e;
+      if ((e = set_g_device(ctx, T, g.p))) return e;
       if ((e = matvec_dev(ctx, RBC3D_TLIST_RBC, 0.0, -ip4, dl_terms, prec))) return e;
       { k_axpby<<<cs_nblk(3 * N, 256), 256, 0, ctx->st>>>((int)(3 * N), 1.0, g.p, 1.0, t.v.p); ++ctx->launches; }
       return sh_anal(ctx, T, t.v.p, nullptr, y);
@@ -395,7 +486,7 @@ extern "C" rbc3d_status rbc3d_solve_rbc_vel(rbc3d_ctx* ctx, const rbc3d_solve_op
   }
   // the surface velocities; rbc%g and its spline are left at the solution
   if ((s = sh_synth(ctx, T, x.p, g.p, false))) return s;
-  if (!all_one && (s = set_g_device(ctx, T, g.p, cg, fe))) return s;
+  if (!all_one && (s = set_g_device(ctx, T, g.p))) return s;
   CUDA_TRY(cudaMemcpyAsync(v, g.p, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, ctx->st));
   if (sol) CUDA_TRY(cudaMemcpyAsync(sol, x.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->st));
   CUDA_TRY(cudaStreamSynchronize(ctx->st));

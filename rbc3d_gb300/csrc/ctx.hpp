@@ -133,11 +133,13 @@ struct WallSpec {
 };
 
 // Spherical-harmonic transform tables of the cell grid at degree < L
-// (cellsolve.cu): Gauss and equiangular pbar rows, weights, cos / sin(m phi),
-// FFT_Diff matrices; kept across calls until the grid or L changes.
+// (cellsolve.cu): Gauss and equiangular pbar rows, the meridian FFT_Diff of
+// the equiangular rows, weights, cos / sin(m phi); kept across calls until
+// the grid or L changes.
 struct ShTabs {
   int L = 0;
-  DBuf<double> PG, PE, wf, cs, sn, Dm, Dn;
+  bool equi_lon = false;  // phi equispaced over an even nlon (FFT_Diff's axis)
+  DBuf<double> PG, PE, dPE, wf, cs, sn;
 };
 
 struct rbc3d_ctx {
@@ -175,6 +177,7 @@ struct rbc3d_ctx {
   DBuf<int> celltype;
   DBuf<double> x, a3, detJ, f, g, sf, sg, area, meshSize;
   DBuf<double> spl;               // ncell * SPL_NSET * m*nlon * SPL_NODE
+  DBuf<double> tan1, tan2;        // set_cells_x: the tangents dx/dtheta, dx/dphi (point layout)
   bool has_f = false, has_g = false;
   double near_rthr = 0;            // 0.5 * min(meshSize): FP32C cross-surface pairs below it go to FP64
 
@@ -242,7 +245,6 @@ struct rbc3d_ctx {
   } mb;
 
   ShTabs shtab;                   // transform tables of the cell solve and the device surface sources
-  DBuf<double> sh_c, sh_e;        // surface sources: coefficients, equiangular staging (grow-only)
   DBuf<double> scratch;           // GMRES basis / temporaries
   DBuf<double> dotpart;           // GMRES: per-slice partial dot products
   DBuf<double> stage;             // staging of uploaded spline tables (grow-only)
@@ -312,6 +314,7 @@ rbc3d_status wall_residual_dev(rbc3d_ctx* ctx, int prec);
 // wallspec.cu
 rbc3d_status wall_spec_predict_dev(rbc3d_ctx* ctx, const double* b_dev, double* x0_dev, double* rem_dev);
 rbc3d_status wall_spec_add_dev(rbc3d_ctx* ctx, const double* b_dev, const double* x_dev);
+rbc3d_status wall_spec_apply_dev(rbc3d_ctx* ctx, const double* v_dev, double* out_dev);
 void wall_spec_release(rbc3d_ctx* ctx);
 
 // selfmix.cu
@@ -338,7 +341,8 @@ void pbar_table(int L, double theta, double* P);
 // geom -> the x, a3 and detJ tables, f / g -> the f detJ / g detJ tables
 rbc3d_status surface_sources_dev(rbc3d_ctx* ctx, int nlat0, bool geom, bool f, bool g);
 // membrane.cu: RBC_ComputeGeometry of the context's cells from ctx->x
-// (device): a3, detJ (point layout) and area into the context's arrays
+// (device): a3, detJ (point layout) and area into the context's arrays,
+// queued on the context stream
 rbc3d_status cells_geometry_dev(rbc3d_ctx* ctx);
 
 // peak.cu

@@ -142,14 +142,25 @@ inline double dev_norm(rbc3d_ctx* ctx, int n, const double* v, double* tmp) {
   return std::sqrt(h);
 }
 
+// No preconditioner (the reference's PCNONE).
+struct NoPrec {
+  bool active() const { return false; }
+  rbc3d_status operator()(const double*, double*) const { return RBC3D_OK; }
+};
+
 // GMRES cycles from x (device, in/out) for A x = b (device).  On entry r must
 // hold b - A x and beta its norm; ttol is the absolute tolerance.  Counts go
-// to S (iterations, converged, rnorm; matvecs through the functor).
-template <class MV>
+// to S (iterations, converged, rnorm; matvecs through the functor).  With an
+// active preconditioner M (pc(in, out): out = M in) the cycles run on A M
+// (right preconditioning: the Arnoldi vectors are z = M v, the update is
+// x += M V y), so the residual they minimise and the convergence test are
+// still those of b - A x.
+template <class MV, class PC = NoPrec>
 rbc3d_status gmres_cycles(rbc3d_ctx* ctx, int n, MV&& matvec, const double* b, double* x, double* r, double beta,
-                          double ttol, int max_it, int R, rbc3d_solve_stats& S) {
+                          double ttol, int max_it, int R, rbc3d_solve_stats& S, PC&& pc = PC()) {
   const size_t ld = (size_t)n;
-  DBuf<double> V, w, H, cs, sn, g, hcol, yv, tmp;
+  DBuf<double> V, w, H, cs, sn, g, hcol, yv, tmp, z, u;
+  if (pc.active()) { CUDA_TRY(z.alloc(n)); CUDA_TRY(u.alloc(n)); }
   CUDA_TRY(V.alloc((size_t)(R + 1) * ld)); CUDA_TRY(w.alloc(n));
   CUDA_TRY(H.alloc((size_t)(R + 1) * R)); CUDA_TRY(cs.alloc(R)); CUDA_TRY(sn.alloc(R)); CUDA_TRY(g.alloc(R + 1));
   CUDA_TRY(hcol.alloc(R + 1)); CUDA_TRY(yv.alloc(R)); CUDA_TRY(tmp.alloc(R + 2));
@@ -170,7 +181,11 @@ rbc3d_status gmres_cycles(rbc3d_ctx* ctx, int n, MV&& matvec, const double* b, d
     CUDA_TRY(cudaMemcpyAsync(g.p, gh.data(), sizeof(double) * (R + 1), cudaMemcpyHostToDevice, ctx->st));
     int k;
     for (k = 0; k < R && its < max_it; ++k) {
-      if ((s = matvec(V.p + k * ld, w.p))) return s;
+      if (pc.active()) {
+        if ((s = pc(V.p + k * ld, z.p)) || (s = matvec(z.p, w.p))) return s;
+      } else if ((s = matvec(V.p + k * ld, w.p))) {
+        return s;
+      }
       dev_dots(ctx, n, k + 1, V.p, ld, w.p, hcol.p);
       { k_orth<<<gm_nblk(n, 256), 256, 0, ctx->st>>>(n, k + 1, V.p, ld, hcol.p, w.p); ++ctx->launches; }
       double hn = dev_norm(ctx, n, w.p, tmp.p);
@@ -183,7 +198,15 @@ rbc3d_status gmres_cycles(rbc3d_ctx* ctx, int n, MV&& matvec, const double* b, d
       if (res <= ttol || hn == 0) { ++k; conv = true; break; }
     }
     { k_backsolve<<<1, 1, 0, ctx->st>>>(k, R + 1, H.p, g.p, yv.p); ++ctx->launches; }
-    { k_xupdate<<<gm_nblk(n, 256), 256, 0, ctx->st>>>(n, k, V.p, ld, yv.p, x); ++ctx->launches; }
+    if (pc.active()) {  // x += M (V y)
+      CUDA_TRY(cudaMemsetAsync(u.p, 0, sizeof(double) * n, ctx->st));
+      { k_xupdate<<<gm_nblk(n, 256), 256, 0, ctx->st>>>(n, k, V.p, ld, yv.p, u.p); ++ctx->launches; }
+      if ((s = pc(u.p, z.p))) return s;
+      { k_axpby<<<gm_nblk(n, 256), 256, 0, ctx->st>>>(n, 1.0, z.p, 1.0, x); ++ctx->launches; }
+    } else {
+      k_xupdate<<<gm_nblk(n, 256), 256, 0, ctx->st>>>(n, k, V.p, ld, yv.p, x);
+      ++ctx->launches;
+    }
     if ((s = residual())) return s;
     beta = dev_norm(ctx, n, r, tmp.p);
     conv = beta <= ttol;  // the true residual decides, not the Givens estimate
@@ -203,10 +226,11 @@ rbc3d_status gmres_cycles(rbc3d_ctx* ctx, int n, MV&& matvec, const double* b, d
 // relative error), so the solve reaches the same ||b - A x|| < ttol as the FP64
 // solve, judged by the FP64 residual.  On entry r and beta hold the FP64
 // residual of x.  S.iterations counts the inner iterations, S.refinements the
-// corrections.
-template <class MV64, class MV32>
+// corrections.  An active preconditioner pc acts in the inner cycles.
+template <class MV64, class MV32, class PC = NoPrec>
 rbc3d_status gmres_ir(rbc3d_ctx* ctx, int n, MV64&& mv64, MV32&& mv32, const double* b, double* x, double* r,
-                      double beta, double ttol, int max_it, int R, double eta, rbc3d_solve_stats& S) {
+                      double beta, double ttol, int max_it, int R, double eta, rbc3d_solve_stats& S,
+                      PC&& pc = PC()) {
   DBuf<double> rhs, d, ri, w;
   CUDA_TRY(rhs.alloc(n)); CUDA_TRY(d.alloc(n)); CUDA_TRY(ri.alloc(n)); CUDA_TRY(w.alloc(n));
   rbc3d_status s;
@@ -219,7 +243,7 @@ rbc3d_status gmres_ir(rbc3d_ctx* ctx, int n, MV64&& mv64, MV32&& mv32, const dou
     CUDA_TRY(cudaMemcpyAsync(ri.p, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->st));
     CUDA_TRY(cudaMemsetAsync(d.p, 0, sizeof(double) * n, ctx->st));
     rbc3d_solve_stats Si{};
-    if ((s = gmres_cycles(ctx, n, mv32, rhs.p, d.p, ri.p, beta, std::max(eta * beta, 0.5 * ttol), max_it - its, R, Si)))
+    if ((s = gmres_cycles(ctx, n, mv32, rhs.p, d.p, ri.p, beta, std::max(eta * beta, 0.5 * ttol), max_it - its, R, Si, pc)))
       return s;
     its += Si.iterations;
     ++refinements;

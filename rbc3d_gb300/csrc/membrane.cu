@@ -172,6 +172,39 @@ __device__ double block_sum(double v, double* red) {
   return s;
 }
 
+// The part of RBC_ComputeGeometry the surface sources need, on the point
+// layout [comp][cell][r]: unit normal a3 = a1 x a2 / |a1 x a2| and detJ =
+// sqrt(det a_ij) / sin(theta) (:425-454, as k_mb_geom) from the tangents
+// a1 = dx/dtheta, a2 = dx/dphi.
+__global__ void k_geom_point(long long n, int nv, int nlat, const double* __restrict__ sinth,
+                             const double* __restrict__ A1, const double* __restrict__ A2, double* __restrict__ a3,
+                             double* __restrict__ detJ) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int r = (int)(t % nv);
+  double a1[3], a2[3];
+  for (int k = 0; k < 3; ++k) { a1[k] = A1[t + k * n]; a2[k] = A2[t + k * n]; }
+  const double a11 = a1[0] * a1[0] + a1[1] * a1[1] + a1[2] * a1[2];
+  const double a12 = a1[0] * a2[0] + a1[1] * a2[1] + a1[2] * a2[2];
+  const double a22 = a2[0] * a2[0] + a2[1] * a2[1] + a2[2] * a2[2];
+  const double detA = a11 * a22 - a12 * a12;
+  double nrm[3] = {a1[1] * a2[2] - a1[2] * a2[1], a1[2] * a2[0] - a1[0] * a2[2], a1[0] * a2[1] - a1[1] * a2[0]};
+  const double nn = sqrt(nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2]);
+  for (int k = 0; k < 3; ++k) a3[t + k * n] = nrm[k] / nn;
+  detJ[t] = sqrt(detA) / sinth[r % nlat];
+}
+
+// area of each cell (:476-480), the reduction of k_mb_sums; one CTA per cell
+__global__ void k_cell_area(int nv, int nlat, const double* __restrict__ w, const double* __restrict__ detJ,
+                            double* __restrict__ area) {
+  __shared__ double red[32];
+  const int cell = blockIdx.x;
+  double s = 0;
+  for (int r = threadIdx.x; r < nv; r += blockDim.x) s += detJ[(size_t)cell * nv + r] * w[r % nlat];
+  const double A = block_sum(s, red);
+  if (threadIdx.x == 0) area[cell] = A;
+}
+
 // area, centroid and volume of each cell (:476-501); one CTA per cell
 __global__ void k_mb_sums(int nv, int nlat, const double* __restrict__ w, const double* __restrict__ X,
                           const double* __restrict__ A3, const double* __restrict__ detJ, double* __restrict__ area,
@@ -465,13 +498,15 @@ rbc3d_status cells_geometry_dev(rbc3d_ctx* ctx) {
   if ((s = mb_tables(ctx))) return s;
   const int nv = ctx->nlat * ctx->nlon;
   const size_t n = (size_t)ctx->ncell * nv;
-  Geom G;
-  if ((s = mb_geometry_dev(ctx, ctx->ncell, ctx->x.p, G))) return s;
-  { k_mb_scatter<<<mb_nblk((long long)n, 256), 256, 0, ctx->st>>>(ctx->ncell, nv, G.A3.p, ctx->a3.p); ++ctx->launches; }
-  CUDA_TRY(cudaMemcpyAsync(ctx->detJ.p, G.detJ.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->st));
-  CUDA_TRY(cudaMemcpyAsync(ctx->area.p, G.area.p, sizeof(double) * ctx->ncell, cudaMemcpyDeviceToDevice, ctx->st));
+  // the point layout [comp][cell][r] is 3 ncell fields of nv points: ShGradGau
+  // of each, no reordering, into tangent buffers kept across calls
+  CUDA_TRY(ctx->tan1.alloc(3 * n)); CUDA_TRY(ctx->tan2.alloc(3 * n));
+  grad(ctx, 3 * ctx->ncell, ctx->x.p, ctx->tan1.p, ctx->tan2.p);
+  { k_geom_point<<<mb_nblk((long long)n, 256), 256, 0, ctx->st>>>((long long)n, nv, ctx->nlat, ctx->mb.sinth.p,
+                                                                   ctx->tan1.p, ctx->tan2.p, ctx->a3.p, ctx->detJ.p);
+    ++ctx->launches; }
+  { k_cell_area<<<ctx->ncell, 256, 0, ctx->st>>>(nv, ctx->nlat, ctx->w.p, ctx->detJ.p, ctx->area.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
-  CUDA_TRY(cudaStreamSynchronize(ctx->st));  // G is freed on return
   return RBC3D_OK;
 }
 

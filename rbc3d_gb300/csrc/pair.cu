@@ -324,9 +324,12 @@ __device__ __forceinline__ float2 ld2(const float* p, int j) { return *reinterpr
 // __fmul2_rn / __fadd2_rn, round-to-nearest like the scalar operations), a
 // source that does not contribute entering with weight 0 and a harmless
 // r^2 = 1 (4.20 -> 3.96 ms against the one-source loop on the 256-cell
-// workload).
+// workload).  Six 128-thread blocks per SM (80 registers a thread, 68 bytes
+// of spills) against the unbounded 96 registers: 3.58 against 3.76 ms alone on the
+// 256-cell workload, the matvec 11.97 against 12.23 ms; Estrin's scheme for
+// the fitted erfc polynomial, or five blocks per SM, measured slower.
 template <bool DL>
-__global__ void __launch_bounds__(TILE) k_pair32(PairArgs a) {
+__global__ void __launch_bounds__(TILE, 6) k_pair32(PairArgs a) {
   __shared__ __align__(16) ChunkX2<DL> s_ch[TILE / 32];
   const int4 unit = a.units[blockIdx.x];
   const int cell = unit.x;

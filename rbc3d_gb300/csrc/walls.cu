@@ -497,6 +497,15 @@ rbc3d_status wall_matmult_dev(rbc3d_ctx* ctx, int prec, const double* u_dev, dou
 }
 
 // NoSlipWall (ModNoSlip.F90:45-150)
+// The learned spectral operator as the solve's right preconditioner (guess
+// mode 5; wallspec.cu).
+struct SpecPrec {
+  rbc3d_ctx* ctx;
+  bool on;
+  bool active() const { return on; }
+  rbc3d_status operator()(const double* in, double* out) const { return wall_spec_apply_dev(ctx, in, out); }
+};
+
 rbc3d_status wall_solve(rbc3d_ctx* ctx, const rbc3d_solve_opts* o, const double* guess, rbc3d_solve_stats* st) {
   WallState& W = ctx->wall;
   if (W.nvert == 0) return RBC3D_OK;
@@ -518,6 +527,8 @@ rbc3d_status wall_solve(rbc3d_ctx* ctx, const rbc3d_solve_opts* o, const double*
                                                        b.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   if (o->guess == 4) {  // the learned spectral operator's prediction (wallspec.cu)
+    if ((s = wall_spec_predict_dev(ctx, b.p, x.p, nullptr))) return s;
+  } else if (o->guess == 5) {  // the same prediction, and the operator as the right preconditioner
     if ((s = wall_spec_predict_dev(ctx, b.p, x.p, nullptr))) return s;
   } else if (o->guess && guess) {
     CUDA_TRY(cudaMemcpyAsync(x.p, guess, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->st));
@@ -589,9 +600,11 @@ rbc3d_status wall_solve(rbc3d_ctx* ctx, const rbc3d_solve_opts* o, const double*
   S.bnorm = dev_norm(ctx, n, b.p, tmp.p);
   // KSPConvergedDefault: ||r|| < max(rtol * ||b||, abstol), ||b|| of the right-hand side
   const double ttol = std::max(o->rtol * S.bnorm, 1e-50);
+  SpecPrec pc{ctx, o->guess == 5};
   if (mixed) {
-    if ((s = gmres_ir(ctx, n, matvec64, matvec, b.p, x.p, r.p, beta, ttol, o->max_it, R, RBC3D_IR_ETA, S))) return s;
-  } else if ((s = gmres_cycles(ctx, n, matvec, b.p, x.p, r.p, beta, ttol, o->max_it, R, S))) {
+    if ((s = gmres_ir(ctx, n, matvec64, matvec, b.p, x.p, r.p, beta, ttol, o->max_it, R, RBC3D_IR_ETA, S, pc)))
+      return s;
+  } else if ((s = gmres_cycles(ctx, n, matvec, b.p, x.p, r.p, beta, ttol, o->max_it, R, S, pc))) {
     return s;
   }
   // every converged solve teaches the spectral model the pair (A x, x) =

@@ -22,6 +22,15 @@
 // side minus its true final residual), not the solve's right-hand side,
 // whose mismatch at the solve tolerance Gram-Schmidt would amplify.
 //
+// As a right preconditioner of the solve (guess mode 5) a mode whose basis
+// spans its block acts as M_m = Z_m Q_m^H, the block's inverse (A M = I up to
+// the PME mesh's translation error); a mode with a partial basis is left
+// alone (M_m = I).  Two completions of a partial basis measured slower than
+// the plain solve on the tube (126 iterations, 10 pairs): the per-mode scalar
+// c_m = sum Re<x_m, b_m> / sum ||b_m||^2 on the whole mode (234), and the
+// same scalar on the basis' orthogonal complement, M_m = Z_m Q_m^H + c_m (I -
+// Q_m Q_m^H) (209; the coupling block c_m Q^H A Q_perp of A M is large).
+//
 // Transforms: cuFFT D2Z / Z2D along the rings of the unique-vertex
 // unknowns (index k*dim + j, k the ring, j = 3 * vertex-in-ring + component);
 // the per-mode work is one CTA per mode in FP64.
@@ -158,6 +167,35 @@ __global__ void __launch_bounds__(SPEC_THREADS) k_spec_predict(int dim, int kmax
   }
 }
 
+// One CTA per mode: the preconditioner, M_m v_m = Z_m Q_m^H v_m for a mode
+// whose basis spans the block, else v_m.
+__global__ void __launch_bounds__(SPEC_THREADS) k_spec_apply(int dim, int kmax, const double2* __restrict__ vh,
+                                                             const double2* __restrict__ Q,
+                                                             const double2* __restrict__ Z,
+                                                             const int* __restrict__ nb,
+                                                             double2* __restrict__ xo) {
+  __shared__ double2 v[SPEC_MAXDIM], h[SPEC_MAXDIM];
+  const int m = blockIdx.x;
+  const int n = nb[m];
+  if (n < dim) {  // partial basis: identity
+    for (int e = threadIdx.x; e < dim; e += blockDim.x) xo[(size_t)m * dim + e] = vh[(size_t)m * dim + e];
+    return;
+  }
+  const double2* Qm = Q + (size_t)m * kmax * dim;
+  const double2* Zm = Z + (size_t)m * kmax * dim;
+  for (int e = threadIdx.x; e < dim; e += blockDim.x) v[e] = vh[(size_t)m * dim + e];
+  __syncthreads();
+  block_dots(Qm, dim, n, v, h);
+  for (int e = threadIdx.x; e < dim; e += blockDim.x) {
+    double2 ax = make_double2(0, 0);
+    for (int j = 0; j < n; ++j) {
+      const double2 hz = cmul(h[j], Zm[(size_t)j * dim + e]);
+      ax.x += hz.x; ax.y += hz.y;
+    }
+    xo[(size_t)m * dim + e] = ax;
+  }
+}
+
 __global__ void k_scale(int n, double a, double* __restrict__ x) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) x[i] *= a;
@@ -269,6 +307,18 @@ rbc3d_status wall_spec_predict_dev(rbc3d_ctx* ctx, const double* b_dev, double* 
   if ((s = inverse(ctx, S.xh.p, x0_dev))) return s;
   if (rem_dev && (s = inverse(ctx, S.rh.p, rem_dev))) return s;
   return RBC3D_OK;
+}
+
+// out = M v (the preconditioner above); v_dev is left unchanged
+rbc3d_status wall_spec_apply_dev(rbc3d_ctx* ctx, const double* v_dev, double* out_dev) {
+  WallSpec& S = ctx->wspec;
+  if (!S.ready) return ctx_fail(ctx, RBC3D_ERR_STATE, "wall spectral model not initialised");
+  rbc3d_status s;
+  if ((s = forward(ctx, v_dev, S.bh.p))) return s;
+  k_spec_apply<<<S.nm, SPEC_THREADS, 0, ctx->st>>>(S.dim, S.kmax, S.bh.p, S.Q.p, S.Z.p, S.nb.p, S.xh.p);
+  ++ctx->launches;
+  CUDA_TRY(cudaGetLastError());
+  return inverse(ctx, S.xh.p, out_dev);
 }
 
 extern "C" rbc3d_status rbc3d_wall_spectral_init(rbc3d_ctx* ctx, int nring, double tau, int record) {

@@ -277,14 +277,19 @@ class WallGuess:
             self.buf.append((X.astype(np.float32), el))
             if len(self.buf) > self.buffer_steps:
                 self.buf.pop(0)
-        # the spectral operator learns the exact pair (A x, x), formed on the device
-        self._ok(self.fn["rbc3d_wall_spectral_add"](self.ctx.h, _ptr(x), None), "rbc3d_wall_spectral_add")
+        self.learn(x)
         self.pairs += 1
         self.hist_b.append(b.copy())
         self.hist_x.append(x.copy())
         if len(self.hist_b) > self.K:
             self.hist_b.pop(0)
             self.hist_x.pop(0)
+
+    def learn(self, x):
+        """The spectral operator learns the exact pair (A x, x), A x formed on
+        the device with the FP64 wall operator."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        self._ok(self.fn["rbc3d_wall_spectral_add"](self.ctx.h, _ptr(x), None), "rbc3d_wall_spectral_add")
 
     def train(self, iters=10, batch=4096, lr=1e-3, rng=None):
         if not self.buf:
@@ -319,16 +324,18 @@ class WallGuess:
     def solve(self, ctx, wall, rtol, max_it, restart, prec, mode="learned"):
         """One NoSlipWall step from the guess `mode`: "learned" (spectral
         operator + network, least-squares combination), "spectral" (the
-        spectral operator alone, predicted on the device: guess mode 4) or
-        "history" (the history projection, scaled).  Returns (stats, accepted,
-        total_ms, b); with accepted False the plain solve (zero increment) was
-        run."""
+        spectral operator alone, predicted on the device: guess mode 4),
+        "preconditioned" (the spectral operator as x0 and as the right
+        preconditioner of GMRES: guess mode 5) or "history" (the history
+        projection, scaled).  Returns (stats, accepted, total_ms, b); with
+        accepted False the plain solve (zero increment) was run."""
         t0 = time.perf_counter()
         f0 = ctx.get_wall_density(wall.nvert)
         b = None
         if self.pairs:
-            if mode == "spectral":
-                st, code = ctx.no_slip_wall(rtol, max_it, restart, prec, check=False, guess_mode=4)
+            if mode in ("spectral", "preconditioned"):
+                st, code = ctx.no_slip_wall(rtol, max_it, restart, prec, check=False,
+                                            guess_mode=4 if mode == "spectral" else 5)
             else:
                 b = self.rhs(ctx, prec)
                 if mode == "learned":

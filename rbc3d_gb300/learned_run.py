@@ -8,9 +8,11 @@ Poiseuille profile and rotates them with its shear (one wall solve per step).
 Every wall no-slip solve runs to ||r|| < rtol ||b|| with GMRES.  The first
 `warm_steps` steps are plain solves (zero increment, i.e. warm start from the
 previous density as NoSlipWall) that fill the history and train the network
-online; afterwards every solve is done three times from the same state --
-plain, history guess only, history + network guess -- and iterations, times
-and final residuals are compared.  The plain solution continues the run and
+online; afterwards every solve is done from the same state plain, from the
+history projection, from the learned spectral operator's prediction, from
+that prediction with the network's correction, and with the spectral
+operator as the right preconditioner, and iterations, times and final
+residuals are compared.  The plain solution continues the run and
 is recorded for the guess, so all arms see the same states.
 
     python -m rbc3d_gb300.learned_run --cells 64 --warm 50 --test 10 --dynamics skalak
@@ -67,7 +69,8 @@ def run(ncell=64, warm_steps=30, test_steps=10, rtol=1e-8, restart=100, max_it=8
     elif dynamics != "kinematic":
         raise ValueError(dynamics)
     ctx.no_slip_wall(rtol, max_it, restart, prec, check=False)  # initial density
-    arms = {"plain": [], "history": [], "spectral": [], "learned": []}
+    arms = {"plain": [], "history": [], "spectral": [], "learned": [], "preconditioned": []}
+    guess_arms = ("history", "spectral", "learned", "preconditioned")
     losses, train_ms = [], []
     state = {"step": 0}
 
@@ -78,7 +81,7 @@ def run(ncell=64, warm_steps=30, test_steps=10, rtol=1e-8, restart=100, max_it=8
         f0 = ctx.get_wall_density(wall.nvert)
         testing = step >= warm_steps
         if testing:
-            for mode in ("history", "spectral", "learned"):
+            for mode in guess_arms:
                 st, ok, ms, _ = guess.solve(ctx, wall, rtol, max_it, restart, prec, mode=mode)
                 arms[mode].append(dict(its=st.iterations, ms=ms, rel=st.rnorm / st.bnorm, accepted=ok,
                                        r0=st.rnorm0 / st.bnorm))
@@ -97,7 +100,7 @@ def run(ncell=64, warm_steps=30, test_steps=10, rtol=1e-8, restart=100, max_it=8
         if log:
             msg = f"step {step}.{stage} plain its {st.iterations} ms {ms:.0f}"
             if testing:
-                for mode in ("history", "spectral", "learned"):
+                for mode in guess_arms:
                     a = arms[mode][-1]
                     msg += f" | {mode} its {a['its']} ms {a['ms']:.0f} r0 {a['r0']:.2e}"
             elif loss is not None:
@@ -128,10 +131,11 @@ def run(ncell=64, warm_steps=30, test_steps=10, rtol=1e-8, restart=100, max_it=8
            "rtol": rtol, "restart": restart, "history": history, "dynamics": dynamics, "dt": dt,
            "solves_per_step": per_step,
            "plain": summary("plain"), "history_only": summary("history"), "spectral_only": summary("spectral"),
-           "learned": summary("learned")}
+           "learned": summary("learned"), "spectral_preconditioned": summary("preconditioned")}
     res["speedup_learned"] = res["plain"]["ms"] / res["learned"]["ms"]
     res["speedup_history_only"] = res["plain"]["ms"] / res["history_only"]["ms"]
     res["speedup_spectral_only"] = res["plain"]["ms"] / res["spectral_only"]["ms"]
+    res["speedup_spectral_preconditioned"] = res["plain"]["ms"] / res["spectral_preconditioned"]["ms"]
     res["learned_over_history_its"] = res["learned"]["its"] / res["history_only"]["its"]
     nb, npairs = guess.basis_sizes()
     res["spectral"] = {"modes": int(nb.size), "pairs": int(npairs), "basis_min": int(nb.min()),
