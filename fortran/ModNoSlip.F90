@@ -8,6 +8,12 @@
 ! at the wall vertices.  The cells' state is pushed first.
 ! Arithmetic: gpu_solve_prec (RBC3D_FP64, or an FP32 mode for the
 ! mixed-precision solve judged on the FP64 residual).
+! NoSlipWall_Rings > 0 (the wall a uniform stack of that many rings along
+! z, as the tube meshes) switches on the learned spectral operator: every
+! converged solve teaches it its exact pair (A x, x), and each solve starts
+! from its prediction with the operator as GMRES's right preconditioner
+! (guess mode 5); the stopping test stays ||b - A x|| < rtol ||b||.  0 (the
+! default) is the reference's solve from a zero increment.
 !-----------------------------------------------------------------------
 module ModNoSlip
 
@@ -25,6 +31,8 @@ module ModNoSlip
 
   integer, save, public :: NoSlipWall_MaxIt = 60      ! KSPSetTolerances max_it of NoSlipWall
   integer, save, public :: NoSlipWall_Restart = 30    ! KSPGMRESSetRestart (PETSc default)
+  integer, save, public :: NoSlipWall_Rings = 0       ! > 0: learned spectral preconditioner
+  logical, save :: spectral_ready = .false.
 
   public :: NoSlipWall, &
             Compute_Wall_Residual_Vel
@@ -45,6 +53,14 @@ contains
     opt%restart = NoSlipWall_Restart
     opt%prec = gpu_solve_prec
     opt%guess = 0
+    if (NoSlipWall_Rings > 0) then
+      if (.not. spectral_ready) then
+        call rbc3d_check(rbc3d_wall_spectral_init(gpu_ctx, int(NoSlipWall_Rings, c_int), 1.0e-7_c_double, 1_c_int), &
+                         'rbc3d_wall_spectral_init')
+        spectral_ready = .true.
+      end if
+      opt%guess = 5
+    end if
     ierr = rbc3d_no_slip_wall(gpu_ctx, opt, c_null_ptr, st)
     if (ierr /= RBC3D_ERR_NOCONV) call rbc3d_check(ierr, 'rbc3d_no_slip_wall')  ! KSP returns at max_it too
     allocate (fw(3*walls(1)%nvert))
