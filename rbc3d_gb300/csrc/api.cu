@@ -70,6 +70,23 @@ StageScope::~StageScope() {
   if (slot >= 0) cudaEventRecord(c->evpool[2 * slot + 1], c->st);
 }
 
+// The current stream waits for spline tables (and the target positions
+// derived from them) that set_cells_x / set_cell_density_x left in flight on
+// the side stream; on the side stream itself the wait is already implied.
+void spl_wait(rbc3d_ctx* ctx) {
+  if (ctx->spl_pending && ctx->ev_spl) cudaStreamWaitEvent(ctx->st, ctx->ev_spl, 0);
+}
+
+// near_rthr, computed on the device by set_cells_x, is read on its first use.
+double near_rthr_now(rbc3d_ctx* ctx) {
+  if (ctx->rthr_pending) {
+    cudaEventSynchronize(ctx->ev_rthr);
+    ctx->near_rthr = *ctx->h_rthr;
+    ctx->rthr_pending = false;
+  }
+  return ctx->near_rthr;
+}
+
 namespace {
 
 inline int nblk(long long n, int b) { return (int)((n + b - 1) / b); }
@@ -171,6 +188,7 @@ rbc3d_status finish_add(rbc3d_ctx* ctx, TargetSet& t, double* v) {
 // Real space + corrections + linear term of AddIntOnRbcs on device (no download).
 rbc3d_status self_stage(rbc3d_ctx* ctx, int which, double c1, double c2, int prec) {
   StageScope sc(ctx, 1);
+  spl_wait(ctx);  // the patch reads the spline tables and the records built from them
   if (prec == RBC3D_FP32M) {
     if (!ctx->phi_uniform) return ctx_fail(ctx, RBC3D_ERR_ARG, "FP32M needs phi(j) = j*2*pi/nlon");
     return run_self_mixed(ctx, which, c1, c2);
@@ -391,7 +409,11 @@ rbc3d_status rbc3d_create(const rbc3d_params* prm, rbc3d_ctx** out) {
     if (cudaStreamCreateWithPriority(&ctx->st, cudaStreamNonBlocking, highest) != cudaSuccess ||
         cudaStreamCreateWithPriority(&ctx->st2, cudaStreamNonBlocking, lowest) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_spl, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_up, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_rthr, cudaEventDisableTiming) != cudaSuccess ||
+        cudaMallocHost((void**)&ctx->h_rthr, sizeof(double)) != cudaSuccess)
       return bail(RBC3D_ERR_CUDA);
   }
   // Ewald tables, ModEwaldFunc.F90:96-104, 151-162
@@ -452,6 +474,10 @@ rbc3d_status rbc3d_destroy(rbc3d_ctx* ctx) {
   for (cudaEvent_t e : ctx->evpool) cudaEventDestroy(e);
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
   if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+  if (ctx->ev_spl) cudaEventDestroy(ctx->ev_spl);
+  if (ctx->ev_up) cudaEventDestroy(ctx->ev_up);
+  if (ctx->ev_rthr) cudaEventDestroy(ctx->ev_rthr);
+  if (ctx->h_rthr) cudaFreeHost(ctx->h_rthr);
   if (ctx->st2) cudaStreamDestroy(ctx->st2);
   if (ctx->t0) { cudaEventDestroy(ctx->t0); cudaEventDestroy(ctx->t1); }
   cudaStream_t st = ctx->st;
@@ -579,7 +605,7 @@ rbc3d_status rbc3d_set_cell_grid(rbc3d_ctx* ctx, const double* th, const double*
   return RBC3D_OK;
 }
 
-rbc3d_status cells_tail(rbc3d_ctx* ctx);
+rbc3d_status cells_tail(rbc3d_ctx* ctx, bool side_tables = false);
 
 rbc3d_status rbc3d_set_cells(rbc3d_ctx* ctx, int ncell, const int* celltype, const double* x, const double* a3,
                              const double* detJ, const double* area, const double* meshSize, const double* spl_x,
@@ -598,10 +624,12 @@ rbc3d_status rbc3d_set_cells(rbc3d_ctx* ctx, int ncell, const int* celltype, con
   if (ncell == 0) return RBC3D_OK;
   size_t N = ctx->npt;
   ctx->h_celltype.assign(celltype, celltype + ncell);
+  spl_wait(ctx);
   {
     double mn = meshSize[0];
     for (int c = 1; c < ncell; ++c) mn = std::min(mn, meshSize[c]);
     ctx->near_rthr = 0.5 * mn;
+    ctx->rthr_pending = false;
   }
   CUDA_TRY(ctx->celltype.upload(celltype, ncell, ctx->st));
   CUDA_TRY(ctx->x.upload(x, 3 * N, ctx->st)); CUDA_TRY(ctx->a3.upload(a3, 3 * N, ctx->st));
@@ -630,7 +658,10 @@ rbc3d_status rbc3d_set_cells(rbc3d_ctx* ctx, int ncell, const int* celltype, con
 // The position-dependent set-up after the cells' arrays are on the device
 // (the spline tables may still be in flight on the side stream, joined by
 // ev_join): source list, tlist_rbc, PME spread plan, FP32M records.
-rbc3d_status cells_tail(rbc3d_ctx* ctx) {
+// side_tables: set_cells_x, whose side stream builds the tables and the
+// target positions derived from them itself (readers wait on ev_spl); the
+// main stream then neither joins it nor waits for the device at the end.
+rbc3d_status cells_tail(rbc3d_ctx* ctx, bool side_tables) {
   rbc3d_status s;
   const int nv = ctx->nlat * ctx->nlon;
   const size_t N = ctx->npt;
@@ -643,8 +674,10 @@ rbc3d_status cells_tail(rbc3d_ctx* ctx) {
   t.sorted = false;
   if ((s = sort_targets(ctx, RBC3D_TLIST_RBC))) return s;
   if ((s = pme_prepare_cells(ctx))) return s;
-  CUDA_TRY(cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0));
-  if ((s = self_mixed_geom(ctx))) return s;
+  if (!side_tables) {
+    CUDA_TRY(cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0));
+    if ((s = self_mixed_geom(ctx))) return s;
+  }
   DBuf<double>& Ac = ctx->acoef_dev;
   CUDA_TRY(Ac.upload(ctx->Acoef, RBC3D_MAX_CELLTYPES, ctx->st));
   CUDA_TRY(t.x.alloc(3 * N)); CUDA_TRY(t.Acoef.alloc(N)); CUDA_TRY(t.meta.alloc(N));
@@ -654,7 +687,7 @@ rbc3d_status cells_tail(rbc3d_ctx* ctx) {
   CUDA_TRY(cudaGetLastError());
   int want = 12 * std::max(ctx->npt, 1024);
   if (ctx->items_cap < want) { ctx->items_cap = want; CUDA_TRY(ctx->items.alloc(want)); }
-  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  if (!side_tables) CUDA_TRY(cudaStreamSynchronize(ctx->st));
   return RBC3D_OK;
 }
 
@@ -665,6 +698,7 @@ rbc3d_status rbc3d_set_cell_density(rbc3d_ctx* ctx, const double* f, const doubl
   if ((f && !spl_F) || (g && !spl_G)) return ctx_fail(ctx, RBC3D_ERR_ARG, "density without spline table");
   size_t N = ctx->npt;
   rbc3d_status s;
+  spl_wait(ctx);  // tables still being built on the side stream are finished first
   if (f) {
     CUDA_TRY(ctx->f.upload(f, 3 * N, ctx->st));
     if ((s = upload_splines(ctx, spl_F, 3, SPL_F))) return s;
@@ -684,6 +718,20 @@ rbc3d_status rbc3d_set_cell_density(rbc3d_ctx* ctx, const double* f, const doubl
 __global__ void k_mesh_size(int ncell, int nlat, const double* __restrict__ area, double* __restrict__ msz) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c < ncell) msz[c] = sqrt(area[c] / ((double)nlat * nlat));  // ModRbc.F90:504
+}
+
+// out = 0.5 * min(v[0..n)) (one block)
+__global__ void __launch_bounds__(256) k_half_min(int n, const double* __restrict__ v, double* __restrict__ out) {
+  __shared__ double red[256];
+  double m = HUGE_VAL;
+  for (int i = threadIdx.x; i < n; i += 256) m = fmin(m, v[i]);
+  red[threadIdx.x] = m;
+  __syncthreads();
+  for (int h = 128; h > 0; h >>= 1) {
+    if (threadIdx.x < h) red[threadIdx.x] = fmin(red[threadIdx.x], red[threadIdx.x + h]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = 0.5 * red[0];
 }
 
 // Cells from their positions alone: RBC_ComputeGeometry (a3, detJ, area,
@@ -706,8 +754,11 @@ rbc3d_status rbc3d_set_cells_x(rbc3d_ctx* ctx, int ncell, const int* celltype, i
   if (ncell == 0) return RBC3D_OK;
   const size_t N = ctx->npt;
   ctx->h_celltype.assign(celltype, celltype + ncell);
+  spl_wait(ctx);  // side-stream readers of the previous cells are done before they are overwritten
   CUDA_TRY(ctx->celltype.upload(celltype, ncell, ctx->st));
   CUDA_TRY(ctx->x.upload(x, 3 * N, ctx->st));
+  // the caller's x may be reused once it has been copied
+  CUDA_TRY(cudaEventRecord(ctx->ev_up, ctx->st));
   CUDA_TRY(ctx->a3.alloc(3 * N)); CUDA_TRY(ctx->detJ.alloc(N));
   CUDA_TRY(ctx->area.alloc(ncell)); CUDA_TRY(ctx->meshSize.alloc(ncell));
   CUDA_TRY(ctx->f.alloc(3 * N)); CUDA_TRY(ctx->g.alloc(3 * N)); CUDA_TRY(ctx->sf.alloc(3 * N)); CUDA_TRY(ctx->sg.alloc(3 * N));
@@ -717,20 +768,27 @@ rbc3d_status rbc3d_set_cells_x(rbc3d_ctx* ctx, int ncell, const int* celltype, i
   rbc3d_status s;
   if ((s = cells_geometry_dev(ctx))) return s;
   { k_mesh_size<<<nblk(ncell, 128), 128, 0, ctx->st>>>(ncell, ctx->nlat, ctx->area.p, ctx->meshSize.p); ++ctx->launches; }
-  std::vector<double> msz(ncell);
-  CUDA_TRY(cudaMemcpyAsync(msz.data(), ctx->meshSize.p, sizeof(double) * ncell, cudaMemcpyDeviceToHost, ctx->st));
-  CUDA_TRY(cudaStreamSynchronize(ctx->st));
-  ctx->near_rthr = 0.5 * *std::min_element(msz.begin(), msz.end());
-  // the spline tables are built on the side stream while the main stream
-  // builds the source list from the positions
+  // near_rthr = 0.5 min(meshSize) comes back to the host in the background
+  CUDA_TRY(ctx->rthr_dev.alloc(1));
+  { k_half_min<<<1, 256, 0, ctx->st>>>(ncell, ctx->meshSize.p, ctx->rthr_dev.p); ++ctx->launches; }
+  CUDA_TRY(cudaMemcpyAsync(ctx->h_rthr, ctx->rthr_dev.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+  CUDA_TRY(cudaEventRecord(ctx->ev_rthr, ctx->st));
+  ctx->rthr_pending = true;
+  // the spline tables and the target positions taken from them are built on
+  // the side stream while the main stream builds the source list, the target
+  // work units and the PME plan from the positions; readers wait on ev_spl
   CUDA_TRY(cudaEventRecord(ctx->ev_fork, ctx->st));
   CUDA_TRY(cudaStreamWaitEvent(ctx->st2, ctx->ev_fork, 0));
   std::swap(ctx->st, ctx->st2);
   s = surface_sources_dev(ctx, nlat0, true, false, false);
+  if (!s) s = self_mixed_geom(ctx);
   std::swap(ctx->st, ctx->st2);
+  CUDA_TRY(cudaEventRecord(ctx->ev_spl, ctx->st2));
   CUDA_TRY(cudaEventRecord(ctx->ev_join, ctx->st2));
+  ctx->spl_pending = true;
   if (s) return s;
-  return cells_tail(ctx);
+  CUDA_TRY(cudaEventSynchronize(ctx->ev_up));
+  return cells_tail(ctx, true);
 }
 
 // Densities from the raw surface values alone: Rbc_BuildSurfaceSource(fFlag /
@@ -741,14 +799,24 @@ rbc3d_status rbc3d_set_cell_density_x(rbc3d_ctx* ctx, int nlat0, const double* f
   if (ctx->npt == 0) return RBC3D_OK;
   const size_t N = ctx->npt;
   rbc3d_status s;
+  spl_wait(ctx);  // side-stream readers of the previous densities are done
   if (f) CUDA_TRY(ctx->f.upload(f, 3 * N, ctx->st));
   if (g) CUDA_TRY(ctx->g.upload(g, 3 * N, ctx->st));
-  if ((s = surface_sources_dev(ctx, nlat0, false, f != nullptr, g != nullptr))) return s;
+  CUDA_TRY(cudaEventRecord(ctx->ev_up, ctx->st));
+  // the f detJ / g detJ tables on the side stream (readers wait on ev_spl),
+  // the source densities on the main stream
+  CUDA_TRY(cudaStreamWaitEvent(ctx->st2, ctx->ev_up, 0));
+  std::swap(ctx->st, ctx->st2);
+  s = surface_sources_dev(ctx, nlat0, false, f != nullptr, g != nullptr);
+  std::swap(ctx->st, ctx->st2);
+  CUDA_TRY(cudaEventRecord(ctx->ev_spl, ctx->st2));
+  ctx->spl_pending = true;
+  if (s) return s;
   if (f) ctx->has_f = true;
   if (g) ctx->has_g = true;
   if ((s = self_mixed_density(ctx, f != nullptr, g != nullptr))) return s;
   if ((s = build_source_density(ctx))) return s;
-  CUDA_TRY(cudaStreamSynchronize(ctx->st));  // the caller's host buffers are free again
+  CUDA_TRY(cudaEventSynchronize(ctx->ev_up));  // the caller's host buffers are free again
   return RBC3D_OK;
 }
 

@@ -375,6 +375,7 @@ rbc3d_status sh_synth(rbc3d_ctx* ctx, const CellSolveTabs& T, const double* c, d
 rbc3d_status build_spline_set(rbc3d_ctx* ctx, const CellSolveTabs& T, const double* v, const double* fac, int nvar,
                               int set) {
   if (!T.equi_lon) return ctx_fail(ctx, RBC3D_ERR_ARG, "spline tables need an equispaced longitude grid of even size");
+  spl_wait(ctx);  // on the main stream: no other build of the tables still in flight
   SplArgs a;
   a.L = T.L; a.nlat = ctx->nlat; a.nlon = ctx->nlon; a.npt = (int)ctx->npt; a.nvar = nvar; a.set = set;
   a.PG = T.PG.p; a.PE = T.PE.p; a.dPE = T.dPE.p; a.wf = T.wf.p; a.cs = T.cs.p; a.sn = T.sn.p;

@@ -908,6 +908,7 @@ rbc3d_status run_self_corr(rbc3d_ctx* ctx, int tlist, double c1, double c2) {
 rbc3d_status run_near_corr(rbc3d_ctx* ctx, int tlist, double c1, double c2, int prec) {
   TargetSet& t = ctx->tl[tlist];
   if (t.n == 0 || ctx->ncell == 0) return RBC3D_OK;
+  spl_wait(ctx);  // the near-singular quadrature interpolates the spline tables
   const double* Bc = ctx->dBcoef.p;
   CorrArgs a;
   fill_args(ctx, tlist, c1, (c2 != 0 && ctx->has_g) ? c2 : 0.0, a, Bc);
@@ -915,7 +916,7 @@ rbc3d_status run_near_corr(rbc3d_ctx* ctx, int tlist, double c1, double c2, int 
   a.screen = (prec != RBC3D_FP64) ? 1 : 0;
   // FP32 modes: pairs closer than rthr were left out of the FP32 pair sum and
   // are added back by the FP64 pass (-1: the FP64 plain form left nothing out)
-  a.rthr = (prec != RBC3D_FP64) ? ctx->near_rthr : -1.0;
+  a.rthr = (prec != RBC3D_FP64) ? near_rthr_now(ctx) : -1.0;
   a.verify = ctx->verify_screen ? 1 : 0;
   a.list = nullptr;
   a.nlist = nullptr;
@@ -962,6 +963,7 @@ extern "C" rbc3d_status rbc3d_inter_cell_repulsion(rbc3d_ctx* ctx, double epsDis
   a.eps = epsDist;
   a.nvert = W.nvert; a.nele = W.nele; a.wx = W.x.p; a.e2v = W.e2v.p;
   a.wcs = W.cstart.p; a.wce = W.cend.p; a.worder = W.order.p;
+  spl_wait(ctx);  // Spline_FindProjection reads the x tables
   DBuf<double> dx, xo, visc;
   DBuf<unsigned long long> cnt;
   CUDA_TRY(dx.alloc(3 * (size_t)n)); CUDA_TRY(xo.alloc(3 * (size_t)n)); CUDA_TRY(cnt.alloc(2));

@@ -150,6 +150,10 @@ struct rbc3d_ctx {
   cudaStream_t st = nullptr;   // main stream (highest priority)
   cudaStream_t st2 = nullptr;  // matvec side stream: self patch and PME next to the pair sums
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // set_cells_x / set_cell_density_x build the spline tables on the side
+  // stream and return; readers on the main stream wait on ev_spl (spl_wait)
+  cudaEvent_t ev_spl = nullptr, ev_up = nullptr;
+  bool spl_pending = false;
   int device = 0;
 
   // Ewald / mask tables
@@ -180,6 +184,10 @@ struct rbc3d_ctx {
   DBuf<double> tan1, tan2;        // set_cells_x: the tangents dx/dtheta, dx/dphi (point layout)
   bool has_f = false, has_g = false;
   double near_rthr = 0;            // 0.5 * min(meshSize): FP32C cross-surface pairs below it go to FP64
+  bool rthr_pending = false;       // set_cells_x: near_rthr still on its way from the device
+  double* h_rthr = nullptr;        // its pinned landing slot
+  cudaEvent_t ev_rthr = nullptr;   // recorded after the copy into h_rthr
+  DBuf<double> rthr_dev;
 
   // sorted sources (cell surface points)
   DBuf<int> s_order, s_cstart, s_cend;
@@ -344,6 +352,11 @@ rbc3d_status surface_sources_dev(rbc3d_ctx* ctx, int nlat0, bool geom, bool f, b
 // (device): a3, detJ (point layout) and area into the context's arrays,
 // queued on the context stream
 rbc3d_status cells_geometry_dev(rbc3d_ctx* ctx);
+// api.cu: near_rthr once its device value has landed (set_cells_x computes it
+// on the device); the current stream waits for spline tables still being
+// built on the side stream
+double near_rthr_now(rbc3d_ctx* ctx);
+void spl_wait(rbc3d_ctx* ctx);
 
 // peak.cu
 rbc3d_status fma_peak(int prec, double* tflops);

@@ -951,7 +951,8 @@ rbc3d_status run_pair_sum(rbc3d_ctx* ctx, int tlist, double c1, double c2, int p
   a.c1 = c1; a.c2 = c2; a.c1f = (float)c1; a.c2f = (float)c2;
   a.rc2 = ctx->prm.rc * ctx->prm.rc; a.rc2_f = (float)a.rc2;
   a.rc2_loose = (float)((ctx->prm.rc + 1e-3) * (ctx->prm.rc + 1e-3)); a.reps2_f = (float)(ctx->T.r_eps * ctx->T.r_eps);
-  a.rthr2_f = (float)(ctx->near_rthr * ctx->near_rthr);
+  const double rthr = near_rthr_now(ctx);
+  a.rthr2_f = (float)(rthr * rthr);
   a.sqpa_f = (float)sqrt(RBC3D_PI / ctx->prm.alpha);
   a.two_isqa_f = (float)(2.0 / sqrt(ctx->prm.alpha));
   a.m8_ispi_f = (float)(-8.0 / sqrt(RBC3D_PI));
