@@ -413,6 +413,7 @@ rbc3d_status rbc3d_create(const rbc3d_params* prm, rbc3d_ctx** out) {
         cudaEventCreateWithFlags(&ctx->ev_spl, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_up, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_rthr, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_geom, cudaEventDisableTiming) != cudaSuccess ||
         cudaMallocHost((void**)&ctx->h_rthr, sizeof(double)) != cudaSuccess)
       return bail(RBC3D_ERR_CUDA);
   }
@@ -477,6 +478,7 @@ rbc3d_status rbc3d_destroy(rbc3d_ctx* ctx) {
   if (ctx->ev_spl) cudaEventDestroy(ctx->ev_spl);
   if (ctx->ev_up) cudaEventDestroy(ctx->ev_up);
   if (ctx->ev_rthr) cudaEventDestroy(ctx->ev_rthr);
+  if (ctx->ev_geom) cudaEventDestroy(ctx->ev_geom);
   if (ctx->h_rthr) cudaFreeHost(ctx->h_rthr);
   if (ctx->st2) cudaStreamDestroy(ctx->st2);
   if (ctx->t0) { cudaEventDestroy(ctx->t0); cudaEventDestroy(ctx->t1); }
@@ -665,7 +667,9 @@ rbc3d_status cells_tail(rbc3d_ctx* ctx, bool side_tables) {
   rbc3d_status s;
   const int nv = ctx->nlat * ctx->nlon;
   const size_t N = ctx->npt;
-  if ((s = build_source_list(ctx))) return s;
+  // set_cells_x: the positions' part now, the normals once the side stream's
+  // geometry is done
+  if ((s = build_source_list(ctx, !side_tables))) return s;
   // tlist_rbc (TargetList_Update, ModTargetList.F90:95-131): its work units
   // and the PME spread plan depend on the positions only, and are built while
   // the spline tables are still being written on the side stream
@@ -674,7 +678,10 @@ rbc3d_status cells_tail(rbc3d_ctx* ctx, bool side_tables) {
   t.sorted = false;
   if ((s = sort_targets(ctx, RBC3D_TLIST_RBC))) return s;
   if ((s = pme_prepare_cells(ctx))) return s;
-  if (!side_tables) {
+  if (side_tables) {
+    CUDA_TRY(cudaStreamWaitEvent(ctx->st, ctx->ev_geom, 0));
+    if ((s = source_normals(ctx))) return s;
+  } else {
     CUDA_TRY(cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0));
     if ((s = self_mixed_geom(ctx))) return s;
   }
@@ -766,21 +773,26 @@ rbc3d_status rbc3d_set_cells_x(rbc3d_ctx* ctx, int ncell, const int* celltype, i
   CUDA_TRY(cudaMemsetAsync(ctx->g.p, 0, sizeof(double) * 3 * N, ctx->st));
   CUDA_TRY(ctx->spl.alloc((size_t)ncell * SPL_NSET * ctx->m * ctx->nlon * SPL_NODE));
   rbc3d_status s;
-  if ((s = cells_geometry_dev(ctx))) return s;
-  { k_mesh_size<<<nblk(ncell, 128), 128, 0, ctx->st>>>(ncell, ctx->nlat, ctx->area.p, ctx->meshSize.p); ++ctx->launches; }
-  // near_rthr = 0.5 min(meshSize) comes back to the host in the background
   CUDA_TRY(ctx->rthr_dev.alloc(1));
-  { k_half_min<<<1, 256, 0, ctx->st>>>(ncell, ctx->meshSize.p, ctx->rthr_dev.p); ++ctx->launches; }
-  CUDA_TRY(cudaMemcpyAsync(ctx->h_rthr, ctx->rthr_dev.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
-  CUDA_TRY(cudaEventRecord(ctx->ev_rthr, ctx->st));
-  ctx->rthr_pending = true;
-  // the spline tables and the target positions taken from them are built on
-  // the side stream while the main stream builds the source list, the target
-  // work units and the PME plan from the positions; readers wait on ev_spl
+  // The side stream derives the geometry (RBC_ComputeGeometry), then the
+  // spline tables and the target positions taken from them, while the main
+  // stream builds the source list, the target work units and the PME plan
+  // from the positions; it takes the sources' normals once the geometry is
+  // done (ev_geom), and the tables' readers wait on ev_spl.  near_rthr =
+  // 0.5 min(meshSize) comes back to the host in the background.
   CUDA_TRY(cudaEventRecord(ctx->ev_fork, ctx->st));
   CUDA_TRY(cudaStreamWaitEvent(ctx->st2, ctx->ev_fork, 0));
   std::swap(ctx->st, ctx->st2);
-  s = surface_sources_dev(ctx, nlat0, true, false, false);
+  s = cells_geometry_dev(ctx);
+  if (!s) {
+    { k_mesh_size<<<nblk(ncell, 128), 128, 0, ctx->st>>>(ncell, ctx->nlat, ctx->area.p, ctx->meshSize.p); ++ctx->launches; }
+    { k_half_min<<<1, 256, 0, ctx->st>>>(ncell, ctx->meshSize.p, ctx->rthr_dev.p); ++ctx->launches; }
+    if (cudaMemcpyAsync(ctx->h_rthr, ctx->rthr_dev.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->st) != cudaSuccess ||
+        cudaEventRecord(ctx->ev_rthr, ctx->st) != cudaSuccess || cudaEventRecord(ctx->ev_geom, ctx->st) != cudaSuccess)
+      s = RBC3D_ERR_CUDA;
+    ctx->rthr_pending = true;
+  }
+  if (!s) s = surface_sources_dev(ctx, nlat0, true, false, false);
   if (!s) s = self_mixed_geom(ctx);
   std::swap(ctx->st, ctx->st2);
   CUDA_TRY(cudaEventRecord(ctx->ev_spl, ctx->st2));

@@ -152,7 +152,7 @@ struct rbc3d_ctx {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   // set_cells_x / set_cell_density_x build the spline tables on the side
   // stream and return; readers on the main stream wait on ev_spl (spl_wait)
-  cudaEvent_t ev_spl = nullptr, ev_up = nullptr;
+  cudaEvent_t ev_spl = nullptr, ev_up = nullptr, ev_geom = nullptr;
   bool spl_pending = false;
   int device = 0;
 
@@ -288,7 +288,8 @@ rbc3d_status ctx_fail(rbc3d_ctx* ctx, int code, const std::string& msg);
 rbc3d_status ctx_fail_cuda(rbc3d_ctx* ctx, cudaError_t e, const char* what);
 
 // pair.cu
-rbc3d_status build_source_list(rbc3d_ctx* ctx);
+rbc3d_status build_source_list(rbc3d_ctx* ctx, bool with_normals = true);
+rbc3d_status source_normals(rbc3d_ctx* ctx);
 rbc3d_status sort_points_by_cell(rbc3d_ctx* ctx, int n, const double* x_dev, DBuf<int>& order, DBuf<int>& cs,
                                 DBuf<int>& ce);
 rbc3d_status matvec_dev(rbc3d_ctx* ctx, int which, double c1, double c2, unsigned terms, int prec);

@@ -51,27 +51,37 @@ __global__ void k_cell_ranges(int n, const int* __restrict__ key, int* __restric
 
 // Gather cell-point geometry into cell-list order.
 __global__ void k_gather_src(int n, int nlat, int nv, const int* __restrict__ order, const double* __restrict__ x,
-                             const double* __restrict__ a3, double* __restrict__ sx, double* __restrict__ sa3,
-                             int4* __restrict__ meta) {
+                             double* __restrict__ sx, int4* __restrict__ meta) {
   int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
   int p = order[q];
-  for (int k = 0; k < 3; ++k) {
-    sx[q + (size_t)k * n] = x[p + (size_t)k * n];
-    sa3[q + (size_t)k * n] = a3[p + (size_t)k * n];
-  }
+  for (int k = 0; k < 3; ++k) sx[q + (size_t)k * n] = x[p + (size_t)k * n];
   int cell = p / nv, r = p - cell * nv;
   meta[q] = make_int4(cell + 1, r % nlat, r / nlat, p);
 }
 
+// The sources' normals, sorted (FP64) and as FP32 records.
+__global__ void k_gather_a3(int n, const int* __restrict__ order, const double* __restrict__ a3,
+                            double* __restrict__ sa3, float4* __restrict__ a4) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  int p = order[q];
+  double v[3];
+  for (int k = 0; k < 3; ++k) {
+    v[k] = a3[p + (size_t)k * n];
+    sa3[q + (size_t)k * n] = v[k];
+  }
+  a4[q] = make_float4((float)v[0], (float)v[1], (float)v[2], 0.f);
+}
+
 __device__ __forceinline__ double min_image(double d, double L, double iL) { return d - round(d * iL) * L; }
 
-// FP32 pair-sum records of the sorted sources (see PairArgs).
-__global__ void k_src_records(int n, const double* __restrict__ sx, const double* __restrict__ sa3,
-                              const int4* __restrict__ meta, const float4* __restrict__ usph, int nlat, int Nc0,
-                              int Nc1, int Nc2, double h0, double h1, double h2, double L0, double L1, double L2,
-                              float4* __restrict__ p0, float4* __restrict__ p1, float4* __restrict__ u4,
-                              float4* __restrict__ a4) {
+// FP32 pair-sum records of the sorted sources (see PairArgs); the normals'
+// records come from k_gather_a3.
+__global__ void k_src_records(int n, const double* __restrict__ sx, const int4* __restrict__ meta,
+                              const float4* __restrict__ usph, int nlat, int Nc0, int Nc1, int Nc2, double h0,
+                              double h1, double h2, double L0, double L1, double L2, float4* __restrict__ p0,
+                              float4* __restrict__ p1, float4* __restrict__ u4) {
   int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
   const int Nc[3] = {Nc0, Nc1, Nc2};
@@ -88,7 +98,6 @@ __global__ void k_src_records(int n, const double* __restrict__ sx, const double
   p0[q] = make_float4(hi[0], hi[1], hi[2], __int_as_float(m.x));
   p1[q] = make_float4(lo[0], lo[1], lo[2], __int_as_float(m.y | (m.z << 16)));
   u4[q] = usph[m.y + nlat * m.z];
-  a4[q] = make_float4((float)sa3[q], (float)sa3[q + n], (float)sa3[q + 2 * (size_t)n], 0.f);
 }
 
 // Bounding box of each tile (TILE consecutive sources of one cell), from the
@@ -834,23 +843,23 @@ rbc3d_status sort_points_by_cell(rbc3d_ctx* ctx, int n, const double* x_dev, DBu
   return sort_points(ctx, n, x_dev, order, cs, ce);
 }
 
-rbc3d_status build_source_list(rbc3d_ctx* ctx) {
+rbc3d_status build_source_list(rbc3d_ctx* ctx, bool with_normals) {
   int n = ctx->npt;
   rbc3d_status s = sort_points(ctx, n, ctx->x.p, ctx->s_order, ctx->s_cstart, ctx->s_cend);
   if (s) return s;
   CUDA_TRY(ctx->s_x.alloc(3 * (size_t)n)); CUDA_TRY(ctx->s_a3.alloc(3 * (size_t)n)); CUDA_TRY(ctx->s_meta.alloc(n));
   CUDA_TRY(ctx->s_f.alloc(3 * (size_t)n)); CUDA_TRY(ctx->s_g.alloc(3 * (size_t)n));
   { k_gather_src<<<nblk(n, 256), 256, 0, ctx->st>>>(n, ctx->nlat, ctx->nlat * ctx->nlon, ctx->s_order.p, ctx->x.p,
-                                                   ctx->a3.p, ctx->s_x.p, ctx->s_a3.p, ctx->s_meta.p); ++ctx->launches; }
+                                                   ctx->s_x.p, ctx->s_meta.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   // FP32 pair-sum records and tile boxes
   CUDA_TRY(ctx->s_p0.alloc(n)); CUDA_TRY(ctx->s_p1.alloc(n)); CUDA_TRY(ctx->s_u4.alloc(n)); CUDA_TRY(ctx->s_a4.alloc(n));
+  if (with_normals && (s = source_normals(ctx))) return s;
   {
     const HashGrid& hg = ctx->hg;
-    k_src_records<<<nblk(n, 256), 256, 0, ctx->st>>>(n, ctx->s_x.p, ctx->s_a3.p, ctx->s_meta.p, ctx->usph.p, ctx->nlat,
+    k_src_records<<<nblk(n, 256), 256, 0, ctx->st>>>(n, ctx->s_x.p, ctx->s_meta.p, ctx->usph.p, ctx->nlat,
                                                      hg.Nc[0], hg.Nc[1], hg.Nc[2], hg.h[0], hg.h[1], hg.h[2], hg.L[0],
-                                                     hg.L[1], hg.L[2], ctx->s_p0.p, ctx->s_p1.p, ctx->s_u4.p,
-                                                     ctx->s_a4.p);
+                                                     hg.L[1], hg.L[2], ctx->s_p0.p, ctx->s_p1.p, ctx->s_u4.p);
     ++ctx->launches;
     CUDA_TRY(cudaGetLastError());
     const int nc = hg.ncells;
@@ -893,6 +902,16 @@ rbc3d_status build_source_list(rbc3d_ctx* ctx) {
   // tlist_rbc shares the source order
   TargetSet& t = ctx->tl[RBC3D_TLIST_RBC];
   t.sorted = false;
+  return RBC3D_OK;
+}
+
+// The sorted sources' normals (a3 in source order and the FP32 records),
+// once a3 is on the device.
+rbc3d_status source_normals(rbc3d_ctx* ctx) {
+  const int n = ctx->npt;
+  if (n == 0) return RBC3D_OK;
+  { k_gather_a3<<<nblk(n, 256), 256, 0, ctx->st>>>(n, ctx->s_order.p, ctx->a3.p, ctx->s_a3.p, ctx->s_a4.p); ++ctx->launches; }
+  CUDA_TRY(cudaGetLastError());
   return RBC3D_OK;
 }
 
