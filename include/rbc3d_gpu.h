@@ -190,7 +190,10 @@ rbc3d_status rbc3d_set_cell_density(rbc3d_ctx* ctx, const double* f,
  * ShAnalGau, ShFilter to degree < nlat0, ShSynthEqu, Spline_Build_On_Sphere;
  * ModRbc.F90:716) + SourceList_UpdateCoord + TargetList_Update;
  * set_cell_density_x = Rbc_BuildSurfaceSource(fFlag/gFlag) +
- * SourceList_UpdateDensity.  x, f, g: N x 3; f or g may be NULL. */
+ * SourceList_UpdateDensity.  x, f, g: N x 3; f or g may be NULL.
+ * Both return once the caller's arrays have been copied; the derivation
+ * continues on the device, ordered before every later call on the context
+ * (an error in it is reported by the next call that waits for it). */
 rbc3d_status rbc3d_set_cells_x(rbc3d_ctx* ctx, int ncell, const int* celltype, int nlat0, const double* x);
 rbc3d_status rbc3d_set_cell_density_x(rbc3d_ctx* ctx, int nlat0, const double* f, const double* g);
 rbc3d_status rbc3d_set_walls(rbc3d_ctx* ctx, int nvert, int nele,
