@@ -414,6 +414,7 @@ rbc3d_status rbc3d_create(const rbc3d_params* prm, rbc3d_ctx** out) {
         cudaEventCreateWithFlags(&ctx->ev_up, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_rthr, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_geom, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_dens, cudaEventDisableTiming) != cudaSuccess ||
         cudaMallocHost((void**)&ctx->h_rthr, sizeof(double)) != cudaSuccess)
       return bail(RBC3D_ERR_CUDA);
   }
@@ -479,6 +480,7 @@ rbc3d_status rbc3d_destroy(rbc3d_ctx* ctx) {
   if (ctx->ev_up) cudaEventDestroy(ctx->ev_up);
   if (ctx->ev_rthr) cudaEventDestroy(ctx->ev_rthr);
   if (ctx->ev_geom) cudaEventDestroy(ctx->ev_geom);
+  if (ctx->ev_dens) cudaEventDestroy(ctx->ev_dens);
   if (ctx->h_rthr) cudaFreeHost(ctx->h_rthr);
   if (ctx->st2) cudaStreamDestroy(ctx->st2);
   if (ctx->t0) { cudaEventDestroy(ctx->t0); cudaEventDestroy(ctx->t1); }
@@ -811,7 +813,8 @@ rbc3d_status rbc3d_set_cell_density_x(rbc3d_ctx* ctx, int nlat0, const double* f
   if (ctx->npt == 0) return RBC3D_OK;
   const size_t N = ctx->npt;
   rbc3d_status s;
-  spl_wait(ctx);  // side-stream readers of the previous densities are done
+  // the side stream's reads of the previous densities are done
+  if (ctx->dens_pending) CUDA_TRY(cudaStreamWaitEvent(ctx->st, ctx->ev_dens, 0));
   if (f) CUDA_TRY(ctx->f.upload(f, 3 * N, ctx->st));
   if (g) CUDA_TRY(ctx->g.upload(g, 3 * N, ctx->st));
   CUDA_TRY(cudaEventRecord(ctx->ev_up, ctx->st));
@@ -820,13 +823,18 @@ rbc3d_status rbc3d_set_cell_density_x(rbc3d_ctx* ctx, int nlat0, const double* f
   CUDA_TRY(cudaStreamWaitEvent(ctx->st2, ctx->ev_up, 0));
   std::swap(ctx->st, ctx->st2);
   s = surface_sources_dev(ctx, nlat0, false, f != nullptr, g != nullptr);
+  if (!s && f) ctx->has_f = true;
+  if (!s && g) ctx->has_g = true;
+  if (!s) s = self_mixed_density(ctx, f != nullptr, g != nullptr);
+  // a context whose matvecs run in FP32D gets its float-float node records
+  // here, on the side stream, ahead of the first matvec's patch
+  if (!s && ctx->ff_rec.p && ctx->phi_uniform)
+    s = self_ff_records(ctx, 1 | (ctx->has_f ? 2 : 0) | (ctx->has_g ? 4 | 8 : 0));
   std::swap(ctx->st, ctx->st2);
   CUDA_TRY(cudaEventRecord(ctx->ev_spl, ctx->st2));
-  ctx->spl_pending = true;
+  CUDA_TRY(cudaEventRecord(ctx->ev_dens, ctx->st2));
+  ctx->spl_pending = ctx->dens_pending = true;
   if (s) return s;
-  if (f) ctx->has_f = true;
-  if (g) ctx->has_g = true;
-  if ((s = self_mixed_density(ctx, f != nullptr, g != nullptr))) return s;
   if ((s = build_source_density(ctx))) return s;
   CUDA_TRY(cudaEventSynchronize(ctx->ev_up));  // the caller's host buffers are free again
   return RBC3D_OK;

@@ -153,7 +153,8 @@ struct rbc3d_ctx {
   // set_cells_x / set_cell_density_x build the spline tables on the side
   // stream and return; readers on the main stream wait on ev_spl (spl_wait)
   cudaEvent_t ev_spl = nullptr, ev_up = nullptr, ev_geom = nullptr;
-  bool spl_pending = false;
+  cudaEvent_t ev_dens = nullptr;  // after the side stream's last reads of f and g
+  bool spl_pending = false, dens_pending = false;
   int device = 0;
 
   // Ewald / mask tables
@@ -258,10 +259,15 @@ struct rbc3d_ctx {
   DBuf<double> stage;             // staging of uploaded spline tables (grow-only)
   // grow-only temporaries of the set-up passes (cudaFree would synchronise the device)
   DBuf<int> sort_key, sort_key2, sort_idx;  // sort_points
+  DBuf<char> scan_tmp;                      // device list builders: scan storage
+  DBuf<int> unit_cnt, unit_off, unit_idx, unit_zero;  // work units: per-cell counts, offsets, sort indices
+  DBuf<long long> unit_key;                 // work units: work keys (before and after the sort)
+  DBuf<int4> unit_tmp;                      // work units before the sort
   DBuf<char> sort_tmp;
   DBuf<int2> list_tmp;                      // build_source_list: tile / chunk lists
   DBuf<int> plan_key, plan_key2, plan_idx;  // build_spread_plan (may run on the side stream)
-  DBuf<char> plan_tmp;
+  DBuf<char> plan_tmp, plan_scan;
+  DBuf<int> plan_ts, plan_te, plan_cnt, plan_off;  // build_spread_plan: tile ranges, chunk counts and offsets
   DBuf<double> vadd;                        // finish_add: the caller's accumulator on the device
   DBuf<double> acoef_dev, mix_xc; // Acoef per cell type; FP32M cell centres
   rbc3d_counts counts{};
@@ -290,6 +296,9 @@ rbc3d_status ctx_fail_cuda(rbc3d_ctx* ctx, cudaError_t e, const char* what);
 // pair.cu
 rbc3d_status build_source_list(rbc3d_ctx* ctx, bool with_normals = true);
 rbc3d_status source_normals(rbc3d_ctx* ctx);
+// selfff.cu: the float-float node records of the sets in `need` (bit 0 x,
+// 1 f, 2 g, 3 a3) that are out of date, on the current stream
+rbc3d_status self_ff_records(rbc3d_ctx* ctx, int need);
 rbc3d_status sort_points_by_cell(rbc3d_ctx* ctx, int n, const double* x_dev, DBuf<int>& order, DBuf<int>& cs,
                                 DBuf<int>& ce);
 rbc3d_status matvec_dev(rbc3d_ctx* ctx, int which, double c1, double c2, unsigned terms, int prec);

@@ -49,6 +49,77 @@ __global__ void k_cell_ranges(int n, const int* __restrict__ key, int* __restric
   if (p == n - 1 || key[p + 1] != k) ce[k] = p + 1;
 }
 
+// Lists built on the device from sorted cell ranges (no host round trip).
+// Every list has a fixed capacity (an upper bound on its length); the
+// entries past its true length are empty (zero counts) and their consumers
+// skip them.
+
+// pieces[c] = ceil(count of cell c / P); pieces[nc] = 0 (the scan's total)
+__global__ void k_piece_counts(int nc, const int* __restrict__ cs, const int* __restrict__ ce, int P,
+                               int* __restrict__ pieces) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c > nc) return;
+  pieces[c] = c < nc ? (ce[c] - cs[c] + P - 1) / P : 0;
+}
+
+// (first, count) of the P-sized pieces of every cell, at off[c] (exclusive
+// scan of the piece counts); entries [off[nc], cap) are cleared
+__global__ void k_fill_pieces(int nc, const int* __restrict__ cs, const int* __restrict__ ce, int P,
+                              const int* __restrict__ off, int cap, int2* __restrict__ out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < nc) {
+    const int b0 = cs[c], e = ce[c];
+    int k = off[c];
+    for (int b = b0; b < e; b += P) out[k++] = make_int2(b, min(P, e - b));
+  }
+  for (int i = off[nc] + c; i < cap; i += gridDim.x * blockDim.x) out[i] = make_int2(0, 0);
+}
+
+// Work units of the pair sums (the cells' targets in equal-sized units of at
+// most TILE), keyed by their work: targets x the sources of the 27
+// neighbour cells.  Unit counts first, then the units at the scanned offsets.
+__global__ void k_unit_counts(int nc, const int* __restrict__ cs, const int* __restrict__ ce, int* __restrict__ cnt) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c > nc) return;
+  cnt[c] = c < nc ? (ce[c] - cs[c] + TILE - 1) / TILE : 0;
+}
+__global__ void k_fill_units(int nc, int Nc0, int Nc1, int Nc2, const int* __restrict__ cs, const int* __restrict__ ce,
+                             const int* __restrict__ ss, const int* __restrict__ se, const int* __restrict__ off,
+                             int cap, int4* __restrict__ units, long long* __restrict__ key, int* __restrict__ idx) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < nc) {
+    const int cnt = ce[c] - cs[c];
+    if (cnt > 0) {
+      const int ci = c % Nc0, cj = (c / Nc0) % Nc1, ck = c / (Nc0 * Nc1);
+      long long nsrc = 0;
+      for (int nb = 0; nb < 27; ++nb) {
+        const int ni = (ci + nb % 3 - 1 + Nc0) % Nc0, nj = (cj + (nb / 3) % 3 - 1 + Nc1) % Nc1;
+        const int nk = (ck + nb / 9 - 1 + Nc2) % Nc2;
+        const int q = ni + Nc0 * (nj + Nc1 * nk);
+        nsrc += se[q] - ss[q];
+      }
+      const int k = (cnt + TILE - 1) / TILE, per = (cnt + k - 1) / k;
+      int u = off[c];
+      for (int b = 0; b < cnt; b += per, ++u) {
+        const int m = min(per, cnt - b);
+        units[u] = make_int4(c, cs[c] + b, m, 0);
+        key[u] = nsrc * m;
+        idx[u] = u;
+      }
+    }
+  }
+  for (int i = off[nc] + c; i < cap; i += gridDim.x * blockDim.x) {
+    units[i] = make_int4(0, 0, 0, 0);
+    key[i] = -1;
+    idx[i] = i;
+  }
+}
+__global__ void k_gather_units(int cap, const int* __restrict__ idx, const int4* __restrict__ in,
+                               int4* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < cap) out[i] = in[idx[i]];
+}
+
 // Gather cell-point geometry into cell-list order.
 __global__ void k_gather_src(int n, int nlat, int nv, const int* __restrict__ order, const double* __restrict__ x,
                              double* __restrict__ sx, int4* __restrict__ meta) {
@@ -594,6 +665,7 @@ __global__ void __launch_bounds__(TILE) k_pair64(PairArgs a) {
   __shared__ TileD sm;
   __shared__ float3 wb[TILE / 32][2];
   const int4 unit = a.units[blockIdx.x];
+  if (unit.z == 0) return;  // an empty entry past the end of the unit list
   const int cell = unit.x;
   const int tid = threadIdx.x;
   const bool active = tid < unit.z;
@@ -747,56 +819,56 @@ rbc3d_status sort_points(rbc3d_ctx* ctx, int n, const double* x_dev, DBuf<int>& 
   CUDA_TRY(cudaMemsetAsync(ce.p, 0, sizeof(int) * hg.ncells, ctx->st));
   { k_cell_ranges<<<nblk(n, 256), 256, 0, ctx->st>>>(n, key2.p, cs.p, ce.p); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
-  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  return RBC3D_OK;
+}
+
+// off = exclusive scan of cnt[0..nc] (nc + 1 entries; off[nc] the total), on the context stream
+rbc3d_status scan_counts(rbc3d_ctx* ctx, int nc, const int* cnt, int* off) {
+  size_t tmp = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, tmp, cnt, off, nc + 1, ctx->st);
+  DBuf<char>& tb = ctx->scan_tmp;
+  CUDA_TRY(tb.alloc(tmp + 1));
+  CUDA_TRY(cub::DeviceScan::ExclusiveSum(tb.p, tmp, cnt, off, nc + 1, ctx->st));
   return RBC3D_OK;
 }
 
 rbc3d_status make_units(rbc3d_ctx* ctx, TargetSet& t, const DBuf<int>& cs, const DBuf<int>& ce) {
-  int nc = ctx->hg.ncells;
-  std::vector<int> hs(nc), he(nc);
-  // stream-ordered reads: cudaMemcpy on the legacy stream does not wait for
-  // the context's non-blocking stream that wrote these arrays
-  CUDA_TRY(cudaMemcpyAsync(hs.data(), cs.p, sizeof(int) * nc, cudaMemcpyDeviceToHost, ctx->st));
-  CUDA_TRY(cudaMemcpyAsync(he.data(), ce.p, sizeof(int) * nc, cudaMemcpyDeviceToHost, ctx->st));
-  // sources per cell (the pair work of a unit is its targets x the sources
-  // of the 27 neighbour cells)
-  CUDA_TRY(cudaStreamSynchronize(ctx->st));
-  std::vector<long long> src(nc, 0);
-  if (ctx->npt > 0 && ctx->s_cstart.p) {
-    std::vector<int> ss(nc), se(nc);
-    CUDA_TRY(cudaMemcpyAsync(ss.data(), ctx->s_cstart.p, sizeof(int) * nc, cudaMemcpyDeviceToHost, ctx->st));
-    CUDA_TRY(cudaMemcpyAsync(se.data(), ctx->s_cend.p, sizeof(int) * nc, cudaMemcpyDeviceToHost, ctx->st));
-    CUDA_TRY(cudaStreamSynchronize(ctx->st));
-    for (int c = 0; c < nc; ++c) src[c] = se[c] - ss[c];
+  const int nc = ctx->hg.ncells;
+  // capacity: every non-empty cell gives at most count / TILE + 1 units
+  const int cap = nc + (t.n + TILE - 1) / TILE;
+  rbc3d_status s;
+  DBuf<int>& cnt = ctx->unit_cnt;
+  CUDA_TRY(cnt.alloc(nc + 1)); CUDA_TRY(ctx->unit_off.alloc(nc + 1));
+  CUDA_TRY(ctx->unit_tmp.alloc(cap)); CUDA_TRY(t.units.alloc(cap));
+  CUDA_TRY(ctx->unit_key.alloc(2 * (size_t)cap)); CUDA_TRY(ctx->unit_idx.alloc(2 * (size_t)cap));
+  // sources per cell: the source list's ranges (or the targets' own when
+  // there is no source list)
+  const bool src = ctx->npt > 0 && ctx->s_cstart.p;
+  const int* ss = src ? ctx->s_cstart.p : cs.p;
+  const int* se = src ? ctx->s_cend.p : ce.p;
+  if (!src) {  // no sources: every unit weighs 0
+    CUDA_TRY(ctx->unit_zero.alloc(nc));
+    CUDA_TRY(cudaMemsetAsync(ctx->unit_zero.p, 0, sizeof(int) * nc, ctx->st));
+    ss = se = ctx->unit_zero.p;
   }
-  const int* N = ctx->hg.Nc;
-  std::vector<std::pair<long long, int4>> u;
-  for (int c = 0; c < nc; ++c) {
-    const int cnt = he[c] - hs[c];
-    if (cnt <= 0) continue;
-    const int ci = c % N[0], cj = (c / N[0]) % N[1], ck = c / (N[0] * N[1]);
-    long long nsrc = 0;
-    for (int nb = 0; nb < 27; ++nb) {
-      const int ni = (ci + nb % 3 - 1 + N[0]) % N[0], nj = (cj + (nb / 3) % 3 - 1 + N[1]) % N[1];
-      const int nk = (ck + nb / 9 - 1 + N[2]) % N[2];
-      nsrc += src[ni + N[0] * (nj + N[1] * nk)];
-    }
-    // equal-sized units of at most TILE targets
-    const int k = (cnt + TILE - 1) / TILE, per = (cnt + k - 1) / k;
-    for (int b = 0; b < cnt; b += per) {
-      const int m = std::min(per, cnt - b);
-      u.push_back({nsrc * m, make_int4(c, hs[c] + b, m, 0)});
-    }
-  }
-  // heaviest units first, so the last wave holds the light ones
-  std::stable_sort(u.begin(), u.end(), [](const std::pair<long long, int4>& x, const std::pair<long long, int4>& y) {
-    return x.first > y.first;
-  });
-  std::vector<int4> uu(u.size());
-  for (size_t i = 0; i < u.size(); ++i) uu[i] = u[i].second;
-  t.nunits = (int)uu.size();
-  if (t.nunits) CUDA_TRY(t.units.upload(uu.data(), uu.size(), ctx->st));
-  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  const int g1 = nblk(nc + 1, 256);
+  { k_unit_counts<<<g1, 256, 0, ctx->st>>>(nc, cs.p, ce.p, cnt.p); ++ctx->launches; }
+  if ((s = scan_counts(ctx, nc, cnt.p, ctx->unit_off.p))) return s;
+  long long* key = ctx->unit_key.p;
+  int* idx = ctx->unit_idx.p;
+  { k_fill_units<<<g1, 256, 0, ctx->st>>>(nc, ctx->hg.Nc[0], ctx->hg.Nc[1], ctx->hg.Nc[2], cs.p, ce.p, ss, se,
+                                          ctx->unit_off.p, cap, ctx->unit_tmp.p, key, idx); ++ctx->launches; }
+  // heaviest units first, so the last wave holds the light ones; the radix
+  // sort is stable, so equal work keeps cell order (as a stable host sort);
+  // the empty tail (key -1) stays last
+  size_t tmp = 0;
+  cub::DeviceRadixSort::SortPairsDescending(nullptr, tmp, key, key + cap, idx, idx + cap, cap, 0, 64, ctx->st);
+  DBuf<char>& tb = ctx->sort_tmp;
+  CUDA_TRY(tb.alloc(tmp + 1));
+  CUDA_TRY(cub::DeviceRadixSort::SortPairsDescending(tb.p, tmp, key, key + cap, idx, idx + cap, cap, 0, 64, ctx->st));
+  { k_gather_units<<<nblk(cap, 256), 256, 0, ctx->st>>>(cap, idx + cap, ctx->unit_tmp.p, t.units.p); ++ctx->launches; }
+  CUDA_TRY(cudaGetLastError());
+  t.nunits = cap;
   return RBC3D_OK;
 }
 
@@ -863,39 +935,26 @@ rbc3d_status build_source_list(rbc3d_ctx* ctx, bool with_normals) {
     ++ctx->launches;
     CUDA_TRY(cudaGetLastError());
     const int nc = hg.ncells;
-    std::vector<int> hs(nc), he(nc), toff(nc + 1, 0);
-    CUDA_TRY(cudaMemcpyAsync(hs.data(), ctx->s_cstart.p, sizeof(int) * nc, cudaMemcpyDeviceToHost, ctx->st));
-    CUDA_TRY(cudaMemcpyAsync(he.data(), ctx->s_cend.p, sizeof(int) * nc, cudaMemcpyDeviceToHost, ctx->st));
-    CUDA_TRY(cudaStreamSynchronize(ctx->st));
-    std::vector<int2> tiles, chunks;
-    std::vector<int> coff(nc + 1, 0);
-    for (int c = 0; c < nc; ++c) {
-      toff[c] = (int)tiles.size();
-      coff[c] = (int)chunks.size();
-      for (int b = hs[c]; b < he[c]; b += TILE) tiles.push_back(make_int2(b, std::min(TILE, he[c] - b)));
-      for (int b = hs[c]; b < he[c]; b += 32) chunks.push_back(make_int2(b, std::min(32, he[c] - b)));
-    }
-    toff[nc] = (int)tiles.size();
-    coff[nc] = (int)chunks.size();
-    CUDA_TRY(ctx->s_coff.upload(coff.data(), coff.size(), ctx->st));
-    CUDA_TRY(ctx->s_cbox.alloc(2 * chunks.size() + 2));
-    // one upload of both lists (chunks, then tiles) into a persistent buffer
+    // tiles of TILE and chunks of 32 consecutive sources of one cell, with
+    // their offsets per cell and bounding boxes
+    const int capt = nc + (n + TILE - 1) / TILE, capc = nc + (n + 31) / 32;
+    CUDA_TRY(ctx->s_toff.alloc(nc + 1)); CUDA_TRY(ctx->s_coff.alloc(nc + 1));
+    CUDA_TRY(ctx->unit_cnt.alloc(nc + 1));
     DBuf<int2>& lt = ctx->list_tmp;
-    std::vector<int2> both(chunks);
-    both.insert(both.end(), tiles.begin(), tiles.end());
-    if (!both.empty()) CUDA_TRY(lt.upload(both.data(), both.size(), ctx->st));
-    if (!chunks.empty()) {
-      { k_tile_boxes<<<(int)chunks.size(), 32, 0, ctx->st>>>(lt.p, ctx->s_p0.p, ctx->s_cbox.p); ++ctx->launches; }
-      CUDA_TRY(cudaGetLastError());
-    }
-    ctx->s_ntiles = (int)tiles.size();
-    CUDA_TRY(ctx->s_toff.upload(toff.data(), toff.size(), ctx->st));
-    CUDA_TRY(ctx->s_tbox.alloc(2 * tiles.size() + 2));
-    if (!tiles.empty()) {
-      { k_tile_boxes<<<(int)tiles.size(), TILE, 0, ctx->st>>>(lt.p + chunks.size(), ctx->s_p0.p, ctx->s_tbox.p); ++ctx->launches; }
-      CUDA_TRY(cudaGetLastError());
-    }
-    CUDA_TRY(cudaStreamSynchronize(ctx->st));  // the host lists are freed on return
+    CUDA_TRY(lt.alloc((size_t)capc + capt));
+    CUDA_TRY(ctx->s_cbox.alloc(2 * (size_t)capc + 2)); CUDA_TRY(ctx->s_tbox.alloc(2 * (size_t)capt + 2));
+    const int g1 = nblk(nc + 1, 256);
+    { k_piece_counts<<<g1, 256, 0, ctx->st>>>(nc, ctx->s_cstart.p, ctx->s_cend.p, 32, ctx->unit_cnt.p); ++ctx->launches; }
+    if ((s = scan_counts(ctx, nc, ctx->unit_cnt.p, ctx->s_coff.p))) return s;
+    { k_fill_pieces<<<g1, 256, 0, ctx->st>>>(nc, ctx->s_cstart.p, ctx->s_cend.p, 32, ctx->s_coff.p, capc, lt.p); ++ctx->launches; }
+    { k_piece_counts<<<g1, 256, 0, ctx->st>>>(nc, ctx->s_cstart.p, ctx->s_cend.p, TILE, ctx->unit_cnt.p); ++ctx->launches; }
+    if ((s = scan_counts(ctx, nc, ctx->unit_cnt.p, ctx->s_toff.p))) return s;
+    { k_fill_pieces<<<g1, 256, 0, ctx->st>>>(nc, ctx->s_cstart.p, ctx->s_cend.p, TILE, ctx->s_toff.p, capt, lt.p + capc);
+      ++ctx->launches; }
+    { k_tile_boxes<<<capc, 32, 0, ctx->st>>>(lt.p, ctx->s_p0.p, ctx->s_cbox.p); ++ctx->launches; }
+    { k_tile_boxes<<<capt, TILE, 0, ctx->st>>>(lt.p + capc, ctx->s_p0.p, ctx->s_tbox.p); ++ctx->launches; }
+    CUDA_TRY(cudaGetLastError());
+    ctx->s_ntiles = capt;
   }
   ctx->src_sorted = true;
   ctx->pme.cplan.valid = false;  // the PME tiles follow the source positions

@@ -135,6 +135,7 @@ __global__ void __launch_bounds__(128) k_spread_tile(SpreadArgs a, TileArgs t, c
   constexpr int P = PT, NR = spread_rounds(PT);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int4 ch = chunk[blockIdx.x];
+  if (ch.y >= ch.z) return;  // an empty entry past the end of the chunk list
   const int nw = blockDim.x >> 5;
   const int B = t.B, B2 = B * B, B3 = B2 * B;
   R* box = reinterpret_cast<R*>(smem_raw);  // [3 nw][B3]
@@ -445,7 +446,29 @@ TileArgs tile_args(const rbc3d_ctx* ctx, size_t elem) {
   return t;
 }
 
-// Bin n sources (SoA positions on the device) by tile; chunks built on the host.
+__global__ void k_key_ranges(int n, const int* __restrict__ key, int* __restrict__ ts, int* __restrict__ te) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const int k = key[p];
+  if (p == 0 || key[p - 1] != k) ts[k] = p;
+  if (p == n - 1 || key[p + 1] != k) te[k] = p + 1;
+}
+__global__ void k_chunk_counts(int nt, const int* __restrict__ ts, const int* __restrict__ te, int* __restrict__ cnt) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k > nt) return;
+  cnt[k] = k < nt ? (te[k] - ts[k] + SPREAD_CHUNK - 1) / SPREAD_CHUNK : 0;
+}
+__global__ void k_fill_chunks(int nt, const int* __restrict__ ts, const int* __restrict__ te, const int* __restrict__ off,
+                              int cap, int4* __restrict__ chunk) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < nt) {
+    int o = off[k];
+    for (int c = ts[k]; c < te[k]; c += SPREAD_CHUNK) chunk[o++] = make_int4(k, c, min(te[k], c + SPREAD_CHUNK), 0);
+  }
+  for (int i = off[nt] + k; i < cap; i += gridDim.x * blockDim.x) chunk[i] = make_int4(0, 0, 0, 0);
+}
+
+// Bin n sources (SoA positions on the device) by tile; chunks built on the device.
 rbc3d_status build_spread_plan(rbc3d_ctx* ctx, int n, const double* x, SpreadArgs a, SpreadPlan& pl) {
   pl.n = n;
   pl.nchunk = 0;
@@ -464,19 +487,26 @@ rbc3d_status build_spread_plan(rbc3d_ctx* ctx, int n, const double* x, SpreadArg
   DBuf<char>& tb = ctx->plan_tmp;
   CUDA_TRY(tb.alloc(tmp + 1));
   CUDA_TRY(cub::DeviceRadixSort::SortPairs(tb.p, tmp, key.p, key2.p, idx.p, pl.perm.p, n, 0, bits, ctx->st));
-  std::vector<int> hk(n);
-  CUDA_TRY(cudaMemcpyAsync(hk.data(), key2.p, sizeof(int) * n, cudaMemcpyDeviceToHost, ctx->st));
-  CUDA_TRY(cudaStreamSynchronize(ctx->st));
-  std::vector<int4> ch;
-  for (int b = 0; b < n;) {
-    int e = b;
-    while (e < n && hk[e] == hk[b]) ++e;
-    for (int c = b; c < e; c += SPREAD_CHUNK) ch.push_back(make_int4(hk[b], c, std::min(e, c + SPREAD_CHUNK), 0));
-    b = e;
-  }
-  pl.nchunk = (int)ch.size();
-  CUDA_TRY(pl.chunk.upload(ch.data(), ch.size(), ctx->st));
-  CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  // chunks of at most SPREAD_CHUNK sources of one tile, in tile order, built
+  // on the device: the tiles' ranges in the sorted keys, their chunk counts,
+  // the counts' scan, the chunks; the list has a fixed capacity and its empty
+  // tail entries are skipped by the spread
+  DBuf<int>&ts = ctx->plan_ts, &te = ctx->plan_te, &cnt = ctx->plan_cnt, &off = ctx->plan_off;
+  CUDA_TRY(ts.alloc(ntiles)); CUDA_TRY(te.alloc(ntiles)); CUDA_TRY(cnt.alloc(ntiles + 1)); CUDA_TRY(off.alloc(ntiles + 1));
+  CUDA_TRY(cudaMemsetAsync(ts.p, 0, sizeof(int) * ntiles, ctx->st));
+  CUDA_TRY(cudaMemsetAsync(te.p, 0, sizeof(int) * ntiles, ctx->st));
+  { k_key_ranges<<<nblk(n, 256), 256, 0, ctx->st>>>(n, key2.p, ts.p, te.p); ++ctx->launches; }
+  { k_chunk_counts<<<nblk(ntiles + 1, 256), 256, 0, ctx->st>>>(ntiles, ts.p, te.p, cnt.p); ++ctx->launches; }
+  size_t stmp = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, stmp, cnt.p, off.p, ntiles + 1, ctx->st);
+  DBuf<char>& sb = ctx->plan_scan;
+  CUDA_TRY(sb.alloc(stmp + 1));
+  CUDA_TRY(cub::DeviceScan::ExclusiveSum(sb.p, stmp, cnt.p, off.p, ntiles + 1, ctx->st));
+  const int cap = ntiles + (n + SPREAD_CHUNK - 1) / SPREAD_CHUNK;
+  CUDA_TRY(pl.chunk.alloc(cap));
+  { k_fill_chunks<<<nblk(ntiles + 1, 256), 256, 0, ctx->st>>>(ntiles, ts.p, te.p, off.p, cap, pl.chunk.p); ++ctx->launches; }
+  CUDA_TRY(cudaGetLastError());
+  pl.nchunk = cap;
   return RBC3D_OK;
 }
 

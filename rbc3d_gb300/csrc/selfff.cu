@@ -475,16 +475,11 @@ void self_ff_invalidate(rbc3d_ctx* ctx, bool geom, bool f, bool g) {
   if (g) ctx->ff_sets &= ~4;
 }
 
-rbc3d_status run_self_ff(rbc3d_ctx* ctx, int tlist, double c1, double c2) {
-  TargetSet& t = ctx->tl[tlist];
-  if (tlist != RBC3D_TLIST_RBC || t.n == 0 || ctx->ncell == 0) return RBC3D_OK;
-  if (!ctx->phi_uniform) return ctx_fail(ctx, RBC3D_ERR_ARG, "FP32D needs phi(j) = j*2*pi/nlon");
-  const bool sl = c1 != 0 && ctx->has_f, dl = c2 != 0 && ctx->has_g;
-  if (!sl && !dl) return RBC3D_OK;
+// The float-float node records of the sets in `need` (bit 0 x, 1 f, 2 g,
+// 3 a3) that are out of date, on the current stream.
+rbc3d_status self_ff_records(rbc3d_ctx* ctx, int need) {
   const long long per = (long long)ctx->m * ctx->nlon;
   const NodeMap map = node_map(ctx->m, ctx->nlon);
-  // records this call reads: x always, f for SL, g and a3 for DL
-  const int need = 1 | (sl ? 2 : 0) | (dl ? 4 | 8 : 0);
   if (!ctx->ff_rec.p || ctx->ff_rec.n < (size_t)ctx->ncell * map.per * FF_PLANES) {
     CUDA_TRY(ctx->ff_rec.alloc((size_t)ctx->ncell * map.per * FF_PLANES));
     ctx->ff_sets = 0;
@@ -501,6 +496,19 @@ rbc3d_status run_self_ff(rbc3d_ctx* ctx, int tlist, double c1, double c2) {
     CUDA_TRY(cudaGetLastError());
     ctx->ff_sets |= build;
   }
+  return RBC3D_OK;
+}
+
+rbc3d_status run_self_ff(rbc3d_ctx* ctx, int tlist, double c1, double c2) {
+  TargetSet& t = ctx->tl[tlist];
+  if (tlist != RBC3D_TLIST_RBC || t.n == 0 || ctx->ncell == 0) return RBC3D_OK;
+  if (!ctx->phi_uniform) return ctx_fail(ctx, RBC3D_ERR_ARG, "FP32D needs phi(j) = j*2*pi/nlon");
+  const bool sl = c1 != 0 && ctx->has_f, dl = c2 != 0 && ctx->has_g;
+  if (!sl && !dl) return RBC3D_OK;
+  const NodeMap map = node_map(ctx->m, ctx->nlon);
+  // records this call reads: x always, f for SL, g and a3 for DL
+  rbc3d_status s = self_ff_records(ctx, 1 | (sl ? 2 : 0) | (dl ? 4 | 8 : 0));
+  if (s) return s;
   FFArgs a;
   a.nt = t.n; a.ncell = ctx->ncell; a.nlat = ctx->nlat; a.nlon = ctx->nlon; a.m = ctx->m;
   a.NQ = ctx->nrad * ctx->nazm; a.nrad = ctx->nrad;
