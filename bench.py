@@ -406,6 +406,8 @@ def main():
     ap.add_argument("--quick", action="store_true", help="one mode's matvec timing only (profiling)")
     ap.add_argument("--quick-prec", choices=("fp32c", "fp32m", "fp32d", "fp64"), default="fp32d",
                     help="the mode --quick times (profiling)")
+    ap.add_argument("--quick-e2e", action="store_true",
+                    help="only the end-to-end FP32D step from positions and raw densities (profiling)")
     ap.add_argument("--no-wall", action="store_true", help="skip the learned-guess wall GMRES comparison")
     ap.add_argument("--no-scaleup", action="store_true", help="skip the 2048-cell (PME 256^3) workload")
     ap.add_argument("--no-cellsolve", action="store_true", help="skip the cell velocity GMRES line")
@@ -431,6 +433,13 @@ def main():
     b = Bench(lib, prm, cells, dist, ws)
     N = b.N
     cpu_on = rank == 0 and ws == 1 and not args.no_cpu
+
+    if args.quick_e2e:
+        e = b.e2e(FP32D, args.steps)
+        if rank == 0:
+            print(json.dumps({"quick_e2e": True, **{k: v for k, v in e.items() if k != "inputs"}}), flush=True)
+        b.close()
+        return 0
 
     # ---- headline: FP32D matvec with every input resident in HBM
     head = {"fp32m": FP32M, "fp32c": FP32C, "fp64": FP64}.get(args.quick_prec, FP32D) if args.quick else FP32D
