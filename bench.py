@@ -632,6 +632,11 @@ def main():
             "rooflines": rooflines,
             "fp32_over_fp64_plain": {"fp32d": value / fp64_value, "fp32c": fp32c_value / fp64_value,
                                      "fp32m": fp32m_value / fp64_value, "target": 20.0,
+                                     "tolerance_vs_oracle": 1e-6,
+                                     "modes_meeting_target": [k for k, r in (("fp32d", value / fp64_value),
+                                                                             ("fp32c", fp32c_value / fp64_value),
+                                                                             ("fp32m", fp32m_value / fp64_value))
+                                                              if r >= 20.0 and (err_oracle or {}).get(k, 1.0) <= 1e-6],
                                      "note": "fp32d: self patch in float-float on the FP32 pipe (GB300 FP64 is "
                                              "1/74 of FP32); fp32c: on the FP64 pipe; fp32m: in FP32 with hi/lo "
                                              "geometry"},
