@@ -561,7 +561,9 @@ def main():
                          "(guess mode 5); each compared step's pair is learned only after every arm has solved it "
                          "(held out)"}
         t1 = time.perf_counter()
-        wm_warm, wm_test = max(10, warm // 2), max(3, test // 2)
+        # as many training steps as the FP64 run, so that the spectral bases
+        # complete and the preconditioner acts on every mode; half the compared steps
+        wm_warm, wm_test = warm, max(3, test // 2)
         wm = wall_run(ncell=64, warm_steps=wm_warm, test_steps=wm_test, rtol=1e-8, restart=300, max_it=900,
                       train_iters=30, history=48, seed=args.seed + rank, prec=FP32M, dynamics="skalak", dt=1e-3)
         log(f"mixed-precision wall GMRES comparison in {time.perf_counter() - t1:.1f}s")
