@@ -86,3 +86,60 @@ def test_device_surface_sources_of_the_synthetic_cells(gpu):
     assert err[12] < 1e-2
     assert err[24] < 3e-4 and err[24] < 0.1 * err[12]
     a_ctx.close()
+
+
+def test_back_to_back_updates_and_buffer_reuse(gpu):
+    """set_cells_x / set_cell_density_x return while the derivation runs on
+    the device: updates issued back to back, and host buffers overwritten as
+    soon as the calls return, give the matvec of the last state as a fresh
+    context computes it."""
+    prm, cells, _ = G.config("C2", ncell=24)
+    prm["Lb"] = [20.0] * 3
+    rng = np.random.default_rng(7)
+    moved = np.ascontiguousarray(cells.x + 0.05 * rng.standard_normal(cells.x.shape))
+    f2 = np.ascontiguousarray(1.5 * cells.f)
+    fresh = Context(gpu, prm)
+    fresh.set_cell_grid(cells.th, cells.phi, cells.w)
+
+    class Raw:
+        pass
+
+    def raw(x):
+        r = Raw()
+        for k in ("nlat", "nlon", "th", "phi", "w", "ncell", "celltype"):
+            setattr(r, k, getattr(cells, k))
+        r.x = x
+        return r
+
+    fresh.set_cells_x(raw(moved), 12)
+    fresh.set_cell_density_x(12, f=f2, g=cells.g)
+    ref = {p: fresh.matvec(TLIST_RBC, C, C, TERM_ALL, p) for p in (FP64, FP32D)}
+    fresh.close()
+    ctx = Context(gpu, prm)
+    ctx.set_cell_grid(cells.th, cells.phi, cells.w)
+    # pinned host buffers: the copies are asynchronous, the calls wait for them
+    xbuf, fbuf, gbuf = gpu.pinned(cells.x.shape), gpu.pinned(cells.f.shape), gpu.pinned(cells.g.shape)
+    xbuf[...] = cells.x
+    fbuf[...] = cells.f
+    gbuf[...] = cells.g
+    ctx.set_cells_x(raw(xbuf), 12)
+    ctx.set_cell_density_x(12, f=fbuf, g=gbuf)
+    ctx.matvec(TLIST_RBC, C, C, TERM_ALL, FP32D)  # a matvec of the first state, then the second state
+    xbuf[...] = moved
+    ctx.set_cells_x(raw(xbuf), 12)
+    xbuf[...] = 0.0          # the caller's buffers are free once the calls return
+    fbuf[...] = f2
+    ctx.set_cell_density_x(12, f=fbuf, g=gbuf)
+    fbuf[...] = 0.0
+    gbuf[...] = 0.0
+    # FP64 to rounding; FP32D to its run-to-run spread (float atomics in the
+    # PME spread, ~3e-8): a stale or half-written input moves it by far more
+    for p, tol in ((FP64, 1e-12), (FP32D, 1e-6)):
+        v = ctx.matvec(TLIST_RBC, C, C, TERM_ALL, p)
+        assert np.linalg.norm(v - ref[p]) <= tol * np.linalg.norm(ref[p]), p
+    # two density updates back to back without a matvec between them
+    ctx.set_cell_density_x(12, f=cells.f, g=cells.g)
+    ctx.set_cell_density_x(12, f=f2, g=cells.g)
+    v = ctx.matvec(TLIST_RBC, C, C, TERM_ALL, FP64)
+    assert np.linalg.norm(v - ref[FP64]) <= 1e-12 * np.linalg.norm(ref[FP64])
+    ctx.close()
