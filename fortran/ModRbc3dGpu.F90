@@ -340,6 +340,10 @@ module ModRbc3dGpu
   type(c_ptr), save :: gpu_ctx = c_null_ptr
   integer(c_int), save :: gpu_matvec_prec = RBC3D_FP32D  ! AddIntOnRbcs, PME_*, residual velocities
   integer(c_int), save :: gpu_solve_prec = RBC3D_FP64    ! NoSlipWall, Solve_RBC_Vel operators
+  ! .true.: Rbc3dGpu_SyncCells sends positions and raw densities only, and the
+  ! library derives the geometry and the spline tables on the device
+  ! (rbc3d_set_cells_x / rbc3d_set_cell_density_x, degree < nlat0)
+  logical, save :: gpu_cells_from_positions = .false.
 
 
 

@@ -102,6 +102,10 @@ contains
     if (nrbc == 0) return
     nv = rbcs(1)%nlat*rbcs(1)%nlon
     npt = nrbc*nv
+    if (gpu_cells_from_positions) then
+      call sync_cells_raw(geom, fFlag, gFlag, nv, npt)
+      return
+    end if
     if (geom) then
       allocate (ct(nrbc), x(npt, 3), a3(npt, 3), detJ(npt), area(nrbc), msz(nrbc))
       ns = spline_size(rbcs(1)%spln_x)
@@ -155,6 +159,59 @@ contains
       if (allocated(g)) deallocate (g, sg)
     end if
   end subroutine Rbc3dGpu_SyncCells
+
+  ! Positions and raw densities only; the library derives a3, detJ, area,
+  ! meshSize and the spline tables (RBC_ComputeGeometry and
+  ! Rbc_BuildSurfaceSource at degree < nlat0) on the device.
+  subroutine sync_cells_raw(geom, fFlag, gFlag, nv, npt)
+    logical, intent(in) :: geom, fFlag, gFlag
+    integer, intent(in) :: nv, npt
+    integer :: irbc, ip, k
+    integer(c_int), allocatable :: ct(:)
+    real(c_double), allocatable, target :: x(:, :), f(:, :), g(:, :)
+    type(c_ptr) :: pf, pg
+    integer(c_int) :: nlat0
+
+    nlat0 = int(rbcs(1)%nlat0, c_int)
+    if (geom) then
+      allocate (ct(nrbc), x(npt, 3))
+      do irbc = 1, nrbc
+        ip = (irbc - 1)*nv
+        do k = 1, 3
+          x(ip + 1:ip + nv, k) = reshape(rbcs(irbc)%x(:, :, k), [nv])
+        end do
+        ct(irbc) = rbcs(irbc)%celltype - 1
+      end do
+      call rbc3d_check(rbc3d_set_cells_x(gpu_ctx, int(nrbc, c_int), ct, nlat0, x), 'rbc3d_set_cells_x')
+      deallocate (ct, x)
+    end if
+    if (fFlag .or. gFlag) then
+      pf = c_null_ptr; pg = c_null_ptr
+      if (fFlag) then
+        allocate (f(npt, 3))
+        do irbc = 1, nrbc
+          ip = (irbc - 1)*nv
+          do k = 1, 3
+            f(ip + 1:ip + nv, k) = reshape(rbcs(irbc)%f(:, :, k), [nv])
+          end do
+        end do
+        pf = c_loc(f)
+      end if
+      if (gFlag) then
+        allocate (g(npt, 3))
+        do irbc = 1, nrbc
+          ip = (irbc - 1)*nv
+          do k = 1, 3
+            g(ip + 1:ip + nv, k) = reshape(rbcs(irbc)%g(:, :, k), [nv])
+          end do
+        end do
+        pg = c_loc(g)
+      end if
+      call rbc3d_check(rbc3d_set_cell_density_x(gpu_ctx, nlat0, pf, pg), 'rbc3d_set_cell_density_x')
+      if (allocated(f)) deallocate (f)
+      if (allocated(g)) deallocate (g)
+    end if
+  end subroutine sync_cells_raw
 
   subroutine Rbc3dGpu_SyncWall
     real(c_double), allocatable :: fw(:)
