@@ -29,6 +29,7 @@ struct CorrArgs {
   unsigned long long* queue;  // k_near's item counter
   const SelfW64* W64;         // k_self: tabulated patch weights (uniform longitudes), or null
   const int* list;            // k_near: items to process (indices), or null for all
+  const float* rep;           // k_near_replay: x and a3 node values in FP32, 24 floats a node
   const unsigned long long* nlist;
   const double* th;
   const double* phi;
@@ -452,19 +453,38 @@ __device__ __forceinline__ void spline_eval32(const double* __restrict__ spl, fl
     f[l] = cx[0] * r0 + cx[1] * r1 + cx[2] * r2 + cx[3] * r3;
   }
 }
+// the same from the replay's FP32 node records (24 floats a node: the x
+// slots' 12 values, then a3's; off 0 for x, 12 for a3), with no conversions
+__device__ __forceinline__ void spline_eval32f(const float* __restrict__ rec, int off, float th, float ph, int m,
+                                               int n, float* f) {
+  int n11, n12, n21, n22;
+  float cx[4], cy[4];
+  spline_weights32(th, ph, m, n, n11, n12, n21, n22, cx, cy);
+  const float* a = rec + (size_t)n11 * 24 + off;
+  const float* b = rec + (size_t)n12 * 24 + off;
+  const float* c = rec + (size_t)n21 * 24 + off;
+  const float* d = rec + (size_t)n22 * 24 + off;
+  for (int l = 0; l < 3; ++l) {
+    float r0 = a[l] * cy[0] + b[l] * cy[1] + a[6 + l] * cy[2] + b[6 + l] * cy[3];
+    float r1 = c[l] * cy[0] + d[l] * cy[1] + c[6 + l] * cy[2] + d[6 + l] * cy[3];
+    float r2 = a[3 + l] * cy[0] + b[3 + l] * cy[1] + a[9 + l] * cy[2] + b[9 + l] * cy[3];
+    float r3 = c[3 + l] * cy[0] + d[3 + l] * cy[1] + c[9 + l] * cy[2] + d[9 + l] * cy[3];
+    f[l] = cx[0] * r0 + cx[1] * r1 + cx[2] * r2 + cx[3] * r3;
+  }
+}
 __device__ __forceinline__ float warp_sumf_(float v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
-// Returns the projection's signed distance a3(x0).(xt - x0) in FP32.
-__device__ float projection_dist32(const double* sx, const double* sa, int m, int n, const double* xtd, double th0d,
-                                   double phi0d) {
+// Returns the projection's signed distance a3(x0).(xt - x0) in FP32, from
+// the cell's FP32 node records (x at offset 0, a3 at 12).
+__device__ float projection_dist32(const float* rc, int m, int n, const double* xtd, double th0d, double phi0d) {
   const int lane = threadIdx.x & 31;
   const float TWO_PI_F = (float)RBC3D_TWO_PI;
   float xt[3] = {(float)xtd[0], (float)xtd[1], (float)xtd[2]};
   float th0 = (float)th0d, phi0 = (float)phi0d;
   float x0[3];
-  spline_eval32(sx, th0, phi0, m, n, x0);
+  spline_eval32f(rc, 0, th0, phi0, m, n, x0);
   float h = fmaxf(TWO_PI_F / m, TWO_PI_F / n);
   for (int iter = 0; iter < 3; ++iter) {
     float px = 0, py = 0, d2 = 0;
@@ -481,11 +501,11 @@ __device__ float projection_dist32(const double* sx, const double* sa, int m, in
       px = thL * cph;
       py = thL * sph;
       float xx[3];
-      spline_eval32(sx, thP, phP, m, n, xx);
+      spline_eval32f(rc, 0, thP, phP, m, n, xx);
       d2 = (xx[0] - xt[0]) * (xx[0] - xt[0]) + (xx[1] - xt[1]) * (xx[1] - xt[1]) + (xx[2] - xt[2]) * (xx[2] - xt[2]);
     } else if (lane == 16) {
       float xx[3];
-      spline_eval32(sx, th0, phi0, m, n, xx);
+      spline_eval32f(rc, 0, th0, phi0, m, n, xx);
       d2 = (xx[0] - xt[0]) * (xx[0] - xt[0]) + (xx[1] - xt[1]) * (xx[1] - xt[1]) + (xx[2] - xt[2]) * (xx[2] - xt[2]);
     }
     float d2c = __shfl_sync(0xffffffffu, d2, 16);
@@ -540,7 +560,7 @@ __device__ float projection_dist32(const double* sx, const double* sa, int m, in
     float thMin = acosf(yv[2]), phiMin = atan2f(yv[1] / nr, yv[0] / nr);
     if (phiMin < 0) phiMin += TWO_PI_F;
     float xMin[3];
-    spline_eval32(sx, thMin, phiMin, m, n, xMin);
+    spline_eval32f(rc, 0, thMin, phiMin, m, n, xMin);
     float d2Min = (xMin[0] - xt[0]) * (xMin[0] - xt[0]) + (xMin[1] - xt[1]) * (xMin[1] - xt[1]) +
                   (xMin[2] - xt[2]) * (xMin[2] - xt[2]);
     if (d2Min > d2c) break;
@@ -549,7 +569,7 @@ __device__ float projection_dist32(const double* sx, const double* sa, int m, in
     h = 0.5f * h;
   }
   float a30[3];
-  spline_eval32(sa, th0, phi0, m, n, a30);
+  spline_eval32f(rc, 12, th0, phi0, m, n, a30);
   return a30[0] * (xt[0] - x0[0]) + a30[1] * (xt[1] - x0[1]) + a30[2] * (xt[2] - x0[2]);
 }
 
@@ -605,8 +625,8 @@ __global__ void __launch_bounds__(128) k_near_replay(CorrArgs a, const int* __re
     size_t q0;
     item_geometry(a, item, x0, xt, q0);
     const double msz = a.meshSize[cell];
-    const float d32 = projection_dist32(set_ptr(a, cell, SPL_X), set_ptr(a, cell, SPL_A3), a.m, a.nlon, xt,
-                                        a.th[item.z], a.phi[item.w]);
+    const float d32 = projection_dist32(a.rep + (size_t)cell * a.m * a.nlon * 24, a.m, a.nlon, xt, a.th[item.z],
+                                        a.phi[item.w]);
     if ((double)d32 > 2.3 * msz) continue;
     if (lane == 0) out[atomicAdd(nout, 1ull)] = idx;
   }
@@ -656,7 +676,8 @@ __global__ void __launch_bounds__(128) k_near(CorrArgs a) {
       // (2) FP32 replay of the projection, margin 0.3*meshSize
       else {
         if (lane == 0) atomicAdd(a.cnt + 8, 1ull);
-        if ((double)projection_dist32(sx, set_ptr(a, cell, SPL_A3), a.m, a.nlon, xt, th0, phi0) > 2.3 * msz)
+        if ((double)projection_dist32(a.rep + (size_t)cell * a.m * a.nlon * 24, a.m, a.nlon, xt, th0, phi0) >
+            2.3 * msz)
           skip = true;
       }
       if (skip && !a.verify) continue;
@@ -699,6 +720,23 @@ __global__ void __launch_bounds__(128) k_near(CorrArgs a) {
       double iA = 1.0 / a.tA[t];
       for (int k = 0; k < 3; ++k) atomicAdd(a.v + t + (size_t)k * a.nt, dv[k] * iA);
     }
+  }
+}
+
+// The FP32 replay's node records: x and a3 of every spline node in FP32,
+// rounded once here instead of at every interpolation (the double-to-float
+// conversions kept the replay on GB300's FP64 pipe: 1.42 -> 1.17 ms for the
+// near-singular stage at 256 cells, the same decisions).
+__global__ void k_rep_rec(long long nn, int per, const double* __restrict__ spl, float* __restrict__ rep) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nn) return;
+  const long long cell = q / per, node = q - cell * per;
+  const double* sx = spl + ((cell * SPL_NSET + SPL_X) * per + node) * SPL_NODE;
+  const double* sa = spl + ((cell * SPL_NSET + SPL_A3) * per + node) * SPL_NODE;
+  float* o = rep + q * 24;
+  for (int k = 0; k < 12; ++k) {
+    o[k] = (float)sx[k];
+    o[12 + k] = (float)sa[k];
   }
 }
 
@@ -922,6 +960,17 @@ rbc3d_status run_near_corr(rbc3d_ctx* ctx, int tlist, double c1, double c2, int 
   a.nlist = nullptr;
   int nsm = 0, per_sm = 0;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);
+  if (a.screen) {  // the FP32 replay reads x and a3 from FP32 node records
+    const int per = ctx->m * ctx->nlon;
+    const long long nn = (long long)ctx->ncell * per;
+    if (!ctx->rep_valid || ctx->rep_rec.n < (size_t)nn * 24) {
+      CUDA_TRY(ctx->rep_rec.alloc((size_t)nn * 24));
+      { k_rep_rec<<<(int)((nn + 255) / 256), 256, 0, ctx->st>>>(nn, per, ctx->spl.p, ctx->rep_rec.p); ++ctx->launches; }
+      CUDA_TRY(cudaGetLastError());
+      ctx->rep_valid = true;
+    }
+    a.rep = ctx->rep_rec.p;
+  }
   if (a.screen && !a.verify) {
     // FP32 modes: geometric screen per thread, FP32 replay per warp, then the
     // FP64 pass on what is left (counters: dcnt[8] replays, dcnt[10] listed)
@@ -934,10 +983,10 @@ rbc3d_status run_near_corr(rbc3d_ctx* ctx, int tlist, double c1, double c2, int 
     a.list = ctx->near_l2.p;
     a.nlist = ctx->dcnt.p + 10;
   }
-  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_near, 128, 0));
   CUDA_TRY(ctx->near_queue.alloc(1));
   CUDA_TRY(cudaMemsetAsync(ctx->near_queue.p, 0, sizeof(unsigned long long), ctx->st));
   a.queue = ctx->near_queue.p;
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_near, 128, 0));
   { k_near<<<nsm * std::max(per_sm, 1), 128, 0, ctx->st>>>(a); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());
   return RBC3D_OK;

@@ -271,6 +271,7 @@ rbc3d_status self_mixed_grid(rbc3d_ctx* ctx, const std::vector<double>& thG, con
 // FP32 node records and target positions for the current geometry.
 rbc3d_status self_mixed_geom(rbc3d_ctx* ctx) {
   self_ff_invalidate(ctx, true, false, false);
+  ctx->rep_valid = false;  // the near pass's FP32 replay records follow the geometry
   const int nv = ctx->nlat * ctx->nlon;
   // cell centres (mean of the grid points) from the uploaded positions
   CUDA_TRY(ctx->mix_xc.alloc(3 * (size_t)ctx->ncell));
