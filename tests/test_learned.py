@@ -189,7 +189,7 @@ def test_spectral_preconditioner(gpu):
     random pairs span every mode's block, A M is the identity up to the PME
     mesh's translation error and the solve takes a few iterations where the
     plain solve takes over a hundred (measured: 1 against 126)."""
-    from rbc3d_gb300.abi import Context
+    from rbc3d_gb300.abi import FP32M, FP64, Context
     from rbc3d_gb300.learned import WallGuess
     prm, cells, wall = G.config("C3", ncell=2)
     ctx = Context(gpu, prm)
@@ -201,10 +201,10 @@ def test_spectral_preconditioner(gpu):
     rng = np.random.default_rng(11)
     zero = np.zeros((3, wall.nvert))
 
-    def solve(mode):
+    def solve(mode, prec=FP64):
         ctx.set_wall_density(zero)
-        st, code = ctx.no_slip_wall(1e-8, 900, 300, check=False, guess_mode=mode)
-        assert code == 0 and st.converged == 1 and st.rnorm <= 1e-8 * st.bnorm, mode
+        st, code = ctx.no_slip_wall(1e-8, 900, 300, prec=prec, check=False, guess_mode=mode)
+        assert code == 0 and st.converged == 1 and st.rnorm <= 1e-8 * st.bnorm, (mode, prec)
         return st.iterations
 
     plain = solve(0)
@@ -216,9 +216,13 @@ def test_spectral_preconditioner(gpu):
     nb, _ = wg.basis_sizes()
     assert nb.min() == blk
     full = solve(5)
-    print(f"plain {plain} its, preconditioned with 10 pairs {partial}, with {blk} pairs {full}")
+    # the mixed-precision solve (FP32M operator inside FP64 refinement) with the
+    # same preconditioner reaches the same FP64 residual
+    mixed = solve(5, FP32M)
+    print(f"plain {plain} its, preconditioned with 10 pairs {partial}, with {blk} pairs {full}, mixed {mixed}")
     assert partial <= 1.1 * plain
     assert full <= 6 and full * 20 <= plain
+    assert mixed <= 10
     wg.mlp.close()
     ctx.close()
 
