@@ -388,7 +388,10 @@ def headline_roofline(r, s_d, targets):
     tpath = os.path.join(HERE, "profiles", "traffic.json")
     if os.path.exists(tpath):
         try:
-            roof["traffic"] = json.load(open(tpath))[key]["bytes_per_target"] * targets
+            rec = json.load(open(tpath))[key]
+            roof["traffic"] = rec["bytes_per_target"] * targets
+            if "ncu_pipes" in rec:
+                roof["ncu_pipes"] = rec["ncu_pipes"]
         except Exception:
             pass
     return roof
