@@ -29,6 +29,7 @@ struct CorrArgs {
   unsigned long long* queue;  // k_near's item counter
   const SelfW64* W64;         // k_self: tabulated patch weights (uniform longitudes), or null
   const int* list;            // k_near: items to process (indices), or null for all
+  long long list_start;       // k_near over a list: its first entry (the staged pass takes those before)
   const float* rep;           // k_near_replay: x and a3 node values in FP32, 24 floats a node
   const unsigned long long* nlist;
   const double* th;
@@ -649,8 +650,8 @@ __global__ void __launch_bounds__(128) k_near(CorrArgs a) {
       it = (long long)__shfl_sync(0xffffffffu, g0, 0);
       it_end = it + GRAB;
     }
-    if (it >= (long long)nitem) break;
-    const long long cur = it++;
+    if (it + a.list_start >= (long long)nitem) break;
+    const long long cur = a.list_start + it++;
     int4 item = a.items[a.list ? a.list[cur] : cur];
     int t = item.x, cell = item.y - 1, ilat0 = item.z, ilon0 = item.w;
     if (cell < 0 || cell >= a.ncell) continue;
@@ -721,6 +722,140 @@ __global__ void __launch_bounds__(128) k_near(CorrArgs a) {
       for (int k = 0; k < 3; ++k) atomicAdd(a.v + t + (size_t)k * a.nt, dv[k] * iA);
     }
   }
+}
+
+// The FP32 modes' FP64 pass over their short list, staged so that its work
+// spreads evenly over the SMs: with one warp per item the pass waited on its
+// slowest items.  (1) k_near_proj, one warp per item: the projection and the
+// correction test; (2) k_near_units, one warp per quadrature (the first
+// re-adds of every item, then the second ones, then the subtracts), each
+// keeping its warp sum; (3) k_near_fin, one thread per item: the combination
+// of RBC_NearSingInt (ModRbcSingInt.F90:103-160) in the order k_near uses, so the
+// sums are k_near's.  Entries past NEAR_STAGE_CAP go through k_near.
+constexpr int NEAR_STAGE_CAP = 65536;
+struct NearPlan {
+  double th0, phi0, x0[3], xt[3], a30[3], dist, dist1;
+  int t, cell, two, ok;
+};
+static_assert(sizeof(NearPlan) <= 16 * sizeof(double), "plan slot");
+
+__device__ __forceinline__ long long near_stage_count(const CorrArgs& a) {
+  unsigned long long n = *a.nlist;
+  if (n > (unsigned long long)a.cap) n = a.cap;
+  if (n > (unsigned long long)NEAR_STAGE_CAP) n = NEAR_STAGE_CAP;
+  return (long long)n;
+}
+
+__global__ void __launch_bounds__(128) k_near_proj(CorrArgs a, NearPlan* __restrict__ plan) {
+  const int lane = threadIdx.x & 31;
+  const long long n = near_stage_count(a);
+  for (;;) {
+    unsigned long long g0 = 0;
+    if (lane == 0) g0 = atomicAdd(a.queue, 1ull);
+    const long long cur = (long long)__shfl_sync(0xffffffffu, g0, 0);
+    if (cur >= n) break;
+    NearPlan P{};
+    const int4 item = a.items[a.list[cur]];
+    const int t = item.x, cell = item.y - 1, ilat0 = item.z, ilon0 = item.w;
+    if (cell >= 0 && cell < a.ncell) {
+      double th0 = a.th[ilat0], phi0 = a.phi[ilon0];
+      const size_t q0 = (size_t)cell * a.nlat * a.nlon + (size_t)ilon0 * a.nlat + ilat0;
+      double x0[3], xt[3];
+      for (int k = 0; k < 3; ++k) {
+        x0[k] = a.x[q0 + (size_t)k * a.npt];
+        double xx = a.tx[t + (size_t)k * a.nt] - x0[k];
+        xx = xx - round(xx * a.iL[k]) * a.L[k];
+        xt[k] = x0[k] + xx;
+      }
+      if (lane == 0) atomicAdd(a.cnt + 9, 1ull);
+      find_projection(set_ptr(a, cell, SPL_X), a.m, a.nlon, xt, th0, phi0, x0);
+      SplW W;
+      double a30[3];
+      spline_weights(th0, phi0, a.m, a.nlon, W);
+      spline_eval(set_ptr(a, cell, SPL_A3), W, 3, a30);
+      const double dist = a30[0] * (xt[0] - x0[0]) + a30[1] * (xt[1] - x0[1]) + a30[2] * (xt[2] - x0[2]);
+      if (!(dist > 2 * a.meshSize[cell])) {
+        if (lane == 0) atomicAdd(a.cnt + 3, 1ull);
+        const double sizePat = a.radius * sqrt(a.area[cell] / (4 * RBC3D_PI));
+        P.dist = dist;
+        P.dist1 = copysign(fabs(0.01 * sizePat), dist);
+        P.two = fabs(dist) < fabs(P.dist1) ? 1 : 0;
+        P.th0 = th0;
+        P.phi0 = phi0;
+        for (int k = 0; k < 3; ++k) {
+          P.x0[k] = x0[k];
+          P.xt[k] = xt[k];
+          P.a30[k] = a30[k];
+        }
+        P.t = t;
+        P.cell = cell;
+        P.ok = 1;
+      }
+    }
+    if (lane == 0) plan[cur] = P;
+  }
+}
+
+__global__ void __launch_bounds__(128) k_near_units(CorrArgs a, const NearPlan* __restrict__ plan,
+                                                    double* __restrict__ part, unsigned long long* __restrict__ queue) {
+  const int lane = threadIdx.x & 31;
+  const long long n = near_stage_count(a);
+  for (;;) {
+    unsigned long long g0 = 0;
+    if (lane == 0) g0 = atomicAdd(queue, 1ull);
+    const long long u = (long long)__shfl_sync(0xffffffffu, g0, 0);
+    if (u >= 3 * n) break;
+    const long long i = u % n;
+    // kind 0: re-add at xt (at xi1 when the target is within dist1);
+    // kind 1: re-add at x0 (only then); kind 2: subtract
+    const int kind = (int)(u / n);
+    const NearPlan P = plan[i];
+    if (!P.ok || (kind == 1 && !P.two)) continue;
+    const double c2 = a.c2 * a.Bc[a.celltype[P.cell]];
+    double dv[3];
+    if (kind == 0) {
+      double xi1[3];
+      for (int k = 0; k < 3; ++k) xi1[k] = P.x0[k] + P.dist1 * P.a30[k];
+      near_readd(a, P.cell, a.c1, c2, P.two ? xi1 : P.xt, P.x0, P.th0, P.phi0, a.radius, dv);
+    } else if (kind == 1) {
+      near_readd(a, P.cell, a.c1, c2, P.x0, P.x0, P.th0, P.phi0, a.radius, dv);
+    } else {
+      near_subtract(a, P.cell, a.c1, c2, P.xt, P.th0, P.phi0, a.radius, a.rthr, dv);
+    }
+    if (lane == 0) {
+      const int o = kind == 2 ? 0 : (kind == 0 ? 3 : 6);
+      for (int k = 0; k < 3; ++k) part[9 * i + o + k] = dv[k];
+    }
+  }
+}
+
+__global__ void k_near_fin(CorrArgs a, const NearPlan* __restrict__ plan, const double* __restrict__ part) {
+  const long long n = near_stage_count(a);
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const NearPlan& P = plan[i];
+  if (!P.ok) return;
+  const double* S = part + 9 * i;
+  double dv[3] = {S[0], S[1], S[2]};
+  if (!P.two) {
+    for (int k = 0; k < 3; ++k) dv[k] += S[3 + k];
+  } else {
+    const double c2 = a.c2 * a.Bc[a.celltype[P.cell]];
+    double dv1[3] = {S[3], S[4], S[5]}, dv0[3] = {S[6], S[7], S[8]};
+    if (c2 != 0.) {
+      SplW W;
+      double dJ0[3], g0[3];
+      spline_weights(P.th0, P.phi0, a.m, a.nlon, W);
+      spline_eval(set_ptr(a, P.cell, SPL_DJ), W, 1, dJ0);
+      spline_eval(set_ptr(a, P.cell, SPL_G), W, 3, g0);
+      for (int k = 0; k < 3; ++k) g0[k] = g0[k] / dJ0[0];
+      for (int k = 0; k < 3; ++k)
+        dv0[k] = (P.dist > 0) ? dv0[k] + c2 * 4 * RBC3D_PI * g0[k] : dv0[k] - c2 * 4 * RBC3D_PI * g0[k];
+    }
+    for (int k = 0; k < 3; ++k) dv[k] += dv0[k] + P.dist / P.dist1 * (dv1[k] - dv0[k]);
+  }
+  const double iA = 1.0 / a.tA[P.t];
+  for (int k = 0; k < 3; ++k) atomicAdd(a.v + P.t + (size_t)k * a.nt, dv[k] * iA);
 }
 
 // The FP32 replay's node records: x and a3 of every spline node in FP32,
@@ -983,9 +1118,26 @@ rbc3d_status run_near_corr(rbc3d_ctx* ctx, int tlist, double c1, double c2, int 
     a.list = ctx->near_l2.p;
     a.nlist = ctx->dcnt.p + 10;
   }
-  CUDA_TRY(ctx->near_queue.alloc(1));
-  CUDA_TRY(cudaMemsetAsync(ctx->near_queue.p, 0, sizeof(unsigned long long), ctx->st));
+  CUDA_TRY(ctx->near_queue.alloc(2));
+  CUDA_TRY(cudaMemsetAsync(ctx->near_queue.p, 0, 2 * sizeof(unsigned long long), ctx->st));
   a.queue = ctx->near_queue.p;
+  a.list_start = 0;
+  if (a.list) {  // the staged pass over the list's first NEAR_STAGE_CAP entries
+    CUDA_TRY(ctx->near_plan.alloc((size_t)NEAR_STAGE_CAP * 16));
+    CUDA_TRY(ctx->near_part.alloc((size_t)NEAR_STAGE_CAP * 9));
+    NearPlan* plan = reinterpret_cast<NearPlan*>(ctx->near_plan.p);
+    int ps = 0, us = 0;
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ps, k_near_proj, 128, 0));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&us, k_near_units, 128, 0));
+    { k_near_proj<<<nsm * std::max(ps, 1), 128, 0, ctx->st>>>(a, plan); ++ctx->launches; }
+    { k_near_units<<<nsm * std::max(us, 1), 128, 0, ctx->st>>>(a, plan, ctx->near_part.p, ctx->near_queue.p + 1);
+      ++ctx->launches; }
+    { k_near_fin<<<NEAR_STAGE_CAP / 128, 128, 0, ctx->st>>>(a, plan, ctx->near_part.p); ++ctx->launches; }
+    CUDA_TRY(cudaGetLastError());
+    // entries past the staged pass's capacity: k_near from there
+    a.list_start = NEAR_STAGE_CAP;
+    CUDA_TRY(cudaMemsetAsync(ctx->near_queue.p, 0, sizeof(unsigned long long), ctx->st));
+  }
   CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_near, 128, 0));
   { k_near<<<nsm * std::max(per_sm, 1), 128, 0, ctx->st>>>(a); ++ctx->launches; }
   CUDA_TRY(cudaGetLastError());

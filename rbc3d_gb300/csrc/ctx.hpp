@@ -208,6 +208,7 @@ struct rbc3d_ctx {
   DBuf<float> mtab32;                   // 1 - mask, FP32
   DBuf<int> near_l1, near_l2;           // near-singular candidates after the screen / the FP32 replay
   DBuf<float> rep_rec;                  // the FP32 replay's node values: x and a3, 4 slots each (24 floats a node)
+  DBuf<double> near_plan, near_part;    // the staged near pass: per-item plans, per-quadrature warp sums
   bool rep_valid = false;               // rep_rec matches the current geometry
   float erfcx_q[16] = {0};   // FP32 erfc fit of the pair kernel
   double erfcx_X = -1.0;
