@@ -50,8 +50,10 @@ struct TargetSet {
   DBuf<int4> meta;      // (surf, ilat, ilon, 0); surf 1-based, -1 for raw
   DBuf<int> order;      // sorted position -> target index
   DBuf<int> cstart, cend;
-  DBuf<int4> units;     // (hash cell, first sorted position, count, 0)
+  DBuf<int4> units;     // (hash cell, first sorted position, count, 0): up to TILE targets (FP64 pair sums)
   int nunits = 0;
+  DBuf<int4> wunits;    // the same with up to 32 targets, one per warp (FP32 pair sums)
+  int nwunits = 0;
   bool sorted = false;
   DBuf<double> v;       // 3n accumulator of the current matvec
   DBuf<double> v2;      // 3n accumulator of the stages on the side stream

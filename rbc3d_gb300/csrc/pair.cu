@@ -6,11 +6,15 @@
 // [start, end) ranges per cell.  The same Nc = max(floor(L/rc), 3) cells are
 // used, so a target visits its 27 neighbour cells exactly as the reference.
 //
-// Pair kernels: one CTA per unit (target cell, <= 128 targets; units of a
-// cell equal-sized, heaviest units launched first); the 27 neighbour cells
-// are streamed through shared memory in tiles of 128 sources, each thread
-// owning one target.  Tiles whose bounding box lies farther than rc from the
-// CTA's (or a warp's) targets are skipped.  FP32: sources carry hi/lo FP32
+// Pair kernels: work units of one target cell's targets (a cell's units
+// equal-sized, heaviest units launched first), each thread owning one
+// target; the 27 neighbour cells are streamed through shared memory.  FP64:
+// one CTA per unit of <= 128 targets, tiles of 128 sources shared by the
+// CTA.  FP32: one warp per unit of <= 32 targets, each warp staging its own
+// 32-source chunks, so the four warps of a CTA may serve different cells
+// (CTA-sized units left 18% of the CTAs' thread slots idle on the 256-cell
+// workload, warp units 5%).  Tiles whose bounding box lies farther than rc
+// from the CTA's (or a warp's) targets are skipped.  FP32: sources carry hi/lo FP32
 // coordinates relative to their own cell centre (from FP64, once per
 // position update) and the targets are shifted into each neighbour cell's
 // frame with an error-free difference, so x_j - x_i keeps full FP32 accuracy
@@ -76,14 +80,15 @@ __global__ void k_fill_pieces(int nc, const int* __restrict__ cs, const int* __r
 }
 
 // Work units of the pair sums (the cells' targets in equal-sized units of at
-// most TILE), keyed by their work: targets x the sources of the 27
+// most `tile`), keyed by their work: targets x the sources of the 27
 // neighbour cells.  Unit counts first, then the units at the scanned offsets.
-__global__ void k_unit_counts(int nc, const int* __restrict__ cs, const int* __restrict__ ce, int* __restrict__ cnt) {
+__global__ void k_unit_counts(int nc, int tile, const int* __restrict__ cs, const int* __restrict__ ce,
+                              int* __restrict__ cnt) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c > nc) return;
-  cnt[c] = c < nc ? (ce[c] - cs[c] + TILE - 1) / TILE : 0;
+  cnt[c] = c < nc ? (ce[c] - cs[c] + tile - 1) / tile : 0;
 }
-__global__ void k_fill_units(int nc, int Nc0, int Nc1, int Nc2, const int* __restrict__ cs, const int* __restrict__ ce,
+__global__ void k_fill_units(int nc, int tile, int Nc0, int Nc1, int Nc2, const int* __restrict__ cs, const int* __restrict__ ce,
                              const int* __restrict__ ss, const int* __restrict__ se, const int* __restrict__ off,
                              int cap, int4* __restrict__ units, long long* __restrict__ key, int* __restrict__ idx) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -98,7 +103,7 @@ __global__ void k_fill_units(int nc, int Nc0, int Nc1, int Nc2, const int* __res
         const int q = ni + Nc0 * (nj + Nc1 * nk);
         nsrc += se[q] - ss[q];
       }
-      const int k = (cnt + TILE - 1) / TILE, per = (cnt + k - 1) / k;
+      const int k = (cnt + tile - 1) / tile, per = (cnt + k - 1) / k;
       int u = off[c];
       for (int b = 0; b < cnt; b += per, ++u) {
         const int m = min(per, cnt - b);
@@ -246,6 +251,7 @@ struct PairArgs {
   const int4* tmeta;
   const int* torder;
   const int4* units;
+  int nunits;  // k_pair32: warp units
   double* v;  // 3*nt accumulator
   // sources (sorted)
   int ns;
@@ -411,14 +417,16 @@ __device__ __forceinline__ float2 ld2(const float* p, int j) { return *reinterpr
 template <bool DL>
 __global__ void __launch_bounds__(TILE, 6) k_pair32(PairArgs a) {
   __shared__ __align__(16) ChunkX2<DL> s_ch[TILE / 32];
-  const int4 unit = a.units[blockIdx.x];
-  const int cell = unit.x;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  if (wid * 32 >= unit.z) return;  // no targets for this warp
-  const bool active = tid < unit.z;
+  const int wu = blockIdx.x * (TILE / 32) + wid;  // this warp's unit
+  if (wu >= a.nunits) return;
+  const int4 unit = a.units[wu];
+  if (unit.z == 0) return;  // the empty tail
+  const int cell = unit.x;
+  const bool active = lane < unit.z;
   const int ci = cell % a.Nc[0], cj = (cell / a.Nc[0]) % a.Nc[1], ck = cell / (a.Nc[0] * a.Nc[1]);
   const double c0[3] = {(ci + 0.5) * a.h[0], (cj + 0.5) * a.h[1], (ck + 0.5) * a.h[2]};
-  int ti = active ? a.torder[unit.y + tid] : 0;
+  int ti = active ? a.torder[unit.y + lane] : 0;
   float th_[3] = {0, 0, 0}, tl_[3] = {0, 0, 0};
   float4 ui = make_float4(0, 0, 0, 0);
   int surf_i = -2, tlat = 0, tlon = 0;
@@ -832,15 +840,41 @@ rbc3d_status scan_counts(rbc3d_ctx* ctx, int nc, const int* cnt, int* off) {
   return RBC3D_OK;
 }
 
-rbc3d_status make_units(rbc3d_ctx* ctx, TargetSet& t, const DBuf<int>& cs, const DBuf<int>& ce) {
+// The units of `tile` targets at most into `units` (cap entries, the empty
+// tail last): per-cell counts, their scan, the units, a stable sort by work.
+rbc3d_status fill_units(rbc3d_ctx* ctx, const DBuf<int>& cs, const DBuf<int>& ce, const int* ss, const int* se,
+                        int tile, int cap, DBuf<int4>& units) {
   const int nc = ctx->hg.ncells;
-  // capacity: every non-empty cell gives at most count / TILE + 1 units
-  const int cap = nc + (t.n + TILE - 1) / TILE;
   rbc3d_status s;
   DBuf<int>& cnt = ctx->unit_cnt;
   CUDA_TRY(cnt.alloc(nc + 1)); CUDA_TRY(ctx->unit_off.alloc(nc + 1));
-  CUDA_TRY(ctx->unit_tmp.alloc(cap)); CUDA_TRY(t.units.alloc(cap));
+  CUDA_TRY(ctx->unit_tmp.alloc(cap)); CUDA_TRY(units.alloc(cap));
   CUDA_TRY(ctx->unit_key.alloc(2 * (size_t)cap)); CUDA_TRY(ctx->unit_idx.alloc(2 * (size_t)cap));
+  const int g1 = nblk(nc + 1, 256);
+  { k_unit_counts<<<g1, 256, 0, ctx->st>>>(nc, tile, cs.p, ce.p, cnt.p); ++ctx->launches; }
+  if ((s = scan_counts(ctx, nc, cnt.p, ctx->unit_off.p))) return s;
+  long long* key = ctx->unit_key.p;
+  int* idx = ctx->unit_idx.p;
+  { k_fill_units<<<g1, 256, 0, ctx->st>>>(nc, tile, ctx->hg.Nc[0], ctx->hg.Nc[1], ctx->hg.Nc[2], cs.p, ce.p, ss, se,
+                                          ctx->unit_off.p, cap, ctx->unit_tmp.p, key, idx); ++ctx->launches; }
+  // heaviest units first, so the last wave holds the light ones; the radix
+  // sort is stable, so equal work keeps cell order (as a stable host sort);
+  // the empty tail (key -1) stays last
+  size_t tmp = 0;
+  cub::DeviceRadixSort::SortPairsDescending(nullptr, tmp, key, key + cap, idx, idx + cap, cap, 0, 64, ctx->st);
+  DBuf<char>& tb = ctx->sort_tmp;
+  CUDA_TRY(tb.alloc(tmp + 1));
+  CUDA_TRY(cub::DeviceRadixSort::SortPairsDescending(tb.p, tmp, key, key + cap, idx, idx + cap, cap, 0, 64, ctx->st));
+  { k_gather_units<<<nblk(cap, 256), 256, 0, ctx->st>>>(cap, idx + cap, ctx->unit_tmp.p, units.p); ++ctx->launches; }
+  CUDA_TRY(cudaGetLastError());
+  return RBC3D_OK;
+}
+
+rbc3d_status make_units(rbc3d_ctx* ctx, TargetSet& t, const DBuf<int>& cs, const DBuf<int>& ce) {
+  const int nc = ctx->hg.ncells;
+  // capacity: every non-empty cell gives at most count / tile + 1 units
+  const int cap = nc + (t.n + TILE - 1) / TILE, wcap = nc + (t.n + 31) / 32;
+  rbc3d_status s;
   // sources per cell: the source list's ranges (or the targets' own when
   // there is no source list)
   const bool src = ctx->npt > 0 && ctx->s_cstart.p;
@@ -851,24 +885,13 @@ rbc3d_status make_units(rbc3d_ctx* ctx, TargetSet& t, const DBuf<int>& cs, const
     CUDA_TRY(cudaMemsetAsync(ctx->unit_zero.p, 0, sizeof(int) * nc, ctx->st));
     ss = se = ctx->unit_zero.p;
   }
-  const int g1 = nblk(nc + 1, 256);
-  { k_unit_counts<<<g1, 256, 0, ctx->st>>>(nc, cs.p, ce.p, cnt.p); ++ctx->launches; }
-  if ((s = scan_counts(ctx, nc, cnt.p, ctx->unit_off.p))) return s;
-  long long* key = ctx->unit_key.p;
-  int* idx = ctx->unit_idx.p;
-  { k_fill_units<<<g1, 256, 0, ctx->st>>>(nc, ctx->hg.Nc[0], ctx->hg.Nc[1], ctx->hg.Nc[2], cs.p, ce.p, ss, se,
-                                          ctx->unit_off.p, cap, ctx->unit_tmp.p, key, idx); ++ctx->launches; }
-  // heaviest units first, so the last wave holds the light ones; the radix
-  // sort is stable, so equal work keeps cell order (as a stable host sort);
-  // the empty tail (key -1) stays last
-  size_t tmp = 0;
-  cub::DeviceRadixSort::SortPairsDescending(nullptr, tmp, key, key + cap, idx, idx + cap, cap, 0, 64, ctx->st);
-  DBuf<char>& tb = ctx->sort_tmp;
-  CUDA_TRY(tb.alloc(tmp + 1));
-  CUDA_TRY(cub::DeviceRadixSort::SortPairsDescending(tb.p, tmp, key, key + cap, idx, idx + cap, cap, 0, 64, ctx->st));
-  { k_gather_units<<<nblk(cap, 256), 256, 0, ctx->st>>>(cap, idx + cap, ctx->unit_tmp.p, t.units.p); ++ctx->launches; }
-  CUDA_TRY(cudaGetLastError());
+  // block units (FP64 pair sums: the block shares its source tiles) and
+  // warp units (FP32 pair sums: each warp stages its own chunks, so a block's
+  // warps may come from different cells and none idles)
+  if ((s = fill_units(ctx, cs, ce, ss, se, TILE, cap, t.units))) return s;
+  if ((s = fill_units(ctx, cs, ce, ss, se, 32, wcap, t.wunits))) return s;
   t.nunits = cap;
+  t.nwunits = wcap;
   return RBC3D_OK;
 }
 
@@ -1047,8 +1070,11 @@ rbc3d_status run_pair_sum(rbc3d_ctx* ctx, int tlist, double c1, double c2, int p
     a.sF4 = ctx->s_F4.p; a.sG4 = ctx->s_G4.p;
     { k_src_dens4<<<nblk(ctx->npt, 256), 256, 0, ctx->st>>>(ctx->npt, c1, c2, ctx->s_f.p, ctx->s_g.p, dl ? 1 : 0,
                                                              ctx->s_F4.p, ctx->s_G4.p); ++ctx->launches; }
-    if (dl) { k_pair32<true><<<t.nunits, TILE, 0, ctx->st>>>(a); ++ctx->launches; }
-    else { k_pair32<false><<<t.nunits, TILE, 0, ctx->st>>>(a); ++ctx->launches; }
+    a.units = t.wunits.p;
+    a.nunits = t.nwunits;
+    const int nb = (t.nwunits + TILE / 32 - 1) / (TILE / 32);
+    if (dl) { k_pair32<true><<<nb, TILE, 0, ctx->st>>>(a); ++ctx->launches; }
+    else { k_pair32<false><<<nb, TILE, 0, ctx->st>>>(a); ++ctx->launches; }
   } else {
     if (dl) { k_pair64<true><<<t.nunits, TILE, 0, ctx->st>>>(a); ++ctx->launches; }
     else { k_pair64<false><<<t.nunits, TILE, 0, ctx->st>>>(a); ++ctx->launches; }

@@ -9,21 +9,24 @@
 //     Oishi, "Accurate sum and dot product", SIAM J. Sci. Comput. 26, 2005):
 //     each product w v split exactly by the FMA form of TwoProduct, the high
 //     parts summed error-free, the rounding errors and the lo-part cross
-//     terms summed in FP32.  The 12 derivative terms come first, from a
-//     power of two `off` at least twice a bound on their sum of |w v| (the
-//     per-cell maxima of the derivative values times the weight-sum bounds
-//     h/4 and h^2/16), so every partial sum stays above every product in
-//     magnitude and Dekker's FastTwoSum (3 operations) is exact where
-//     Knuth's TwoSum takes 6; off is then subtracted exactly and the 4 value
-//     terms are added with TwoSum;
+//     terms summed in FP32.  The sums start from a power of two `off` at
+//     least twice a bound on their sum of |w v| (the per-cell maxima of the
+//     node values times the weight-sum bounds 1, h/4 and h^2/16), so every
+//     partial sum stays above every product in magnitude and Dekker's
+//     FastTwoSum (3 operations) is exact where Knuth's TwoSum takes 6; off
+//     is subtracted exactly at the end.  The FP32 correction term is rounded
+//     on the scale of off, so for the position x, whose interpolant is
+//     differenced against the target, the bound covers the 12 derivative
+//     terms only: off is subtracted before the 4 value terms, which are
+//     added with TwoSum (all 16 from the larger offset: the corrections
+//     move from 2.3e-12 to 2.3e-11 of the FP64 patch);
 //   * the Ewald kernel (EwaldCoeff_SL / _DL, ModEwaldFunc.F90:86-180, the
 //     same tables as hi/lo) is evaluated with Dekker's float-float product
 //     and sum, and 1/r by rsqrtf, an FP32 Newton step and a float-float
 //     Newton step.
-// The patch corrections agree with the FP64 kernel to 2.3e-12 relative
+// The patch corrections agree with the FP64 kernel to a few 1e-12 relative
 // (rel-L2, 256-cell workload); the interpolation sums carry errors of a few
-// 1e-12 of sum |w v| (the FP32 correction term is rounded on the scale of
-// the FastTwoSum offset).
+// 1e-12 of sum |w v| (x) or of the cell's maxima (f, g, a3).
 //
 // Data layout.  Per node and slot d (u, u_th, u_ph, u_thph) the 12 values x
 // (relative to the cell centre), f and g density sets and a3 (three
@@ -192,7 +195,8 @@ __device__ __forceinline__ ff dot3(const ff* a, const ff* b) {
 
 // One target of the own-cell patch: warp index w (cell, latitude ring,
 // longitude), its grid point p, position, DL factor, record base and the
-// starting offsets of the derivative-term sums of its cell.
+// starting offsets of its cell's sums (x: the derivative terms'; f, g, a3:
+// all 16 terms').
 struct Tgt {
   int p, cell, ilat0, ilon0;
   ff xi[3];
@@ -214,16 +218,20 @@ __device__ __forceinline__ Tgt target(const FFArgs& a, int w) {
   T.xi[0] = {th4.x, tl4.x}; T.xi[1] = {th4.y, tl4.y}; T.xi[2] = {th4.z, tl4.z};
   T.c2m = DL ? a.c2B[a.celltype[T.cell]] : ff{0.f, 0.f};
   T.base = a.rec + (size_t)T.cell * FF_PLANES * a.map.per;
-  float off[4];
+  float off[4], offd[2];
 #pragma unroll
   for (int s = 0; s < 4; ++s) {
     const uint4 b = __ldg(a.bnd + (size_t)s * a.ncell + T.cell);
-    const float B = 1.01f * (a.hq1 * __uint_as_float(b.y) + a.hq2 * __uint_as_float(b.z) + a.hq12 * __uint_as_float(b.w));
+    const float Bd = a.hq1 * __uint_as_float(b.y) + a.hq2 * __uint_as_float(b.z) + a.hq12 * __uint_as_float(b.w);
     int e;
-    frexpf(2.f * B, &e);  // 2 B < 2^e
+    frexpf(2.f * 1.01f * (__uint_as_float(b.x) + Bd), &e);  // 2 B < 2^e
     off[s] = ldexpf(1.f, e);
+    if (s < 2) {  // x, and f where it shares a pair with x
+      frexpf(2.f * 1.01f * Bd, &e);
+      offd[s] = ldexpf(1.f, e);
+    }
   }
-  T.offs[0] = make_float2(off[0], off[0]); T.offs[1] = make_float2(off[0], off[1]);
+  T.offs[0] = make_float2(offd[0], offd[0]); T.offs[1] = make_float2(offd[0], offd[1]);
   T.offs[2] = make_float2(off[1], off[1]); T.offs[3] = make_float2(off[2], off[2]);
   T.offs[4] = make_float2(off[2], off[3]); T.offs[5] = make_float2(off[3], off[3]);
   return T;
@@ -233,6 +241,7 @@ __device__ __forceinline__ Tgt target(const FFArgs& a, int w) {
 template <bool SL, bool DL>
 __device__ __forceinline__ void patch_point(const FFArgs& a, const Tgt& T, int q, ffacc* acc) {
   constexpr int NP = DL ? 6 : 3;  // value pairs per slot: (x.x x.y) (x.z f.x) (f.y f.z) | (g.x g.y) (g.z a.x) (a.y a.z)
+  constexpr int NX = 2;           // the pairs that hold x: value terms by TwoSum
   const size_t per = (size_t)a.map.per;
   const size_t plane = (size_t)a.nlat * a.NQ;
   const size_t wi = (size_t)T.ilat0 * a.NQ + q;
@@ -243,13 +252,14 @@ __device__ __forceinline__ void patch_point(const FFArgs& a, const Tgt& T, int q
   Dot2 d2[NP];
 #pragma unroll
   for (int k = 0; k < NP; ++k) { d2[k].s = T.offs[k]; d2[k].c = make_float2(0.f, 0.f); }
-  // slots u_th, u_ph, u_thph first (FastTwoSum from off), then u (TwoSum)
+  // slots u_th, u_ph, u_thph first (FastTwoSum from off), then u (the x
+  // pairs: off subtracted, TwoSum; the others: FastTwoSum, off subtracted after)
 #pragma unroll
   for (int dd = 0; dd < 4; ++dd) {
     const int d = (dd + 1) & 3;
     if (d == 0) {
 #pragma unroll
-      for (int k = 0; k < NP; ++k) d2[k].s = sub2(d2[k].s, T.offs[k]);  // exact: off/2 <= s <= 3 off/2
+      for (int k = 0; k < NX; ++k) d2[k].s = sub2(d2[k].s, T.offs[k]);  // exact: off/2 <= s <= 3 off/2
     }
     const float4 wh4 = __ldg(a.w + d * plane + wi), wl4 = __ldg(a.w + (4 + d) * plane + wi);
     const float whs[4] = {wh4.x, wh4.y, wh4.z, wh4.w}, wls[4] = {wl4.x, wl4.y, wl4.z, wl4.w};
@@ -268,11 +278,13 @@ __device__ __forceinline__ void patch_point(const FFArgs& a, const Tgt& T, int q
       }
 #pragma unroll
       for (int i = 0; i < NP; ++i) {
-        if (d == 0) d2[i].add<false>(wh, nwh, wl, vh[i], vl[i]);
+        if (d == 0 && i < NX) d2[i].add<false>(wh, nwh, wl, vh[i], vl[i]);
         else d2[i].add<true>(wh, nwh, wl, vh[i], vl[i]);
       }
     }
   }
+#pragma unroll
+  for (int k = NX; k < NP; ++k) d2[k].s = sub2(d2[k].s, T.offs[k]);
   // interpolated x (relative to the cell centre), f, g, a3
   ff xx[3], F[3], G[3], A[3];
   xx[0] = ff_sub(d2[0].x(), T.xi[0]);
