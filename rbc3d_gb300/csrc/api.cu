@@ -395,6 +395,8 @@ rbc3d_status rbc3d_create(const rbc3d_params* prm, rbc3d_ctx** out) {
   {
     const char* e = getenv("RBC3D_VERIFY_SCREEN");
     ctx->verify_screen = e && e[0] == '1';
+    const char* c = getenv("RBC3D_NEAR_STAGE_CAP");  // a smaller capacity sends the rest through k_near
+    if (c && *c) ctx->near_stage_cap = std::max(0, std::min(atoi(c), NEAR_STAGE_CAP));
   }
   for (int d = 0; d < 3; ++d) ctx->iLb[d] = 1. / prm->Lb[d];
   for (int l = 0; l < prm->ncelltypes; ++l) {  // initCOEFs, ModConf.F90:327-344

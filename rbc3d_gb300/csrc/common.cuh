@@ -9,6 +9,7 @@
 #define RBC3D_I_2PI (1.0 / RBC3D_TWO_PI)
 #define EWALD_NTAB 8192  // Ntable, ModEwaldFunc.F90:9
 #define MASK_NTAB 8192   // MaskFunc table size, ModBasicMath.F90:356
+#define NEAR_STAGE_CAP 65536  // list entries of the FP32 modes' staged near-singular pass
 
 // Number of doubles per spline node per variable set: 4 kinds (u, u1, u2,
 // u12) x 3 variables.  Sets: x, a3, FdetJ, GdetJ, detJ (detJ uses var 0).

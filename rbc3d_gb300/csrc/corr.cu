@@ -30,6 +30,7 @@ struct CorrArgs {
   const SelfW64* W64;         // k_self: tabulated patch weights (uniform longitudes), or null
   const int* list;            // k_near: items to process (indices), or null for all
   long long list_start;       // k_near over a list: its first entry (the staged pass takes those before)
+  int stage_cap;              // the staged pass: entries it takes from the list's head
   const float* rep;           // k_near_replay: x and a3 node values in FP32, 24 floats a node
   const unsigned long long* nlist;
   const double* th;
@@ -731,8 +732,8 @@ __global__ void __launch_bounds__(128) k_near(CorrArgs a) {
 // re-adds of every item, then the second ones, then the subtracts), each
 // keeping its warp sum; (3) k_near_fin, one thread per item: the combination
 // of RBC_NearSingInt (ModRbcSingInt.F90:103-160) in the order k_near uses, so the
-// sums are k_near's.  Entries past NEAR_STAGE_CAP go through k_near.
-constexpr int NEAR_STAGE_CAP = 65536;
+// sums are k_near's.  Entries past its capacity (NEAR_STAGE_CAP, or less when
+// RBC3D_NEAR_STAGE_CAP asks for it) go through k_near.
 struct NearPlan {
   double th0, phi0, x0[3], xt[3], a30[3], dist, dist1;
   int t, cell, two, ok;
@@ -742,7 +743,7 @@ static_assert(sizeof(NearPlan) <= 16 * sizeof(double), "plan slot");
 __device__ __forceinline__ long long near_stage_count(const CorrArgs& a) {
   unsigned long long n = *a.nlist;
   if (n > (unsigned long long)a.cap) n = a.cap;
-  if (n > (unsigned long long)NEAR_STAGE_CAP) n = NEAR_STAGE_CAP;
+  if (n > (unsigned long long)a.stage_cap) n = a.stage_cap;
   return (long long)n;
 }
 
@@ -1122,9 +1123,10 @@ rbc3d_status run_near_corr(rbc3d_ctx* ctx, int tlist, double c1, double c2, int 
   CUDA_TRY(cudaMemsetAsync(ctx->near_queue.p, 0, 2 * sizeof(unsigned long long), ctx->st));
   a.queue = ctx->near_queue.p;
   a.list_start = 0;
-  if (a.list) {  // the staged pass over the list's first NEAR_STAGE_CAP entries
-    CUDA_TRY(ctx->near_plan.alloc((size_t)NEAR_STAGE_CAP * 16));
-    CUDA_TRY(ctx->near_part.alloc((size_t)NEAR_STAGE_CAP * 9));
+  a.stage_cap = std::max(0, std::min(ctx->near_stage_cap, NEAR_STAGE_CAP));
+  if (a.list && a.stage_cap > 0) {  // the staged pass over the list's first stage_cap entries
+    CUDA_TRY(ctx->near_plan.alloc((size_t)a.stage_cap * 16));
+    CUDA_TRY(ctx->near_part.alloc((size_t)a.stage_cap * 9));
     NearPlan* plan = reinterpret_cast<NearPlan*>(ctx->near_plan.p);
     int ps = 0, us = 0;
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ps, k_near_proj, 128, 0));
@@ -1132,10 +1134,10 @@ rbc3d_status run_near_corr(rbc3d_ctx* ctx, int tlist, double c1, double c2, int 
     { k_near_proj<<<nsm * std::max(ps, 1), 128, 0, ctx->st>>>(a, plan); ++ctx->launches; }
     { k_near_units<<<nsm * std::max(us, 1), 128, 0, ctx->st>>>(a, plan, ctx->near_part.p, ctx->near_queue.p + 1);
       ++ctx->launches; }
-    { k_near_fin<<<NEAR_STAGE_CAP / 128, 128, 0, ctx->st>>>(a, plan, ctx->near_part.p); ++ctx->launches; }
+    { k_near_fin<<<(a.stage_cap + 127) / 128, 128, 0, ctx->st>>>(a, plan, ctx->near_part.p); ++ctx->launches; }
     CUDA_TRY(cudaGetLastError());
     // entries past the staged pass's capacity: k_near from there
-    a.list_start = NEAR_STAGE_CAP;
+    a.list_start = a.stage_cap;
     CUDA_TRY(cudaMemsetAsync(ctx->near_queue.p, 0, sizeof(unsigned long long), ctx->st));
   }
   CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_near, 128, 0));

@@ -280,6 +280,7 @@ struct rbc3d_ctx {
   // stage timers: event pairs recorded around each stage, read on demand
   bool prof = false;
   bool verify_screen = false;  // RBC3D_VERIFY_SCREEN=1: check near-singular screens in FP64
+  int near_stage_cap = NEAR_STAGE_CAP;  // RBC3D_NEAR_STAGE_CAP: list entries of the staged near pass
   long long launches = 0;  // kernels of this library launched on the context
   std::vector<cudaEvent_t> evpool;
   std::vector<int> rec_stage;

@@ -84,6 +84,30 @@ def test_near_screen_agrees_with_fp64(gpu, sldl_case, monkeypatch):
     assert cnt["screen_misses"] == 0 and cnt["nearsing_items"] > 0
 
 
+@pytest.mark.parametrize("cap", ["0", "7"])
+def test_near_stage_capacity(gpu, sldl_case, monkeypatch, cap):
+    """The FP32 modes' FP64 pass over their short list runs staged
+    (projections, one warp per quadrature, combination) up to a capacity and
+    through the one-warp-per-item kernel past it.  With the capacity cut to 0
+    or 7 entries (RBC3D_NEAR_STAGE_CAP) every entry is still taken once: the
+    same projection and correction counts, and per target the same
+    corrections up to the order of the accumulation."""
+    prm, cells = sldl_case
+    g = setup(gpu, prm, cells, True)
+    ref = g.matvec(TLIST_RBC, C, C, TERM_CORR, FP32D)
+    cref = g.counts()
+    g.close()
+    monkeypatch.setenv("RBC3D_NEAR_STAGE_CAP", cap)
+    h = setup(gpu, prm, cells, True)
+    v = h.matvec(TLIST_RBC, C, C, TERM_CORR, FP32D)
+    cnt = h.counts()
+    h.close()
+    assert cref["near_projections"] > 7 and cref["nearsing_items"] > 0
+    assert cnt["near_projections"] == cref["near_projections"]
+    assert cnt["nearsing_items"] == cref["nearsing_items"]
+    assert np.abs(v - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
 def test_l2_entry_points_compose(gpu, sldl_case):
     """AddIntOnRbcs + PME_* called separately equal the composite matvec."""
     prm, cells = sldl_case
