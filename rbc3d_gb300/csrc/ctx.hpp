@@ -202,6 +202,8 @@ struct rbc3d_ctx {
   DBuf<float4> s_p0, s_p1, s_u4, s_a4, s_F4, s_G4;
   DBuf<int> s_toff, s_coff;
   DBuf<float4> s_tbox, s_cbox;  // per 128-source tile and per 32-source chunk
+  DBuf<float4> s_op0, s_op1;    // own-cell pair records in point order (k_pair_own32)
+  DBuf<int> s_inv;              // point -> sorted source position
   int s_ntiles = 0;
   DBuf<unsigned long long> near_queue;  // work counter of the near-singular kernel
   DBuf<double> dBcoef;                  // Bcoef per cell type on the device

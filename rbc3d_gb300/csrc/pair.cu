@@ -14,7 +14,11 @@
 // 32-source chunks, so the four warps of a CTA may serve different cells
 // (CTA-sized units left 18% of the CTAs' thread slots idle on the 256-cell
 // workload, warp units 5%).  Tiles whose bounding box lies farther than rc
-// from the CTA's (or a warp's) targets are skipped.  FP32: sources carry hi/lo FP32
+// from the CTA's (or a warp's) targets are skipped.  FP32 with cell targets:
+// the own-cell pairs (79% of the pairs on the 256-cell workload) go to a
+// dense per-cell pass (k_pair_own32), and k_pair32 skips the target's own
+// surface (whole tiles and chunks when a warp's targets share one surface).
+// FP32: sources carry hi/lo FP32
 // coordinates relative to their own cell centre (from FP64, once per
 // position update) and the targets are shifted into each neighbour cell's
 // frame with an error-free difference, so x_j - x_i keeps full FP32 accuracy
@@ -24,6 +28,7 @@
 #include <cub/cub.cuh>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <vector>
 
@@ -177,15 +182,18 @@ __global__ void k_src_records(int n, const double* __restrict__ sx, const int4* 
 }
 
 // Bounding box of each tile (TILE consecutive sources of one cell), from the
-// hi coordinates; tiles listed as (first source, count).
+// hi coordinates, with the range of the sources' surfaces in w (int bits);
+// tiles listed as (first source, count).
 __global__ void k_tile_boxes(const int2* __restrict__ tiles, const float4* __restrict__ p0, float4* __restrict__ box) {
   const int2 t = tiles[blockIdx.x];
   const float big = 3.0e38f;
   float3 lo = make_float3(big, big, big), hi = make_float3(-big, -big, -big);
+  int smin = INT_MAX, smax = INT_MIN;
   for (int i = threadIdx.x; i < t.y; i += blockDim.x) {
     const float4 p = p0[t.x + i];
     lo.x = fminf(lo.x, p.x); lo.y = fminf(lo.y, p.y); lo.z = fminf(lo.z, p.z);
     hi.x = fmaxf(hi.x, p.x); hi.y = fmaxf(hi.y, p.y); hi.z = fmaxf(hi.z, p.z);
+    smin = min(smin, __float_as_int(p.w)); smax = max(smax, __float_as_int(p.w));
   }
   for (int o = 16; o > 0; o >>= 1) {
     lo.x = fminf(lo.x, __shfl_xor_sync(0xffffffffu, lo.x, o));
@@ -194,19 +202,45 @@ __global__ void k_tile_boxes(const int2* __restrict__ tiles, const float4* __res
     hi.x = fmaxf(hi.x, __shfl_xor_sync(0xffffffffu, hi.x, o));
     hi.y = fmaxf(hi.y, __shfl_xor_sync(0xffffffffu, hi.y, o));
     hi.z = fmaxf(hi.z, __shfl_xor_sync(0xffffffffu, hi.z, o));
+    smin = min(smin, __shfl_xor_sync(0xffffffffu, smin, o));
+    smax = max(smax, __shfl_xor_sync(0xffffffffu, smax, o));
   }
   __shared__ float3 red[32][2];
+  __shared__ int sred[32][2];
   const int w = threadIdx.x >> 5;
-  if ((threadIdx.x & 31) == 0) { red[w][0] = lo; red[w][1] = hi; }
+  if ((threadIdx.x & 31) == 0) { red[w][0] = lo; red[w][1] = hi; sred[w][0] = smin; sred[w][1] = smax; }
   __syncthreads();
   if (threadIdx.x == 0) {
     for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
       lo.x = fminf(lo.x, red[k][0].x); lo.y = fminf(lo.y, red[k][0].y); lo.z = fminf(lo.z, red[k][0].z);
       hi.x = fmaxf(hi.x, red[k][1].x); hi.y = fmaxf(hi.y, red[k][1].y); hi.z = fmaxf(hi.z, red[k][1].z);
+      smin = min(smin, sred[k][0]); smax = max(smax, sred[k][1]);
     }
-    box[2 * blockIdx.x] = make_float4(lo.x, lo.y, lo.z, 0.f);
-    box[2 * blockIdx.x + 1] = make_float4(hi.x, hi.y, hi.z, 0.f);
+    box[2 * blockIdx.x] = make_float4(lo.x, lo.y, lo.z, __int_as_float(smin));
+    box[2 * blockIdx.x + 1] = make_float4(hi.x, hi.y, hi.z, __int_as_float(smax));
   }
+}
+
+// Point-order records of the own-cell pair sums: hi/lo FP32 of the position
+// relative to the cell's first point (minimum image: a cell spans less than
+// half the box), the grid indices, and the point's sorted source position.
+__global__ void k_own_records(int n, int nlat, int nv, const double* __restrict__ x, const int* __restrict__ order,
+                              double L0, double L1, double L2, float4* __restrict__ op0, float4* __restrict__ op1,
+                              int* __restrict__ sinv) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) sinv[order[q]] = q;
+  const int p = q;
+  if (p >= n) return;
+  const int cell = p / nv, r = p - cell * nv;
+  const double L[3] = {L0, L1, L2};
+  float hi[3], lo[3];
+  for (int k = 0; k < 3; ++k) {
+    const double d = min_image(x[p + (size_t)k * n] - x[(size_t)cell * nv + (size_t)k * n], L[k], 1.0 / L[k]);
+    hi[k] = (float)d;
+    lo[k] = (float)(d - (double)hi[k]);
+  }
+  op0[p] = make_float4(hi[0], hi[1], hi[2], __int_as_float((r % nlat) | ((r / nlat) << 16)));
+  op1[p] = make_float4(lo[0], lo[1], lo[2], 0.f);
 }
 
 // c1 f dS and c2 g dS Bcoef of the sorted sources in FP32 (per call).
@@ -298,6 +332,12 @@ struct PairArgs {
   int4* items;
   int cap;
   unsigned long long* cnt;  // [0] items, [1] pairs, [2] overflow
+  // own-cell pairs of the FP32 modes (cell targets, same-cell weight table):
+  // k_pair_own32 takes them and k_pair32 skips same-surface sources
+  int own_split;
+  const float4* op0;  // per point (point order): (x, y, z) hi relative to its cell's first point, id bits
+  const float4* op1;  // lo
+  const int* sinv;    // point -> sorted source position
 };
 
 
@@ -394,6 +434,54 @@ struct ChunkX2 {
 __device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
 __device__ __forceinline__ float2 ld2(const float* p, int j) { return *reinterpret_cast<const float2*>(p + j); }
 
+// The Ewald real-space kernels (EwaldCoeff_SL / EwaldCoeff_DL,
+// ModEwaldFunc.F90:86-180) of two sources at once in packed FP32x2
+// arithmetic, added to (cx, cy, cz) with the weights wa, wb: pair vectors
+// (xx, yy, zz) with squares r2 (a source of weight 0 enters with r^2 = 1),
+// the sources' c1 f dS (f*), c2 g dS Bcoef (g*) and normals (n*).
+template <bool DL>
+__device__ __forceinline__ void ewald_pair2(const PairArgs& a, float2 xx, float2 yy, float2 zz, float2 r2, float wa,
+                                            float wb, float2 fx, float2 fy, float2 fz, float2 gx, float2 gy, float2 gz,
+                                            float2 nx, float2 ny, float2 nz, float& cx, float& cy, float& cz) {
+  const float2 sqpa2 = f2(a.sqpa_f, a.sqpa_f), half2 = f2(0.5f, 0.5f), one2 = f2(1.f, 1.f);
+  const float2 tisqa2 = f2(a.two_isqa_f, a.two_isqa_f);
+  const float2 rs = f2(wa != 0.f ? r2.x : 1.f, wb != 0.f ? r2.y : 1.f);
+  const float2 rinv = f2(rsqrtf(rs.x), rsqrtf(rs.y));
+  const float2 r = __fmul2_rn(rs, rinv);
+  const float2 st = __fmul2_rn(r, sqpa2);
+  const float2 ex = f2(__expf(-st.x * st.x), __expf(-st.y * st.y));
+  const float2 den = __ffma2_rn(half2, st, one2);
+  const float2 tq = f2(__fdividef(1.f, den.x), __fdividef(1.f, den.y));
+  float2 Q = f2(a.erfcx_q[ERFCX_DEG], a.erfcx_q[ERFCX_DEG]);
+#pragma unroll
+  for (int k = ERFCX_DEG - 1; k >= 0; --k) Q = __ffma2_rn(Q, tq, f2(a.erfcx_q[k], a.erfcx_q[k]));
+  const float2 c1 = __fmul2_rn(ex, __fmul2_rn(tq, Q)), c2 = __fmul2_rn(tisqa2, ex);
+  const float2 ir2 = __fmul2_rn(rinv, rinv);
+  const float2 c1r = __fmul2_rn(c1, rinv);
+  const float2 A = __fmul2_rn(__fadd2_rn(c1r, c2), ir2);
+  const float2 B = __fadd2_rn(c1r, f2(-c2.x, -c2.y));
+  const float2 Ad = __fmul2_rn(A, __ffma2_rn(xx, fx, __ffma2_rn(yy, fy, __fmul2_rn(zz, fz))));
+  float2 vx = __ffma2_rn(Ad, xx, __fmul2_rn(B, fx));
+  float2 vy = __ffma2_rn(Ad, yy, __fmul2_rn(B, fy));
+  float2 vz = __ffma2_rn(Ad, zz, __fmul2_rn(B, fz));
+  if (DL) {
+    const float2 st2 = __fmul2_rn(st, st);
+    const float2 cdl = __fmul2_rn(f2(a.m8_ispi_f, a.m8_ispi_f),
+                                  __ffma2_rn(ex, __fmul2_rn(st, __fadd2_rn(f2(1.5f, 1.5f), st2)),
+                                             __fmul2_rn(f2(a.q75_spi_f, a.q75_spi_f), c1)));
+    const float2 Adl = __fmul2_rn(__fmul2_rn(cdl, __fmul2_rn(ir2, ir2)), rinv);
+    const float2 dg = __ffma2_rn(xx, gx, __ffma2_rn(yy, gy, __fmul2_rn(zz, gz)));
+    const float2 da = __ffma2_rn(xx, nx, __ffma2_rn(yy, ny, __fmul2_rn(zz, nz)));
+    const float2 t = __fmul2_rn(__fmul2_rn(Adl, dg), da);
+    vx = __ffma2_rn(t, xx, vx);
+    vy = __ffma2_rn(t, yy, vy);
+    vz = __ffma2_rn(t, zz, vz);
+  }
+  cx = fmaf(wb, vx.y, fmaf(wa, vx.x, cx));
+  cy = fmaf(wb, vy.y, fmaf(wa, vy.x, cy));
+  cz = fmaf(wb, vz.y, fmaf(wa, vz.x, cz));
+}
+
 // FP32 real-space pair sums (EwaldCoeff_SL / EwaldCoeff_DL of ModEwaldFunc
 // over the 27 neighbour hash cells, AddIntOnRbcs ModIntOnRbcs.F90:25-160).
 // One CTA per (hash cell, up to TILE targets).  Sources carry FP32 hi/lo
@@ -456,9 +544,13 @@ __global__ void __launch_bounds__(TILE, 6) k_pair32(PairArgs a) {
   int run_surf = -3, run_id = -1;
   float run_d2 = 3.4e38f;
   unsigned npairs = 0;  // < 2^32 pairs per target
-  // Ewald constants as packed pairs
-  const float2 sqpa2 = f2(a.sqpa_f, a.sqpa_f), half2 = f2(0.5f, 0.5f), one2 = f2(1.f, 1.f);
-  const float2 tisqa2 = f2(a.two_isqa_f, a.two_isqa_f);
+  // own-cell pairs left to k_pair_own32: the warp's surface when all its
+  // targets share one (whole tiles and chunks of it are skipped), else -7
+  int wsurf = -7;
+  if (a.own_split) {
+    const int s0 = __shfl_sync(0xffffffffu, surf_i, 0);
+    wsurf = __all_sync(0xffffffffu, !active || surf_i == s0) ? s0 : -7;
+  }
 
   // per-source bookkeeping in source order: neighbour-surface runs, the pair
   // count, the weight (0 when the pair does not contribute here)
@@ -522,12 +614,14 @@ __global__ void __launch_bounds__(TILE, 6) k_pair32(PairArgs a) {
     for (int base = sbeg, tt = t0; base < send; base += TILE, ++tt) {
       const float4 blo = a.tbox[2 * tt], bhi = a.tbox[2 * tt + 1];
       if (boxes_apart(wlo, whi, make_float3(blo.x, blo.y, blo.z), make_float3(bhi.x, bhi.y, bhi.z), a.rc2_f)) continue;
+      if (__float_as_int(blo.w) == wsurf && __float_as_int(bhi.w) == wsurf) continue;  // own cell only
       const int tend = min(base + TILE, send);
       for (int cb = base, cc = a.coff[ncell] + (base - sbeg) / 32; cb < tend; cb += 32, ++cc) {
         {
           const float4 clo4 = a.cbox[2 * cc], chi4 = a.cbox[2 * cc + 1];
           if (boxes_apart(wlo, whi, make_float3(clo4.x, clo4.y, clo4.z), make_float3(chi4.x, chi4.y, chi4.z), a.rc2_f))
             continue;  // uniform over the warp
+          if (__float_as_int(clo4.w) == wsurf && __float_as_int(chi4.w) == wsurf) continue;  // own cell only
         }
         const int cnt = min(32, tend - cb);
         __syncwarp();
@@ -552,8 +646,9 @@ __global__ void __launch_bounds__(TILE, 6) k_pair32(PairArgs a) {
           const float2 hx = __fadd2_rn(ld2(C.hx, j), nth0), hy = __fadd2_rn(ld2(C.hy, j), nth1),
                        hz = __fadd2_rn(ld2(C.hz, j), nth2);
           const float2 h2 = __ffma2_rn(hx, hx, __ffma2_rn(hy, hy, __fmul2_rn(hz, hz)));
-          bool oka = h2.x <= a.rc2_loose, okb = h2.y <= a.rc2_loose;
           const int sa = C.surf[j], sb = C.surf[j + 1];
+          bool oka = h2.x <= a.rc2_loose && !(a.own_split && sa == surf_i);
+          bool okb = h2.y <= a.rc2_loose && !(a.own_split && sb == surf_i);
           if (!(oka || okb)) continue;
           const float2 xx = __fadd2_rn(hx, __fadd2_rn(ld2(C.lx, j), ntl0));
           const float2 yy = __fadd2_rn(hy, __fadd2_rn(ld2(C.ly, j), ntl1));
@@ -564,48 +659,14 @@ __global__ void __launch_bounds__(TILE, 6) k_pair32(PairArgs a) {
           const float wa = weight(sa, C.id[j], r2.x, oka, cb + j);
           const float wb = weight(sb, C.id[j + 1], r2.y, okb, cb + j + 1);
           if (wa == 0.f && wb == 0.f) continue;
-          const float2 rs = f2(wa != 0.f ? r2.x : 1.f, wb != 0.f ? r2.y : 1.f);
-          const float2 rinv = f2(rsqrtf(rs.x), rsqrtf(rs.y));
-          const float2 r = __fmul2_rn(rs, rinv);
-          const float2 st = __fmul2_rn(r, sqpa2);
-          const float2 ex = f2(__expf(-st.x * st.x), __expf(-st.y * st.y));
-          const float2 den = __ffma2_rn(half2, st, one2);
-          const float2 tq = f2(__fdividef(1.f, den.x), __fdividef(1.f, den.y));
-          float2 Q = f2(a.erfcx_q[ERFCX_DEG], a.erfcx_q[ERFCX_DEG]);
-#pragma unroll
-          for (int k = ERFCX_DEG - 1; k >= 0; --k) Q = __ffma2_rn(Q, tq, f2(a.erfcx_q[k], a.erfcx_q[k]));
-          const float2 c1 = __fmul2_rn(ex, __fmul2_rn(tq, Q)), c2 = __fmul2_rn(tisqa2, ex);
-          const float2 ir2 = __fmul2_rn(rinv, rinv);
-          const float2 c1r = __fmul2_rn(c1, rinv);
-          const float2 A = __fmul2_rn(__fadd2_rn(c1r, c2), ir2);
-          const float2 B = __fadd2_rn(c1r, f2(-c2.x, -c2.y));
-          const float2 fx = ld2(C.fx, j), fy = ld2(C.fy, j), fz = ld2(C.fz, j);
-          const float2 Ad = __fmul2_rn(A, __ffma2_rn(xx, fx, __ffma2_rn(yy, fy, __fmul2_rn(zz, fz))));
-          float2 vx = __ffma2_rn(Ad, xx, __fmul2_rn(B, fx));
-          float2 vy = __ffma2_rn(Ad, yy, __fmul2_rn(B, fy));
-          float2 vz = __ffma2_rn(Ad, zz, __fmul2_rn(B, fz));
-          if (DL) {
-            const float2 st2 = __fmul2_rn(st, st);
-            const float2 cdl = __fmul2_rn(f2(a.m8_ispi_f, a.m8_ispi_f),
-                                          __ffma2_rn(ex, __fmul2_rn(st, __fadd2_rn(f2(1.5f, 1.5f), st2)),
-                                                     __fmul2_rn(f2(a.q75_spi_f, a.q75_spi_f), c1)));
-            const float2 Adl = __fmul2_rn(__fmul2_rn(cdl, __fmul2_rn(ir2, ir2)), rinv);
-            const float2 gx = ld2(C.gx, j), gy = ld2(C.gy, j), gz = ld2(C.gz, j);
-            const float2 ax = ld2(C.ax, j), ay = ld2(C.ay, j), az = ld2(C.az, j);
-            const float2 dg = __ffma2_rn(xx, gx, __ffma2_rn(yy, gy, __fmul2_rn(zz, gz)));
-            const float2 da = __ffma2_rn(xx, ax, __ffma2_rn(yy, ay, __fmul2_rn(zz, az)));
-            const float2 t = __fmul2_rn(__fmul2_rn(Adl, dg), da);
-            vx = __ffma2_rn(t, xx, vx);
-            vy = __ffma2_rn(t, yy, vy);
-            vz = __ffma2_rn(t, zz, vz);
-          }
-          cx = fmaf(wb, vx.y, fmaf(wa, vx.x, cx));
-          cy = fmaf(wb, vy.y, fmaf(wa, vy.x, cy));
-          cz = fmaf(wb, vz.y, fmaf(wa, vz.x, cz));
+          const float2 z2 = f2(0.f, 0.f);
+          ewald_pair2<DL>(a, xx, yy, zz, r2, wa, wb, ld2(C.fx, j), ld2(C.fy, j), ld2(C.fz, j),
+                          DL ? ld2(C.gx, j) : z2, DL ? ld2(C.gy, j) : z2, DL ? ld2(C.gz, j) : z2,
+                          DL ? ld2(C.ax, j) : z2, DL ? ld2(C.ay, j) : z2, DL ? ld2(C.az, j) : z2, cx, cy, cz);
         }
         if (j < cnt) {  // the odd last source
           const float hx = C.hx[j] - tsh[0], hy = C.hy[j] - tsh[1], hz = C.hz[j] - tsh[2];
-          bool ok = hx * hx + hy * hy + hz * hz <= a.rc2_loose;
+          bool ok = hx * hx + hy * hy + hz * hz <= a.rc2_loose && !(a.own_split && C.surf[j] == surf_i);
           float xx = 0.f, yy = 0.f, zz = 0.f, r2 = 0.f;
           if (ok) {
             xx = __fadd_rn(hx, C.lx[j] - tsl[0]);
@@ -665,6 +726,112 @@ __global__ void __launch_bounds__(TILE, 6) k_pair32(PairArgs a) {
   unsigned long long np = npairs;
   for (int o = 16; o > 0; o >>= 1) np += __shfl_xor_sync(0xffffffffu, np, o);
   if ((tid & 31) == 0 && np) atomicAdd(a.cnt + 1, np);
+}
+
+// Own-cell pairs of the FP32 modes: the pairs of AddIntOnRbcs whose source
+// lies on the target's own cell with the weight 1 - MaskFunc of the same-cell
+// table (ModIntOnRbcs.F90:77-80).  Every point of a biconcave cell lies
+// within rc of every other (79% of the pairs within rc on the 256-cell
+// workload), so per cell this is a dense all-pairs pass: the cell's points
+// stream through shared memory in tiles of OWN_TILE, all threads reading the
+// same source (broadcast), each thread owning one target of a block of
+// OWN_TILE in ring-major order, whose at most OWN_ROWS latitude rings' rows
+// of the weight table are staged in shared memory.  No cell lists, culling
+// or neighbour bookkeeping; the pair arithmetic is k_pair32's (ewald_pair2),
+// positions hi/lo FP32 relative to the cell's first point, FP32 sums per
+// 32 sources, Kahan-compensated across them.  Adds to the accumulator after
+// k_pair32 on the same stream.
+constexpr int OWN_TILE = 128;
+template <bool DL>
+__global__ void __launch_bounds__(OWN_TILE) k_pair_own32(PairArgs a) {
+  __shared__ __align__(16) float s_src[15][OWN_TILE];  // hi xyz, lo xyz, f xyz, g xyz, normal xyz
+  __shared__ int s_id[OWN_TILE];
+  extern __shared__ float s_mask[];  // rows lat0.. of the table, nlat * nhalf each
+  const int nlat = a.nlat, nlon = a.nlon, nv = nlat * nlon, rowlen = nlat * a.nhalf;
+  const int bpc = (nv + OWN_TILE - 1) / OWN_TILE;
+  const int cell = blockIdx.x / bpc, b = blockIdx.x - cell * bpc;
+  const int k = b * OWN_TILE + threadIdx.x;  // ring-major index of the target in its cell
+  const bool active = k < nv;
+  const int tlat = active ? k / nlon : 0, tlon = active ? k - tlat * nlon : 0;
+  const int lat0 = b * OWN_TILE / nlon;
+  const int nrow = min(nlat - 1, (b * OWN_TILE + OWN_TILE - 1) / nlon) - lat0 + 1;
+  for (int i = threadIdx.x; i < nrow * rowlen; i += OWN_TILE) s_mask[i] = a.mtab32[(size_t)lat0 * rowlen + i];
+  const int p = cell * nv + tlon * nlat + tlat;  // the target's point index (= its target index)
+  float4 t0 = make_float4(0.f, 0.f, 0.f, 0.f), t1 = t0;
+  if (active) { t0 = a.op0[p]; t1 = a.op1[p]; }
+  const float2 nth0 = f2(-t0.x, -t0.x), nth1 = f2(-t0.y, -t0.y), nth2 = f2(-t0.z, -t0.z);
+  const float2 ntl0 = f2(-t1.x, -t1.x), ntl1 = f2(-t1.y, -t1.y), ntl2 = f2(-t1.z, -t1.z);
+  const float* mrow = s_mask + (tlat - lat0) * rowlen;
+  Kahan3 acc;
+  acc.zero();
+  unsigned npairs = 0;
+  const float2 z2 = f2(0.f, 0.f);
+  for (int base = 0; base < nv; base += OWN_TILE) {
+    __syncthreads();  // the previous tile is consumed
+    {
+      const int i = threadIdx.x, js = base + i;
+      if (js < nv) {
+        const int ps = cell * nv + js, q = a.sinv[ps];
+        const float4 q0 = a.op0[ps], q1 = a.op1[ps], f = a.sF4[q];
+        s_src[0][i] = q0.x; s_src[1][i] = q0.y; s_src[2][i] = q0.z;
+        s_src[3][i] = q1.x; s_src[4][i] = q1.y; s_src[5][i] = q1.z;
+        s_src[6][i] = f.x; s_src[7][i] = f.y; s_src[8][i] = f.z;
+        s_id[i] = __float_as_int(q0.w);
+        if (DL) {
+          const float4 g = a.sG4[q], an = a.sa4[q];
+          s_src[9][i] = g.x; s_src[10][i] = g.y; s_src[11][i] = g.z;
+          s_src[12][i] = an.x; s_src[13][i] = an.y; s_src[14][i] = an.z;
+        }
+      } else {  // padding: a source beyond rc of every target
+        for (int c = 0; c < 15; ++c) s_src[c][i] = 0.f;
+        s_src[0][i] = 1.0e18f;
+        s_id[i] = 0;
+      }
+    }
+    __syncthreads();
+    if (!active) continue;
+    const int cnt = min(OWN_TILE, nv - base);
+    for (int c0 = 0; c0 < cnt; c0 += 32) {
+      const int c1e = min(c0 + 32, (cnt + 1) & ~1);
+      float cx = 0.f, cy = 0.f, cz = 0.f;
+      for (int j = c0; j < c1e; j += 2) {
+        const float2 xx = __fadd2_rn(__fadd2_rn(ld2(s_src[0], j), nth0), __fadd2_rn(ld2(s_src[3], j), ntl0));
+        const float2 yy = __fadd2_rn(__fadd2_rn(ld2(s_src[1], j), nth1), __fadd2_rn(ld2(s_src[4], j), ntl1));
+        const float2 zz = __fadd2_rn(__fadd2_rn(ld2(s_src[2], j), nth2), __fadd2_rn(ld2(s_src[5], j), ntl2));
+        const float2 r2 = __ffma2_rn(xx, xx, __ffma2_rn(yy, yy, __fmul2_rn(zz, zz)));
+        const bool oka = r2.x <= a.rc2_f, okb = r2.y <= a.rc2_f;
+        npairs += (unsigned)oka + (unsigned)okb;
+        float wa = 0.f, wb = 0.f;
+        if (oka && !(r2.x < a.reps2_f)) {
+          const int id = s_id[j];
+          int dl = abs((id >> 16) - tlon);
+          dl = min(dl, nlon - dl);
+          wa = mrow[(id & 0xffff) * a.nhalf + dl];
+        }
+        if (okb && !(r2.y < a.reps2_f)) {
+          const int id = s_id[j + 1];
+          int dl = abs((id >> 16) - tlon);
+          dl = min(dl, nlon - dl);
+          wb = mrow[(id & 0xffff) * a.nhalf + dl];
+        }
+        if (wa == 0.f && wb == 0.f) continue;
+        ewald_pair2<DL>(a, xx, yy, zz, r2, wa, wb, ld2(s_src[6], j), ld2(s_src[7], j), ld2(s_src[8], j),
+                        DL ? ld2(s_src[9], j) : z2, DL ? ld2(s_src[10], j) : z2, DL ? ld2(s_src[11], j) : z2,
+                        DL ? ld2(s_src[12], j) : z2, DL ? ld2(s_src[13], j) : z2, DL ? ld2(s_src[14], j) : z2,
+                        cx, cy, cz);
+      }
+      acc.add(0, cx);
+      acc.add(1, cy);
+      acc.add(2, cz);
+    }
+  }
+  if (active) {
+    const double iA = 1.0 / a.tA[p];
+    for (int c = 0; c < 3; ++c) a.v[p + (size_t)c * a.nt] += ((double)acc.s[c] - (double)acc.c[c]) * iA;
+  }
+  unsigned long long np = npairs;
+  for (int o = 16; o > 0; o >>= 1) np += __shfl_xor_sync(0xffffffffu, np, o);
+  if ((threadIdx.x & 31) == 0 && np) atomicAdd(a.cnt + 1, np);
 }
 
 // FP64 plain form: the same traversal with the reference arithmetic.
@@ -956,6 +1123,10 @@ rbc3d_status build_source_list(rbc3d_ctx* ctx, bool with_normals) {
                                                      hg.Nc[0], hg.Nc[1], hg.Nc[2], hg.h[0], hg.h[1], hg.h[2], hg.L[0],
                                                      hg.L[1], hg.L[2], ctx->s_p0.p, ctx->s_p1.p, ctx->s_u4.p);
     ++ctx->launches;
+    CUDA_TRY(ctx->s_op0.alloc(n)); CUDA_TRY(ctx->s_op1.alloc(n)); CUDA_TRY(ctx->s_inv.alloc(n));
+    { k_own_records<<<nblk(n, 256), 256, 0, ctx->st>>>(n, ctx->nlat, ctx->nlat * ctx->nlon, ctx->x.p, ctx->s_order.p,
+                                                       hg.L[0], hg.L[1], hg.L[2], ctx->s_op0.p, ctx->s_op1.p,
+                                                       ctx->s_inv.p); ++ctx->launches; }
     CUDA_TRY(cudaGetLastError());
     const int nc = hg.ncells;
     // tiles of TILE and chunks of 32 consecutive sources of one cell, with
@@ -1072,10 +1243,31 @@ rbc3d_status run_pair_sum(rbc3d_ctx* ctx, int tlist, double c1, double c2, int p
                                                              ctx->s_F4.p, ctx->s_G4.p); ++ctx->launches; }
     a.units = t.wunits.p;
     a.nunits = t.nwunits;
+    // own-cell pairs of the cell targets by the dense pass when the
+    // same-cell weights come from the table (uniform longitudes)
+    const int nrow = std::min(ctx->nlat, (OWN_TILE - 1) / std::max(ctx->nlon, 1) + 2);
+    const size_t own_sm = sizeof(float) * (size_t)nrow * ctx->nlat * a.nhalf;
+    const bool own = tlist == RBC3D_TLIST_RBC && a.mtab32 && t.n == ctx->npt && ctx->s_op0.p && own_sm <= 160 * 1024;
+    a.own_split = own ? 1 : 0;
+    a.op0 = ctx->s_op0.p; a.op1 = ctx->s_op1.p; a.sinv = ctx->s_inv.p;
     const int nb = (t.nwunits + TILE / 32 - 1) / (TILE / 32);
     if (dl) { k_pair32<true><<<nb, TILE, 0, ctx->st>>>(a); ++ctx->launches; }
     else { k_pair32<false><<<nb, TILE, 0, ctx->st>>>(a); ++ctx->launches; }
+    if (own) {
+      const int nv = ctx->nlat * ctx->nlon, nbo = ctx->ncell * ((nv + OWN_TILE - 1) / OWN_TILE);
+      if (dl) {
+        if (own_sm > 48 * 1024)
+          CUDA_TRY(cudaFuncSetAttribute(k_pair_own32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)own_sm));
+        k_pair_own32<true><<<nbo, OWN_TILE, own_sm, ctx->st>>>(a);
+      } else {
+        if (own_sm > 48 * 1024)
+          CUDA_TRY(cudaFuncSetAttribute(k_pair_own32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)own_sm));
+        k_pair_own32<false><<<nbo, OWN_TILE, own_sm, ctx->st>>>(a);
+      }
+      ++ctx->launches;
+    }
   } else {
+    a.own_split = 0;
     if (dl) { k_pair64<true><<<t.nunits, TILE, 0, ctx->st>>>(a); ++ctx->launches; }
     else { k_pair64<false><<<t.nunits, TILE, 0, ctx->st>>>(a); ++ctx->launches; }
   }
