@@ -434,15 +434,14 @@ struct ChunkX2 {
 __device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
 __device__ __forceinline__ float2 ld2(const float* p, int j) { return *reinterpret_cast<const float2*>(p + j); }
 
-// The Ewald real-space kernels (EwaldCoeff_SL / EwaldCoeff_DL,
-// ModEwaldFunc.F90:86-180) of two sources at once in packed FP32x2
-// arithmetic, added to (cx, cy, cz) with the weights wa, wb: pair vectors
-// (xx, yy, zz) with squares r2 (a source of weight 0 enters with r^2 = 1),
-// the sources' c1 f dS (f*), c2 g dS Bcoef (g*) and normals (n*).
+// The coefficients of the Ewald real-space kernels (EwaldCoeff_SL /
+// EwaldCoeff_DL, ModEwaldFunc.F90:86-180) at two pair distances at once, in
+// packed FP32x2 arithmetic: the Stokeslet term A (x.f) x + B f and the
+// stresslet factor Adl of (x.g)(x.n) x, for squared distances r2 (a pair of
+// weight 0 enters with r^2 = 1, harmless).
 template <bool DL>
-__device__ __forceinline__ void ewald_pair2(const PairArgs& a, float2 xx, float2 yy, float2 zz, float2 r2, float wa,
-                                            float wb, float2 fx, float2 fy, float2 fz, float2 gx, float2 gy, float2 gz,
-                                            float2 nx, float2 ny, float2 nz, float& cx, float& cy, float& cz) {
+__device__ __forceinline__ void ewald_coef2(const PairArgs& a, float2 r2, float wa, float wb, float2& A, float2& B,
+                                            float2& Adl) {
   const float2 sqpa2 = f2(a.sqpa_f, a.sqpa_f), half2 = f2(0.5f, 0.5f), one2 = f2(1.f, 1.f);
   const float2 tisqa2 = f2(a.two_isqa_f, a.two_isqa_f);
   const float2 rs = f2(wa != 0.f ? r2.x : 1.f, wb != 0.f ? r2.y : 1.f);
@@ -458,18 +457,27 @@ __device__ __forceinline__ void ewald_pair2(const PairArgs& a, float2 xx, float2
   const float2 c1 = __fmul2_rn(ex, __fmul2_rn(tq, Q)), c2 = __fmul2_rn(tisqa2, ex);
   const float2 ir2 = __fmul2_rn(rinv, rinv);
   const float2 c1r = __fmul2_rn(c1, rinv);
-  const float2 A = __fmul2_rn(__fadd2_rn(c1r, c2), ir2);
-  const float2 B = __fadd2_rn(c1r, f2(-c2.x, -c2.y));
-  const float2 Ad = __fmul2_rn(A, __ffma2_rn(xx, fx, __ffma2_rn(yy, fy, __fmul2_rn(zz, fz))));
-  float2 vx = __ffma2_rn(Ad, xx, __fmul2_rn(B, fx));
-  float2 vy = __ffma2_rn(Ad, yy, __fmul2_rn(B, fy));
-  float2 vz = __ffma2_rn(Ad, zz, __fmul2_rn(B, fz));
+  A = __fmul2_rn(__fadd2_rn(c1r, c2), ir2);
+  B = __fadd2_rn(c1r, f2(-c2.x, -c2.y));
   if (DL) {
     const float2 st2 = __fmul2_rn(st, st);
     const float2 cdl = __fmul2_rn(f2(a.m8_ispi_f, a.m8_ispi_f),
                                   __ffma2_rn(ex, __fmul2_rn(st, __fadd2_rn(f2(1.5f, 1.5f), st2)),
                                              __fmul2_rn(f2(a.q75_spi_f, a.q75_spi_f), c1)));
-    const float2 Adl = __fmul2_rn(__fmul2_rn(cdl, __fmul2_rn(ir2, ir2)), rinv);
+    Adl = __fmul2_rn(__fmul2_rn(cdl, __fmul2_rn(ir2, ir2)), rinv);
+  }
+}
+
+// A (x.f) x + B f + Adl (x.g)(x.n) x for two pairs (DL: the last term)
+template <bool DL>
+__device__ __forceinline__ void ewald_apply2(float2 xx, float2 yy, float2 zz, float2 A, float2 B, float2 Adl,
+                                             float2 fx, float2 fy, float2 fz, float2 gx, float2 gy, float2 gz,
+                                             float2 nx, float2 ny, float2 nz, float2& vx, float2& vy, float2& vz) {
+  const float2 Ad = __fmul2_rn(A, __ffma2_rn(xx, fx, __ffma2_rn(yy, fy, __fmul2_rn(zz, fz))));
+  vx = __ffma2_rn(Ad, xx, __fmul2_rn(B, fx));
+  vy = __ffma2_rn(Ad, yy, __fmul2_rn(B, fy));
+  vz = __ffma2_rn(Ad, zz, __fmul2_rn(B, fz));
+  if (DL) {
     const float2 dg = __ffma2_rn(xx, gx, __ffma2_rn(yy, gy, __fmul2_rn(zz, gz)));
     const float2 da = __ffma2_rn(xx, nx, __ffma2_rn(yy, ny, __fmul2_rn(zz, nz)));
     const float2 t = __fmul2_rn(__fmul2_rn(Adl, dg), da);
@@ -477,6 +485,18 @@ __device__ __forceinline__ void ewald_pair2(const PairArgs& a, float2 xx, float2
     vy = __ffma2_rn(t, yy, vy);
     vz = __ffma2_rn(t, zz, vz);
   }
+}
+
+// The Ewald real-space kernels of two sources at once added to (cx, cy, cz)
+// with the weights wa, wb: pair vectors (xx, yy, zz) with squares r2, the
+// sources' c1 f dS (f*), c2 g dS Bcoef (g*) and normals (n*).
+template <bool DL>
+__device__ __forceinline__ void ewald_pair2(const PairArgs& a, float2 xx, float2 yy, float2 zz, float2 r2, float wa,
+                                            float wb, float2 fx, float2 fy, float2 fz, float2 gx, float2 gy, float2 gz,
+                                            float2 nx, float2 ny, float2 nz, float& cx, float& cy, float& cz) {
+  float2 A, B, Adl, vx, vy, vz;
+  ewald_coef2<DL>(a, r2, wa, wb, A, B, Adl);
+  ewald_apply2<DL>(xx, yy, zz, A, B, Adl, fx, fy, fz, gx, gy, gz, nx, ny, nz, vx, vy, vz);
   cx = fmaf(wb, vx.y, fmaf(wa, vx.x, cx));
   cy = fmaf(wb, vy.y, fmaf(wa, vy.x, cy));
   cz = fmaf(wb, vz.y, fmaf(wa, vz.x, cz));
@@ -732,106 +752,156 @@ __global__ void __launch_bounds__(TILE, 6) k_pair32(PairArgs a) {
 // lies on the target's own cell with the weight 1 - MaskFunc of the same-cell
 // table (ModIntOnRbcs.F90:77-80).  Every point of a biconcave cell lies
 // within rc of every other (79% of the pairs within rc on the 256-cell
-// workload), so per cell this is a dense all-pairs pass: the cell's points
-// stream through shared memory in tiles of OWN_TILE, all threads reading the
-// same source (broadcast), each thread owning one target of a block of
-// OWN_TILE in ring-major order, whose at most OWN_ROWS latitude rings' rows
-// of the weight table are staged in shared memory.  No cell lists, culling
-// or neighbour bookkeeping; the pair arithmetic is k_pair32's (ewald_pair2),
-// positions hi/lo FP32 relative to the cell's first point, FP32 sums per
-// 32 sources, Kahan-compensated across them.  Adds to the accumulator after
-// k_pair32 on the same stream.
+// workload), so per cell this is a dense all-pairs pass over tiles of
+// OWN_TILE points in ring-major order, one CTA per (target tile T, source
+// tile S >= T).  Pair (i, j) and pair (j, i) share the distance, the weight
+// (the table is symmetric) and the kernel coefficients, so off the diagonal
+// a CTA evaluates them once and adds both: to its target i (registers) and
+// to its source j (per-warp sums in shared memory; at step s lane l takes
+// the source pair (l + s) mod OWN_TILE/2, so the lanes of a warp touch
+// distinct sources and read consecutive ones).  A diagonal CTA (S = T) takes
+// every ordered pair of its tile one way.  The pair arithmetic is k_pair32's
+// (ewald_coef2 / ewald_apply2), positions hi/lo FP32 relative to the cell's
+// first point, FP32 sums per 32 sources (Kahan-compensated across them) and
+// per warp, added to the accumulator in FP64 atomically, after k_pair32 on
+// the same stream.  The target tile's at most (OWN_TILE - 1) / nlon + 2
+// latitude rings' rows of the weight table sit in shared memory.
 constexpr int OWN_TILE = 128;
 template <bool DL>
 __global__ void __launch_bounds__(OWN_TILE) k_pair_own32(PairArgs a) {
   __shared__ __align__(16) float s_src[15][OWN_TILE];  // hi xyz, lo xyz, f xyz, g xyz, normal xyz
-  __shared__ int s_id[OWN_TILE];
+  __shared__ __align__(16) int s_id[OWN_TILE];
+  __shared__ __align__(16) float s_rev[OWN_TILE / 32][3][OWN_TILE];  // per warp: the sources' sums
   extern __shared__ float s_mask[];  // rows lat0.. of the table, nlat * nhalf each
   const int nlat = a.nlat, nlon = a.nlon, nv = nlat * nlon, rowlen = nlat * a.nhalf;
-  const int bpc = (nv + OWN_TILE - 1) / OWN_TILE;
-  const int cell = blockIdx.x / bpc, b = blockIdx.x - cell * bpc;
-  const int k = b * OWN_TILE + threadIdx.x;  // ring-major index of the target in its cell
+  const int ntile = (nv + OWN_TILE - 1) / OWN_TILE, npt = ntile * (ntile + 1) / 2;
+  const int cell = blockIdx.x / npt;
+  int r = blockIdx.x - cell * npt, T = 0;
+  while (r >= ntile - T) { r -= ntile - T; ++T; }
+  const int S = T + r;
+  const bool diag = S == T;
+  const int tid = threadIdx.x, wid = tid >> 5;
+  const int k = T * OWN_TILE + tid;  // ring-major index of the target in its cell
   const bool active = k < nv;
   const int tlat = active ? k / nlon : 0, tlon = active ? k - tlat * nlon : 0;
-  const int lat0 = b * OWN_TILE / nlon;
-  const int nrow = min(nlat - 1, (b * OWN_TILE + OWN_TILE - 1) / nlon) - lat0 + 1;
-  for (int i = threadIdx.x; i < nrow * rowlen; i += OWN_TILE) s_mask[i] = a.mtab32[(size_t)lat0 * rowlen + i];
+  const int lat0 = T * OWN_TILE / nlon;
+  const int nrow = min(nlat - 1, (T * OWN_TILE + OWN_TILE - 1) / nlon) - lat0 + 1;
+  for (int i = tid; i < nrow * rowlen; i += OWN_TILE) s_mask[i] = a.mtab32[(size_t)lat0 * rowlen + i];
   const int p = cell * nv + tlon * nlat + tlat;  // the target's point index (= its target index)
-  float4 t0 = make_float4(0.f, 0.f, 0.f, 0.f), t1 = t0;
-  if (active) { t0 = a.op0[p]; t1 = a.op1[p]; }
+  // the source tile, and the per-warp sums cleared
+  const int js = S * OWN_TILE + tid;
+  int ps = 0;
+  if (js < nv) {
+    const int sl = js / nlon;
+    ps = cell * nv + (js - sl * nlon) * nlat + sl;
+    const int q = a.sinv[ps];
+    const float4 q0 = a.op0[ps], q1 = a.op1[ps], f = a.sF4[q];
+    s_src[0][tid] = q0.x; s_src[1][tid] = q0.y; s_src[2][tid] = q0.z;
+    s_src[3][tid] = q1.x; s_src[4][tid] = q1.y; s_src[5][tid] = q1.z;
+    s_src[6][tid] = f.x; s_src[7][tid] = f.y; s_src[8][tid] = f.z;
+    s_id[tid] = __float_as_int(q0.w);
+    if (DL) {
+      const float4 g = a.sG4[q], an = a.sa4[q];
+      s_src[9][tid] = g.x; s_src[10][tid] = g.y; s_src[11][tid] = g.z;
+      s_src[12][tid] = an.x; s_src[13][tid] = an.y; s_src[14][tid] = an.z;
+    }
+  } else {  // padding: a source beyond rc of every target
+    for (int c = 0; c < 15; ++c) s_src[c][tid] = 0.f;
+    s_src[0][tid] = 1.0e18f;
+    s_id[tid] = 0;
+  }
+  for (int w = 0; w < OWN_TILE / 32; ++w)
+    for (int c = 0; c < 3; ++c) s_rev[w][c][tid] = 0.f;
+  // the target: position, and off the diagonal its densities for the reverse terms
+  float4 t0 = make_float4(0.f, 0.f, 0.f, 0.f), t1 = t0, tf = t0, tg = t0, tn = t0;
+  if (active) {
+    t0 = a.op0[p];
+    t1 = a.op1[p];
+    if (!diag) {
+      const int q = a.sinv[p];
+      tf = a.sF4[q];
+      if (DL) { tg = a.sG4[q]; tn = a.sa4[q]; }
+    }
+  }
+  __syncthreads();
   const float2 nth0 = f2(-t0.x, -t0.x), nth1 = f2(-t0.y, -t0.y), nth2 = f2(-t0.z, -t0.z);
   const float2 ntl0 = f2(-t1.x, -t1.x), ntl1 = f2(-t1.y, -t1.y), ntl2 = f2(-t1.z, -t1.z);
+  const float2 tfx = f2(tf.x, tf.x), tfy = f2(tf.y, tf.y), tfz = f2(tf.z, tf.z);
+  const float2 tgx = f2(tg.x, tg.x), tgy = f2(tg.y, tg.y), tgz = f2(tg.z, tg.z);
+  const float2 tnx = f2(-tn.x, -tn.x), tny = f2(-tn.y, -tn.y), tnz = f2(-tn.z, -tn.z);  // (x.g)(-x.n) x: reverse sign
   const float* mrow = s_mask + (tlat - lat0) * rowlen;
   Kahan3 acc;
   acc.zero();
   unsigned npairs = 0;
   const float2 z2 = f2(0.f, 0.f);
-  for (int base = 0; base < nv; base += OWN_TILE) {
-    __syncthreads();  // the previous tile is consumed
-    {
-      const int i = threadIdx.x, js = base + i;
-      if (js < nv) {
-        const int ps = cell * nv + js, q = a.sinv[ps];
-        const float4 q0 = a.op0[ps], q1 = a.op1[ps], f = a.sF4[q];
-        s_src[0][i] = q0.x; s_src[1][i] = q0.y; s_src[2][i] = q0.z;
-        s_src[3][i] = q1.x; s_src[4][i] = q1.y; s_src[5][i] = q1.z;
-        s_src[6][i] = f.x; s_src[7][i] = f.y; s_src[8][i] = f.z;
-        s_id[i] = __float_as_int(q0.w);
-        if (DL) {
-          const float4 g = a.sG4[q], an = a.sa4[q];
-          s_src[9][i] = g.x; s_src[10][i] = g.y; s_src[11][i] = g.z;
-          s_src[12][i] = an.x; s_src[13][i] = an.y; s_src[14][i] = an.z;
+  float cx = 0.f, cy = 0.f, cz = 0.f;
+  for (int step = 0; step < OWN_TILE / 2; ++step) {
+    if (active) {
+      const int j = 2 * ((tid + step) & (OWN_TILE / 2 - 1));
+      const float2 xx = __fadd2_rn(__fadd2_rn(ld2(s_src[0], j), nth0), __fadd2_rn(ld2(s_src[3], j), ntl0));
+      const float2 yy = __fadd2_rn(__fadd2_rn(ld2(s_src[1], j), nth1), __fadd2_rn(ld2(s_src[4], j), ntl1));
+      const float2 zz = __fadd2_rn(__fadd2_rn(ld2(s_src[2], j), nth2), __fadd2_rn(ld2(s_src[5], j), ntl2));
+      const float2 r2 = __ffma2_rn(xx, xx, __ffma2_rn(yy, yy, __fmul2_rn(zz, zz)));
+      const bool oka = r2.x <= a.rc2_f, okb = r2.y <= a.rc2_f;
+      npairs += ((unsigned)oka + (unsigned)okb) * (diag ? 1u : 2u);
+      const int2 id = *reinterpret_cast<const int2*>(s_id + j);
+      float wa = 0.f, wb = 0.f;
+      if (oka && !(r2.x < a.reps2_f)) {
+        int dl = abs((id.x >> 16) - tlon);
+        dl = min(dl, nlon - dl);
+        wa = mrow[(id.x & 0xffff) * a.nhalf + dl];
+      }
+      if (okb && !(r2.y < a.reps2_f)) {
+        int dl = abs((id.y >> 16) - tlon);
+        dl = min(dl, nlon - dl);
+        wb = mrow[(id.y & 0xffff) * a.nhalf + dl];
+      }
+      if (wa != 0.f || wb != 0.f) {
+        float2 A, B, Adl, vx, vy, vz;
+        ewald_coef2<DL>(a, r2, wa, wb, A, B, Adl);
+        ewald_apply2<DL>(xx, yy, zz, A, B, Adl, ld2(s_src[6], j), ld2(s_src[7], j), ld2(s_src[8], j),
+                         DL ? ld2(s_src[9], j) : z2, DL ? ld2(s_src[10], j) : z2, DL ? ld2(s_src[11], j) : z2,
+                         DL ? ld2(s_src[12], j) : z2, DL ? ld2(s_src[13], j) : z2, DL ? ld2(s_src[14], j) : z2, vx,
+                         vy, vz);
+        cx = fmaf(wb, vx.y, fmaf(wa, vx.x, cx));
+        cy = fmaf(wb, vy.y, fmaf(wa, vy.x, cy));
+        cz = fmaf(wb, vz.y, fmaf(wa, vz.x, cz));
+        if (!diag) {  // pair (j, i): the vector is -x, so only the stresslet term changes sign
+          ewald_apply2<DL>(xx, yy, zz, A, B, Adl, tfx, tfy, tfz, tgx, tgy, tgz, tnx, tny, tnz, vx, vy, vz);
+          const float2 w2 = f2(wa, wb);
+          float2* rx = reinterpret_cast<float2*>(&s_rev[wid][0][j]);
+          float2* ry = reinterpret_cast<float2*>(&s_rev[wid][1][j]);
+          float2* rz = reinterpret_cast<float2*>(&s_rev[wid][2][j]);
+          *rx = __ffma2_rn(w2, vx, *rx);
+          *ry = __ffma2_rn(w2, vy, *ry);
+          *rz = __ffma2_rn(w2, vz, *rz);
         }
-      } else {  // padding: a source beyond rc of every target
-        for (int c = 0; c < 15; ++c) s_src[c][i] = 0.f;
-        s_src[0][i] = 1.0e18f;
-        s_id[i] = 0;
+      }
+      if ((step & 15) == 15) {
+        acc.add(0, cx);
+        acc.add(1, cy);
+        acc.add(2, cz);
+        cx = cy = cz = 0.f;
       }
     }
-    __syncthreads();
-    if (!active) continue;
-    const int cnt = min(OWN_TILE, nv - base);
-    for (int c0 = 0; c0 < cnt; c0 += 32) {
-      const int c1e = min(c0 + 32, (cnt + 1) & ~1);
-      float cx = 0.f, cy = 0.f, cz = 0.f;
-      for (int j = c0; j < c1e; j += 2) {
-        const float2 xx = __fadd2_rn(__fadd2_rn(ld2(s_src[0], j), nth0), __fadd2_rn(ld2(s_src[3], j), ntl0));
-        const float2 yy = __fadd2_rn(__fadd2_rn(ld2(s_src[1], j), nth1), __fadd2_rn(ld2(s_src[4], j), ntl1));
-        const float2 zz = __fadd2_rn(__fadd2_rn(ld2(s_src[2], j), nth2), __fadd2_rn(ld2(s_src[5], j), ntl2));
-        const float2 r2 = __ffma2_rn(xx, xx, __ffma2_rn(yy, yy, __fmul2_rn(zz, zz)));
-        const bool oka = r2.x <= a.rc2_f, okb = r2.y <= a.rc2_f;
-        npairs += (unsigned)oka + (unsigned)okb;
-        float wa = 0.f, wb = 0.f;
-        if (oka && !(r2.x < a.reps2_f)) {
-          const int id = s_id[j];
-          int dl = abs((id >> 16) - tlon);
-          dl = min(dl, nlon - dl);
-          wa = mrow[(id & 0xffff) * a.nhalf + dl];
-        }
-        if (okb && !(r2.y < a.reps2_f)) {
-          const int id = s_id[j + 1];
-          int dl = abs((id >> 16) - tlon);
-          dl = min(dl, nlon - dl);
-          wb = mrow[(id & 0xffff) * a.nhalf + dl];
-        }
-        if (wa == 0.f && wb == 0.f) continue;
-        ewald_pair2<DL>(a, xx, yy, zz, r2, wa, wb, ld2(s_src[6], j), ld2(s_src[7], j), ld2(s_src[8], j),
-                        DL ? ld2(s_src[9], j) : z2, DL ? ld2(s_src[10], j) : z2, DL ? ld2(s_src[11], j) : z2,
-                        DL ? ld2(s_src[12], j) : z2, DL ? ld2(s_src[13], j) : z2, DL ? ld2(s_src[14], j) : z2,
-                        cx, cy, cz);
-      }
-      acc.add(0, cx);
-      acc.add(1, cy);
-      acc.add(2, cz);
-    }
+    __syncwarp();  // the lanes' per-warp sums of this step are written before the next step's
   }
+  __syncthreads();
   if (active) {
     const double iA = 1.0 / a.tA[p];
-    for (int c = 0; c < 3; ++c) a.v[p + (size_t)c * a.nt] += ((double)acc.s[c] - (double)acc.c[c]) * iA;
+    for (int c = 0; c < 3; ++c) atomicAdd(a.v + p + (size_t)c * a.nt, ((double)acc.s[c] - (double)acc.c[c]) * iA);
+  }
+  if (!diag && js < nv) {
+    const double iA = 1.0 / a.tA[ps];
+    for (int c = 0; c < 3; ++c) {
+      float sum = 0.f;
+      for (int w = 0; w < OWN_TILE / 32; ++w) sum += s_rev[w][c][tid];
+      atomicAdd(a.v + ps + (size_t)c * a.nt, (double)sum * iA);
+    }
   }
   unsigned long long np = npairs;
   for (int o = 16; o > 0; o >>= 1) np += __shfl_xor_sync(0xffffffffu, np, o);
-  if ((threadIdx.x & 31) == 0 && np) atomicAdd(a.cnt + 1, np);
+  if ((tid & 31) == 0 && np) atomicAdd(a.cnt + 1, np);
 }
 
 // FP64 plain form: the same traversal with the reference arithmetic.
@@ -1254,7 +1324,7 @@ rbc3d_status run_pair_sum(rbc3d_ctx* ctx, int tlist, double c1, double c2, int p
     if (dl) { k_pair32<true><<<nb, TILE, 0, ctx->st>>>(a); ++ctx->launches; }
     else { k_pair32<false><<<nb, TILE, 0, ctx->st>>>(a); ++ctx->launches; }
     if (own) {
-      const int nv = ctx->nlat * ctx->nlon, nbo = ctx->ncell * ((nv + OWN_TILE - 1) / OWN_TILE);
+      const int nv = ctx->nlat * ctx->nlon, nt = (nv + OWN_TILE - 1) / OWN_TILE, nbo = ctx->ncell * (nt * (nt + 1) / 2);
       if (dl) {
         if (own_sm > 48 * 1024)
           CUDA_TRY(cudaFuncSetAttribute(k_pair_own32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)own_sm));
