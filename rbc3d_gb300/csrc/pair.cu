@@ -518,12 +518,16 @@ __device__ __forceinline__ void ewald_pair2(const PairArgs& a, float2 xx, float2
 // __fmul2_rn / __fadd2_rn, round-to-nearest like the scalar operations), a
 // source that does not contribute entering with weight 0 and a harmless
 // r^2 = 1 (4.20 -> 3.96 ms against the one-source loop on the 256-cell
-// workload).  Six 128-thread blocks per SM (80 registers a thread, 68 bytes
-// of spills) against the unbounded 96 registers: 3.58 against 3.76 ms alone on the
-// 256-cell workload, the matvec 11.97 against 12.23 ms; Estrin's scheme for
-// the fitted erfc polynomial, or five blocks per SM, measured slower.
+// workload).  Eight 128-thread blocks per SM (64 registers a thread, 132
+// bytes of spills): with the own-cell pairs taken by k_pair_own32 this
+// kernel runs a little longer than at six blocks (80 registers), but the
+// PME spread beside it gets its SMs sooner (the FP32D matvec 10.62 -> 10.52
+// ms on the 256-cell workload; four, five and seven blocks: 10.65, 10.61,
+// 10.58).  Before the own-cell split, six blocks against the unbounded 96
+// registers: 3.58 against 3.76 ms alone; Estrin's scheme for the fitted erfc
+// polynomial measured slower.
 template <bool DL>
-__global__ void __launch_bounds__(TILE, 6) k_pair32(PairArgs a) {
+__global__ void __launch_bounds__(TILE, 8) k_pair32(PairArgs a) {
   __shared__ __align__(16) ChunkX2<DL> s_ch[TILE / 32];
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int wu = blockIdx.x * (TILE / 32) + wid;  // this warp's unit
