@@ -357,7 +357,7 @@ def rooflines_of(b, counts, peak32, peak64, hbm_peak, hbm_src, sm_mhz):
                 "frac": a / peak, "work": work}
 
     r = {
-        "k_pair32": fl("k_pair32", s_c["pair"], pair_fl, peak32, "fp32",
+        "k_pair32": fl("k_pair32 + k_pair_own32 (the pair-sum stage)", s_c["pair"], pair_fl, peak32, "fp32",
                        f"{pairs} pairs within rc x {FLOP_PAIR_SL + FLOP_PAIR_DL} flops"),
         "k_self_ff": fl("k_self_ff", s_d["self"], self_fl, peak32, "fp32",
                         f"{counts['self_items']} targets x {NQ} patch points x {FLOP_SELFQ_SLDL} flops of the FP64 "
